@@ -1,0 +1,148 @@
+/*
+ * peps_mg.h -- C-ABI of the GB300 (sm_103a) multigrid V-cycle solver.
+ *
+ * Drop-in for the solve path of PEPS_MG (Fortran module `multigrid`).  Every entry
+ * point is `extern "C"`, takes plain pointers and sizes, returns an int status and
+ * never aborts the process.  Grid arrays are Fortran-ordered (i fastest) with one
+ * ghost layer, (0:nx+1, 0:ny+1, 0:nz+1), 8-byte doubles; a Fortran caller passes
+ * c_loc(x(0,0,0)).  Physical-boundary ghost cells hold the Dirichlet values, exactly
+ * as in the reference, and are never overwritten.
+ *
+ * Interface citations are relative to the reference project root.
+ */
+#ifndef PEPS_MG_H
+#define PEPS_MG_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Status codes.  The reference prints and stops (MPI_Finalize; stop / MPI_Abort);
+ * this library returns one of these instead. */
+#define PMG_OK 0
+#define PMG_EINVAL 1      /* argument or configuration the reference rejects          */
+#define PMG_ENOMEM 2      /* device or host allocation failed                         */
+#define PMG_EDIVERGED 3   /* residual norm became NaN or Inf                          */
+#define PMG_ETIMEOUT 4    /* a bounded device loop gave up, or the abort flag was set */
+#define PMG_ECUDA 5       /* CUDA runtime error (see pmg_last_error)                  */
+
+/* aggregation_method (&control aggregation_method, src/multigrid.f90:113-124) */
+#define PMG_CGS 0
+#define PMG_CGA 1
+#define PMG_CGPSA 2
+
+/* coarsest-level solver: the reference calls rbgs_solver_poisson_matrix
+ * (src/multigrid.f90:1837-1849); CG selects cg_solver_poisson_matrix
+ * (src/cg_poisson_matrix.f90:47) with the same 1000-iteration cap and tolerance. */
+#define PMG_COARSE_RBGS 0
+#define PMG_COARSE_CG 1
+
+/* precision of the V-cycle */
+#define PMG_FP64 0        /* plain FP64, bitwise the reference's arithmetic             */
+#define PMG_MIXED 1       /* FP32 V-cycles inside FP64 defect correction                */
+
+typedef struct pmg_ctx pmg_ctx;
+
+/* Solver configuration: the caller's subdomain mesh plus &control of PARA_INPUT.inp
+ * (src/main_peps.f90:44-60).  Mesh arrays are host memory, nx+2 (ny+2, nz+2) values
+ * each, indexed 0..n+1 as the subdomain type of src/geometry.f90:59-118. */
+typedef struct {
+    int nx, ny, nz;
+    const double *dxm, *dxg, *xg;
+    const double *dym, *dyg, *yg;
+    const double *dzm, *dzg, *zg;
+    int number_of_levels;      /* coarse levels below the finest (the finest is level 0) */
+    int number_of_vcycles;     /* V-cycle cap                                            */
+    int aggregation_method;    /* PMG_CGS / PMG_CGA / PMG_CGPSA                          */
+    int cga_level;             /* CGA_level                                              */
+    int cgpsa_level[3];        /* CGPSA_level(3)                                         */
+    int coarse_solver;         /* PMG_COARSE_RBGS or PMG_COARSE_CG                       */
+    int precision;             /* PMG_FP64 or PMG_MIXED                                  */
+} pmg_config_t;
+
+/* Per-solve report (replaces the reference's rank-0 prints, src/multigrid.f90:1972). */
+typedef struct {
+    int cycles;                /* V-cycles run                                           */
+    int converged;             /* 1 if sqrt(rsd/res0) < tolerance was reached            */
+    double res0;               /* sqrt(res0tol)                                          */
+    double final_ratio;        /* sqrt(rsd_val/res0tol) after the last cycle             */
+    double *history;           /* optional, 3*number_of_vcycles doubles:                 */
+                               /*   sqrt(rsd_val), sqrt(res0tol), sqrt(rsd_val/res0tol)  */
+    int *coarse_iterations;    /* optional, number_of_vcycles ints                       */
+    float elapsed_ms;          /* device time of the whole call (CUDA events)            */
+} pmg_report_t;
+
+/* multigrid_create(sdm, nlevel, ncycle, aggr_method, single_aggr_level,
+ * adaptive_aggr_level) -- src/multigrid.f90:75.  Builds the level hierarchy (level
+ * sizes, meshes, coefficient tables) and allocates the device state.  `stream` is a
+ * cudaStream_t (NULL = legacy default stream); all device work of the context is
+ * issued on it.  The finest-level operator is the reference's a_poisson built by
+ * matrix_heptadiagonal_create (src/matrix.f90:39) from the same mesh. */
+int pmg_create(pmg_ctx **ctx, const pmg_config_t *cfg, void *stream);
+
+/* multigrid_solve_vcycle(sol, rsd, a_poisson, rhs, sdm, maxiteration, tolerance,
+ * omega_sor) -- src/multigrid.f90:1864.  sol (in/out), rsd (out: final residual,
+ * ghosts zero) and rhs (in) are (nx+2)(ny+2)(nz+2) doubles, either all device memory
+ * or all host memory (host buffers are staged through the device).  report may be
+ * NULL. */
+int pmg_solve_vcycle(pmg_ctx *ctx, double *sol, double *rsd, const double *rhs, int maxiteration,
+                     double tolerance, double omega_sor, pmg_report_t *report);
+
+/* multigrid_destroy -- src/multigrid.f90:1320 */
+int pmg_destroy(pmg_ctx *ctx);
+
+/* Level sizes of the hierarchy without creating a context (host only, no GPU needed):
+ * the one-rank rules of multigrid_subdomain_create_CGS / _CGA / _CGPSA
+ * (src/multigrid.f90:167-402, 503-838, 998-1288).  sizes receives 3*(n_levels+1) ints
+ * (level 0 = nx,ny,nz), lv_coarsest the last level at which each axis was halved.
+ * Returns PMG_EINVAL where the reference stops with an error. */
+int pmg_level_sizes(int nx, int ny, int nz, int n_levels, int aggregation_method, int cga_level, int *sizes,
+                    int lv_coarsest[3]);
+
+/* Hierarchy queries: level 0 is the caller's subdomain, 1..number_of_levels the
+ * coarse levels (mg_sdm(l) of src/multigrid.f90:54). */
+int pmg_level_dims(const pmg_ctx *ctx, int level, int dims[3]);
+int pmg_level_mesh(const pmg_ctx *ctx, int level, int axis, double *dm, double *dg, double *xg);
+int pmg_coarsest_levels(const pmg_ctx *ctx, int lv_coarsest[3]);
+
+/* ---- Lower API: operate on device arrays of one level's shape ------------------ */
+/* Calls are asynchronous on the context stream unless they return a scalar.        */
+
+/* mv_mul_poisson_matrix(y, a_poisson, x, dm, is_serial) -- src/poisson_matrix_operator.f90:110 */
+int pmg_mv_mul(pmg_ctx *ctx, int level, double *y, const double *x);
+/* vv_dot_3d_matrix(result, x, y, nx, ny, nz, is_serial) -- src/poisson_matrix_operator.f90:40 */
+int pmg_vv_dot(pmg_ctx *ctx, int level, const double *x, const double *y, double *result);
+/* multigrid_residual(rsd, a_poisson, x, rhs, dm, is_aggregated) -- src/multigrid.f90:1782 */
+int pmg_residual(pmg_ctx *ctx, int level, double *r, const double *x, const double *b);
+/* rbgs_iterator_poisson_matrix(sol, a_poisson, rhs, dm, maxiteration, omega, ...) --
+ * src/rbgs_poisson_matrix.f90:191 */
+int pmg_rbgs_iterator(pmg_ctx *ctx, int level, double *x, const double *b, int maxiteration, double omega);
+/* rbgs_solver_poisson_matrix(sol, a_poisson, rhs, dm, maxiteration, tolerance, omega,
+ * ...) -- src/rbgs_poisson_matrix.f90:47.  iterations/ratio may be NULL. */
+int pmg_rbgs_solver(pmg_ctx *ctx, int level, double *x, const double *b, int maxiteration, double tolerance,
+                    double omega, int *iterations, double *ratio);
+/* cg_iterator_poisson_matrix -- src/cg_poisson_matrix.f90:157 */
+int pmg_cg_iterator(pmg_ctx *ctx, int level, double *x, const double *b, int maxiteration);
+/* cg_solver_poisson_matrix -- src/cg_poisson_matrix.f90:47 */
+int pmg_cg_solver(pmg_ctx *ctx, int level, double *x, const double *b, int maxiteration, double tolerance,
+                  int *iterations, double *ratio);
+/* multigrid_restriction(val_c, val_f, dm_c, dm_f, level) -- src/multigrid.f90:1345.
+ * level is the fine level; val_c is zeroed (ghosts included) then filled. */
+int pmg_restriction(pmg_ctx *ctx, int level, double *val_c, const double *val_f);
+/* multigrid_prolongation_linear_on_nonuniform_grid(val_f, val_c, dm_f, dm_c, level) --
+ * src/multigrid.f90:1516.  Writes only the interior children of val_f. */
+int pmg_prolongation(pmg_ctx *ctx, int level, double *val_f, const double *val_c);
+/* Fused prolongation + correction x_f = x_f + P x_c, the pair of statements at
+ * src/multigrid.f90:1957-1958 (interior; the reference's ghost add is of zeros). */
+int pmg_prolong_add(pmg_ctx *ctx, int level, double *x_f, const double *x_c);
+
+/* Wait for all work issued on the context stream. */
+int pmg_sync(pmg_ctx *ctx);
+/* Text of the last CUDA error seen by this thread ("" if none). */
+const char *pmg_last_error(void);
+const char *pmg_status_string(int status);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* PEPS_MG_H */

@@ -1,0 +1,12 @@
+"""peps_mg_gb300 -- GB300 (sm_103a) multigrid V-cycle solver for the 3-D Poisson
+equation on cell-centred, non-uniform Cartesian grids; a drop-in for the solve path of
+PEPS_MG (multigrid_create / multigrid_solve_vcycle / multigrid_destroy).
+"""
+from . import geometry  # noqa: F401
+from ._lib import (PMG_CGA, PMG_CGPSA, PMG_CGS, PMG_COARSE_CG, PMG_COARSE_RBGS, PMG_FP64,  # noqa: F401
+                   PMG_MIXED, PmgError, load)
+from .multigrid import (Multigrid, SolveReport, level_sizes, multigrid_create, multigrid_destroy,  # noqa: F401
+                        multigrid_solve_vcycle)
+
+__all__ = ["Multigrid", "SolveReport", "PmgError", "multigrid_create", "multigrid_solve_vcycle",
+           "multigrid_destroy", "level_sizes", "geometry", "load"]

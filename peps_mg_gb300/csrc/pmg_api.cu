@@ -1,0 +1,962 @@
+// pmg_api.cu -- host side of the library: the level hierarchy, the per-level
+// coefficient and transfer tables, the device state, the FP64 V-cycle driver and the
+// C-ABI entry points declared in include/peps_mg.h.
+//
+// Host arithmetic that feeds the kernels (mesh coarsening, coefficient tables,
+// transfer weights) is compiled with -ffp-contract=off and follows the reference
+// expressions cited beside it, so the tables hold exactly the values the reference
+// computes inline.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "../../include/peps_mg.h"
+#include "pmg_ctx.h"
+
+namespace pmg {
+
+static thread_local std::string g_last_error;
+
+void set_error(const std::string &msg) { g_last_error = msg; }
+
+int cuda_status(cudaError_t e, const char *what)
+{
+    if (e == cudaSuccess) return PMG_OK;
+    set_error(std::string(what) + ": " + cudaGetErrorString(e));
+    return e == cudaErrorMemoryAllocation ? PMG_ENOMEM : PMG_ECUDA;
+}
+
+#define PMG_TRY(expr)                      \
+    do {                                   \
+        int _rc = (expr);                  \
+        if (_rc != PMG_OK) return _rc;     \
+    } while (0)
+
+#define PMG_CUDA(expr, what) PMG_TRY(cuda_status((expr), (what)))
+
+// ---------------------------------------------------------------------------------
+// Level-size rules at one rank (CGS src/multigrid.f90:221-309, CGA :541-740, CGPSA
+// :1029-1201 with its aggregation levels forced to 0 at one rank, :1032-1036).
+// ---------------------------------------------------------------------------------
+int level_sizes(const int n0[3], int n_levels, int method, int cga_level, std::vector<std::array<int, 3>> &sizes,
+                int lvc[3])
+{
+    if (n_levels <= 1 || n_levels >= kMaxLevels) {
+        set_error("number_of_levels must be larger than 1 (and below the library limit)");
+        return PMG_EINVAL;
+    }
+    int n[3] = {n0[0], n0[1], n0[2]};
+    lvc[0] = lvc[1] = lvc[2] = 0;
+    sizes.assign((size_t)n_levels + 1, {0, 0, 0});
+    sizes[0] = {n[0], n[1], n[2]};
+    if (method == PMG_CGS) {
+        if (cga_level != 0) {
+            set_error("Aggregation level should be 0 for CGS method");
+            return PMG_EINVAL;
+        }
+        for (int l = 1; l <= n_levels; ++l)
+            for (int d = 0; d < 3; ++d) {
+                if (n[d] % 2 == 0) {
+                    n[d] /= 2;
+                    lvc[d] = l;
+                }
+                sizes[l][d] = n[d];
+            }
+        if (n_levels > std::max(lvc[0], std::max(lvc[1], lvc[2]))) {
+            set_error("Number of levels is greater than the coarsest level in global domain");
+            return PMG_EINVAL;
+        }
+    } else if (method == PMG_CGA) {
+        if (cga_level == 0) {
+            set_error("Aggregation level should be larger than 0");
+            return PMG_EINVAL;
+        }
+        for (int l = 1; l <= n_levels; ++l) {
+            for (int d = 0; d < 3; ++d) {
+                if (l <= cga_level) {
+                    if (n[d] % 2 == 1) {
+                        set_error("grid coarsening impossible at or before the aggregation level (odd size)");
+                        return PMG_EINVAL;
+                    }
+                    sizes[l][d] = n[d] / 2;
+                    if (l == cga_level) lvc[d] = l;
+                } else if (n[d] % 2 == 1) {
+                    sizes[l][d] = n[d];
+                } else {
+                    sizes[l][d] = n[d] / 2;
+                    lvc[d] = l;
+                }
+            }
+            for (int d = 0; d < 3; ++d) n[d] = sizes[l][d];
+            if (((long long)n[0] * n[1] * n[2]) % 2 == 1) break;
+        }
+        if (n_levels > std::max(lvc[0], std::max(lvc[1], lvc[2]))) {
+            set_error("Number of levels is greater than the coarsest level in global domain");
+            return PMG_EINVAL;
+        }
+    } else if (method == PMG_CGPSA) {
+        for (int l = 1; l <= n_levels; ++l) {
+            for (int d = 0; d < 3; ++d) {
+                if (n[d] % 2 == 1) {
+                    sizes[l][d] = n[d];
+                } else {
+                    sizes[l][d] = n[d] / 2;
+                    lvc[d] = l;
+                }
+            }
+            for (int d = 0; d < 3; ++d) n[d] = sizes[l][d];
+            if (((long long)n[0] * n[1] * n[2]) % 2 == 1) break;
+        }
+        if (n_levels != std::max(lvc[0], std::max(lvc[1], lvc[2]))) {
+            set_error("Number of levels should be equal to the coarsest level in global domain");
+            return PMG_EINVAL;
+        }
+    } else {
+        set_error("Aggregation method should be 0, 1, or 2");
+        return PMG_EINVAL;
+    }
+    return PMG_OK;
+}
+
+// Mesh of a coarse level along one axis (src/multigrid.f90:450-491 and :872-987).
+static void coarsen_axis(int method, int agg_level, int n, const std::vector<double> &dm_f,
+                         const std::vector<double> &dg_f, const std::vector<double> &xg_f, double ox, int lv,
+                         int lv_coarsest, std::vector<double> &dm, std::vector<double> &dg, std::vector<double> &xg)
+{
+    dm.assign((size_t)n + 2, 0.0);
+    dg.assign((size_t)n + 2, 0.0);
+    xg.assign((size_t)n + 2, 0.0);
+    if (lv <= lv_coarsest) {
+        for (int i = 1; i <= n; ++i) dm[i] = dm_f[2 * i - 1] + dm_f[2 * i];
+        dm[0] = dm_f[0];
+        dm[n + 1] = dm_f[2 * n + 1];
+        double x0;
+        if (method == PMG_CGS || (method == PMG_CGA && lv <= agg_level))
+            x0 = ox - 0.5 * dm[0];
+        else
+            x0 = (xg_f[0] + 0.5 * dm_f[0]) - 0.5 * dm[0];
+        xg[0] = x0;
+        for (int i = 1; i <= n; ++i) {
+            dg[i] = 0.5 * (dm[i] + dm[i - 1]);
+            xg[i] = xg[i - 1] + dg[i];
+        }
+        dg[n + 1] = 0.5 * (dm[n + 1] + dm[n]);
+        xg[n + 1] = xg[n] + dg[n + 1];
+    } else {
+        dm = dm_f;
+        dg = dg_f;
+        xg = xg_f;
+    }
+}
+
+// ---------------------------------------------------------------------------------
+// Device tables
+// ---------------------------------------------------------------------------------
+static void axis_coeff_tables(const std::vector<double> &dm, const std::vector<double> &dg, int n,
+                              std::vector<double> &cm, std::vector<double> &cp, std::vector<double> &s)
+{
+    cm.assign((size_t)n + 2, 0.0);
+    cp.assign((size_t)n + 2, 0.0);
+    s.assign((size_t)n + 2, 0.0);
+    for (int i = 1; i <= n; ++i) {
+        cm[i] = 1.0 / (dm[i] * dg[i]);        // dxmp2i, src/matrix.f90:75
+        cp[i] = 1.0 / (dm[i] * dg[i + 1]);    // dxmn2i, src/matrix.f90:76
+        s[i] = cm[i] + cp[i];                 // first partial sum of c0, src/matrix.f90:82
+    }
+}
+
+// Restriction weight dxf on the fine index (src/multigrid.f90:1415-1425).
+static void restrict_weights(const std::vector<double> &dm_c, const std::vector<double> &dm_f, int nf, bool stride1,
+                             std::vector<double> &w)
+{
+    w.assign((size_t)nf + 2, 0.0);
+    if (stride1) {
+        w = dm_f;
+    } else {
+        for (int i = 1; i <= nf; ++i) w[i] = dm_c[(i - 1) / 2 + 1] - dm_f[i];
+    }
+}
+
+// Prolongation weights dxp/dxn on the fine index (src/multigrid.f90:1594-1612).
+static void prolong_weights(const std::vector<double> &dm_c, const std::vector<double> &dm_f, int nc, int nf,
+                            bool stride1, std::vector<double> &dp, std::vector<double> &dn)
+{
+    dp.assign((size_t)nf + 2, 0.0);
+    dn.assign((size_t)nf + 2, 0.0);
+    if (stride1) {
+        dp = dm_c;
+        dn = dm_c;
+        dp.resize((size_t)nf + 2, 0.0);
+        dn.resize((size_t)nf + 2, 0.0);
+    } else {
+        for (int i = 1; i <= nc; ++i) {
+            const int f = 2 * i;
+            dp[f - 1] = 1.0 * dm_f[f - 2] + 0.5 * dm_f[f - 1];
+            dp[f] = 0.5 * dm_f[f - 1];
+            dn[f - 1] = 0.5 * dm_f[f];
+            dn[f] = 1.0 * dm_f[f + 1] + 0.5 * dm_f[f];
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------------
+// Context life cycle
+// ---------------------------------------------------------------------------------
+static int validate_mesh(const pmg_config_t *c)
+{
+    if (!c->dxm || !c->dxg || !c->dym || !c->dyg || !c->dzm || !c->dzg) {
+        set_error("mesh arrays dxm/dxg/dym/dyg/dzm/dzg are required");
+        return PMG_EINVAL;
+    }
+    if (c->nx < 1 || c->ny < 1 || c->nz < 1) {
+        set_error("nx, ny, nz must be positive");
+        return PMG_EINVAL;
+    }
+    if ((long long)(c->nx + 2) * (c->ny + 2) >= (1LL << 31)) {
+        set_error("plane of the grid is too large");
+        return PMG_EINVAL;
+    }
+    return PMG_OK;
+}
+
+int Ctx::build(const pmg_config_t *c, cudaStream_t s)
+{
+    PMG_TRY(validate_mesh(c));
+    if (c->number_of_vcycles < 0) {
+        set_error("number_of_vcycles must be non-negative");
+        return PMG_EINVAL;
+    }
+    if (c->coarse_solver != PMG_COARSE_RBGS && c->coarse_solver != PMG_COARSE_CG) {
+        set_error("coarse_solver must be PMG_COARSE_RBGS or PMG_COARSE_CG");
+        return PMG_EINVAL;
+    }
+    if (c->precision != PMG_FP64 && c->precision != PMG_MIXED) {
+        set_error("precision must be PMG_FP64 or PMG_MIXED");
+        return PMG_EINVAL;
+    }
+    stream = s;
+    nl = c->number_of_levels;
+    n_vcycles = c->number_of_vcycles;
+    method = c->aggregation_method;
+    cga_level = c->cga_level;
+    for (int d = 0; d < 3; ++d) cgpsa_level[d] = c->cgpsa_level[d];
+    coarse_solver = c->coarse_solver;
+    precision = c->precision;
+    const int n0[3] = {c->nx, c->ny, c->nz};
+    std::vector<std::array<int, 3>> sizes;
+    PMG_TRY(level_sizes(n0, nl, method, cga_level, sizes, lvc));
+
+    lv.resize((size_t)nl + 1);
+    const double *fm[3] = {c->dxm, c->dym, c->dzm}, *fg[3] = {c->dxg, c->dyg, c->dzg}, *fx[3] = {c->xg, c->yg, c->zg};
+    double o[3];
+    for (int l = 0; l <= nl; ++l) {
+        Level &L = lv[l];
+        for (int d = 0; d < 3; ++d) L.n[d] = sizes[l][d];
+        L.sy = L.n[0] + 2;
+        L.sz = (long long)(L.n[0] + 2) * (L.n[1] + 2);
+        L.total = (size_t)L.sz * (size_t)(L.n[2] + 2);
+        for (int d = 0; d < 3; ++d) {
+            const int n = L.n[d];
+            if (l == 0) {
+                L.dm[d].assign(fm[d], fm[d] + n + 2);
+                L.dg[d].assign(fg[d], fg[d] + n + 2);
+                if (fx[d])
+                    L.xg[d].assign(fx[d], fx[d] + n + 2);
+                else {
+                    // cell centres from the widths when the caller gives none
+                    L.xg[d].assign((size_t)n + 2, 0.0);
+                    for (int i = 1; i <= n + 1; ++i) L.xg[d][i] = L.xg[d][i - 1] + L.dg[d][i];
+                }
+                o[d] = L.xg[d][1] - 0.5 * L.dm[d][1];   // sdm%ox, src/geometry.f90:378-380
+            } else {
+                const Level &F = lv[l - 1];
+                coarsen_axis(method, cga_level, n, F.dm[d], F.dg[d], F.xg[d], o[d], l, lvc[d], L.dm[d], L.dg[d],
+                             L.xg[d]);
+            }
+            for (int i = 1; i <= n; ++i)
+                if (!(L.dm[d][i] > 0.0) || !(L.dg[d][i] > 0.0) || !(L.dg[d][i + 1] > 0.0)) {
+                    set_error("mesh widths and spacings of interior cells must be positive");
+                    return PMG_EINVAL;
+                }
+        }
+    }
+
+    // ---- host tables ------------------------------------------------------------
+    std::vector<double> blob;
+    auto push = [&](const std::vector<double> &v) {
+        size_t off = blob.size();
+        blob.insert(blob.end(), v.begin(), v.end());
+        // keep every table 16-byte aligned
+        if (blob.size() % 2) blob.push_back(0.0);
+        return off;
+    };
+    struct Off {
+        size_t cm[3], cp[3], s;
+        size_t w[3], pp[3], pn[3];
+    };
+    std::vector<Off> off((size_t)nl + 1);
+    for (int l = 0; l <= nl; ++l) {
+        const Level &L = lv[l];
+        for (int d = 0; d < 3; ++d) {
+            std::vector<double> cm, cp, s;
+            axis_coeff_tables(L.dm[d], L.dg[d], L.n[d], cm, cp, s);
+            off[l].cm[d] = push(cm);
+            off[l].cp[d] = push(cp);
+            if (d == 0) off[l].s = push(s);
+        }
+        if (l < nl) {
+            const Level &C = lv[l + 1];
+            for (int d = 0; d < 3; ++d) {
+                const bool s1 = l >= lvc[d];
+                std::vector<double> w, dp, dn;
+                restrict_weights(C.dm[d], L.dm[d], L.n[d], s1, w);
+                prolong_weights(C.dm[d], L.dm[d], C.n[d], L.n[d], s1, dp, dn);
+                off[l].w[d] = push(w);
+                off[l].pp[d] = push(dp);
+                off[l].pn[d] = push(dn);
+            }
+        }
+    }
+    PMG_CUDA(cudaMalloc(&d_tables, blob.size() * sizeof(double)), "table allocation");
+    PMG_CUDA(cudaMemcpy(d_tables, blob.data(), blob.size() * sizeof(double), cudaMemcpyHostToDevice), "table copy");
+    tables_host = blob;
+
+    K.resize((size_t)nl + 1);
+    X.resize((size_t)nl);
+    for (int l = 0; l <= nl; ++l) {
+        const Level &L = lv[l];
+        LevelK<double> &k = K[l];
+        k.nx = L.n[0]; k.ny = L.n[1]; k.nz = L.n[2];
+        k.sy = L.sy; k.sz = L.sz;
+        k.cxm = d_tables + off[l].cm[0]; k.cxp = d_tables + off[l].cp[0]; k.sx = d_tables + off[l].s;
+        k.cym = d_tables + off[l].cm[1]; k.cyp = d_tables + off[l].cp[1];
+        k.czm = d_tables + off[l].cm[2]; k.czp = d_tables + off[l].cp[2];
+        if (l < nl) {
+            const Level &C = lv[l + 1];
+            XferK<double> &x = X[l];
+            x.ncx = C.n[0]; x.ncy = C.n[1]; x.ncz = C.n[2];
+            x.csy = C.sy; x.csz = C.sz;
+            x.fsy = L.sy; x.fsz = L.sz;
+            x.stx = l >= lvc[0] ? 1 : 2;
+            x.sty = l >= lvc[1] ? 1 : 2;
+            x.stz = l >= lvc[2] ? 1 : 2;
+            x.wx = d_tables + off[l].w[0]; x.wy = d_tables + off[l].w[1]; x.wz = d_tables + off[l].w[2];
+            x.pxp = d_tables + off[l].pp[0]; x.pxn = d_tables + off[l].pn[0];
+            x.pyp = d_tables + off[l].pp[1]; x.pyn = d_tables + off[l].pn[1];
+            x.pzp = d_tables + off[l].pp[2]; x.pzn = d_tables + off[l].pn[2];
+        }
+    }
+
+    // ---- execution mapping --------------------------------------------------------
+    // CGS: every level on the full grid; the coarsest solve in the single-CTA kernel.
+    // CGA: from CGA_level on, the whole coarse tail runs in one CTA (the reference
+    //      gathers everything onto rank 0 there, src/multigrid.f90:2095-2135).
+    // CGPSA: an axis is collapsed to one CTA column from its CGPSA_level on (the
+    //      reference aggregates that axis there); once all three are collapsed the
+    //      rest of the tail runs in the single-CTA kernel.
+    launch.assign((size_t)nl + 1, Launch{{false, false, false}});
+    tail_l0 = nl;
+    if (method == PMG_CGA) {
+        tail_l0 = std::min(std::max(cga_level, 1), nl);
+    } else if (method == PMG_CGPSA) {
+        bool every_axis = true;
+        int last = 0;
+        for (int d = 0; d < 3; ++d) {
+            if (cgpsa_level[d] > 0) {
+                for (int l = cgpsa_level[d]; l <= nl; ++l) launch[l].collapse[d] = true;
+                last = std::max(last, cgpsa_level[d]);
+            } else {
+                every_axis = false;
+            }
+        }
+        if (every_axis) tail_l0 = std::min(last, nl);
+    }
+    // A level too large for one CTA is kept on the grid kernels.
+    while (tail_l0 <= nl && lv[tail_l0].total > kTailMaxCells) ++tail_l0;
+
+    // ---- device arrays -------------------------------------------------------------
+    size_t max_part = 1;
+    for (int l = 1; l <= nl; ++l) {
+        Level &L = lv[l];
+        PMG_CUDA(cudaMalloc(&L.x, L.total * sizeof(double)), "level allocation");
+        PMG_CUDA(cudaMalloc(&L.b, L.total * sizeof(double)), "level allocation");
+        PMG_CUDA(cudaMalloc(&L.r, L.total * sizeof(double)), "level allocation");
+        PMG_CUDA(cudaMemset(L.x, 0, L.total * sizeof(double)), "level init");
+        PMG_CUDA(cudaMemset(L.b, 0, L.total * sizeof(double)), "level init");
+        PMG_CUDA(cudaMemset(L.r, 0, L.total * sizeof(double)), "level init");
+    }
+    for (int l = 0; l <= nl; ++l) {
+        dim3 g, b;
+        grid_for_cells(K[l], launch[l], &g, &b);
+        max_part = std::max(max_part, (size_t)g.x * g.y * g.z);
+    }
+    npart_cap = max_part;
+    PMG_CUDA(cudaMalloc(&d_partials, npart_cap * sizeof(double)), "scratch allocation");
+    PMG_CUDA(cudaMalloc(&d_scal, 16 * sizeof(double)), "scratch allocation");
+    PMG_CUDA(cudaMalloc(&d_iscal, 16 * sizeof(int)), "scratch allocation");
+    PMG_CUDA(cudaMemset(d_iscal, 0, 16 * sizeof(int)), "scratch init");
+    {
+        const Level &C = lv[nl];
+        for (double **p : {&d_cp, &d_cap, &d_crr}) {
+            PMG_CUDA(cudaMalloc(p, C.total * sizeof(double)), "coarse scratch");
+            PMG_CUDA(cudaMemset(*p, 0, C.total * sizeof(double)), "coarse scratch");
+        }
+    }
+    PMG_CUDA(cudaMalloc(&d_tail, sizeof(TailDesc<double>)), "tail descriptor");
+    PMG_CUDA(cudaEventCreate(&ev0), "event");
+    PMG_CUDA(cudaEventCreate(&ev1), "event");
+    return PMG_OK;
+}
+
+Ctx::~Ctx()
+{
+    for (auto &L : lv) {
+        cudaFree(L.x);
+        cudaFree(L.b);
+        cudaFree(L.r);
+    }
+    cudaFree(d_tables);
+    cudaFree(d_partials);
+    cudaFree(d_scal);
+    cudaFree(d_iscal);
+    cudaFree(d_cp);
+    cudaFree(d_cap);
+    cudaFree(d_crr);
+    cudaFree(d_tail);
+    cudaFree(stage_sol);
+    cudaFree(stage_rsd);
+    cudaFree(stage_rhs);
+    for (auto &v : scratch_levels) cudaFree(v);
+    if (ev0) cudaEventDestroy(ev0);
+    if (ev1) cudaEventDestroy(ev1);
+    destroy_mixed();
+}
+
+// Sum of x*y (or of r^2 from residual partials) into d_scal[slot].
+int Ctx::dot(int l, const double *x, const double *y, int slot)
+{
+    int np = 0;
+    PMG_TRY(f64_dot_partials(K[l], launch[l], x, y, d_partials, &np, stream));
+    return f64_reduce(d_partials, np, d_scal + slot, stream);
+}
+
+int Ctx::residual_norm(int l, double *r, const double *x, const double *b, int slot)
+{
+    int np = 0;
+    PMG_TRY(f64_residual(K[l], launch[l], r, x, b, d_partials, &np, stream));
+    return f64_reduce(d_partials, np, d_scal + slot, stream);
+}
+
+int Ctx::fetch_scalars(double *h, int n)
+{
+    PMG_CUDA(cudaMemcpyAsync(h, d_scal, sizeof(double) * n, cudaMemcpyDeviceToHost, stream), "scalar read");
+    PMG_CUDA(cudaStreamSynchronize(stream), "stream sync");
+    return PMG_OK;
+}
+
+// Upload the tail descriptor for levels l0..nl.
+int Ctx::upload_tail(int l0, int maxit, double omega, double tol)
+{
+    TailDesc<double> &D = tail_host;
+    std::memset(&D, 0, sizeof(D));
+    D.l0 = l0;
+    D.nl = nl;
+    D.maxit = maxit;
+    D.coarse_solver = coarse_solver;
+    D.coarse_maxit = 1000;   // src/multigrid.f90:1948
+    D.omega = omega;
+    D.omw = 1.0 - omega;
+    D.tol = tol;
+    D.p = d_cp;
+    D.ap = d_cap;
+    D.rr = d_crr;
+    D.iters_out = d_iscal + 1;
+    for (int l = 0; l <= nl; ++l) {
+        D.L[l] = K[l];
+        if (l < nl) D.X[l] = X[l];
+        D.x[l] = lv[l].x;
+        D.b[l] = lv[l].b;
+        D.r[l] = lv[l].r;
+    }
+    PMG_CUDA(cudaMemcpyAsync(d_tail, &D, sizeof(D), cudaMemcpyHostToDevice, stream), "tail descriptor upload");
+    return PMG_OK;
+}
+
+// Coarsest-level solve with the grid kernels (a coarsest level too large for one CTA).
+int Ctx::coarse_solve_grid(double tol, double omega, int *iters)
+{
+    Level &C = lv[nl];
+    PMG_CUDA(cudaMemsetAsync(C.x, 0, C.total * sizeof(double), stream), "coarse init");
+    if (coarse_solver == PMG_COARSE_CG) return cg_dev(nl, C.x, C.b, 1000, tol, true, iters, nullptr);
+    return rbgs_solver_dev(nl, C.x, C.b, 1000, tol, omega, iters, nullptr);
+}
+
+// One V-cycle from the finest level (src/multigrid.f90:1931-1967), FP64.
+int Ctx::vcycle_f64(double *sol, double *rsd, const double *rhs, int maxit, double omega, double tol,
+                    int *coarse_iters)
+{
+    const Level &S = lv[0];
+    (void)S;
+    PMG_TRY(f64_rbgs_sweeps(K[0], launch[0], sol, rhs, maxit, omega, stream));
+    PMG_TRY(f64_residual(K[0], launch[0], rsd, sol, rhs, nullptr, nullptr, stream));
+    PMG_TRY(f64_restrict(X[0], launch[1], rsd, lv[1].b, stream));
+    const int grid_end = std::min(tail_l0, nl);
+    for (int l = 1; l < grid_end; ++l) {
+        Level &L = lv[l];
+        PMG_CUDA(cudaMemsetAsync(L.x, 0, L.total * sizeof(double), stream), "level reset");
+        PMG_TRY(f64_rbgs_sweeps(K[l], launch[l], L.x, L.b, maxit, omega, stream));
+        PMG_TRY(f64_residual(K[l], launch[l], L.r, L.x, L.b, nullptr, nullptr, stream));
+        PMG_TRY(f64_restrict(X[l], launch[l + 1], L.r, lv[l + 1].b, stream));
+    }
+    if (tail_l0 <= nl) {
+        PMG_TRY(f64_tail(d_tail, stream));
+        if (coarse_iters) {
+            int h = 0;
+            PMG_CUDA(cudaMemcpyAsync(&h, d_iscal + 1, sizeof(int), cudaMemcpyDeviceToHost, stream), "iters");
+            PMG_CUDA(cudaStreamSynchronize(stream), "sync");
+            *coarse_iters = h;
+        }
+    } else {
+        PMG_TRY(coarse_solve_grid(tol, omega, coarse_iters));
+    }
+    for (int l = grid_end - 1; l >= 1; --l) {
+        Level &L = lv[l];
+        PMG_TRY(f64_prolong(X[l], launch[l + 1], lv[l + 1].x, L.x, true, stream));
+        PMG_TRY(f64_rbgs_sweeps(K[l], launch[l], L.x, L.b, maxit, omega, stream));
+    }
+    PMG_TRY(f64_prolong(X[0], launch[1], lv[1].x, sol, true, stream));
+    PMG_TRY(f64_rbgs_sweeps(K[0], launch[0], sol, rhs, maxit, omega, stream));
+    return PMG_OK;
+}
+
+int Ctx::solve_f64(double *sol, double *rsd, const double *rhs, int maxit, double tol, double omega,
+                   pmg_report_t *rep)
+{
+    const Level &S = lv[0];
+    // rsd(:,:,:) = 0 then r = b - A x (src/multigrid.f90:1794-1805, :1924-1925)
+    PMG_CUDA(cudaMemsetAsync(rsd, 0, S.total * sizeof(double), stream), "rsd init");
+    PMG_TRY(residual_norm(0, rsd, sol, rhs, 0));
+    double h[2];
+    PMG_TRY(fetch_scalars(h, 1));
+    const double res0tol = h[0];
+    if (tail_l0 <= nl) PMG_TRY(upload_tail(tail_l0, maxit, omega, tol));
+    int cycles = 0, converged = 0;
+    double ratio = 0.0;
+    for (int cyc = 1; cyc <= n_vcycles; ++cyc) {
+        int ci = 0;
+        PMG_TRY(vcycle_f64(sol, rsd, rhs, maxit, omega, tol, rep && rep->coarse_iterations ? &ci : nullptr));
+        PMG_TRY(residual_norm(0, rsd, sol, rhs, 1));     // :1970-1971
+        PMG_TRY(fetch_scalars(h, 2));
+        const double rsd_val = h[1];
+        ratio = std::sqrt(rsd_val / res0tol);
+        cycles = cyc;
+        if (rep) {
+            if (rep->history) {
+                rep->history[3 * (cyc - 1) + 0] = std::sqrt(rsd_val);
+                rep->history[3 * (cyc - 1) + 1] = std::sqrt(res0tol);
+                rep->history[3 * (cyc - 1) + 2] = ratio;
+            }
+            if (rep->coarse_iterations) rep->coarse_iterations[cyc - 1] = ci;
+        }
+        if (!std::isfinite(rsd_val)) {
+            if (rep) {
+                rep->cycles = cycles;
+                rep->converged = 0;
+                rep->res0 = std::sqrt(res0tol);
+                rep->final_ratio = ratio;
+            }
+            set_error("residual norm is not finite");
+            return PMG_EDIVERGED;
+        }
+        if (ratio < tol) {                                 // :1973
+            converged = 1;
+            break;
+        }
+    }
+    if (rep) {
+        rep->cycles = cycles;
+        rep->converged = converged;
+        rep->res0 = std::sqrt(res0tol);
+        rep->final_ratio = ratio;
+    }
+    return PMG_OK;
+}
+
+// ---------------------------------------------------------------------------------
+// Device-looped solvers for the lower API (any level size)
+// ---------------------------------------------------------------------------------
+int Ctx::level_scratch(int l, double **bufs, int count)
+{
+    // count full-size arrays of level l, zero-initialised (ghosts stay zero)
+    const size_t need = lv[l].total * (size_t)count;
+    if (scratch_cap < need) {
+        for (auto &v : scratch_levels) cudaFree(v);
+        scratch_levels.clear();
+        double *p = nullptr;
+        PMG_CUDA(cudaMalloc(&p, need * sizeof(double)), "scratch allocation");
+        scratch_levels.push_back(p);
+        scratch_cap = need;
+    }
+    PMG_CUDA(cudaMemsetAsync(scratch_levels[0], 0, need * sizeof(double), stream), "scratch init");
+    for (int q = 0; q < count; ++q) bufs[q] = scratch_levels[0] + (size_t)q * lv[l].total;
+    return PMG_OK;
+}
+
+// rbgs_solver_poisson_matrix (src/rbgs_poisson_matrix.f90:47-179)
+int Ctx::rbgs_solver_dev(int l, double *x, const double *b, int maxit, double tol, double omega, int *iters,
+                         double *ratio_out)
+{
+    double *rs;
+    PMG_TRY(level_scratch(l, &rs, 1));
+    PMG_TRY(residual_norm(l, rs, x, b, 2));
+    double h[4];
+    PMG_TRY(fetch_scalars(h, 3));
+    const double r0 = h[2];
+    double rn = r0;
+    int it = 0;
+    for (it = 0; it < maxit; ++it) {
+        PMG_TRY(f64_rbgs_sweeps(K[l], launch[l], x, b, 1, omega, stream));
+        PMG_TRY(residual_norm(l, rs, x, b, 3));
+        PMG_TRY(fetch_scalars(h, 4));
+        rn = h[3];
+        if (std::sqrt(rn / r0) <= tol) break;
+    }
+    if (iters) *iters = it;
+    if (ratio_out) *ratio_out = std::sqrt(rn / r0);
+    return PMG_OK;
+}
+
+// cg_solver_poisson_matrix / cg_iterator_poisson_matrix (src/cg_poisson_matrix.f90)
+int Ctx::cg_dev(int l, double *x, const double *b, int maxit, double tol, bool check, int *iters,
+                double *ratio_out)
+{
+    double *bufs[3];
+    PMG_TRY(level_scratch(l, bufs, 3));
+    double *p = bufs[0], *ap = bufs[1], *rs = bufs[2];
+    double *s = d_scal;   // 4: rsd0tol, 5: temp1, 6: temp2 (p.Ap), 7: alpha, 8: temp2 (r.r), 9: beta
+    PMG_TRY(f64_residual(K[l], launch[l], rs, x, b, nullptr, nullptr, stream));
+    PMG_TRY(f64_copy_interior(K[l], p, rs, stream));
+    double r0 = 0.0, t2 = 0.0;
+    if (check) {
+        PMG_TRY(dot(l, rs, rs, 4));
+        double h[5];
+        PMG_TRY(fetch_scalars(h, 5));
+        r0 = h[4];
+    }
+    int it = 0;
+    for (it = 0; it < maxit; ++it) {
+        PMG_TRY(dot(l, rs, rs, 5));
+        PMG_TRY(f64_mv_mul(K[l], launch[l], ap, p, stream));
+        PMG_TRY(dot(l, ap, p, 6));
+        PMG_TRY(f64_cg_scalar(s + 5, s + 6, s + 7, stream));
+        PMG_TRY(f64_cg_update_xr(K[l], launch[l], s + 7, x, rs, p, ap, stream));
+        PMG_TRY(dot(l, rs, rs, 8));
+        if (check) {
+            double h[9];
+            PMG_TRY(fetch_scalars(h, 9));
+            t2 = h[8];
+            if (std::sqrt(t2 / r0) < tol) break;
+        }
+        PMG_TRY(f64_cg_scalar(s + 8, s + 5, s + 9, stream));
+        PMG_TRY(f64_cg_update_p(K[l], launch[l], s + 9, p, rs, stream));
+    }
+    if (!check) {
+        double h[9];
+        PMG_TRY(fetch_scalars(h, 9));
+        t2 = h[8];
+    }
+    if (iters) *iters = it;
+    if (ratio_out) *ratio_out = check ? std::sqrt(t2 / r0) : std::sqrt(t2);
+    return PMG_OK;
+}
+
+// Stage host buffers through the device when the caller passes host memory.
+static bool is_device_ptr(const void *p)
+{
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
+}
+
+int Ctx::solve(double *sol, double *rsd, const double *rhs, int maxit, double tol, double omega, pmg_report_t *rep)
+{
+    if (!sol || !rsd || !rhs) {
+        set_error("sol, rsd and rhs are required");
+        return PMG_EINVAL;
+    }
+    if (maxit < 0) {
+        set_error("maxiteration must be non-negative");
+        return PMG_EINVAL;
+    }
+    const bool dev = is_device_ptr(sol);
+    if (dev != is_device_ptr(rhs) || dev != is_device_ptr(rsd)) {
+        set_error("sol, rsd and rhs must all be device memory or all host memory");
+        return PMG_EINVAL;
+    }
+    const size_t bytes = lv[0].total * sizeof(double);
+    PMG_CUDA(cudaEventRecord(ev0, stream), "event");
+    double *s = sol, *r = rsd;
+    const double *b = rhs;
+    if (!dev) {
+        if (!stage_sol) {
+            PMG_CUDA(cudaMalloc(&stage_sol, bytes), "staging allocation");
+            PMG_CUDA(cudaMalloc(&stage_rsd, bytes), "staging allocation");
+            PMG_CUDA(cudaMalloc(&stage_rhs, bytes), "staging allocation");
+        }
+        PMG_CUDA(cudaMemcpyAsync(stage_sol, sol, bytes, cudaMemcpyHostToDevice, stream), "H2D");
+        PMG_CUDA(cudaMemcpyAsync(stage_rhs, rhs, bytes, cudaMemcpyHostToDevice, stream), "H2D");
+        s = stage_sol;
+        r = stage_rsd;
+        b = stage_rhs;
+    }
+    int rc = precision == PMG_MIXED ? solve_mixed(s, r, b, maxit, tol, omega, rep)
+                                    : solve_f64(s, r, b, maxit, tol, omega, rep);
+    if (rc != PMG_OK && rc != PMG_EDIVERGED) return rc;
+    if (!dev) {
+        PMG_CUDA(cudaMemcpyAsync(sol, stage_sol, bytes, cudaMemcpyDeviceToHost, stream), "D2H");
+        PMG_CUDA(cudaMemcpyAsync(rsd, stage_rsd, bytes, cudaMemcpyDeviceToHost, stream), "D2H");
+    }
+    PMG_CUDA(cudaEventRecord(ev1, stream), "event");
+    PMG_CUDA(cudaEventSynchronize(ev1), "event sync");
+    if (rep) {
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, ev0, ev1);
+        rep->elapsed_ms = ms;
+    }
+    return rc;
+}
+
+}  // namespace pmg
+
+// =====================================================================================
+// C-ABI
+// =====================================================================================
+using pmg::Ctx;
+using pmg::cuda_status;
+
+struct pmg_ctx {
+    Ctx impl;
+};
+
+static int check_ctx_level(const pmg_ctx *c, int level)
+{
+    if (!c) {
+        pmg::set_error("null context");
+        return PMG_EINVAL;
+    }
+    if (level < 0 || level > c->impl.nl) {
+        pmg::set_error("level out of range");
+        return PMG_EINVAL;
+    }
+    return PMG_OK;
+}
+
+extern "C" {
+
+int pmg_create(pmg_ctx **ctx, const pmg_config_t *cfg, void *stream)
+{
+    if (!ctx || !cfg) {
+        pmg::set_error("ctx and cfg are required");
+        return PMG_EINVAL;
+    }
+    *ctx = nullptr;
+    pmg_ctx *c = new (std::nothrow) pmg_ctx();
+    if (!c) return PMG_ENOMEM;
+    const int rc = c->impl.build(cfg, (cudaStream_t)stream);
+    if (rc != PMG_OK) {
+        delete c;
+        return rc;
+    }
+    *ctx = c;
+    return PMG_OK;
+}
+
+int pmg_destroy(pmg_ctx *ctx)
+{
+    if (!ctx) return PMG_OK;
+    cudaStreamSynchronize(ctx->impl.stream);
+    delete ctx;
+    return PMG_OK;
+}
+
+int pmg_solve_vcycle(pmg_ctx *ctx, double *sol, double *rsd, const double *rhs, int maxiteration, double tolerance,
+                     double omega_sor, pmg_report_t *report)
+{
+    if (!ctx) {
+        pmg::set_error("null context");
+        return PMG_EINVAL;
+    }
+    return ctx->impl.solve(sol, rsd, rhs, maxiteration, tolerance, omega_sor, report);
+}
+
+int pmg_level_sizes(int nx, int ny, int nz, int n_levels, int aggregation_method, int cga_level, int *sizes,
+                    int lv_coarsest[3])
+{
+    if (!sizes || !lv_coarsest) {
+        pmg::set_error("sizes and lv_coarsest are required");
+        return PMG_EINVAL;
+    }
+    if (nx < 1 || ny < 1 || nz < 1) {
+        pmg::set_error("nx, ny, nz must be positive");
+        return PMG_EINVAL;
+    }
+    const int n0[3] = {nx, ny, nz};
+    std::vector<std::array<int, 3>> sz;
+    PMG_TRY(pmg::level_sizes(n0, n_levels, aggregation_method, cga_level, sz, lv_coarsest));
+    for (size_t l = 0; l < sz.size(); ++l)
+        for (int d = 0; d < 3; ++d) sizes[3 * l + d] = sz[l][d];
+    return PMG_OK;
+}
+
+int pmg_level_dims(const pmg_ctx *ctx, int level, int dims[3])
+{
+    PMG_TRY(check_ctx_level(ctx, level));
+    for (int d = 0; d < 3; ++d) dims[d] = ctx->impl.lv[level].n[d];
+    return PMG_OK;
+}
+
+int pmg_level_mesh(const pmg_ctx *ctx, int level, int axis, double *dm, double *dg, double *xg)
+{
+    PMG_TRY(check_ctx_level(ctx, level));
+    if (axis < 0 || axis > 2) {
+        pmg::set_error("axis out of range");
+        return PMG_EINVAL;
+    }
+    const auto &L = ctx->impl.lv[level];
+    const size_t n = L.dm[axis].size();
+    if (dm) std::memcpy(dm, L.dm[axis].data(), n * sizeof(double));
+    if (dg) std::memcpy(dg, L.dg[axis].data(), n * sizeof(double));
+    if (xg) std::memcpy(xg, L.xg[axis].data(), n * sizeof(double));
+    return PMG_OK;
+}
+
+int pmg_coarsest_levels(const pmg_ctx *ctx, int lv_coarsest[3])
+{
+    PMG_TRY(check_ctx_level(ctx, 0));
+    for (int d = 0; d < 3; ++d) lv_coarsest[d] = ctx->impl.lvc[d];
+    return PMG_OK;
+}
+
+int pmg_mv_mul(pmg_ctx *ctx, int level, double *y, const double *x)
+{
+    PMG_TRY(check_ctx_level(ctx, level));
+    Ctx &c = ctx->impl;
+    const auto &L = c.lv[level];
+    // y = 0 everywhere, then the interior (src/poisson_matrix_operator.f90:136-159)
+    PMG_TRY(pmg::zero_ghosts_f64(y, L.n[0], L.n[1], L.n[2], c.stream));
+    return pmg::f64_mv_mul(c.K[level], c.launch[level], y, x, c.stream);
+}
+
+int pmg_vv_dot(pmg_ctx *ctx, int level, const double *x, const double *y, double *result)
+{
+    PMG_TRY(check_ctx_level(ctx, level));
+    Ctx &c = ctx->impl;
+    PMG_TRY(c.dot(level, x, y, 10));
+    double h[11];
+    PMG_TRY(c.fetch_scalars(h, 11));
+    if (result) *result = h[10];
+    return PMG_OK;
+}
+
+int pmg_residual(pmg_ctx *ctx, int level, double *r, const double *x, const double *b)
+{
+    PMG_TRY(check_ctx_level(ctx, level));
+    Ctx &c = ctx->impl;
+    const auto &L = c.lv[level];
+    PMG_TRY(pmg::zero_ghosts_f64(r, L.n[0], L.n[1], L.n[2], c.stream));
+    return pmg::f64_residual(c.K[level], c.launch[level], r, x, b, nullptr, nullptr, c.stream);
+}
+
+int pmg_rbgs_iterator(pmg_ctx *ctx, int level, double *x, const double *b, int maxiteration, double omega)
+{
+    PMG_TRY(check_ctx_level(ctx, level));
+    Ctx &c = ctx->impl;
+    return pmg::f64_rbgs_sweeps(c.K[level], c.launch[level], x, b, maxiteration, omega, c.stream);
+}
+
+int pmg_rbgs_solver(pmg_ctx *ctx, int level, double *x, const double *b, int maxiteration, double tolerance,
+                    double omega, int *iterations, double *ratio)
+{
+    PMG_TRY(check_ctx_level(ctx, level));
+    return ctx->impl.rbgs_solver_dev(level, x, b, maxiteration, tolerance, omega, iterations, ratio);
+}
+
+int pmg_cg_iterator(pmg_ctx *ctx, int level, double *x, const double *b, int maxiteration)
+{
+    PMG_TRY(check_ctx_level(ctx, level));
+    return ctx->impl.cg_dev(level, x, b, maxiteration, 0.0, false, nullptr, nullptr);
+}
+
+int pmg_cg_solver(pmg_ctx *ctx, int level, double *x, const double *b, int maxiteration, double tolerance,
+                  int *iterations, double *ratio)
+{
+    PMG_TRY(check_ctx_level(ctx, level));
+    return ctx->impl.cg_dev(level, x, b, maxiteration, tolerance, true, iterations, ratio);
+}
+
+int pmg_restriction(pmg_ctx *ctx, int level, double *val_c, const double *val_f)
+{
+    PMG_TRY(check_ctx_level(ctx, level));
+    Ctx &c = ctx->impl;
+    if (level >= c.nl) {
+        pmg::set_error("restriction needs a level below the coarsest");
+        return PMG_EINVAL;
+    }
+    const auto &C = c.lv[level + 1];
+    PMG_CUDA(cudaMemsetAsync(val_c, 0, C.total * sizeof(double), c.stream), "restriction init");
+    return pmg::f64_restrict(c.X[level], c.launch[level + 1], val_f, val_c, c.stream);
+}
+
+int pmg_prolongation(pmg_ctx *ctx, int level, double *val_f, const double *val_c)
+{
+    PMG_TRY(check_ctx_level(ctx, level));
+    Ctx &c = ctx->impl;
+    if (level >= c.nl) {
+        pmg::set_error("prolongation needs a level below the coarsest");
+        return PMG_EINVAL;
+    }
+    return pmg::f64_prolong(c.X[level], c.launch[level + 1], val_c, val_f, false, c.stream);
+}
+
+int pmg_prolong_add(pmg_ctx *ctx, int level, double *x_f, const double *x_c)
+{
+    PMG_TRY(check_ctx_level(ctx, level));
+    Ctx &c = ctx->impl;
+    if (level >= c.nl) {
+        pmg::set_error("prolongation needs a level below the coarsest");
+        return PMG_EINVAL;
+    }
+    return pmg::f64_prolong(c.X[level], c.launch[level + 1], x_c, x_f, true, c.stream);
+}
+
+int pmg_sync(pmg_ctx *ctx)
+{
+    if (!ctx) return PMG_EINVAL;
+    return pmg::cuda_status(cudaStreamSynchronize(ctx->impl.stream), "sync");
+}
+
+const char *pmg_last_error(void) { return pmg::g_last_error.c_str(); }
+
+const char *pmg_status_string(int status)
+{
+    switch (status) {
+    case PMG_OK: return "ok";
+    case PMG_EINVAL: return "invalid argument";
+    case PMG_ENOMEM: return "out of memory";
+    case PMG_EDIVERGED: return "diverged";
+    case PMG_ETIMEOUT: return "timeout";
+    case PMG_ECUDA: return "cuda error";
+    default: return "unknown";
+    }
+}
+
+}  // extern "C"

@@ -1,0 +1,77 @@
+// pmg_ctx.h -- the solver context behind the opaque pmg_ctx handle.
+#pragma once
+
+#include <array>
+#include <vector>
+
+#include "../../include/peps_mg.h"
+#include "pmg_internal.h"
+
+namespace pmg {
+
+// Levels above this many cells (ghosts included) stay on the grid kernels instead of
+// the single-CTA tail.
+constexpr size_t kTailMaxCells = 1u << 18;
+
+struct Level {
+    int n[3] = {0, 0, 0};
+    int sy = 0;
+    long long sz = 0;
+    size_t total = 0;
+    std::vector<double> dm[3], dg[3], xg[3];
+    double *x = nullptr, *b = nullptr, *r = nullptr;   // device, levels >= 1
+};
+
+struct MixedState;   // FP32 V-cycle state (pmg_mixed.cu)
+
+int level_sizes(const int n0[3], int n_levels, int method, int cga_level, std::vector<std::array<int, 3>> &sizes,
+                int lvc[3]);
+
+struct Ctx {
+    cudaStream_t stream = nullptr;
+    int nl = 0, n_vcycles = 0, method = 0, cga_level = 0, cgpsa_level[3] = {0, 0, 0};
+    int coarse_solver = 0, precision = 0;
+    int lvc[3] = {0, 0, 0};
+    std::vector<Level> lv;
+    std::vector<double> tables_host;
+    double *d_tables = nullptr;
+    std::vector<LevelK<double>> K;
+    std::vector<XferK<double>> X;
+    std::vector<Launch> launch;
+    int tail_l0 = 0;
+    TailDesc<double> tail_host;
+    TailDesc<double> *d_tail = nullptr;
+    double *d_partials = nullptr;
+    size_t npart_cap = 0;
+    double *d_scal = nullptr;
+    int *d_iscal = nullptr;
+    double *d_cp = nullptr, *d_cap = nullptr, *d_crr = nullptr;
+    double *stage_sol = nullptr, *stage_rsd = nullptr, *stage_rhs = nullptr;
+    std::vector<double *> scratch_levels;
+    size_t scratch_cap = 0;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    MixedState *mixed = nullptr;
+
+    int build(const pmg_config_t *c, cudaStream_t s);
+    ~Ctx();
+
+    int dot(int l, const double *x, const double *y, int slot);
+    int residual_norm(int l, double *r, const double *x, const double *b, int slot);
+    int fetch_scalars(double *h, int n);
+    int upload_tail(int l0, int maxit, double omega, double tol);
+    int coarse_solve_grid(double tol, double omega, int *iters);
+    int vcycle_f64(double *sol, double *rsd, const double *rhs, int maxit, double omega, double tol,
+                   int *coarse_iters);
+    int solve_f64(double *sol, double *rsd, const double *rhs, int maxit, double tol, double omega,
+                  pmg_report_t *rep);
+    int solve_mixed(double *sol, double *rsd, const double *rhs, int maxit, double tol, double omega,
+                    pmg_report_t *rep);
+    void destroy_mixed();
+    int solve(double *sol, double *rsd, const double *rhs, int maxit, double tol, double omega, pmg_report_t *rep);
+    int level_scratch(int l, double **bufs, int count);
+    int rbgs_solver_dev(int l, double *x, const double *b, int maxit, double tol, double omega, int *iters,
+                        double *ratio_out);
+    int cg_dev(int l, double *x, const double *b, int maxit, double tol, bool check, int *iters, double *ratio_out);
+};
+
+}  // namespace pmg

@@ -1,0 +1,542 @@
+// pmg_f64.cu -- FP64 kernels of the V-cycle that reproduce the reference's arithmetic
+// bit for bit.  Compiled with --fmad=false; every floating-point operation is also
+// spelled out with an explicit round-to-nearest intrinsic in pmg_common.cuh.
+//
+// All grid kernels use grid-stride loops along all three axes, so a level can be run
+// with any grid shape: the full grid (CGS), or with an axis collapsed to one CTA
+// column (the CGPSA per-axis step-down), without changing any cell's arithmetic.
+#include <cuda_runtime.h>
+
+#include "pmg_internal.h"
+
+namespace pmg {
+
+namespace {
+
+constexpr int kBX = 32, kBY = 8;          // 256-thread CTAs for the grid kernels
+constexpr int kTailThreads = 1024;        // single-CTA persistent tail
+constexpr int kMaxGridZ = 65535;
+
+__device__ __forceinline__ int tid_in_block()
+{
+    return threadIdx.x + blockDim.x * threadIdx.y;
+}
+
+__device__ __forceinline__ int block_lin()
+{
+    return blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z);
+}
+
+// One colour of the red-black sweep.  colour 0 is the reference's first half-sweep:
+// ista = 1 + mod(j+k, 2) (src/rbgs_poisson_matrix.f90:242); colour 1 the second
+// (:260).  Thread t of a row updates i = 2t + ista.
+__global__ void __launch_bounds__(kBX *kBY) k_rbgs_f64(LevelK<double> L, double *__restrict__ x,
+                                                       const double *__restrict__ b, double omega, double omw,
+                                                       int colour)
+{
+    for (int k = blockIdx.z + 1; k <= L.nz; k += gridDim.z)
+        for (int j = blockIdx.y * blockDim.y + threadIdx.y + 1; j <= L.ny; j += gridDim.y * blockDim.y) {
+            const int ista = 1 + ((j + k + colour) & 1);
+            for (int i = ista + 2 * (blockIdx.x * blockDim.x + threadIdx.x); i <= L.nx;
+                 i += 2 * gridDim.x * blockDim.x) {
+                const double v = rbgs_cell_f64(L, x, b, i, j, k, omega, omw);
+                x[lin(i, j, k, L.sy, L.sz)] = v;
+            }
+        }
+}
+
+// r = b - A x on the interior (src/multigrid.f90:1795-1805); optional per-block sum of r^2.
+template <bool NORM>
+__global__ void __launch_bounds__(kBX *kBY) k_residual_f64(LevelK<double> L, double *__restrict__ r,
+                                                           const double *__restrict__ x,
+                                                           const double *__restrict__ b, double *partials)
+{
+    double acc = 0.0;
+    for (int k = blockIdx.z + 1; k <= L.nz; k += gridDim.z)
+        for (int j = blockIdx.y * blockDim.y + threadIdx.y + 1; j <= L.ny; j += gridDim.y * blockDim.y)
+            for (int i = blockIdx.x * blockDim.x + threadIdx.x + 1; i <= L.nx; i += gridDim.x * blockDim.x) {
+                const long long p = lin(i, j, k, L.sy, L.sz);
+                const double v = __dsub_rn(b[p], ax_cell_f64(L, x, i, j, k));
+                r[p] = v;
+                if (NORM) acc = __dadd_rn(acc, __dmul_rn(v, v));
+            }
+    if (NORM) {
+        __shared__ double sw[kBX * kBY / 32];
+        const double s = block_sum(acc, sw);
+        if (tid_in_block() == 0) partials[block_lin()] = s;
+    }
+}
+
+__global__ void __launch_bounds__(kBX *kBY) k_mvmul_f64(LevelK<double> L, double *__restrict__ y,
+                                                        const double *__restrict__ x)
+{
+    for (int k = blockIdx.z + 1; k <= L.nz; k += gridDim.z)
+        for (int j = blockIdx.y * blockDim.y + threadIdx.y + 1; j <= L.ny; j += gridDim.y * blockDim.y)
+            for (int i = blockIdx.x * blockDim.x + threadIdx.x + 1; i <= L.nx; i += gridDim.x * blockDim.x)
+                y[lin(i, j, k, L.sy, L.sz)] = ax_cell_f64(L, x, i, j, k);
+}
+
+__global__ void __launch_bounds__(kBX *kBY) k_dot_f64(LevelK<double> L, const double *__restrict__ x,
+                                                      const double *__restrict__ y, double *partials)
+{
+    double acc = 0.0;
+    for (int k = blockIdx.z + 1; k <= L.nz; k += gridDim.z)
+        for (int j = blockIdx.y * blockDim.y + threadIdx.y + 1; j <= L.ny; j += gridDim.y * blockDim.y)
+            for (int i = blockIdx.x * blockDim.x + threadIdx.x + 1; i <= L.nx; i += gridDim.x * blockDim.x) {
+                const long long p = lin(i, j, k, L.sy, L.sz);
+                acc = __dadd_rn(acc, __dmul_rn(x[p], y[p]));
+            }
+    __shared__ double sw[kBX * kBY / 32];
+    const double s = block_sum(acc, sw);
+    if (tid_in_block() == 0) partials[block_lin()] = s;
+}
+
+__global__ void __launch_bounds__(1024) k_reduce_f64(const double *__restrict__ partials, int n, double *out)
+{
+    double acc = 0.0;
+    for (int q = threadIdx.x; q < n; q += blockDim.x) acc = __dadd_rn(acc, partials[q]);
+    __shared__ double sw[32];
+    const double s = block_sum(acc, sw);
+    if (threadIdx.x == 0) *out = s;
+}
+
+__global__ void __launch_bounds__(kBX *kBY) k_restrict_f64(XferK<double> X, const double *__restrict__ vf,
+                                                           double *__restrict__ vc)
+{
+    for (int k = blockIdx.z + 1; k <= X.ncz; k += gridDim.z)
+        for (int j = blockIdx.y * blockDim.y + threadIdx.y + 1; j <= X.ncy; j += gridDim.y * blockDim.y)
+            for (int i = blockIdx.x * blockDim.x + threadIdx.x + 1; i <= X.ncx; i += gridDim.x * blockDim.x)
+                vc[lin(i, j, k, X.csy, X.csz)] = restrict_cell_f64(X, vf, i, j, k);
+}
+
+template <bool ADD>
+__global__ void __launch_bounds__(kBX *kBY) k_prolong_f64(XferK<double> X, const double *__restrict__ vc,
+                                                          double *__restrict__ vf)
+{
+    for (int k = blockIdx.z + 1; k <= X.ncz; k += gridDim.z)
+        for (int j = blockIdx.y * blockDim.y + threadIdx.y + 1; j <= X.ncy; j += gridDim.y * blockDim.y)
+            for (int i = blockIdx.x * blockDim.x + threadIdx.x + 1; i <= X.ncx; i += gridDim.x * blockDim.x)
+                prolong_cell_f64<ADD>(X, vc, vf, i, j, k);
+}
+
+// Zero the six ghost faces of a (nx+2)(ny+2)(nz+2) array.
+__global__ void k_zero_ghosts_f64(double *a, int nx, int ny, int nz)
+{
+    const int sy = nx + 2;
+    const long long sz = (long long)(nx + 2) * (ny + 2);
+    const long long nxy = sz, nxz = (long long)(nx + 2) * (nz + 2), nyz = (long long)(ny + 2) * (nz + 2);
+    const long long total = 2 * (nxy + nxz + nyz);
+    for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < total;
+         q += (long long)gridDim.x * blockDim.x) {
+        long long r = q;
+        int face = 0;
+        if (r < 2 * nxy) {
+            face = (int)(r / nxy);
+            r %= nxy;
+            const int i = (int)(r % sy), j = (int)(r / sy);
+            a[lin(i, j, face ? nz + 1 : 0, sy, sz)] = 0.0;
+            continue;
+        }
+        r -= 2 * nxy;
+        if (r < 2 * nxz) {
+            face = (int)(r / nxz);
+            r %= nxz;
+            const int i = (int)(r % sy), k = (int)(r / sy);
+            a[lin(i, face ? ny + 1 : 0, k, sy, sz)] = 0.0;
+            continue;
+        }
+        r -= 2 * nxz;
+        face = (int)(r / nyz);
+        r %= nyz;
+        const int j = (int)(r % (ny + 2)), k = (int)(r / (ny + 2));
+        a[lin(face ? nx + 1 : 0, j, k, sy, sz)] = 0.0;
+    }
+}
+
+// Interior copy dst = src (src/cg_poisson_matrix.f90:88: p = rsd).
+__global__ void k_copy_interior_f64(LevelK<double> L, double *__restrict__ d, const double *__restrict__ s)
+{
+    for (int k = blockIdx.z + 1; k <= L.nz; k += gridDim.z)
+        for (int j = blockIdx.y * blockDim.y + threadIdx.y + 1; j <= L.ny; j += gridDim.y * blockDim.y)
+            for (int i = blockIdx.x * blockDim.x + threadIdx.x + 1; i <= L.nx; i += gridDim.x * blockDim.x) {
+                const long long p = lin(i, j, k, L.sy, L.sz);
+                d[p] = s[p];
+            }
+}
+
+__global__ void k_cg_scalar_f64(const double *num, const double *den, double *out)
+{
+    *out = __ddiv_rn(*num, *den);
+}
+
+// sol = sol + alpha p ; rsd = rsd - alpha Ap (src/cg_poisson_matrix.f90:117-118)
+__global__ void __launch_bounds__(kBX *kBY) k_cg_xr_f64(LevelK<double> L, const double *alpha_p,
+                                                        double *__restrict__ x, double *__restrict__ r,
+                                                        const double *__restrict__ p,
+                                                        const double *__restrict__ ap)
+{
+    const double alpha = *alpha_p;
+    for (int k = blockIdx.z + 1; k <= L.nz; k += gridDim.z)
+        for (int j = blockIdx.y * blockDim.y + threadIdx.y + 1; j <= L.ny; j += gridDim.y * blockDim.y)
+            for (int i = blockIdx.x * blockDim.x + threadIdx.x + 1; i <= L.nx; i += gridDim.x * blockDim.x) {
+                const long long q = lin(i, j, k, L.sy, L.sz);
+                x[q] = __dadd_rn(x[q], __dmul_rn(alpha, p[q]));
+                r[q] = __dsub_rn(r[q], __dmul_rn(alpha, ap[q]));
+            }
+}
+
+// p = rsd + beta p (src/cg_poisson_matrix.f90:134)
+__global__ void __launch_bounds__(kBX *kBY) k_cg_p_f64(LevelK<double> L, const double *beta_p,
+                                                       double *__restrict__ p, const double *__restrict__ r)
+{
+    const double beta = *beta_p;
+    for (int k = blockIdx.z + 1; k <= L.nz; k += gridDim.z)
+        for (int j = blockIdx.y * blockDim.y + threadIdx.y + 1; j <= L.ny; j += gridDim.y * blockDim.y)
+            for (int i = blockIdx.x * blockDim.x + threadIdx.x + 1; i <= L.nx; i += gridDim.x * blockDim.x) {
+                const long long q = lin(i, j, k, L.sy, L.sz);
+                p[q] = __dadd_rn(r[q], __dmul_rn(beta, p[q]));
+            }
+}
+
+__global__ void k_check_f64(const double *num, const double *den, double tol, int le, int iter, int *flag,
+                            int *iter_out)
+{
+    if (*flag) return;
+    const double ratio = sqrt(__ddiv_rn(*num, *den));
+    const bool done = le ? (ratio <= tol) : (ratio < tol);
+    if (done) {
+        *flag = 1;
+        *iter_out = iter;
+    }
+}
+
+// ------------------------------------------------------------------------------------
+// Single-CTA persistent coarse tail.  Runs, for levels l0..nl of one V-cycle, exactly
+// the operation sequence of src/multigrid.f90:1936-1962 (the part of the CGA cycle that
+// rank 0 executes after the gather, :2108-2135): smoothing, residual and restriction
+// down to the coarsest level, the coarsest-level solve (:1819-1851), then prolongation,
+// correction and smoothing back up to l0.  Phases are separated by __syncthreads();
+// every cell is computed by the same per-cell functions as the grid kernels.
+// ------------------------------------------------------------------------------------
+__device__ void tail_zero(double *a, long long n)
+{
+    for (long long q = threadIdx.x; q < n; q += blockDim.x) a[q] = 0.0;
+}
+
+__device__ void tail_rbgs(const LevelK<double> &L, double *x, const double *b, int iters, double omega, double omw)
+{
+    const int hx = (L.nx + 1) / 2;
+    const long long nq = (long long)hx * L.ny * L.nz;
+    for (int it = 0; it < iters; ++it)
+        for (int colour = 0; colour < 2; ++colour) {
+            for (long long q = threadIdx.x; q < nq; q += blockDim.x) {
+                const int t = (int)(q % hx);
+                const long long rr = q / hx;
+                const int j = (int)(rr % L.ny) + 1, k = (int)(rr / L.ny) + 1;
+                const int i = 2 * t + 1 + ((j + k + colour) & 1);
+                if (i <= L.nx) x[lin(i, j, k, L.sy, L.sz)] = rbgs_cell_f64(L, x, b, i, j, k, omega, omw);
+            }
+            __syncthreads();
+        }
+}
+
+// r = b - A x; returns sum(r^2) over the block (fixed order) when NORM.
+template <bool NORM>
+__device__ double tail_residual(const LevelK<double> &L, double *r, const double *x, const double *b, double *sw)
+{
+    const long long n = (long long)L.nx * L.ny * L.nz;
+    double acc = 0.0;
+    for (long long q = threadIdx.x; q < n; q += blockDim.x) {
+        const int i = (int)(q % L.nx) + 1;
+        const long long rr = q / L.nx;
+        const int j = (int)(rr % L.ny) + 1, k = (int)(rr / L.ny) + 1;
+        const long long p = lin(i, j, k, L.sy, L.sz);
+        const double v = __dsub_rn(b[p], ax_cell_f64(L, x, i, j, k));
+        r[p] = v;
+        if (NORM) acc = __dadd_rn(acc, __dmul_rn(v, v));
+    }
+    __syncthreads();
+    if (NORM) return block_sum(acc, sw);
+    return 0.0;
+}
+
+__device__ double tail_dot(const LevelK<double> &L, const double *x, const double *y, double *sw)
+{
+    const long long n = (long long)L.nx * L.ny * L.nz;
+    double acc = 0.0;
+    for (long long q = threadIdx.x; q < n; q += blockDim.x) {
+        const int i = (int)(q % L.nx) + 1;
+        const long long rr = q / L.nx;
+        const int j = (int)(rr % L.ny) + 1, k = (int)(rr / L.ny) + 1;
+        const long long p = lin(i, j, k, L.sy, L.sz);
+        acc = __dadd_rn(acc, __dmul_rn(x[p], y[p]));
+    }
+    return block_sum(acc, sw);
+}
+
+__device__ void tail_mvmul(const LevelK<double> &L, double *y, const double *x)
+{
+    const long long n = (long long)L.nx * L.ny * L.nz;
+    for (long long q = threadIdx.x; q < n; q += blockDim.x) {
+        const int i = (int)(q % L.nx) + 1;
+        const long long rr = q / L.nx;
+        const int j = (int)(rr % L.ny) + 1, k = (int)(rr / L.ny) + 1;
+        y[lin(i, j, k, L.sy, L.sz)] = ax_cell_f64(L, x, i, j, k);
+    }
+    __syncthreads();
+}
+
+__device__ void tail_restrict(const XferK<double> &X, const double *vf, double *vc)
+{
+    const long long n = (long long)X.ncx * X.ncy * X.ncz;
+    for (long long q = threadIdx.x; q < n; q += blockDim.x) {
+        const int i = (int)(q % X.ncx) + 1;
+        const long long rr = q / X.ncx;
+        const int j = (int)(rr % X.ncy) + 1, k = (int)(rr / X.ncy) + 1;
+        vc[lin(i, j, k, X.csy, X.csz)] = restrict_cell_f64(X, vf, i, j, k);
+    }
+    __syncthreads();
+}
+
+__device__ void tail_prolong_add(const XferK<double> &X, const double *vc, double *vf)
+{
+    const long long n = (long long)X.ncx * X.ncy * X.ncz;
+    for (long long q = threadIdx.x; q < n; q += blockDim.x) {
+        const int i = (int)(q % X.ncx) + 1;
+        const long long rr = q / X.ncx;
+        const int j = (int)(rr % X.ncy) + 1, k = (int)(rr / X.ncy) + 1;
+        prolong_cell_f64<true>(X, vc, vf, i, j, k);
+    }
+    __syncthreads();
+}
+
+__device__ void tail_interior_op(const LevelK<double> &L, int op, double s, double *a, double *bb, const double *c,
+                                 const double *d)
+{
+    // op 0: a = c (copy); op 1: a += s c, bb -= s d; op 2: a = c + s a
+    const long long n = (long long)L.nx * L.ny * L.nz;
+    for (long long q = threadIdx.x; q < n; q += blockDim.x) {
+        const int i = (int)(q % L.nx) + 1;
+        const long long rr = q / L.nx;
+        const int j = (int)(rr % L.ny) + 1, k = (int)(rr / L.ny) + 1;
+        const long long p = lin(i, j, k, L.sy, L.sz);
+        if (op == 0) {
+            a[p] = c[p];
+        } else if (op == 1) {
+            a[p] = __dadd_rn(a[p], __dmul_rn(s, c[p]));
+            bb[p] = __dsub_rn(bb[p], __dmul_rn(s, d[p]));
+        } else {
+            a[p] = __dadd_rn(c[p], __dmul_rn(s, a[p]));
+        }
+    }
+    __syncthreads();
+}
+
+__global__ void __launch_bounds__(kTailThreads) k_tail_f64(const TailDesc<double> *__restrict__ Dp)
+{
+    __shared__ double sw[kTailThreads / 32];
+    const TailDesc<double> &D = *Dp;
+    const double omega = D.omega, omw = D.omw;
+    for (int l = D.l0; l < D.nl; ++l) {
+        const LevelK<double> L = D.L[l];
+        const XferK<double> X = D.X[l];
+        double *x = D.x[l], *b = D.b[l], *r = D.r[l], *bc = D.b[l + 1];
+        tail_zero(x, (long long)L.sz * (L.nz + 2));
+        __syncthreads();
+        tail_rbgs(L, x, b, D.maxit, omega, omw);
+        tail_residual<false>(L, r, x, b, sw);
+        tail_restrict(X, r, bc);
+    }
+    // coarsest level, src/multigrid.f90:1819-1851
+    {
+        const LevelK<double> L = D.L[D.nl];
+        double *x = D.x[D.nl];
+        const double *b = D.b[D.nl];
+        tail_zero(x, (long long)L.sz * (L.nz + 2));
+        __syncthreads();
+        int iters = 0;
+        if ((long long)L.nx * L.ny * L.nz == 1) {
+            if (threadIdx.x == 0) {
+                const long long p = lin(1, 1, 1, L.sy, L.sz);
+                x[p] = __ddiv_rn(b[p], diag_f64(L, 1, 1, 1));
+            }
+            __syncthreads();
+        } else if (D.coarse_solver == 0) {
+            // rbgs_solver_poisson_matrix (src/rbgs_poisson_matrix.f90:69-171)
+            const double r0 = tail_residual<true>(L, D.rr, x, b, sw);
+            int it = 0;
+            for (it = 0; it < D.coarse_maxit; ++it) {
+                tail_rbgs(L, x, b, 1, omega, omw);
+                const double rn = tail_residual<true>(L, D.rr, x, b, sw);
+                if (sqrt(__ddiv_rn(rn, r0)) <= D.tol) break;
+            }
+            iters = it;
+        } else {
+            // cg_solver_poisson_matrix (src/cg_poisson_matrix.f90:80-138)
+            double *p = D.p, *ap = D.ap, *rsd = D.rr;
+            tail_residual<false>(L, rsd, x, b, sw);
+            tail_interior_op(L, 0, 0.0, p, nullptr, rsd, nullptr);
+            const double r0 = tail_dot(L, rsd, rsd, sw);
+            int it = 0;
+            for (it = 0; it < D.coarse_maxit; ++it) {
+                const double t1 = tail_dot(L, rsd, rsd, sw);
+                tail_mvmul(L, ap, p);
+                const double t2a = tail_dot(L, ap, p, sw);
+                const double alpha = __ddiv_rn(t1, t2a);
+                tail_interior_op(L, 1, alpha, x, rsd, p, ap);
+                const double t2 = tail_dot(L, rsd, rsd, sw);
+                if (sqrt(__ddiv_rn(t2, r0)) < D.tol) break;
+                const double beta = __ddiv_rn(t2, t1);
+                tail_interior_op(L, 2, beta, p, nullptr, rsd, nullptr);
+            }
+            iters = it;
+        }
+        if (threadIdx.x == 0 && D.iters_out) *D.iters_out = iters;
+        __syncthreads();
+    }
+    for (int l = D.nl - 1; l >= D.l0; --l) {
+        const LevelK<double> L = D.L[l];
+        const XferK<double> X = D.X[l];
+        double *x = D.x[l], *b = D.b[l], *xc = D.x[l + 1];
+        tail_prolong_add(X, xc, x);
+        tail_rbgs(L, x, b, D.maxit, omega, omw);
+    }
+}
+
+dim3 grid3(int nx_threads, int ny, int nz, const Launch &ln)
+{
+    dim3 g;
+    g.x = ln.collapse[0] ? 1u : (unsigned)((nx_threads + kBX - 1) / kBX);
+    g.y = ln.collapse[1] ? 1u : (unsigned)((ny + kBY - 1) / kBY);
+    g.z = ln.collapse[2] ? 1u : (unsigned)(nz < kMaxGridZ ? nz : kMaxGridZ);
+    if (g.x == 0) g.x = 1;
+    if (g.y == 0) g.y = 1;
+    if (g.z == 0) g.z = 1;
+    return g;
+}
+
+}  // namespace
+
+void grid_for_cells(const LevelK<double> &L, const Launch &ln, dim3 *grid, dim3 *block)
+{
+    *grid = grid3(L.nx, L.ny, L.nz, ln);
+    *block = dim3(kBX, kBY, 1);
+}
+
+int f64_rbgs_sweeps(const LevelK<double> &L, const Launch &ln, double *x, const double *b, int iters,
+                    double omega, cudaStream_t s)
+{
+    const double omw = 1.0 - omega;   // (1.0d0-omega), src/rbgs_poisson_matrix.f90:250
+    const dim3 g = grid3((L.nx + 1) / 2, L.ny, L.nz, ln), bl(kBX, kBY, 1);
+    for (int it = 0; it < iters; ++it)
+        for (int c = 0; c < 2; ++c) k_rbgs_f64<<<g, bl, 0, s>>>(L, x, b, omega, omw, c);
+    return cuda_status(cudaGetLastError(), "rbgs sweep");
+}
+
+int f64_residual(const LevelK<double> &L, const Launch &ln, double *r, const double *x, const double *b,
+                 double *partials, int *npart, cudaStream_t s)
+{
+    const dim3 g = grid3(L.nx, L.ny, L.nz, ln), bl(kBX, kBY, 1);
+    if (partials) {
+        k_residual_f64<true><<<g, bl, 0, s>>>(L, r, x, b, partials);
+        *npart = (int)(g.x * g.y * g.z);
+    } else {
+        k_residual_f64<false><<<g, bl, 0, s>>>(L, r, x, b, nullptr);
+    }
+    return cuda_status(cudaGetLastError(), "residual");
+}
+
+int f64_mv_mul(const LevelK<double> &L, const Launch &ln, double *y, const double *x, cudaStream_t s)
+{
+    const dim3 g = grid3(L.nx, L.ny, L.nz, ln), bl(kBX, kBY, 1);
+    k_mvmul_f64<<<g, bl, 0, s>>>(L, y, x);
+    return cuda_status(cudaGetLastError(), "mv_mul");
+}
+
+int f64_dot_partials(const LevelK<double> &L, const Launch &ln, const double *x, const double *y,
+                     double *partials, int *npart, cudaStream_t s)
+{
+    const dim3 g = grid3(L.nx, L.ny, L.nz, ln), bl(kBX, kBY, 1);
+    k_dot_f64<<<g, bl, 0, s>>>(L, x, y, partials);
+    *npart = (int)(g.x * g.y * g.z);
+    return cuda_status(cudaGetLastError(), "dot");
+}
+
+int f64_reduce(const double *partials, int n, double *out, cudaStream_t s)
+{
+    k_reduce_f64<<<1, 1024, 0, s>>>(partials, n, out);
+    return cuda_status(cudaGetLastError(), "reduce");
+}
+
+int f64_restrict(const XferK<double> &X, const Launch &ln, const double *vf, double *vc, cudaStream_t s)
+{
+    const dim3 g = grid3(X.ncx, X.ncy, X.ncz, ln), bl(kBX, kBY, 1);
+    k_restrict_f64<<<g, bl, 0, s>>>(X, vf, vc);
+    return cuda_status(cudaGetLastError(), "restriction");
+}
+
+int f64_prolong(const XferK<double> &X, const Launch &ln, const double *vc, double *vf, bool add,
+                cudaStream_t s)
+{
+    const dim3 g = grid3(X.ncx, X.ncy, X.ncz, ln), bl(kBX, kBY, 1);
+    if (add)
+        k_prolong_f64<true><<<g, bl, 0, s>>>(X, vc, vf);
+    else
+        k_prolong_f64<false><<<g, bl, 0, s>>>(X, vc, vf);
+    return cuda_status(cudaGetLastError(), "prolongation");
+}
+
+int zero_ghosts_f64(double *a, int nx, int ny, int nz, cudaStream_t s)
+{
+    const long long total = 2LL * ((long long)(nx + 2) * (ny + 2) + (long long)(nx + 2) * (nz + 2) +
+                                   (long long)(ny + 2) * (nz + 2));
+    long long blocks = (total + 255) / 256;
+    if (blocks > 4096) blocks = 4096;
+    k_zero_ghosts_f64<<<(unsigned)blocks, 256, 0, s>>>(a, nx, ny, nz);
+    return cuda_status(cudaGetLastError(), "zero ghosts");
+}
+
+int f64_tail(const TailDesc<double> *dev_desc, cudaStream_t s)
+{
+    k_tail_f64<<<1, kTailThreads, 0, s>>>(dev_desc);
+    return cuda_status(cudaGetLastError(), "coarse tail");
+}
+
+int f64_copy_interior(const LevelK<double> &L, double *dst, const double *src, cudaStream_t s)
+{
+    const Launch ln{{false, false, false}};
+    const dim3 g = grid3(L.nx, L.ny, L.nz, ln), bl(kBX, kBY, 1);
+    k_copy_interior_f64<<<g, bl, 0, s>>>(L, dst, src);
+    return cuda_status(cudaGetLastError(), "copy");
+}
+
+int f64_cg_scalar(const double *num, const double *den, double *out, cudaStream_t s)
+{
+    k_cg_scalar_f64<<<1, 1, 0, s>>>(num, den, out);
+    return cuda_status(cudaGetLastError(), "cg scalar");
+}
+
+int f64_cg_update_xr(const LevelK<double> &L, const Launch &ln, const double *alpha, double *x, double *r,
+                     const double *p, const double *ap, cudaStream_t s)
+{
+    const dim3 g = grid3(L.nx, L.ny, L.nz, ln), bl(kBX, kBY, 1);
+    k_cg_xr_f64<<<g, bl, 0, s>>>(L, alpha, x, r, p, ap);
+    return cuda_status(cudaGetLastError(), "cg update");
+}
+
+int f64_cg_update_p(const LevelK<double> &L, const Launch &ln, const double *beta, double *p, const double *r,
+                    cudaStream_t s)
+{
+    const dim3 g = grid3(L.nx, L.ny, L.nz, ln), bl(kBX, kBY, 1);
+    k_cg_p_f64<<<g, bl, 0, s>>>(L, beta, p, r);
+    return cuda_status(cudaGetLastError(), "cg update p");
+}
+
+int f64_check(const double *num, const double *den, double tol, int le, int iter, int *flag, int *iter_out,
+              cudaStream_t s)
+{
+    k_check_f64<<<1, 1, 0, s>>>(num, den, tol, le, iter, flag, iter_out);
+    return cuda_status(cudaGetLastError(), "check");
+}
+
+}  // namespace pmg

@@ -1,0 +1,220 @@
+"""FP64 parity of the sm_103a kernels against the oracle (through the C-ABI).
+
+Iterates (RBGS, restriction, prolongation, residual, the V-cycle solution) must be
+bit-identical to the oracle.  Reductions (dot, norms, CG scalars) use a different
+summation order, so norms, residual histories and CG iterates are compared with a
+relative tolerance of 1e-12.
+"""
+import numpy as np
+import pytest
+
+torch = pytest.importorskip("torch")
+pytestmark = pytest.mark.gpu
+
+import peps_mg_gb300 as pmg  # noqa: E402
+from oracle import oracle as O  # noqa: E402
+from tests.helpers import from_dev, mesh_of, rel, sine_problem, tanh_z_problem, to_dev  # noqa: E402
+
+TOL = 1e-12
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _need_gpu():
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    torch.cuda.init()
+
+
+def F(a):
+    return np.asfortranarray(np.array(a, dtype=np.float64))
+
+
+def test_operator_kernels_bitwise(golden):
+    g = golden
+    with pmg.Multigrid(mesh_of(g, "A_"), 2, 1) as mg:
+        x, b, y = to_dev(g["A_x"]), to_dev(g["A_b"]), to_dev(g["A_y"])
+        out = torch.full_like(x, 7.0)
+        mg.mv_mul(0, out, x)
+        assert np.array_equal(from_dev(out), g["A_mv"])
+        out.fill_(5.0)
+        mg.residual(0, out, x, b)
+        assert np.array_equal(from_dev(out), g["A_res"])
+        d = mg.vv_dot(0, x, y)
+        assert abs(d - g["A_dot"][0]) <= TOL * abs(g["A_dot"][0])
+
+
+@pytest.mark.parametrize("tag,omega,it", [("w16", 1.6, 2), ("w10", 1.0, 3)])
+def test_rbgs_iterator_bitwise(golden, tag, omega, it):
+    g = golden
+    with pmg.Multigrid(mesh_of(g, "A_"), 2, 1) as mg:
+        x = to_dev(g["A_x"])
+        mg.rbgs_iterator(0, x, to_dev(g["A_b"]), it, omega)
+        assert np.array_equal(from_dev(x), g["A_rbgs_" + tag])
+
+
+def test_rbgs_and_cg_solvers(golden):
+    g = golden
+    with pmg.Multigrid(mesh_of(g, "A_"), 2, 1) as mg:
+        x = to_dev(g["A_x"])
+        it, ratio = mg.rbgs_solver(0, x, to_dev(g["A_b"]), 50, 1e-6, 1.3)
+        assert it == g["A_rbgs_solver_iters"][0]
+        assert np.array_equal(from_dev(x), g["A_rbgs_solver_x"])
+        x = to_dev(g["A_x"])
+        it, ratio = mg.cg_solver(0, x, to_dev(g["A_b"]), 200, 1e-9)
+        assert it == g["A_cg_solver_iters"][0]
+        assert rel(from_dev(x), g["A_cg_solver_x"]) < TOL * 100
+        x = to_dev(g["A_x"])
+        mg.cg_iterator(0, x, to_dev(g["A_b"]), 5)
+        assert rel(from_dev(x), g["A_cg_iter5_x"]) < TOL
+
+
+def test_hierarchy_and_transfers_bitwise(golden):
+    g = golden
+    with pmg.Multigrid(mesh_of(g, "B_"), 3, 1) as mg:
+        for l in range(4):
+            assert mg.level_dims(l) == tuple(g["B_sizes"][l])
+        assert mg.coarsest_levels() == tuple(g["B_lvc"])
+        for l in range(1, 4):
+            for d, a in enumerate("xyz"):
+                dm, dg, _ = mg.level_mesh(l, d)
+                assert np.array_equal(dm, g["B_L%d_d%sm" % (l, a)])
+                assert np.array_equal(dg, g["B_L%d_d%sg" % (l, a)])
+        for l in range(3):
+            vc = to_dev(np.full(np.array(g["B_P%d_in" % l]).shape, 3.0))
+            mg.restriction(l, vc, to_dev(g["B_R%d_in" % l]))
+            assert np.array_equal(from_dev(vc), g["B_R%d_out" % l]), l
+            base = to_dev(g["B_P%d_base" % l])
+            mg.prolongation(l, base, to_dev(g["B_P%d_in" % l]))
+            assert np.array_equal(from_dev(base), g["B_P%d_out" % l]), l
+            # fused x += P e equals the reference's write-then-add on the interior
+            xf = to_dev(g["B_P%d_base" % l])
+            mg.prolong_add(l, xf, to_dev(g["B_P%d_in" % l]))
+            expect = np.array(g["B_P%d_base" % l])
+            written = np.array(g["B_P%d_out" % l])
+            expect[1:-1, 1:-1, 1:-1] = expect[1:-1, 1:-1, 1:-1] + written[1:-1, 1:-1, 1:-1]
+            assert np.array_equal(from_dev(xf), expect), l
+
+
+@pytest.mark.parametrize("tag,method,cga,cs", [("cgs_rbgs", "cgs", 0, "rbgs"), ("cgs_cg", "cgs", 0, "cg"),
+                                               ("cga_rbgs", "cga", 2, "rbgs"), ("cgpsa_rbgs", "cgpsa", 0, "rbgs")])
+def test_vcycle_golden(golden, tag, method, cga, cs):
+    g = golden
+    with pmg.Multigrid(mesh_of(g, "B_"), 3, 40, method, cga, (1, 2, 1), coarse_solver=cs) as mg:
+        sol = to_dev(g["C_sol0"])
+        rsd = torch.full_like(sol, 9.0)
+        rep = mg.solve_vcycle(sol, rsd, to_dev(g["C_rhs"]), 2, 1e-9, 1.2)
+    hist = g["C_%s_hist" % tag]
+    assert rep.cycles == len(hist)
+    assert rel(rep.history, hist) < TOL
+    if cs == "rbgs":
+        assert np.array_equal(rep.coarse_iterations, g["C_%s_citers" % tag])
+        assert np.array_equal(from_dev(sol), g["C_%s_sol" % tag])
+        assert np.array_equal(from_dev(rsd), g["C_%s_rsd" % tag])
+    else:
+        assert rel(from_dev(sol), g["C_%s_sol" % tag]) < TOL
+        assert rel(from_dev(rsd), g["C_%s_rsd" % tag]) < 1e-6
+
+
+@pytest.mark.parametrize("coarse", ["rbgs", "cg"])
+def test_unit_cube_64(coarse):
+    """The 64^3 benchmark problem (4 levels down to 4^3), against the oracle."""
+    mesh, rhs, u = sine_problem(64)
+    cs = 0 if coarse == "rbgs" else 1
+    omg = O.OracleMG(mesh, 4, 100, 0, 0, cs)
+    osol, orsd = O.field(64, 64, 64), O.field(64, 64, 64)
+    ncyc, hist, ci = omg.solve(osol, orsd, F(rhs), 2, 1e-10, 1.0)
+    with pmg.Multigrid(mesh, 4, 100, "cgs", coarse_solver=coarse) as mg:
+        sol = torch.zeros(66 ** 3, dtype=torch.float64, device="cuda")
+        rsd = torch.zeros_like(sol)
+        rep = mg.solve_vcycle(sol, rsd, to_dev(rhs).reshape(-1), 2, 1e-10, 1.0)
+    s = from_dev(sol.reshape(66, 66, 66))
+    assert rep.converged and rep.cycles == ncyc
+    assert rel(rep.history, hist) < TOL
+    if coarse == "rbgs":
+        assert np.array_equal(rep.coarse_iterations, ci)
+        assert np.array_equal(s, osol)
+    else:
+        assert rel(s, osol) < TOL
+    mse = np.mean((s[1:-1, 1:-1, 1:-1] - u) ** 2)
+    assert mse < 1e-6
+
+
+def test_aggregation_methods_identical():
+    """CGS, CGA (single-CTA coarse tail from the aggregation level) and CGPSA (per-axis
+    CTA step-down) run the same arithmetic and give identical bits (tanh-z grid)."""
+    n = 64
+    mesh, rhs = tanh_z_problem(n)
+    omg = O.OracleMG(mesh, 5, 60, 0)
+    osol, orsd = O.field(n, n, n), O.field(n, n, n)
+    ncyc, hist, ci = omg.solve(osol, orsd, F(rhs), 2, 1e-10, 1.0)
+    sols = []
+    for method, cga, cg3 in (("cgs", 0, (0, 0, 0)), ("cga", 3, (0, 0, 0)), ("cgpsa", 0, (2, 3, 4)),
+                             ("cgpsa", 0, (1, 1, 1))):
+        with pmg.Multigrid(mesh, 5, 60, method, cga, cg3) as mg:
+            sol = torch.zeros((n + 2,) * 3, dtype=torch.float64, device="cuda")
+            rsd = torch.zeros_like(sol)
+            rep = mg.solve_vcycle(sol, rsd, to_dev(rhs), 2, 1e-10, 1.0)
+        assert rep.cycles == ncyc, method
+        assert rel(rep.history, hist) < TOL
+        assert np.array_equal(rep.coarse_iterations, ci)
+        sols.append(from_dev(sol))
+        assert np.array_equal(sols[-1], osol), method
+
+
+def test_host_buffers_match_device():
+    mesh, rhs, _ = sine_problem(32)
+    with pmg.Multigrid(mesh, 3, 30, "cgs") as mg:
+        hs, hr = pmg.geometry.field(32, 32, 32), pmg.geometry.field(32, 32, 32)
+        rep_h = mg.solve_vcycle(hs, hr, F(rhs), 2, 1e-10, 1.0)
+        ds = torch.zeros((34,) * 3, dtype=torch.float64, device="cuda")
+        dr = torch.zeros_like(ds)
+        rep_d = mg.solve_vcycle(ds, dr, to_dev(rhs), 2, 1e-10, 1.0)
+    assert np.array_equal(hs, from_dev(ds))
+    assert np.array_equal(hr, from_dev(dr))
+    assert np.array_equal(rep_h.history, rep_d.history)
+
+
+def test_dirichlet_ghosts_and_odd_sizes():
+    """Non-zero Dirichlet values in the ghost layer and odd sizes that stop coarsening
+    in one axis (stride-1 transfers), CG coarse solver on a multi-cell coarsest level."""
+    rng = np.random.default_rng(11)
+    nx, ny, nz = 24, 20, 7
+    mesh = [pmg.geometry.mesh_from_widths(rng.uniform(0.5, 1.5, n) / n) for n in (nx, ny, nz)]
+    rhs = pmg.geometry.field(nx, ny, nz)
+    rhs[1:-1, 1:-1, 1:-1] = rng.uniform(-1, 1, (nx, ny, nz))
+    sol0 = pmg.geometry.field(nx, ny, nz)
+    sol0[0, :, :] = 1.0
+    sol0[:, :, -1] = -0.5
+    for cs in (0, 1):
+        omg = O.OracleMG(mesh, 2, 50, 0, 0, cs)
+        osol, orsd = F(sol0), O.field(nx, ny, nz)
+        ncyc, hist, ci = omg.solve(osol, orsd, F(rhs), 2, 1e-11, 1.3)
+        with pmg.Multigrid(mesh, 2, 50, "cgs", coarse_solver=cs) as mg:
+            sol, rsd = to_dev(sol0), torch.zeros((nz + 2, ny + 2, nx + 2), dtype=torch.float64, device="cuda")
+            rep = mg.solve_vcycle(sol, rsd, to_dev(rhs), 2, 1e-11, 1.3)
+        assert rep.cycles == ncyc
+        assert rel(rep.history, hist) < TOL
+        s = from_dev(sol)
+        if cs == 0:
+            assert np.array_equal(s, osol)
+        else:
+            assert rel(s, osol) < TOL
+        assert np.array_equal(s[0], sol0[0]) and np.array_equal(s[:, :, -1], sol0[:, :, -1])
+
+
+def test_invalid_configuration_raises():
+    mesh, _, _ = sine_problem(16)
+    with pytest.raises(pmg.PmgError):
+        pmg.Multigrid(mesh, 7, 10, "cgs")
+    with pytest.raises(pmg.PmgError):
+        pmg.Multigrid(mesh, 2, 10, "cga", 0)
+
+
+def test_nan_rhs_reports_divergence():
+    mesh, rhs, _ = sine_problem(16)
+    rhs[5, 5, 5] = np.nan
+    with pmg.Multigrid(mesh, 2, 5, "cgs") as mg:
+        sol = torch.zeros((18,) * 3, dtype=torch.float64, device="cuda")
+        with pytest.raises(pmg.PmgError) as e:
+            mg.solve_vcycle(sol, torch.zeros_like(sol), to_dev(rhs), 1, 1e-10, 1.0)
+        assert e.value.status == 3
