@@ -58,6 +58,7 @@ typedef struct {
     int cgpsa_level[3];        /* CGPSA_level(3)                                         */
     int coarse_solver;         /* PMG_COARSE_RBGS or PMG_COARSE_CG                       */
     int precision;             /* PMG_FP64 or PMG_MIXED                                  */
+    int mixed_inner_cycles;    /* PMG_MIXED: FP32 V-cycles per FP64 correction (0 = 2)   */
 } pmg_config_t;
 
 /* Per-solve report (replaces the reference's rank-0 prints, src/multigrid.f90:1972). */
@@ -70,6 +71,7 @@ typedef struct {
                                /*   sqrt(rsd_val), sqrt(res0tol), sqrt(rsd_val/res0tol)  */
     int *coarse_iterations;    /* optional, number_of_vcycles ints                       */
     float elapsed_ms;          /* device time of the whole call (CUDA events)            */
+    int inner_cycles;          /* PMG_MIXED: FP32 V-cycles run in total (else = cycles)  */
 } pmg_report_t;
 
 /* multigrid_create(sdm, nlevel, ncycle, aggr_method, single_aggr_level,

@@ -24,13 +24,13 @@ class PmgConfig(ctypes.Structure):
                 ("dzm", c_void_p), ("dzg", c_void_p), ("zg", c_void_p),
                 ("number_of_levels", c_int), ("number_of_vcycles", c_int),
                 ("aggregation_method", c_int), ("cga_level", c_int), ("cgpsa_level", c_int * 3),
-                ("coarse_solver", c_int), ("precision", c_int)]
+                ("coarse_solver", c_int), ("precision", c_int), ("mixed_inner_cycles", c_int)]
 
 
 class PmgReport(ctypes.Structure):
     _fields_ = [("cycles", c_int), ("converged", c_int), ("res0", c_double), ("final_ratio", c_double),
                 ("history", ctypes.POINTER(c_double)), ("coarse_iterations", ctypes.POINTER(c_int)),
-                ("elapsed_ms", c_float)]
+                ("elapsed_ms", c_float), ("inner_cycles", c_int)]
 
 
 # symbol -> argtypes (restype int unless noted)
