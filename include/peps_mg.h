@@ -138,6 +138,27 @@ int pmg_prolongation(pmg_ctx *ctx, int level, double *val_f, const double *val_c
  * src/multigrid.f90:1957-1958 (interior; the reference's ghost add is of zeros). */
 int pmg_prolong_add(pmg_ctx *ctx, int level, double *x_f, const double *x_c);
 
+/* ---- Telemetry (no counterpart in the reference; it only prints MPI_Wtime) ------ */
+/* Kernel classes of pmg_profile_read (finest-level launches only). */
+#define PMG_PROF_SMOOTH32 0       /* FP32 RBGS half-sweep                    */
+#define PMG_PROF_OUTER_RESIDUAL 1 /* FP64 outer residual of PMG_MIXED        */
+#define PMG_PROF_RESRESTRICT32 2  /* FP32 residual fused with restriction    */
+#define PMG_PROF_PROLONG32 3      /* FP32 prolongation + correction          */
+#define PMG_PROF_ADD_CORRECTION 4 /* FP64 x += e                             */
+#define PMG_PROF_TAIL32 5         /* FP32 single-CTA coarse tail             */
+#define PMG_PROF_SMOOTH64 6       /* FP64 RBGS half-sweep                    */
+#define PMG_PROF_RESIDUAL64 7     /* FP64 residual                           */
+#define PMG_PROF_RESTRICT64 8     /* FP64 restriction                        */
+#define PMG_PROF_PROLONG64 9      /* FP64 prolongation + correction          */
+#define PMG_PROF_TAIL64 10        /* FP64 single-CTA coarse tail             */
+/* Enable (1) or disable (0) CUDA-event timing of the finest-level launches; resets
+ * the accumulated figures. */
+int pmg_profile(pmg_ctx *ctx, int enable);
+/* Accumulated device time, launch count and algorithmic bytes per launch of a class. */
+int pmg_profile_read(pmg_ctx *ctx, int kernel_class, double *total_ms, long long *launches, double *bytes);
+/* Kernels launched by this library so far (all contexts of the process). */
+int pmg_launch_count(long long *count);
+
 /* Wait for all work issued on the context stream. */
 int pmg_sync(pmg_ctx *ctx);
 /* Text of the last CUDA error seen by this thread ("" if none). */

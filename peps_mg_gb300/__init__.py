@@ -5,7 +5,7 @@ PEPS_MG (multigrid_create / multigrid_solve_vcycle / multigrid_destroy).
 from . import geometry  # noqa: F401
 from ._lib import (PMG_CGA, PMG_CGPSA, PMG_CGS, PMG_COARSE_CG, PMG_COARSE_RBGS, PMG_FP64,  # noqa: F401
                    PMG_MIXED, PmgError, load)
-from .multigrid import (Multigrid, SolveReport, level_sizes, multigrid_create, multigrid_destroy,  # noqa: F401
+from .multigrid import (PROF_CLASSES, Multigrid, SolveReport, launch_count, level_sizes, multigrid_create, multigrid_destroy,  # noqa: F401
                         multigrid_solve_vcycle)
 
 __all__ = ["Multigrid", "SolveReport", "PmgError", "multigrid_create", "multigrid_solve_vcycle",

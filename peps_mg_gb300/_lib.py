@@ -55,6 +55,10 @@ _SIGS = {
     "pmg_restriction": [c_void_p, c_int, c_void_p, c_void_p],
     "pmg_prolongation": [c_void_p, c_int, c_void_p, c_void_p],
     "pmg_prolong_add": [c_void_p, c_int, c_void_p, c_void_p],
+    "pmg_profile": [c_void_p, c_int],
+    "pmg_profile_read": [c_void_p, c_int, ctypes.POINTER(c_double), ctypes.POINTER(ctypes.c_longlong),
+                         ctypes.POINTER(c_double)],
+    "pmg_launch_count": [ctypes.POINTER(ctypes.c_longlong)],
     "pmg_sync": [c_void_p],
     "pmg_last_error": [],
     "pmg_status_string": [c_int],

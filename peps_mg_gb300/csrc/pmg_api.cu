@@ -9,6 +9,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -30,6 +31,76 @@ int cuda_status(cudaError_t e, const char *what)
     if (e == cudaSuccess) return PMG_OK;
     set_error(std::string(what) + ": " + cudaGetErrorString(e));
     return e == cudaErrorMemoryAllocation ? PMG_ENOMEM : PMG_ECUDA;
+}
+
+static std::atomic<long long> g_launches{0};
+void count_launches(long long n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
+long long launches_total() { return g_launches.load(); }
+
+Profiler::~Profiler()
+{
+    for (auto e : pool) cudaEventDestroy(e);
+    for (auto &r : pending) {
+        cudaEventDestroy(r.a);
+        cudaEventDestroy(r.b);
+    }
+}
+
+void Profiler::reset()
+{
+    for (int c = 0; c < PC_COUNT; ++c) {
+        total_ms[c] = 0.0;
+        count[c] = 0;
+        bytes[c] = 0.0;
+    }
+}
+
+cudaEvent_t Profiler::get()
+{
+    if (!pool.empty()) {
+        cudaEvent_t e = pool.back();
+        pool.pop_back();
+        return e;
+    }
+    cudaEvent_t e = nullptr;
+    cudaEventCreate(&e);
+    return e;
+}
+
+int Profiler::begin(cudaStream_t s)
+{
+    if (!on) return -1;
+    Rec r{0, 0, 0.0, get(), get()};
+    cudaEventRecord(r.a, s);
+    pending.push_back(r);
+    return (int)pending.size() - 1;
+}
+
+void Profiler::end(int idx, int cls, int launches, double bytes_per_launch, cudaStream_t s)
+{
+    if (idx < 0 || !on) return;
+    Rec &r = pending[idx];
+    r.cls = cls;
+    r.launches = launches;
+    r.bytes = bytes_per_launch;
+    cudaEventRecord(r.b, s);
+}
+
+void Profiler::flush()
+{
+    for (auto &r : pending) {
+        float ms = 0.f;
+        if (cudaEventElapsedTime(&ms, r.a, r.b) == cudaSuccess) {
+            total_ms[r.cls] += ms;
+            count[r.cls] += r.launches;
+            bytes[r.cls] = r.bytes;
+        } else {
+            cudaGetLastError();
+        }
+        pool.push_back(r.a);
+        pool.push_back(r.b);
+    }
+    pending.clear();
 }
 
 #define PMG_TRY(expr)                      \
@@ -248,6 +319,11 @@ int Ctx::build(const pmg_config_t *c, cudaStream_t s)
     for (int d = 0; d < 3; ++d) cgpsa_level[d] = c->cgpsa_level[d];
     coarse_solver = c->coarse_solver;
     precision = c->precision;
+    mixed_inner = c->mixed_inner_cycles;
+    if (mixed_inner < 0) {
+        set_error("mixed_inner_cycles must be non-negative");
+        return PMG_EINVAL;
+    }
     const int n0[3] = {c->nx, c->ny, c->nz};
     std::vector<std::array<int, 3>> sizes;
     PMG_TRY(level_sizes(n0, nl, method, cga_level, sizes, lvc));
@@ -501,11 +577,16 @@ int Ctx::coarse_solve_grid(double tol, double omega, int *iters)
 int Ctx::vcycle_f64(double *sol, double *rsd, const double *rhs, int maxit, double omega, double tol,
                     int *coarse_iters)
 {
-    const Level &S = lv[0];
-    (void)S;
+    const double N = (double)K[0].nx * K[0].ny * K[0].nz;
+    int pi = prof.begin(stream);
     PMG_TRY(f64_rbgs_sweeps(K[0], launch[0], sol, rhs, maxit, omega, stream));
+    prof.end(pi, PC_SMOOTH64, 2 * maxit, 16.0 * N, stream);
+    pi = prof.begin(stream);
     PMG_TRY(f64_residual(K[0], launch[0], rsd, sol, rhs, nullptr, nullptr, stream));
+    prof.end(pi, PC_RES64, 1, 24.0 * N, stream);
+    pi = prof.begin(stream);
     PMG_TRY(f64_restrict(X[0], launch[1], rsd, lv[1].b, stream));
+    prof.end(pi, PC_RESTRICT64, 1, 9.0 * N, stream);
     const int grid_end = std::min(tail_l0, nl);
     for (int l = 1; l < grid_end; ++l) {
         Level &L = lv[l];
@@ -515,7 +596,9 @@ int Ctx::vcycle_f64(double *sol, double *rsd, const double *rhs, int maxit, doub
         PMG_TRY(f64_restrict(X[l], launch[l + 1], L.r, lv[l + 1].b, stream));
     }
     if (tail_l0 <= nl) {
+        pi = prof.begin(stream);
         PMG_TRY(f64_tail(d_tail, stream));
+        prof.end(pi, PC_TAIL64, 1, 0.0, stream);
         if (coarse_iters) {
             int h = 0;
             PMG_CUDA(cudaMemcpyAsync(&h, d_iscal + 1, sizeof(int), cudaMemcpyDeviceToHost, stream), "iters");
@@ -530,8 +613,12 @@ int Ctx::vcycle_f64(double *sol, double *rsd, const double *rhs, int maxit, doub
         PMG_TRY(f64_prolong(X[l], launch[l + 1], lv[l + 1].x, L.x, true, stream));
         PMG_TRY(f64_rbgs_sweeps(K[l], launch[l], L.x, L.b, maxit, omega, stream));
     }
+    pi = prof.begin(stream);
     PMG_TRY(f64_prolong(X[0], launch[1], lv[1].x, sol, true, stream));
+    prof.end(pi, PC_PROLONG64, 1, 17.0 * N, stream);
+    pi = prof.begin(stream);
     PMG_TRY(f64_rbgs_sweeps(K[0], launch[0], sol, rhs, maxit, omega, stream));
+    prof.end(pi, PC_SMOOTH64, 2 * maxit, 16.0 * N, stream);
     return PMG_OK;
 }
 
@@ -551,7 +638,9 @@ int Ctx::solve_f64(double *sol, double *rsd, const double *rhs, int maxit, doubl
     for (int cyc = 1; cyc <= n_vcycles; ++cyc) {
         int ci = 0;
         PMG_TRY(vcycle_f64(sol, rsd, rhs, maxit, omega, tol, rep && rep->coarse_iterations ? &ci : nullptr));
+        int pr = prof.begin(stream);
         PMG_TRY(residual_norm(0, rsd, sol, rhs, 1));     // :1970-1971
+        prof.end(pr, PC_RES64, 1, 24.0 * (double)K[0].nx * K[0].ny * K[0].nz, stream);
         PMG_TRY(fetch_scalars(h, 2));
         const double rsd_val = h[1];
         ratio = std::sqrt(rsd_val / res0tol);
@@ -584,6 +673,7 @@ int Ctx::solve_f64(double *sol, double *rsd, const double *rhs, int maxit, doubl
         rep->converged = converged;
         rep->res0 = std::sqrt(res0tol);
         rep->final_ratio = ratio;
+        rep->inner_cycles = cycles;
     }
     return PMG_OK;
 }
@@ -727,6 +817,7 @@ int Ctx::solve(double *sol, double *rsd, const double *rhs, int maxit, double to
     }
     PMG_CUDA(cudaEventRecord(ev1, stream), "event");
     PMG_CUDA(cudaEventSynchronize(ev1), "event sync");
+    prof.flush();
     if (rep) {
         float ms = 0.f;
         cudaEventElapsedTime(&ms, ev0, ev1);
@@ -936,6 +1027,40 @@ int pmg_prolong_add(pmg_ctx *ctx, int level, double *x_f, const double *x_c)
         return PMG_EINVAL;
     }
     return pmg::f64_prolong(c.X[level], c.launch[level + 1], x_c, x_f, true, c.stream);
+}
+
+int pmg_profile(pmg_ctx *ctx, int enable)
+{
+    PMG_TRY(check_ctx_level(ctx, 0));
+    Ctx &c = ctx->impl;
+    cudaStreamSynchronize(c.stream);
+    c.prof.flush();
+    c.prof.reset();
+    c.prof.on = enable != 0;
+    return PMG_OK;
+}
+
+int pmg_profile_read(pmg_ctx *ctx, int kernel_class, double *total_ms, long long *launches, double *bytes)
+{
+    PMG_TRY(check_ctx_level(ctx, 0));
+    if (kernel_class < 0 || kernel_class >= pmg::PC_COUNT) {
+        pmg::set_error("kernel class out of range");
+        return PMG_EINVAL;
+    }
+    Ctx &c = ctx->impl;
+    cudaStreamSynchronize(c.stream);
+    c.prof.flush();
+    if (total_ms) *total_ms = c.prof.total_ms[kernel_class];
+    if (launches) *launches = c.prof.count[kernel_class];
+    if (bytes) *bytes = c.prof.bytes[kernel_class];
+    return PMG_OK;
+}
+
+int pmg_launch_count(long long *count)
+{
+    if (!count) return PMG_EINVAL;
+    *count = pmg::launches_total();
+    return PMG_OK;
 }
 
 int pmg_sync(pmg_ctx *ctx)

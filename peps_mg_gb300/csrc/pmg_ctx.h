@@ -24,13 +24,36 @@ struct Level {
 
 struct MixedState;   // FP32 V-cycle state (pmg_mixed.cu)
 
+// Event-pair timing of finest-level launches, accumulated per kernel class.
+struct Profiler {
+    bool on = false;
+    struct Rec {
+        int cls;
+        int launches;
+        double bytes;
+        cudaEvent_t a, b;
+    };
+    std::vector<cudaEvent_t> pool;
+    std::vector<Rec> pending;
+    double total_ms[PC_COUNT] = {};
+    long long count[PC_COUNT] = {};
+    double bytes[PC_COUNT] = {};
+    ~Profiler();
+    void reset();
+    cudaEvent_t get();
+    // begin/end around `launches` launches of class cls moving `bytes` per launch
+    int begin(cudaStream_t s);
+    void end(int idx, int cls, int launches, double bytes_per_launch, cudaStream_t s);
+    void flush();   // call after the stream is synchronised
+};
+
 int level_sizes(const int n0[3], int n_levels, int method, int cga_level, std::vector<std::array<int, 3>> &sizes,
                 int lvc[3]);
 
 struct Ctx {
     cudaStream_t stream = nullptr;
     int nl = 0, n_vcycles = 0, method = 0, cga_level = 0, cgpsa_level[3] = {0, 0, 0};
-    int coarse_solver = 0, precision = 0;
+    int coarse_solver = 0, precision = 0, mixed_inner = 0;
     int lvc[3] = {0, 0, 0};
     std::vector<Level> lv;
     std::vector<double> tables_host;
@@ -51,6 +74,7 @@ struct Ctx {
     size_t scratch_cap = 0;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     MixedState *mixed = nullptr;
+    Profiler prof;
 
     int build(const pmg_config_t *c, cudaStream_t s);
     ~Ctx();
@@ -66,6 +90,10 @@ struct Ctx {
                   pmg_report_t *rep);
     int solve_mixed(double *sol, double *rsd, const double *rhs, int maxit, double tol, double omega,
                     pmg_report_t *rep);
+    int setup_mixed();
+    int upload_tail32(int maxit, double omega, double tol);
+    int vcycle32(int maxit, double omega, bool zero_start);
+    int outer_residual(double *sol, double *rsd, const double *rhs, int slot);
     void destroy_mixed();
     int solve(double *sol, double *rsd, const double *rhs, int maxit, double tol, double omega, pmg_report_t *rep);
     int level_scratch(int l, double **bufs, int count);

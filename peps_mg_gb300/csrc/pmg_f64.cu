@@ -430,6 +430,7 @@ int f64_rbgs_sweeps(const LevelK<double> &L, const Launch &ln, double *x, const 
     const dim3 g = grid3((L.nx + 1) / 2, L.ny, L.nz, ln), bl(kBX, kBY, 1);
     for (int it = 0; it < iters; ++it)
         for (int c = 0; c < 2; ++c) k_rbgs_f64<<<g, bl, 0, s>>>(L, x, b, omega, omw, c);
+    count_launches(2LL * iters);
     return cuda_status(cudaGetLastError(), "rbgs sweep");
 }
 
@@ -443,6 +444,7 @@ int f64_residual(const LevelK<double> &L, const Launch &ln, double *r, const dou
     } else {
         k_residual_f64<false><<<g, bl, 0, s>>>(L, r, x, b, nullptr);
     }
+    count_launches(1);
     return cuda_status(cudaGetLastError(), "residual");
 }
 
@@ -450,6 +452,7 @@ int f64_mv_mul(const LevelK<double> &L, const Launch &ln, double *y, const doubl
 {
     const dim3 g = grid3(L.nx, L.ny, L.nz, ln), bl(kBX, kBY, 1);
     k_mvmul_f64<<<g, bl, 0, s>>>(L, y, x);
+    count_launches(1);
     return cuda_status(cudaGetLastError(), "mv_mul");
 }
 
@@ -459,12 +462,14 @@ int f64_dot_partials(const LevelK<double> &L, const Launch &ln, const double *x,
     const dim3 g = grid3(L.nx, L.ny, L.nz, ln), bl(kBX, kBY, 1);
     k_dot_f64<<<g, bl, 0, s>>>(L, x, y, partials);
     *npart = (int)(g.x * g.y * g.z);
+    count_launches(1);
     return cuda_status(cudaGetLastError(), "dot");
 }
 
 int f64_reduce(const double *partials, int n, double *out, cudaStream_t s)
 {
     k_reduce_f64<<<1, 1024, 0, s>>>(partials, n, out);
+    count_launches(1);
     return cuda_status(cudaGetLastError(), "reduce");
 }
 
@@ -472,6 +477,7 @@ int f64_restrict(const XferK<double> &X, const Launch &ln, const double *vf, dou
 {
     const dim3 g = grid3(X.ncx, X.ncy, X.ncz, ln), bl(kBX, kBY, 1);
     k_restrict_f64<<<g, bl, 0, s>>>(X, vf, vc);
+    count_launches(1);
     return cuda_status(cudaGetLastError(), "restriction");
 }
 
@@ -483,6 +489,7 @@ int f64_prolong(const XferK<double> &X, const Launch &ln, const double *vc, doub
         k_prolong_f64<true><<<g, bl, 0, s>>>(X, vc, vf);
     else
         k_prolong_f64<false><<<g, bl, 0, s>>>(X, vc, vf);
+    count_launches(1);
     return cuda_status(cudaGetLastError(), "prolongation");
 }
 
@@ -493,12 +500,14 @@ int zero_ghosts_f64(double *a, int nx, int ny, int nz, cudaStream_t s)
     long long blocks = (total + 255) / 256;
     if (blocks > 4096) blocks = 4096;
     k_zero_ghosts_f64<<<(unsigned)blocks, 256, 0, s>>>(a, nx, ny, nz);
+    count_launches(1);
     return cuda_status(cudaGetLastError(), "zero ghosts");
 }
 
 int f64_tail(const TailDesc<double> *dev_desc, cudaStream_t s)
 {
     k_tail_f64<<<1, kTailThreads, 0, s>>>(dev_desc);
+    count_launches(1);
     return cuda_status(cudaGetLastError(), "coarse tail");
 }
 
@@ -507,12 +516,14 @@ int f64_copy_interior(const LevelK<double> &L, double *dst, const double *src, c
     const Launch ln{{false, false, false}};
     const dim3 g = grid3(L.nx, L.ny, L.nz, ln), bl(kBX, kBY, 1);
     k_copy_interior_f64<<<g, bl, 0, s>>>(L, dst, src);
+    count_launches(1);
     return cuda_status(cudaGetLastError(), "copy");
 }
 
 int f64_cg_scalar(const double *num, const double *den, double *out, cudaStream_t s)
 {
     k_cg_scalar_f64<<<1, 1, 0, s>>>(num, den, out);
+    count_launches(1);
     return cuda_status(cudaGetLastError(), "cg scalar");
 }
 
@@ -521,6 +532,7 @@ int f64_cg_update_xr(const LevelK<double> &L, const Launch &ln, const double *al
 {
     const dim3 g = grid3(L.nx, L.ny, L.nz, ln), bl(kBX, kBY, 1);
     k_cg_xr_f64<<<g, bl, 0, s>>>(L, alpha, x, r, p, ap);
+    count_launches(1);
     return cuda_status(cudaGetLastError(), "cg update");
 }
 
@@ -529,6 +541,7 @@ int f64_cg_update_p(const LevelK<double> &L, const Launch &ln, const double *bet
 {
     const dim3 g = grid3(L.nx, L.ny, L.nz, ln), bl(kBX, kBY, 1);
     k_cg_p_f64<<<g, bl, 0, s>>>(L, beta, p, r);
+    count_launches(1);
     return cuda_status(cudaGetLastError(), "cg update p");
 }
 
@@ -536,6 +549,7 @@ int f64_check(const double *num, const double *den, double tol, int le, int iter
               cudaStream_t s)
 {
     k_check_f64<<<1, 1, 0, s>>>(num, den, tol, le, iter, flag, iter_out);
+    count_launches(1);
     return cuda_status(cudaGetLastError(), "check");
 }
 

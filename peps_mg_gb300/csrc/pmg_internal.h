@@ -67,6 +67,26 @@ int f64_check(const double *num, const double *den, double tol, int le, int iter
 // Fixed launch shapes (shared with the host driver for partial-sum sizing).
 void grid_for_cells(const LevelK<double> &L, const Launch &ln, dim3 *grid, dim3 *block);
 
+// ---- telemetry --------------------------------------------------------------------
+// Kernel classes timed by the optional profiler (finest level only).
+enum ProfClass {
+    PC_SMOOTH32 = 0,     // FP32 RBGS half-sweep                     8 B/cell algorithmic
+    PC_OUTER_RES = 1,    // FP64 outer residual (+FP32 copy, norm)  28 B/cell
+    PC_RESRESTRICT32 = 2,// FP32 residual fused with restriction   8.5 B/cell
+    PC_PROLONG32 = 3,    // FP32 prolongation + correction         8.5 B/cell
+    PC_ADDCORR = 4,      // FP64 x += e                             20 B/cell
+    PC_TAIL32 = 5,       // FP32 single-CTA coarse tail
+    PC_SMOOTH64 = 6,     // FP64 RBGS half-sweep                    16 B/cell
+    PC_RES64 = 7,        // FP64 residual (+norm)                   24 B/cell
+    PC_RESTRICT64 = 8,   // FP64 restriction                         9 B/cell
+    PC_PROLONG64 = 9,    // FP64 prolongation + correction          17 B/cell
+    PC_TAIL64 = 10,      // FP64 single-CTA coarse tail
+    PC_COUNT = 11
+};
+// Number of kernels this library has launched (all contexts).
+void count_launches(long long n);
+long long launches_total();
+
 // ---- errors ---------------------------------------------------------------------
 void set_error(const std::string &msg);
 int cuda_status(cudaError_t e, const char *what);

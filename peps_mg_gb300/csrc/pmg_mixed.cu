@@ -1,14 +1,665 @@
-// pmg_mixed.cu -- FP32 V-cycles inside FP64 defect correction (placeholder).
+// pmg_mixed.cu -- mixed precision: FP32 V-cycles inside FP64 defect correction.
+//
+//   r   = b - A x                  (FP64, with the FP64 norm used for convergence)
+//   A e = r                        (FP32 V-cycles, e starting at 0, homogeneous ghosts)
+//   x   = x + e                    (FP64)
+//
+// repeated until sqrt(|r|^2 / |r0|^2) < tolerance, the reference's convergence test
+// (src/multigrid.f90:1970-1973).  The FP32 V-cycle follows the operation sequence of
+// the reference cycle (src/multigrid.f90:1931-1967) with the same smoother, transfer
+// operators and coarsest-level solver, but in FP32 arithmetic with FMA contraction and
+// approximate reciprocals; the coarsest-level solver's dot products and convergence
+// test stay in FP64.  The finest FP32 residual is fused with the restriction.
+//
+// This translation unit is compiled with --fmad=true.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <vector>
+
 #include "pmg_ctx.h"
 
 namespace pmg {
 
-struct MixedState {};
+namespace {
 
-int Ctx::solve_mixed(double *, double *, const double *, int, double, double, pmg_report_t *)
+constexpr int kBX = 32, kBY = 8;
+constexpr int kTail32Threads = 1024;
+constexpr int kMaxGridZ = 65535;
+
+__device__ __forceinline__ int tid2() { return threadIdx.x + blockDim.x * threadIdx.y; }
+__device__ __forceinline__ int blin() { return blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z); }
+
+// ---------------------------------------------------------------------------------
+// FP32 per-cell arithmetic
+// ---------------------------------------------------------------------------------
+__device__ __forceinline__ float diag32(const LevelK<float> &L, int i, int j, int k)
 {
-    set_error("mixed precision not built yet");
-    return PMG_EINVAL;
+    return -((L.sx[i] + (L.cym[j] + L.cyp[j])) + (L.czm[k] + L.czp[k]));
+}
+
+__device__ __forceinline__ float nbsum32(const LevelK<float> &L, const float *x, long long p, int i, int j, int k)
+{
+    float t = L.cxm[i] * x[p - 1];
+    t = fmaf(L.cxp[i], x[p + 1], t);
+    t = fmaf(L.cym[j], x[p - L.sy], t);
+    t = fmaf(L.cyp[j], x[p + L.sy], t);
+    t = fmaf(L.czm[k], x[p - L.sz], t);
+    t = fmaf(L.czp[k], x[p + L.sz], t);
+    return t;
+}
+
+__device__ __forceinline__ float rbgs32(const LevelK<float> &L, const float *x, const float *b, int i, int j, int k,
+                                        float omega, float omw)
+{
+    const long long p = lin(i, j, k, L.sy, L.sz);
+    const float t = nbsum32(L, x, p, i, j, k);
+    const float c0 = diag32(L, i, j, k);
+    return fmaf(omw, x[p], __fdividef(omega * (b[p] - t), c0));
+}
+
+__device__ __forceinline__ float resid32(const LevelK<float> &L, const float *x, const float *b, int i, int j, int k)
+{
+    const long long p = lin(i, j, k, L.sy, L.sz);
+    return b[p] - fmaf(diag32(L, i, j, k), x[p], nbsum32(L, x, p, i, j, k));
+}
+
+// Restriction weights of one coarse cell (src/multigrid.f90:1474-1482) applied to
+// values v[0..7] in the reference's term order.
+__device__ __forceinline__ float restrict_combine32(const XferK<float> &X, int ip, int iz, int jp, int jz, int kp,
+                                                    int kz, const float v[8])
+{
+    const float xz = X.wx[iz], xp = X.wx[ip], yz = X.wy[jz], yp = X.wy[jp], zz = X.wz[kz], zp = X.wz[kp];
+    const float w[8] = {xz * yz * zz, xp * yz * zz, xz * yp * zz, xp * yp * zz,
+                        xz * yz * zp, xp * yz * zp, xz * yp * zp, xp * yp * zp};
+    float vol = 0.f, s = 0.f;
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+        vol += w[q];
+        s = fmaf(w[q], v[q], s);
+    }
+    return __fdividef(s, vol);
+}
+
+// Fused residual + restriction: b_c(i,j,k) = R (b_f - A_f e_f) without storing the
+// fine residual (src/multigrid.f90:1932-1933 and :1939-1940).
+__device__ __forceinline__ float resrestrict_cell32(const LevelK<float> &F, const XferK<float> &X, const float *e,
+                                                    const float *b, int i, int j, int k)
+{
+    const int ip = i * X.stx, iz = ip - (X.stx - 1);
+    const int jp = j * X.sty, jz = jp - (X.sty - 1);
+    const int kp = k * X.stz, kz = kp - (X.stz - 1);
+    // children in the reference's term order: (p,p,p) (z,p,p) (p,z,p) (z,z,p) (p,p,z) (z,p,z) (p,z,z) (z,z,z)
+    float v[8];
+    v[0] = resid32(F, e, b, ip, jp, kp);
+    v[1] = resid32(F, e, b, iz, jp, kp);
+    v[2] = resid32(F, e, b, ip, jz, kp);
+    v[3] = resid32(F, e, b, iz, jz, kp);
+    v[4] = resid32(F, e, b, ip, jp, kz);
+    v[5] = resid32(F, e, b, iz, jp, kz);
+    v[6] = resid32(F, e, b, ip, jz, kz);
+    v[7] = resid32(F, e, b, iz, jz, kz);
+    return restrict_combine32(X, ip, iz, jp, jz, kp, kz, v);
+}
+
+__device__ __forceinline__ float prolong_child32(float ax, float bx, float ay, float by, float az, float bz,
+                                                 float v000, float v100, float v010, float v001, float v110,
+                                                 float v101, float v011, float v111)
+{
+    const float axy = ax * ay, bxy = bx * ay, axby = ax * by, bxby = bx * by;
+    float t = axy * az * v000;
+    t = fmaf(bxy * az, v100, t);
+    t = fmaf(axby * az, v010, t);
+    t = fmaf(axy * bz, v001, t);
+    t = fmaf(bxby * az, v110, t);
+    t = fmaf(bxy * bz, v101, t);
+    t = fmaf(axby * bz, v011, t);
+    t = fmaf(bxby * bz, v111, t);
+    return __fdividef(t, (ax + bx) * (ay + by) * (az + bz));
+}
+
+// e_f += P e_c for the children of one coarse cell (src/multigrid.f90:1652-1758 and
+// the correction x = x + r of :1958).
+__device__ __forceinline__ void prolong_add_cell32(const XferK<float> &X, const float *vc, float *vf, int i, int j,
+                                                   int k)
+{
+    const int ox = X.stx - 1, oy = X.sty - 1, oz = X.stz - 1;
+    const int ip = i * X.stx, iz = ip - ox;
+    const int jp = j * X.sty, jz = jp - oy;
+    const int kp = k * X.stz, kz = kp - oz;
+    const int csy = X.csy;
+    const long long csz = X.csz;
+    auto V = [&](int a, int b, int c) { return vc[lin(a, b, c, csy, csz)]; };
+#pragma unroll
+    for (int sk = 0; sk < 2; ++sk) {
+        if (sk == 0 && oz == 0) continue;
+        const float az = sk ? X.pzn[kp] : X.pzp[kz];
+        const float bz = sk ? X.pzn[kz] : X.pzp[kp];
+        const int kn = sk ? k + oz : k - oz;
+        const int kf = sk ? kp : kz;
+#pragma unroll
+        for (int sj = 0; sj < 2; ++sj) {
+            if (sj == 0 && oy == 0) continue;
+            const float ay = sj ? X.pyn[jp] : X.pyp[jz];
+            const float by = sj ? X.pyn[jz] : X.pyp[jp];
+            const int jn = sj ? j + oy : j - oy;
+            const int jf = sj ? jp : jz;
+#pragma unroll
+            for (int si = 0; si < 2; ++si) {
+                if (si == 0 && ox == 0) continue;
+                const float ax = si ? X.pxn[ip] : X.pxp[iz];
+                const float bx = si ? X.pxn[iz] : X.pxp[ip];
+                const int in = si ? i + ox : i - ox;
+                const int ifn = si ? ip : iz;
+                const float v = prolong_child32(ax, bx, ay, by, az, bz, V(i, j, k), V(in, j, k), V(i, jn, k),
+                                                V(i, j, kn), V(in, jn, k), V(in, j, kn), V(i, jn, kn),
+                                                V(in, jn, kn));
+                const long long q = lin(ifn, jf, kf, X.fsy, X.fsz);
+                vf[q] += v;
+            }
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------------
+// FP32 grid kernels
+// ---------------------------------------------------------------------------------
+// colour half-sweep; ZERO = the first half-sweep from e = 0, writing every interior
+// cell (colour-0 cells get omega b / c0, colour-1 cells 0), so e needs no reset pass.
+template <bool ZERO>
+__global__ void __launch_bounds__(kBX *kBY) k_rbgs32(LevelK<float> L, float *__restrict__ x,
+                                                     const float *__restrict__ b, float omega, float omw, int colour)
+{
+    for (int k = blockIdx.z + 1; k <= L.nz; k += gridDim.z)
+        for (int j = blockIdx.y * blockDim.y + threadIdx.y + 1; j <= L.ny; j += gridDim.y * blockDim.y) {
+            if (ZERO) {
+                for (int i = blockIdx.x * blockDim.x + threadIdx.x + 1; i <= L.nx; i += gridDim.x * blockDim.x) {
+                    const long long p = lin(i, j, k, L.sy, L.sz);
+                    const bool mine = ((i + j + k + colour) & 1) == 1;
+                    x[p] = mine ? __fdividef(omega * b[p], diag32(L, i, j, k)) : 0.f;
+                }
+            } else {
+                const int ista = 1 + ((j + k + colour) & 1);
+                for (int i = ista + 2 * (blockIdx.x * blockDim.x + threadIdx.x); i <= L.nx;
+                     i += 2 * gridDim.x * blockDim.x)
+                    x[lin(i, j, k, L.sy, L.sz)] = rbgs32(L, x, b, i, j, k, omega, omw);
+            }
+        }
+}
+
+__global__ void __launch_bounds__(kBX *kBY) k_resrestrict32(LevelK<float> F, XferK<float> X,
+                                                            const float *__restrict__ e, const float *__restrict__ b,
+                                                            float *__restrict__ bc)
+{
+    for (int k = blockIdx.z + 1; k <= X.ncz; k += gridDim.z)
+        for (int j = blockIdx.y * blockDim.y + threadIdx.y + 1; j <= X.ncy; j += gridDim.y * blockDim.y)
+            for (int i = blockIdx.x * blockDim.x + threadIdx.x + 1; i <= X.ncx; i += gridDim.x * blockDim.x)
+                bc[lin(i, j, k, X.csy, X.csz)] = resrestrict_cell32(F, X, e, b, i, j, k);
+}
+
+__global__ void __launch_bounds__(kBX *kBY) k_prolong_add32(XferK<float> X, const float *__restrict__ vc,
+                                                            float *__restrict__ vf)
+{
+    for (int k = blockIdx.z + 1; k <= X.ncz; k += gridDim.z)
+        for (int j = blockIdx.y * blockDim.y + threadIdx.y + 1; j <= X.ncy; j += gridDim.y * blockDim.y)
+            for (int i = blockIdx.x * blockDim.x + threadIdx.x + 1; i <= X.ncx; i += gridDim.x * blockDim.x)
+                prolong_add_cell32(X, vc, vf, i, j, k);
+}
+
+// ---------------------------------------------------------------------------------
+// FP64 outer kernels
+// ---------------------------------------------------------------------------------
+// r = b - A x in FP64 (FMA form: r = b + d x - sum c x_nb with d = -c0), stored both
+// as the FP64 residual and as the FP32 right-hand side of the inner system, with the
+// per-block sum of r^2.
+__global__ void __launch_bounds__(kBX *kBY) k_outer_residual(LevelK<double> L, const double *__restrict__ x,
+                                                             const double *__restrict__ b, double *__restrict__ r,
+                                                             float *__restrict__ r32, double *partials)
+{
+    double acc = 0.0;
+    for (int k = blockIdx.z + 1; k <= L.nz; k += gridDim.z) {
+        const double dz = L.czm[k] + L.czp[k];
+        for (int j = blockIdx.y * blockDim.y + threadIdx.y + 1; j <= L.ny; j += gridDim.y * blockDim.y) {
+            const double dyz = (L.cym[j] + L.cyp[j]) + dz;
+            for (int i = blockIdx.x * blockDim.x + threadIdx.x + 1; i <= L.nx; i += gridDim.x * blockDim.x) {
+                const long long p = lin(i, j, k, L.sy, L.sz);
+                const double d = L.sx[i] + dyz;
+                double v = fma(d, x[p], b[p]);
+                v = fma(-L.cxm[i], x[p - 1], v);
+                v = fma(-L.cxp[i], x[p + 1], v);
+                v = fma(-L.cym[j], x[p - L.sy], v);
+                v = fma(-L.cyp[j], x[p + L.sy], v);
+                v = fma(-L.czm[k], x[p - L.sz], v);
+                v = fma(-L.czp[k], x[p + L.sz], v);
+                r[p] = v;
+                r32[p] = (float)v;
+                acc = fma(v, v, acc);
+            }
+        }
+    }
+    __shared__ double sw[kBX * kBY / 32];
+    const double s = block_sum(acc, sw);
+    if (tid2() == 0) partials[blin()] = s;
+}
+
+// x = x + e (the FP64 correction)
+__global__ void __launch_bounds__(kBX *kBY) k_add_correction(LevelK<double> L, double *__restrict__ x,
+                                                             const float *__restrict__ e)
+{
+    for (int k = blockIdx.z + 1; k <= L.nz; k += gridDim.z)
+        for (int j = blockIdx.y * blockDim.y + threadIdx.y + 1; j <= L.ny; j += gridDim.y * blockDim.y)
+            for (int i = blockIdx.x * blockDim.x + threadIdx.x + 1; i <= L.nx; i += gridDim.x * blockDim.x) {
+                const long long p = lin(i, j, k, L.sy, L.sz);
+                x[p] = x[p] + (double)e[p];
+            }
+}
+
+// ---------------------------------------------------------------------------------
+// FP32 single-CTA coarse tail (same sequence as the FP64 tail in pmg_f64.cu); the
+// coarsest solver's dot products and its convergence test are FP64.
+// ---------------------------------------------------------------------------------
+template <typename F>
+__device__ __forceinline__ void for_cells(int nx, int ny, int nz, F f)
+{
+    const long long n = (long long)nx * ny * nz;
+    for (long long q = threadIdx.x; q < n; q += blockDim.x) {
+        const int i = (int)(q % nx) + 1;
+        const long long rr = q / nx;
+        f(i, (int)(rr % ny) + 1, (int)(rr / ny) + 1);
+    }
+}
+
+__device__ void t32_sweeps(const LevelK<float> &L, float *x, const float *b, int iters, float omega, float omw,
+                           bool zero_start)
+{
+    const int hx = (L.nx + 1) / 2;
+    const long long nq = (long long)hx * L.ny * L.nz;
+    for (int it = 0; it < iters; ++it)
+        for (int colour = 0; colour < 2; ++colour) {
+            if (zero_start && it == 0 && colour == 0) {
+                for_cells(L.nx, L.ny, L.nz, [&](int i, int j, int k) {
+                    const long long p = lin(i, j, k, L.sy, L.sz);
+                    x[p] = ((i + j + k) & 1) ? __fdividef(omega * b[p], diag32(L, i, j, k)) : 0.f;
+                });
+            } else {
+                for (long long q = threadIdx.x; q < nq; q += blockDim.x) {
+                    const int t = (int)(q % hx);
+                    const long long rr = q / hx;
+                    const int j = (int)(rr % L.ny) + 1, k = (int)(rr / L.ny) + 1;
+                    const int i = 2 * t + 1 + ((j + k + colour) & 1);
+                    if (i <= L.nx) x[lin(i, j, k, L.sy, L.sz)] = rbgs32(L, x, b, i, j, k, omega, omw);
+                }
+            }
+            __syncthreads();
+        }
+}
+
+__device__ double t32_residual_norm(const LevelK<float> &L, float *r, const float *x, const float *b, double *sw)
+{
+    double acc = 0.0;
+    for_cells(L.nx, L.ny, L.nz, [&](int i, int j, int k) {
+        const float v = resid32(L, x, b, i, j, k);
+        r[lin(i, j, k, L.sy, L.sz)] = v;
+        acc += (double)v * (double)v;
+    });
+    __syncthreads();
+    return block_sum(acc, sw);
+}
+
+__device__ double t32_dot(const LevelK<float> &L, const float *x, const float *y, double *sw)
+{
+    double acc = 0.0;
+    for_cells(L.nx, L.ny, L.nz, [&](int i, int j, int k) {
+        const long long p = lin(i, j, k, L.sy, L.sz);
+        acc += (double)x[p] * (double)y[p];
+    });
+    return block_sum(acc, sw);
+}
+
+__global__ void __launch_bounds__(kTail32Threads) k_tail32(const TailDesc<float> *__restrict__ Dp)
+{
+    __shared__ double sw[kTail32Threads / 32];
+    const TailDesc<float> &D = *Dp;
+    const float omega = D.omega, omw = D.omw;
+    for (int l = D.l0; l < D.nl; ++l) {
+        const LevelK<float> L = D.L[l];
+        const XferK<float> X = D.X[l];
+        float *x = D.x[l], *bc = D.b[l + 1];
+        const float *b = D.b[l];
+        t32_sweeps(L, x, b, D.maxit, omega, omw, true);
+        for_cells(X.ncx, X.ncy, X.ncz, [&](int i, int j, int k) {
+            bc[lin(i, j, k, X.csy, X.csz)] = resrestrict_cell32(L, X, x, b, i, j, k);
+        });
+        __syncthreads();
+    }
+    {
+        const LevelK<float> L = D.L[D.nl];
+        float *x = D.x[D.nl];
+        const float *b = D.b[D.nl];
+        const long long tot = (long long)L.sz * (L.nz + 2);
+        for (long long q = threadIdx.x; q < tot; q += blockDim.x) x[q] = 0.f;
+        __syncthreads();
+        int iters = 0;
+        if ((long long)L.nx * L.ny * L.nz == 1) {
+            if (threadIdx.x == 0) {
+                const long long p = lin(1, 1, 1, L.sy, L.sz);
+                x[p] = b[p] / diag32(L, 1, 1, 1);
+            }
+            __syncthreads();
+        } else if (D.coarse_solver == 0) {
+            const double r0 = t32_residual_norm(L, D.rr, x, b, sw);
+            int it;
+            for (it = 0; it < D.coarse_maxit; ++it) {
+                t32_sweeps(L, x, b, 1, omega, omw, false);
+                const double rn = t32_residual_norm(L, D.rr, x, b, sw);
+                if (sqrt(rn / r0) <= D.tol) break;
+            }
+            iters = it;
+        } else {
+            float *p = D.p, *ap = D.ap, *rs = D.rr;
+            t32_residual_norm(L, rs, x, b, sw);
+            for_cells(L.nx, L.ny, L.nz, [&](int i, int j, int k) {
+                const long long q = lin(i, j, k, L.sy, L.sz);
+                p[q] = rs[q];
+            });
+            __syncthreads();
+            const double r0 = t32_dot(L, rs, rs, sw);
+            int it;
+            for (it = 0; it < D.coarse_maxit; ++it) {
+                const double t1 = t32_dot(L, rs, rs, sw);
+                for_cells(L.nx, L.ny, L.nz, [&](int i, int j, int k) {
+                    const long long q = lin(i, j, k, L.sy, L.sz);
+                    ap[q] = fmaf(diag32(L, i, j, k), p[q], nbsum32(L, p, q, i, j, k));
+                });
+                __syncthreads();
+                const double t2a = t32_dot(L, ap, p, sw);
+                const float alpha = (float)(t1 / t2a);
+                for_cells(L.nx, L.ny, L.nz, [&](int i, int j, int k) {
+                    const long long q = lin(i, j, k, L.sy, L.sz);
+                    x[q] = fmaf(alpha, p[q], x[q]);
+                    rs[q] = fmaf(-alpha, ap[q], rs[q]);
+                });
+                __syncthreads();
+                const double t2 = t32_dot(L, rs, rs, sw);
+                if (sqrt(t2 / r0) < D.tol) break;
+                const float beta = (float)(t2 / t1);
+                for_cells(L.nx, L.ny, L.nz, [&](int i, int j, int k) {
+                    const long long q = lin(i, j, k, L.sy, L.sz);
+                    p[q] = fmaf(beta, p[q], rs[q]);
+                });
+                __syncthreads();
+            }
+            iters = it;
+        }
+        if (threadIdx.x == 0 && D.iters_out) *D.iters_out = iters;
+        __syncthreads();
+    }
+    for (int l = D.nl - 1; l >= D.l0; --l) {
+        const LevelK<float> L = D.L[l];
+        const XferK<float> X = D.X[l];
+        float *x = D.x[l], *xc = D.x[l + 1];
+        const float *b = D.b[l];
+        for_cells(X.ncx, X.ncy, X.ncz, [&](int i, int j, int k) { prolong_add_cell32(X, xc, x, i, j, k); });
+        __syncthreads();
+        t32_sweeps(L, x, b, D.maxit, omega, omw, false);
+    }
+}
+
+dim3 grid3m(int nxt, int ny, int nz, const Launch &ln)
+{
+    dim3 g;
+    g.x = ln.collapse[0] ? 1u : (unsigned)std::max(1, (nxt + kBX - 1) / kBX);
+    g.y = ln.collapse[1] ? 1u : (unsigned)std::max(1, (ny + kBY - 1) / kBY);
+    g.z = ln.collapse[2] ? 1u : (unsigned)std::max(1, std::min(nz, kMaxGridZ));
+    return g;
+}
+
+}  // namespace
+
+struct MixedState {
+    std::vector<float> tables_host;
+    float *tables = nullptr;
+    std::vector<LevelK<float>> K;
+    std::vector<XferK<float>> X;
+    std::vector<float *> e, b;       // e[l], b[l]; b[0] is the FP32 outer residual
+    float *cp = nullptr, *cap = nullptr, *crr = nullptr;
+    TailDesc<float> tail_host;
+    TailDesc<float> *d_tail = nullptr;
+    int inner = 2;
+    ~MixedState()
+    {
+        cudaFree(tables);
+        for (auto p : e) cudaFree(p);
+        for (auto p : b) cudaFree(p);
+        cudaFree(cp);
+        cudaFree(cap);
+        cudaFree(crr);
+        cudaFree(d_tail);
+    }
+};
+
+#define PMG_TRY_M(expr)                \
+    do {                               \
+        int _rc = (expr);              \
+        if (_rc != PMG_OK) return _rc; \
+    } while (0)
+
+static int mstatus(cudaError_t e, const char *what) { return cuda_status(e, what); }
+
+int Ctx::setup_mixed()
+{
+    if (mixed) return PMG_OK;
+    if (tail_l0 > nl) {
+        set_error("mixed precision needs a coarsest level small enough for the single-CTA coarse solver");
+        return PMG_EINVAL;
+    }
+    MixedState *m = new (std::nothrow) MixedState();
+    if (!m) return PMG_ENOMEM;
+    mixed = m;
+    m->inner = mixed_inner > 0 ? mixed_inner : 2;
+    m->tables_host.resize(tables_host.size());
+    for (size_t q = 0; q < tables_host.size(); ++q) m->tables_host[q] = (float)tables_host[q];
+    PMG_TRY_M(mstatus(cudaMalloc(&m->tables, m->tables_host.size() * sizeof(float)), "mixed tables"));
+    PMG_TRY_M(mstatus(cudaMemcpy(m->tables, m->tables_host.data(), m->tables_host.size() * sizeof(float),
+                                 cudaMemcpyHostToDevice),
+                      "mixed tables"));
+    auto F = [&](const double *p) { return (const float *)(m->tables + (p - d_tables)); };
+    m->K.resize((size_t)nl + 1);
+    m->X.resize((size_t)nl);
+    for (int l = 0; l <= nl; ++l) {
+        const LevelK<double> &k = K[l];
+        LevelK<float> &f = m->K[l];
+        f.nx = k.nx; f.ny = k.ny; f.nz = k.nz; f.sy = k.sy; f.sz = k.sz;
+        f.cxm = F(k.cxm); f.cxp = F(k.cxp); f.sx = F(k.sx);
+        f.cym = F(k.cym); f.cyp = F(k.cyp); f.czm = F(k.czm); f.czp = F(k.czp);
+        if (l < nl) {
+            const XferK<double> &x = X[l];
+            XferK<float> &y = m->X[l];
+            y.ncx = x.ncx; y.ncy = x.ncy; y.ncz = x.ncz; y.csy = x.csy; y.csz = x.csz;
+            y.fsy = x.fsy; y.fsz = x.fsz; y.stx = x.stx; y.sty = x.sty; y.stz = x.stz;
+            y.wx = F(x.wx); y.wy = F(x.wy); y.wz = F(x.wz);
+            y.pxp = F(x.pxp); y.pxn = F(x.pxn); y.pyp = F(x.pyp); y.pyn = F(x.pyn);
+            y.pzp = F(x.pzp); y.pzn = F(x.pzn);
+        }
+    }
+    m->e.assign((size_t)nl + 1, nullptr);
+    m->b.assign((size_t)nl + 1, nullptr);
+    for (int l = 0; l <= nl; ++l) {
+        const size_t bytes = lv[l].total * sizeof(float);
+        PMG_TRY_M(mstatus(cudaMalloc(&m->e[l], bytes), "mixed level allocation"));
+        PMG_TRY_M(mstatus(cudaMalloc(&m->b[l], bytes), "mixed level allocation"));
+        PMG_TRY_M(mstatus(cudaMemset(m->e[l], 0, bytes), "mixed level init"));
+        PMG_TRY_M(mstatus(cudaMemset(m->b[l], 0, bytes), "mixed level init"));
+    }
+    const size_t cb = lv[nl].total * sizeof(float);
+    for (float **p : {&m->cp, &m->cap, &m->crr}) {
+        PMG_TRY_M(mstatus(cudaMalloc(p, cb), "mixed coarse scratch"));
+        PMG_TRY_M(mstatus(cudaMemset(*p, 0, cb), "mixed coarse scratch"));
+    }
+    PMG_TRY_M(mstatus(cudaMalloc(&m->d_tail, sizeof(TailDesc<float>)), "mixed tail descriptor"));
+    return PMG_OK;
+}
+
+int Ctx::upload_tail32(int maxit, double omega, double tol)
+{
+    MixedState *m = mixed;
+    TailDesc<float> &D = m->tail_host;
+    std::memset(&D, 0, sizeof(D));
+    D.l0 = tail_l0;
+    D.nl = nl;
+    D.maxit = maxit;
+    D.coarse_solver = coarse_solver;
+    D.coarse_maxit = 1000;
+    D.omega = (float)omega;
+    D.omw = (float)(1.0 - omega);
+    D.tol = tol;
+    D.p = m->cp;
+    D.ap = m->cap;
+    D.rr = m->crr;
+    D.iters_out = d_iscal + 2;
+    for (int l = 0; l <= nl; ++l) {
+        D.L[l] = m->K[l];
+        if (l < nl) D.X[l] = m->X[l];
+        D.x[l] = m->e[l];
+        D.b[l] = m->b[l];
+        D.r[l] = nullptr;
+    }
+    return mstatus(cudaMemcpyAsync(m->d_tail, &D, sizeof(D), cudaMemcpyHostToDevice, stream), "tail upload");
+}
+
+// One FP32 V-cycle on A e = b[0] (e = e[0]); zero_start: e[0] enters as 0.
+int Ctx::vcycle32(int maxit, double omega, bool zero_start)
+{
+    MixedState *m = mixed;
+    const float om = (float)omega, omw = (float)(1.0 - omega);
+    const dim3 bl(kBX, kBY, 1);
+    const double N = (double)m->K[0].nx * m->K[0].ny * m->K[0].nz;
+    long long nlaunch = 0;
+    auto sweeps = [&](int l, bool zs) {
+        const LevelK<float> &L = m->K[l];
+        const dim3 gc = grid3m((L.nx + 1) / 2, L.ny, L.nz, launch[l]), gf = grid3m(L.nx, L.ny, L.nz, launch[l]);
+        const int pi = l == 0 ? prof.begin(stream) : -1;
+        for (int it = 0; it < maxit; ++it)
+            for (int c = 0; c < 2; ++c) {
+                if (zs && it == 0 && c == 0)
+                    k_rbgs32<true><<<gf, bl, 0, stream>>>(L, m->e[l], m->b[l], om, omw, c);
+                else
+                    k_rbgs32<false><<<gc, bl, 0, stream>>>(L, m->e[l], m->b[l], om, omw, c);
+                ++nlaunch;
+            }
+        prof.end(pi, PC_SMOOTH32, 2 * maxit, 8.0 * N, stream);
+        if (zs && maxit == 0) cudaMemsetAsync(m->e[l], 0, lv[l].total * sizeof(float), stream);
+    };
+    sweeps(0, zero_start);
+    {
+        const XferK<float> &X0 = m->X[0];
+        const int pi = prof.begin(stream);
+        k_resrestrict32<<<grid3m(X0.ncx, X0.ncy, X0.ncz, launch[1]), bl, 0, stream>>>(m->K[0], X0, m->e[0], m->b[0],
+                                                                                     m->b[1]);
+        prof.end(pi, PC_RESRESTRICT32, 1, 8.5 * N, stream);
+        ++nlaunch;
+    }
+    for (int l = 1; l < tail_l0; ++l) {
+        sweeps(l, true);
+        const XferK<float> &Xl = m->X[l];
+        k_resrestrict32<<<grid3m(Xl.ncx, Xl.ncy, Xl.ncz, launch[l + 1]), bl, 0, stream>>>(m->K[l], Xl, m->e[l],
+                                                                                         m->b[l], m->b[l + 1]);
+        ++nlaunch;
+    }
+    {
+        const int pi = prof.begin(stream);
+        k_tail32<<<1, kTail32Threads, 0, stream>>>(m->d_tail);
+        prof.end(pi, PC_TAIL32, 1, 0.0, stream);
+        ++nlaunch;
+    }
+    for (int l = tail_l0 - 1; l >= 0; --l) {
+        const XferK<float> &Xl = m->X[l];
+        const int pi = l == 0 ? prof.begin(stream) : -1;
+        k_prolong_add32<<<grid3m(Xl.ncx, Xl.ncy, Xl.ncz, launch[l + 1]), bl, 0, stream>>>(Xl, m->e[l + 1], m->e[l]);
+        prof.end(pi, PC_PROLONG32, 1, 8.5 * N, stream);
+        ++nlaunch;
+        sweeps(l, false);
+    }
+    count_launches(nlaunch);
+    return cuda_status(cudaGetLastError(), "fp32 v-cycle");
+}
+
+int Ctx::outer_residual(double *sol, double *rsd, const double *rhs, int slot)
+{
+    const LevelK<double> &L = K[0];
+    const dim3 g = grid3m(L.nx, L.ny, L.nz, launch[0]), bl(kBX, kBY, 1);
+    const int pi = prof.begin(stream);
+    k_outer_residual<<<g, bl, 0, stream>>>(L, sol, rhs, rsd, mixed->b[0], d_partials);
+    prof.end(pi, PC_OUTER_RES, 1, 28.0 * (double)L.nx * L.ny * L.nz, stream);
+    count_launches(1);
+    PMG_TRY_M(cuda_status(cudaGetLastError(), "outer residual"));
+    return f64_reduce(d_partials, (int)(g.x * g.y * g.z), d_scal + slot, stream);
+}
+
+int Ctx::solve_mixed(double *sol, double *rsd, const double *rhs, int maxit, double tol, double omega,
+                     pmg_report_t *rep)
+{
+    PMG_TRY_M(setup_mixed());
+    MixedState *m = mixed;
+    const Level &S = lv[0];
+    PMG_TRY_M(mstatus(cudaMemsetAsync(rsd, 0, S.total * sizeof(double), stream), "rsd init"));
+    PMG_TRY_M(outer_residual(sol, rsd, rhs, 0));
+    double h[2];
+    PMG_TRY_M(fetch_scalars(h, 1));
+    const double res0tol = h[0];
+    PMG_TRY_M(upload_tail32(maxit, omega, tol));
+    int cycles = 0, converged = 0, inner_total = 0;
+    double ratio = 0.0;
+    const LevelK<double> &L = K[0];
+    const dim3 g = grid3m(L.nx, L.ny, L.nz, launch[0]), bl(kBX, kBY, 1);
+    for (int cyc = 1; cyc <= n_vcycles; ++cyc) {
+        for (int q = 0; q < m->inner; ++q) PMG_TRY_M(vcycle32(maxit, omega, q == 0));
+        inner_total += m->inner;
+        const int pi = prof.begin(stream);
+        k_add_correction<<<g, bl, 0, stream>>>(L, sol, m->e[0]);
+        prof.end(pi, PC_ADDCORR, 1, 20.0 * (double)L.nx * L.ny * L.nz, stream);
+        count_launches(1);
+        PMG_TRY_M(outer_residual(sol, rsd, rhs, 1));
+        PMG_TRY_M(fetch_scalars(h, 2));
+        const double rsd_val = h[1];
+        ratio = std::sqrt(rsd_val / res0tol);
+        cycles = cyc;
+        if (rep && rep->history) {
+            rep->history[3 * (cyc - 1) + 0] = std::sqrt(rsd_val);
+            rep->history[3 * (cyc - 1) + 1] = std::sqrt(res0tol);
+            rep->history[3 * (cyc - 1) + 2] = ratio;
+        }
+        if (rep && rep->coarse_iterations) {
+            int ci = 0;
+            cudaMemcpy(&ci, d_iscal + 2, sizeof(int), cudaMemcpyDeviceToHost);
+            rep->coarse_iterations[cyc - 1] = ci;
+        }
+        if (!std::isfinite(rsd_val)) {
+            if (rep) {
+                rep->cycles = cycles;
+                rep->converged = 0;
+                rep->res0 = std::sqrt(res0tol);
+                rep->final_ratio = ratio;
+                rep->inner_cycles = inner_total;
+            }
+            set_error("residual norm is not finite");
+            return PMG_EDIVERGED;
+        }
+        if (ratio < tol) {
+            converged = 1;
+            break;
+        }
+    }
+    if (rep) {
+        rep->cycles = cycles;
+        rep->converged = converged;
+        rep->res0 = std::sqrt(res0tol);
+        rep->final_ratio = ratio;
+        rep->inner_cycles = inner_total;
+    }
+    return PMG_OK;
 }
 
 void Ctx::destroy_mixed()

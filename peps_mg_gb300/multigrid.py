@@ -46,6 +46,7 @@ class SolveReport:
     history: np.ndarray = dfield(repr=False)      # (cycles, 3): sqrt(rsd), sqrt(res0), ratio
     coarse_iterations: np.ndarray = dfield(repr=False)
     elapsed_ms: float = 0.0
+    inner_cycles: int = 0
 
     def log_lines(self):
         """The reference's per-cycle log lines (src/multigrid.f90:1972)."""
@@ -82,7 +83,8 @@ def _default_stream():
 
 class Multigrid:
     def __init__(self, mesh, number_of_levels, number_of_vcycles, aggregation_method="cgs", cga_level=0,
-                 cgpsa_level=(0, 0, 0), coarse_solver="rbgs", precision="fp64", stream=None):
+                 cgpsa_level=(0, 0, 0), coarse_solver="rbgs", precision="fp64", mixed_inner_cycles=0,
+                 stream=None):
         self._lib = _lib.load()
         (dxm, dxg, xg), (dym, dyg, yg), (dzm, dzg, zg) = [tuple(np.ascontiguousarray(a, dtype=np.float64)
                                                                for a in m) for m in mesh]
@@ -99,6 +101,7 @@ class Multigrid:
         cfg.cgpsa_level[:] = [int(v) for v in cgpsa_level]
         cfg.coarse_solver = _code(_COARSE, coarse_solver)
         cfg.precision = _code(_PREC, precision)
+        cfg.mixed_inner_cycles = int(mixed_inner_cycles)
         self.number_of_levels = cfg.number_of_levels
         self.number_of_vcycles = cfg.number_of_vcycles
         self.precision = cfg.precision
@@ -173,7 +176,7 @@ class Multigrid:
                                         float(omega_sor), ctypes.byref(rep))
         out = SolveReport(rep.cycles, bool(rep.converged), rep.res0, rep.final_ratio,
                           hist[:3 * rep.cycles].reshape(rep.cycles, 3).copy(), citers[:rep.cycles].copy(),
-                          rep.elapsed_ms)
+                          rep.elapsed_ms, rep.inner_cycles)
         if rc == _lib.PMG_EDIVERGED:
             err = _lib.PmgError(rc, "multigrid_solve_vcycle")
             err.report = out
@@ -231,6 +234,29 @@ class Multigrid:
 
     def sync(self):
         check(self._lib.pmg_sync(self._h), "sync")
+
+    # -- telemetry ----------------------------------------------------------------------------
+    def profile(self, enable=True):
+        """Enable (and reset) or disable CUDA-event timing of the finest-level launches."""
+        check(self._lib.pmg_profile(self._h, 1 if enable else 0), "profile")
+
+    def profile_read(self, kernel_class):
+        """(total_ms, launches, algorithmic bytes per launch) of a PROF_* kernel class."""
+        t, n, b = ctypes.c_double(), ctypes.c_longlong(), ctypes.c_double()
+        check(self._lib.pmg_profile_read(self._h, int(kernel_class), ctypes.byref(t), ctypes.byref(n),
+                                         ctypes.byref(b)), "profile_read")
+        return t.value, n.value, b.value
+
+
+PROF_CLASSES = {0: "smooth32", 1: "outer_residual64", 2: "resrestrict32", 3: "prolong32", 4: "add_correction64",
+                5: "tail32", 6: "smooth64", 7: "residual64", 8: "restrict64", 9: "prolong64", 10: "tail64"}
+
+
+def launch_count():
+    """Kernels launched by the library in this process so far."""
+    n = ctypes.c_longlong()
+    check(_lib.load().pmg_launch_count(ctypes.byref(n)), "launch_count")
+    return n.value
 
 
 def level_sizes(n, number_of_levels, aggregation_method="cgs", cga_level=0):

@@ -1,0 +1,95 @@
+"""Mixed precision (FP32 V-cycles inside FP64 defect correction) against the FP64 oracle.
+
+Both solvers stop at a relative residual of 1e-10 (FP64 norms), so their solutions
+agree to about that level times the conditioning of the discrete problem; the test
+bound on the solution is 1e-8 relative to max|u|, and the final FP64 residual ratio
+must be below the tolerance.
+"""
+import numpy as np
+import pytest
+
+torch = pytest.importorskip("torch")
+pytestmark = pytest.mark.gpu
+
+import peps_mg_gb300 as pmg  # noqa: E402
+from oracle import oracle as O  # noqa: E402
+from peps_mg_gb300 import problems  # noqa: E402
+from tests.helpers import from_dev, rel, to_dev  # noqa: E402
+
+SOL_TOL = 1e-8
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _need_gpu():
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+
+
+def oracle_solution(mesh, rhs, n_levels, method=0, cga=0, cs=0, maxit=2, omega=1.0, tol=1e-10):
+    n = tuple(len(m[0]) - 2 for m in mesh)
+    omg = O.OracleMG(mesh, n_levels, 100, method, cga, cs)
+    sol, rsd = O.field(*n), O.field(*n)
+    ncyc, hist, _ = omg.solve(sol, rsd, np.asfortranarray(rhs), maxit, tol, omega)
+    return sol, ncyc
+
+
+def mixed_solve(mesh, rhs, n_levels, inner=2, **kw):
+    with pmg.Multigrid(mesh, n_levels, 100, precision="mixed", mixed_inner_cycles=inner, **kw) as mg:
+        sol = torch.zeros(tuple(reversed(rhs.shape)), dtype=torch.float64, device="cuda")
+        rsd = torch.zeros_like(sol)
+        rep = mg.solve_vcycle(sol, rsd, to_dev(rhs), 2, 1e-10, 1.0)
+    return from_dev(sol), from_dev(rsd), rep
+
+
+@pytest.mark.parametrize("inner", [1, 2, 3])
+def test_mixed_sine_64(inner):
+    mesh, rhs, u = problems.sine(64)
+    ref, _ = oracle_solution(mesh, rhs, 4)
+    sol, rsd, rep = mixed_solve(mesh, rhs, 4, inner=inner)
+    assert rep.converged and rep.final_ratio < 1e-10
+    assert rep.inner_cycles == inner * rep.cycles
+    assert rel(sol, ref) < SOL_TOL
+    # the returned residual is the FP64 residual of the returned solution
+    c = O.matrix_create(mesh)
+    r = O.residual(c, np.asfortranarray(sol), np.asfortranarray(rhs))
+    assert rel(rsd, r) < 1e-6
+    assert np.sqrt(O.vv_dot(r, r)) / rep.res0 < 1e-10 * 1.01
+
+
+def test_mixed_gaussian_blobs_96():
+    mesh, rhs = problems.gaussian_blobs(96)
+    ref, _ = oracle_solution(mesh, rhs, 5)
+    sol, _, rep = mixed_solve(mesh, rhs, 5)
+    assert rep.converged
+    assert rel(sol, ref) < SOL_TOL
+
+
+@pytest.mark.parametrize("method,cga,cg3,cs", [("cga", 2, (0, 0, 0), "rbgs"), ("cgpsa", 0, (1, 2, 3), "rbgs"),
+                                               ("cgs", 0, (0, 0, 0), "cg")])
+def test_mixed_tanh_z(method, cga, cg3, cs):
+    mesh, rhs = problems.tanh_z(64)
+    ref, _ = oracle_solution(mesh, rhs, 5, cs=1 if cs == "cg" else 0)
+    sol, _, rep = mixed_solve(mesh, rhs, 5, aggregation_method=method, cga_level=cga, cgpsa_level=cg3,
+                              coarse_solver=cs)
+    assert rep.converged
+    assert rel(sol, ref) < SOL_TOL
+
+
+def test_mixed_host_buffers():
+    mesh, rhs, _ = problems.sine(32)
+    with pmg.Multigrid(mesh, 3, 50, precision="mixed") as mg:
+        hs, hr = pmg.geometry.field(32, 32, 32), pmg.geometry.field(32, 32, 32)
+        rep = mg.solve_vcycle(hs, hr, np.asfortranarray(rhs), 2, 1e-10, 1.0)
+        ds = torch.zeros((34,) * 3, dtype=torch.float64, device="cuda")
+        dr = torch.zeros_like(ds)
+        rep2 = mg.solve_vcycle(ds, dr, to_dev(rhs), 2, 1e-10, 1.0)
+    assert rep.converged and np.array_equal(hs, from_dev(ds)) and np.array_equal(rep.history, rep2.history)
+
+
+def test_mixed_faster_cycles_than_fp64_history():
+    """The mixed solver reaches the tolerance in no more FP64 residual evaluations than
+    the plain FP64 solver needs V-cycles (two FP32 cycles per correction)."""
+    mesh, rhs, _ = problems.sine(64)
+    _, ncyc = oracle_solution(mesh, rhs, 4)
+    _, _, rep = mixed_solve(mesh, rhs, 4, inner=2)
+    assert rep.cycles <= (ncyc + 1) // 2 + 1
