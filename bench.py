@@ -46,6 +46,8 @@ def parse():
     p.add_argument("--n", type=int, default=N_DEFAULT)
     p.add_argument("--inner", type=int, default=2, help="FP32 V-cycles per FP64 correction")
     p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--quick", action="store_true",
+                   help="time the mixed solve only (no FP64 comparison, e2e or CPU baseline); for profiling")
     return p.parse_args()
 
 
@@ -249,6 +251,13 @@ def run_ours(args):
         ms = float(t.item())
     rep = reps[-1]
     assert rep.converged and rep.final_ratio < TOL, "mixed solve did not converge"
+
+    if args.quick:
+        if rank == 0:
+            print(json.dumps({"metric": METRIC, "value": round(ms, 3), "unit": "ms", "quick": True,
+                              "kernels": {k: v for k, v in prof.items() if v[1]}, "gpu_launches": launches}))
+        mg.destroy()
+        return
 
     # error of the mixed solution against the plain FP64 solution
     mg64 = pmg.Multigrid(mesh, nl, 100, "cgs", precision="fp64", stream=stream.cuda_stream)
