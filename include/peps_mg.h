@@ -159,6 +159,11 @@ int pmg_profile_read(pmg_ctx *ctx, int kernel_class, double *total_ms, long long
 /* Kernels launched by this library so far (all contexts of the process). */
 int pmg_launch_count(long long *count);
 
+/* Self-test of the integer-pipe conversions used by the mixed-precision outer kernels
+ * (no counterpart in the reference): out32[q] = (float)in64[q] rounded to nearest even,
+ * out64[q] = (double)in32[q]; device pointers, synchronous. */
+int pmg_selftest_convert(const double *in64, float *out32, const float *in32, double *out64, int n);
+
 /* Wait for all work issued on the context stream. */
 int pmg_sync(pmg_ctx *ctx);
 /* Text of the last CUDA error seen by this thread ("" if none). */

@@ -59,6 +59,7 @@ _SIGS = {
     "pmg_profile_read": [c_void_p, c_int, ctypes.POINTER(c_double), ctypes.POINTER(ctypes.c_longlong),
                          ctypes.POINTER(c_double)],
     "pmg_launch_count": [ctypes.POINTER(ctypes.c_longlong)],
+    "pmg_selftest_convert": [c_void_p, c_void_p, c_void_p, c_void_p, c_int],
     "pmg_sync": [c_void_p],
     "pmg_last_error": [],
     "pmg_status_string": [c_int],

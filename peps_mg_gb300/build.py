@@ -25,6 +25,7 @@ UNITS = {
     "pmg_api.cu": ["--fmad=false"],
     "pmg_f64.cu": ["--fmad=false"],
     "pmg_mixed.cu": ["--fmad=true"],
+    "pmg_smooth32.cu": ["--fmad=true"],
 }
 
 

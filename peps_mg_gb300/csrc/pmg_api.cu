@@ -560,8 +560,22 @@ int Ctx::upload_tail(int l0, int maxit, double omega, double tol)
         D.b[l] = lv[l].b;
         D.r[l] = lv[l].r;
     }
+    fill_coarse64(D.C64, D.cx64, D.cb64, D.cp64, D.cap64, D.crr64, D.omega64, D.omw64, omega);
     PMG_CUDA(cudaMemcpyAsync(d_tail, &D, sizeof(D), cudaMemcpyHostToDevice, stream), "tail descriptor upload");
     return PMG_OK;
+}
+
+void Ctx::fill_coarse64(LevelK<double> &C, double *&x, double *&b, double *&p, double *&ap, double *&rr, double &om,
+                        double &omw, double omega) const
+{
+    C = K[nl];
+    x = lv[nl].x;
+    b = lv[nl].b;
+    p = d_cp;
+    ap = d_cap;
+    rr = d_crr;
+    om = omega;
+    omw = 1.0 - omega;
 }
 
 // Coarsest-level solve with the grid kernels (a coarsest level too large for one CTA).
@@ -1061,6 +1075,17 @@ int pmg_launch_count(long long *count)
     if (!count) return PMG_EINVAL;
     *count = pmg::launches_total();
     return PMG_OK;
+}
+
+int pmg_selftest_convert(const double *in64, float *out32, const float *in32, double *out64, int n)
+{
+    if (n < 0 || (n > 0 && (!in64 || !out32 || !in32 || !out64))) {
+        pmg::set_error("invalid conversion self-test arguments");
+        return PMG_EINVAL;
+    }
+    if (n == 0) return PMG_OK;
+    PMG_TRY(pmg::convert_selftest(in64, out32, in32, out64, n, nullptr));
+    return pmg::cuda_status(cudaDeviceSynchronize(), "conversion self-test");
 }
 
 int pmg_sync(pmg_ctx *ctx)

@@ -83,6 +83,8 @@ struct Ctx {
     int residual_norm(int l, double *r, const double *x, const double *b, int slot);
     int fetch_scalars(double *h, int n);
     int upload_tail(int l0, int maxit, double omega, double tol);
+    void fill_coarse64(LevelK<double> &C, double *&x, double *&b, double *&p, double *&ap, double *&rr, double &om,
+                       double &omw, double omega) const;
     int coarse_solve_grid(double tol, double omega, int *iters);
     int vcycle_f64(double *sol, double *rsd, const double *rhs, int maxit, double omega, double tol,
                    int *coarse_iters);

@@ -8,6 +8,7 @@
 #include <cuda_runtime.h>
 
 #include "pmg_internal.h"
+#include "pmg_tail64.cuh"
 
 namespace pmg {
 
@@ -218,120 +219,6 @@ __global__ void k_check_f64(const double *num, const double *den, double tol, in
 // correction and smoothing back up to l0.  Phases are separated by __syncthreads();
 // every cell is computed by the same per-cell functions as the grid kernels.
 // ------------------------------------------------------------------------------------
-__device__ void tail_zero(double *a, long long n)
-{
-    for (long long q = threadIdx.x; q < n; q += blockDim.x) a[q] = 0.0;
-}
-
-__device__ void tail_rbgs(const LevelK<double> &L, double *x, const double *b, int iters, double omega, double omw)
-{
-    const int hx = (L.nx + 1) / 2;
-    const long long nq = (long long)hx * L.ny * L.nz;
-    for (int it = 0; it < iters; ++it)
-        for (int colour = 0; colour < 2; ++colour) {
-            for (long long q = threadIdx.x; q < nq; q += blockDim.x) {
-                const int t = (int)(q % hx);
-                const long long rr = q / hx;
-                const int j = (int)(rr % L.ny) + 1, k = (int)(rr / L.ny) + 1;
-                const int i = 2 * t + 1 + ((j + k + colour) & 1);
-                if (i <= L.nx) x[lin(i, j, k, L.sy, L.sz)] = rbgs_cell_f64(L, x, b, i, j, k, omega, omw);
-            }
-            __syncthreads();
-        }
-}
-
-// r = b - A x; returns sum(r^2) over the block (fixed order) when NORM.
-template <bool NORM>
-__device__ double tail_residual(const LevelK<double> &L, double *r, const double *x, const double *b, double *sw)
-{
-    const long long n = (long long)L.nx * L.ny * L.nz;
-    double acc = 0.0;
-    for (long long q = threadIdx.x; q < n; q += blockDim.x) {
-        const int i = (int)(q % L.nx) + 1;
-        const long long rr = q / L.nx;
-        const int j = (int)(rr % L.ny) + 1, k = (int)(rr / L.ny) + 1;
-        const long long p = lin(i, j, k, L.sy, L.sz);
-        const double v = __dsub_rn(b[p], ax_cell_f64(L, x, i, j, k));
-        r[p] = v;
-        if (NORM) acc = __dadd_rn(acc, __dmul_rn(v, v));
-    }
-    __syncthreads();
-    if (NORM) return block_sum(acc, sw);
-    return 0.0;
-}
-
-__device__ double tail_dot(const LevelK<double> &L, const double *x, const double *y, double *sw)
-{
-    const long long n = (long long)L.nx * L.ny * L.nz;
-    double acc = 0.0;
-    for (long long q = threadIdx.x; q < n; q += blockDim.x) {
-        const int i = (int)(q % L.nx) + 1;
-        const long long rr = q / L.nx;
-        const int j = (int)(rr % L.ny) + 1, k = (int)(rr / L.ny) + 1;
-        const long long p = lin(i, j, k, L.sy, L.sz);
-        acc = __dadd_rn(acc, __dmul_rn(x[p], y[p]));
-    }
-    return block_sum(acc, sw);
-}
-
-__device__ void tail_mvmul(const LevelK<double> &L, double *y, const double *x)
-{
-    const long long n = (long long)L.nx * L.ny * L.nz;
-    for (long long q = threadIdx.x; q < n; q += blockDim.x) {
-        const int i = (int)(q % L.nx) + 1;
-        const long long rr = q / L.nx;
-        const int j = (int)(rr % L.ny) + 1, k = (int)(rr / L.ny) + 1;
-        y[lin(i, j, k, L.sy, L.sz)] = ax_cell_f64(L, x, i, j, k);
-    }
-    __syncthreads();
-}
-
-__device__ void tail_restrict(const XferK<double> &X, const double *vf, double *vc)
-{
-    const long long n = (long long)X.ncx * X.ncy * X.ncz;
-    for (long long q = threadIdx.x; q < n; q += blockDim.x) {
-        const int i = (int)(q % X.ncx) + 1;
-        const long long rr = q / X.ncx;
-        const int j = (int)(rr % X.ncy) + 1, k = (int)(rr / X.ncy) + 1;
-        vc[lin(i, j, k, X.csy, X.csz)] = restrict_cell_f64(X, vf, i, j, k);
-    }
-    __syncthreads();
-}
-
-__device__ void tail_prolong_add(const XferK<double> &X, const double *vc, double *vf)
-{
-    const long long n = (long long)X.ncx * X.ncy * X.ncz;
-    for (long long q = threadIdx.x; q < n; q += blockDim.x) {
-        const int i = (int)(q % X.ncx) + 1;
-        const long long rr = q / X.ncx;
-        const int j = (int)(rr % X.ncy) + 1, k = (int)(rr / X.ncy) + 1;
-        prolong_cell_f64<true>(X, vc, vf, i, j, k);
-    }
-    __syncthreads();
-}
-
-__device__ void tail_interior_op(const LevelK<double> &L, int op, double s, double *a, double *bb, const double *c,
-                                 const double *d)
-{
-    // op 0: a = c (copy); op 1: a += s c, bb -= s d; op 2: a = c + s a
-    const long long n = (long long)L.nx * L.ny * L.nz;
-    for (long long q = threadIdx.x; q < n; q += blockDim.x) {
-        const int i = (int)(q % L.nx) + 1;
-        const long long rr = q / L.nx;
-        const int j = (int)(rr % L.ny) + 1, k = (int)(rr / L.ny) + 1;
-        const long long p = lin(i, j, k, L.sy, L.sz);
-        if (op == 0) {
-            a[p] = c[p];
-        } else if (op == 1) {
-            a[p] = __dadd_rn(a[p], __dmul_rn(s, c[p]));
-            bb[p] = __dsub_rn(bb[p], __dmul_rn(s, d[p]));
-        } else {
-            a[p] = __dadd_rn(c[p], __dmul_rn(s, a[p]));
-        }
-    }
-    __syncthreads();
-}
-
 __global__ void __launch_bounds__(kTailThreads) k_tail_f64(const TailDesc<double> *__restrict__ Dp)
 {
     __shared__ double sw[kTailThreads / 32];
@@ -349,48 +236,8 @@ __global__ void __launch_bounds__(kTailThreads) k_tail_f64(const TailDesc<double
     }
     // coarsest level, src/multigrid.f90:1819-1851
     {
-        const LevelK<double> L = D.L[D.nl];
-        double *x = D.x[D.nl];
-        const double *b = D.b[D.nl];
-        tail_zero(x, (long long)L.sz * (L.nz + 2));
-        __syncthreads();
-        int iters = 0;
-        if ((long long)L.nx * L.ny * L.nz == 1) {
-            if (threadIdx.x == 0) {
-                const long long p = lin(1, 1, 1, L.sy, L.sz);
-                x[p] = __ddiv_rn(b[p], diag_f64(L, 1, 1, 1));
-            }
-            __syncthreads();
-        } else if (D.coarse_solver == 0) {
-            // rbgs_solver_poisson_matrix (src/rbgs_poisson_matrix.f90:69-171)
-            const double r0 = tail_residual<true>(L, D.rr, x, b, sw);
-            int it = 0;
-            for (it = 0; it < D.coarse_maxit; ++it) {
-                tail_rbgs(L, x, b, 1, omega, omw);
-                const double rn = tail_residual<true>(L, D.rr, x, b, sw);
-                if (sqrt(__ddiv_rn(rn, r0)) <= D.tol) break;
-            }
-            iters = it;
-        } else {
-            // cg_solver_poisson_matrix (src/cg_poisson_matrix.f90:80-138)
-            double *p = D.p, *ap = D.ap, *rsd = D.rr;
-            tail_residual<false>(L, rsd, x, b, sw);
-            tail_interior_op(L, 0, 0.0, p, nullptr, rsd, nullptr);
-            const double r0 = tail_dot(L, rsd, rsd, sw);
-            int it = 0;
-            for (it = 0; it < D.coarse_maxit; ++it) {
-                const double t1 = tail_dot(L, rsd, rsd, sw);
-                tail_mvmul(L, ap, p);
-                const double t2a = tail_dot(L, ap, p, sw);
-                const double alpha = __ddiv_rn(t1, t2a);
-                tail_interior_op(L, 1, alpha, x, rsd, p, ap);
-                const double t2 = tail_dot(L, rsd, rsd, sw);
-                if (sqrt(__ddiv_rn(t2, r0)) < D.tol) break;
-                const double beta = __ddiv_rn(t2, t1);
-                tail_interior_op(L, 2, beta, p, nullptr, rsd, nullptr);
-            }
-            iters = it;
-        }
+        const int iters = coarse_solve_f64(D.C64, D.cx64, D.cb64, D.cp64, D.cap64, D.crr64, D.coarse_solver,
+                                           D.coarse_maxit, D.tol, D.omega64, D.omw64, sw);
         if (threadIdx.x == 0 && D.iters_out) *D.iters_out = iters;
         __syncthreads();
     }

@@ -33,6 +33,10 @@ struct TailDesc {
     LevelK<T> L[kMaxLevels];
     XferK<T> X[kMaxLevels];       // X[l]: transfer between l and l+1
     T *x[kMaxLevels], *b[kMaxLevels], *r[kMaxLevels];
+    // The coarsest-level solve always runs in FP64 on the FP64 copy of that level.
+    LevelK<double> C64;
+    double *cx64, *cb64, *cp64, *cap64, *crr64;
+    double omega64, omw64;
 };
 
 // ---- FP64 (bitwise) launchers, pmg_f64.cu -------------------------------------
@@ -63,6 +67,15 @@ int f64_cg_update_p(const LevelK<double> &L, const Launch &ln, const double *bet
 // < tol (le=0); also records the iteration.
 int f64_check(const double *num, const double *den, double tol, int le, int iter, int *flag, int *iter_out,
               cudaStream_t s);
+
+// ---- FP32 fused smoother, pmg_smooth32.cu ----------------------------------------
+// One out-of-place red-black iteration e_out = RB(e_in) of a whole level (zero_in: e_in
+// is zero and is not read).  Needs the padded FP32 layout checked by rb32_fused_layout_ok.
+bool rb32_fused_layout_ok(const LevelK<float> &L, const void *e, const void *b);
+int rb32_fused(const LevelK<float> &L, const Launch &ln, const float *ein, float *eout, const float *b, float omega,
+               float omw, bool zero_in, cudaStream_t s);
+// Integer-pipe precision conversions used by the outer kernels (self-test hook).
+int convert_selftest(const double *in64, float *out32, const float *in32, double *out64, int n, cudaStream_t s);
 
 // Fixed launch shapes (shared with the host driver for partial-sum sizing).
 void grid_for_cells(const LevelK<double> &L, const Launch &ln, dim3 *grid, dim3 *block);

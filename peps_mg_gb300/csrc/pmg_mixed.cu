@@ -20,6 +20,7 @@
 #include <vector>
 
 #include "pmg_ctx.h"
+#include "pmg_tail64.cuh"
 
 namespace pmg {
 
@@ -211,31 +212,76 @@ __global__ void __launch_bounds__(kBX *kBY) k_prolong_add32(XferK<float> X, cons
 // ---------------------------------------------------------------------------------
 // FP64 outer kernels
 // ---------------------------------------------------------------------------------
-// r = b - A x in FP64 (FMA form: r = b + d x - sum c x_nb with d = -c0), stored both
-// as the FP64 residual and as the FP32 right-hand side of the inner system, with the
-// per-block sum of r^2.
-__global__ void __launch_bounds__(kBX *kBY) k_outer_residual(LevelK<double> L, const double *__restrict__ x,
+// Round-to-nearest-even double -> float, from the IEEE-754 encodings, on the integer
+// pipe (the FP64 pipe is the bottleneck of the outer kernels).  Results that are not
+// normal floats (zero, subnormal, overflow, NaN) use the hardware conversion.
+__device__ __forceinline__ float f64_to_f32_rn(double v)
+{
+    const unsigned long long bits = (unsigned long long)__double_as_longlong(v);
+    const int e = (int)((bits >> 52) & 0x7ff) - 1023;
+    if (e < -126 || e > 127) return __double2float_rn(v);
+    const unsigned long long m = bits & 0xFFFFFFFFFFFFFull;
+    const unsigned hi = (unsigned)(m >> 29);
+    const unsigned long long rem = m & 0x1FFFFFFFull;
+    unsigned f = ((unsigned)(e + 127) << 23) | hi;
+    if (rem > 0x10000000ull || (rem == 0x10000000ull && (hi & 1u))) f += 1u;   // carry may reach the exponent
+    f |= (unsigned)(bits >> 32) & 0x80000000u;
+    return __uint_as_float(f);
+}
+
+// Exact float -> double from the encodings (integer pipe); subnormal, Inf and NaN
+// inputs use the hardware conversion.
+__device__ __forceinline__ double f32_to_f64(float f)
+{
+    const unsigned u = __float_as_uint(f);
+    const unsigned e = (u >> 23) & 0xffu;
+    const unsigned long long sign = (unsigned long long)(u & 0x80000000u) << 32;
+    if (e == 0u) {
+        if ((u & 0x7fffffu) == 0u) return __longlong_as_double((long long)sign);
+        return (double)f;
+    }
+    if (e == 255u) return (double)f;
+    const unsigned long long bits = sign | ((unsigned long long)(e + 896u) << 52) |
+                                    ((unsigned long long)(u & 0x7fffffu) << 29);
+    return __longlong_as_double((long long)bits);
+}
+
+// r = b - A x in FP64 (FMA form: r = b + d x - sum c x_nb with d = -c0, the diagonal
+// from the per-axis sums dxx = cxm+cxp, dyy, dzz), stored both as the FP64 residual and
+// as the FP32 right-hand side of the inner system, with the per-block sum of r^2.
+// Each thread handles four cells of a row, 32 apart.
+constexpr int kOuterVec = 4;
+__global__ void __launch_bounds__(kBX *kBY) k_outer_residual(LevelK<double> L, const double *__restrict__ dyy,
+                                                             const double *__restrict__ dzz,
+                                                             const double *__restrict__ x,
                                                              const double *__restrict__ b, double *__restrict__ r,
-                                                             float *__restrict__ r32, double *partials)
+                                                             float *__restrict__ r32, int sy32, long long sz32,
+                                                             double *partials)
 {
     double acc = 0.0;
     for (int k = blockIdx.z + 1; k <= L.nz; k += gridDim.z) {
-        const double dz = L.czm[k] + L.czp[k];
+        const double dz = dzz[k];
         for (int j = blockIdx.y * blockDim.y + threadIdx.y + 1; j <= L.ny; j += gridDim.y * blockDim.y) {
-            const double dyz = (L.cym[j] + L.cyp[j]) + dz;
-            for (int i = blockIdx.x * blockDim.x + threadIdx.x + 1; i <= L.nx; i += gridDim.x * blockDim.x) {
-                const long long p = lin(i, j, k, L.sy, L.sz);
-                const double d = L.sx[i] + dyz;
-                double v = fma(d, x[p], b[p]);
-                v = fma(-L.cxm[i], x[p - 1], v);
-                v = fma(-L.cxp[i], x[p + 1], v);
-                v = fma(-L.cym[j], x[p - L.sy], v);
-                v = fma(-L.cyp[j], x[p + L.sy], v);
-                v = fma(-L.czm[k], x[p - L.sz], v);
-                v = fma(-L.czp[k], x[p + L.sz], v);
-                r[p] = v;
-                r32[p] = (float)v;
-                acc = fma(v, v, acc);
+            const double dyz = dyy[j] + dz;
+            for (int i0 = blockIdx.x * (blockDim.x * kOuterVec) + threadIdx.x + 1; i0 <= L.nx;
+                 i0 += gridDim.x * blockDim.x * kOuterVec) {
+#pragma unroll
+                for (int u = 0; u < kOuterVec; ++u) {
+                    const int i = i0 + u * kBX;
+                    if (i > L.nx) break;
+                    const long long p = lin(i, j, k, L.sy, L.sz);
+                    const double d = L.sx[i] + dyz;
+                    double v = fma(d, x[p], b[p]);
+                    v = fma(-L.cxm[i], x[p - 1], v);
+                    v = fma(-L.cxp[i], x[p + 1], v);
+                    v = fma(-L.cym[j], x[p - L.sy], v);
+                    v = fma(-L.cyp[j], x[p + L.sy], v);
+                    v = fma(-L.czm[k], x[p - L.sz], v);
+                    v = fma(-L.czp[k], x[p + L.sz], v);
+                    r[p] = v;
+                    r32[lin(i, j, k, sy32, sz32)] = f64_to_f32_rn(v);
+                    acc = fma(v, v, acc);
+                }
             }
         }
     }
@@ -246,14 +292,23 @@ __global__ void __launch_bounds__(kBX *kBY) k_outer_residual(LevelK<double> L, c
 
 // x = x + e (the FP64 correction)
 __global__ void __launch_bounds__(kBX *kBY) k_add_correction(LevelK<double> L, double *__restrict__ x,
-                                                             const float *__restrict__ e)
+                                                             const float *__restrict__ e, int sy32, long long sz32)
 {
     for (int k = blockIdx.z + 1; k <= L.nz; k += gridDim.z)
         for (int j = blockIdx.y * blockDim.y + threadIdx.y + 1; j <= L.ny; j += gridDim.y * blockDim.y)
             for (int i = blockIdx.x * blockDim.x + threadIdx.x + 1; i <= L.nx; i += gridDim.x * blockDim.x) {
                 const long long p = lin(i, j, k, L.sy, L.sz);
-                x[p] = x[p] + (double)e[p];
+                x[p] = x[p] + f32_to_f64(e[lin(i, j, k, sy32, sz32)]);
             }
+}
+
+// Test hook: convert n values with the integer-pipe conversions.
+__global__ void k_convert_test(const double *in64, float *out32, const float *in32, double *out64, int n)
+{
+    for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < n; q += gridDim.x * blockDim.x) {
+        out32[q] = f64_to_f32_rn(in64[q]);
+        out64[q] = f32_to_f64(in32[q]);
+    }
 }
 
 // ---------------------------------------------------------------------------------
@@ -296,28 +351,6 @@ __device__ void t32_sweeps(const LevelK<float> &L, float *x, const float *b, int
         }
 }
 
-__device__ double t32_residual_norm(const LevelK<float> &L, float *r, const float *x, const float *b, double *sw)
-{
-    double acc = 0.0;
-    for_cells(L.nx, L.ny, L.nz, [&](int i, int j, int k) {
-        const float v = resid32(L, x, b, i, j, k);
-        r[lin(i, j, k, L.sy, L.sz)] = v;
-        acc += (double)v * (double)v;
-    });
-    __syncthreads();
-    return block_sum(acc, sw);
-}
-
-__device__ double t32_dot(const LevelK<float> &L, const float *x, const float *y, double *sw)
-{
-    double acc = 0.0;
-    for_cells(L.nx, L.ny, L.nz, [&](int i, int j, int k) {
-        const long long p = lin(i, j, k, L.sy, L.sz);
-        acc += (double)x[p] * (double)y[p];
-    });
-    return block_sum(acc, sw);
-}
-
 __global__ void __launch_bounds__(kTail32Threads) k_tail32(const TailDesc<float> *__restrict__ Dp)
 {
     __shared__ double sw[kTail32Threads / 32];
@@ -334,65 +367,22 @@ __global__ void __launch_bounds__(kTail32Threads) k_tail32(const TailDesc<float>
         });
         __syncthreads();
     }
+    // coarsest level: solved in FP64 (b converted up, x converted down), so its
+    // convergence test against the FP64 tolerance is attainable
     {
         const LevelK<float> L = D.L[D.nl];
+        const LevelK<double> &C = D.C64;
         float *x = D.x[D.nl];
         const float *b = D.b[D.nl];
-        const long long tot = (long long)L.sz * (L.nz + 2);
-        for (long long q = threadIdx.x; q < tot; q += blockDim.x) x[q] = 0.f;
+        for_cells(L.nx, L.ny, L.nz, [&](int i, int j, int k) {
+            D.cb64[lin(i, j, k, C.sy, C.sz)] = (double)b[lin(i, j, k, L.sy, L.sz)];
+        });
         __syncthreads();
-        int iters = 0;
-        if ((long long)L.nx * L.ny * L.nz == 1) {
-            if (threadIdx.x == 0) {
-                const long long p = lin(1, 1, 1, L.sy, L.sz);
-                x[p] = b[p] / diag32(L, 1, 1, 1);
-            }
-            __syncthreads();
-        } else if (D.coarse_solver == 0) {
-            const double r0 = t32_residual_norm(L, D.rr, x, b, sw);
-            int it;
-            for (it = 0; it < D.coarse_maxit; ++it) {
-                t32_sweeps(L, x, b, 1, omega, omw, false);
-                const double rn = t32_residual_norm(L, D.rr, x, b, sw);
-                if (sqrt(rn / r0) <= D.tol) break;
-            }
-            iters = it;
-        } else {
-            float *p = D.p, *ap = D.ap, *rs = D.rr;
-            t32_residual_norm(L, rs, x, b, sw);
-            for_cells(L.nx, L.ny, L.nz, [&](int i, int j, int k) {
-                const long long q = lin(i, j, k, L.sy, L.sz);
-                p[q] = rs[q];
-            });
-            __syncthreads();
-            const double r0 = t32_dot(L, rs, rs, sw);
-            int it;
-            for (it = 0; it < D.coarse_maxit; ++it) {
-                const double t1 = t32_dot(L, rs, rs, sw);
-                for_cells(L.nx, L.ny, L.nz, [&](int i, int j, int k) {
-                    const long long q = lin(i, j, k, L.sy, L.sz);
-                    ap[q] = fmaf(diag32(L, i, j, k), p[q], nbsum32(L, p, q, i, j, k));
-                });
-                __syncthreads();
-                const double t2a = t32_dot(L, ap, p, sw);
-                const float alpha = (float)(t1 / t2a);
-                for_cells(L.nx, L.ny, L.nz, [&](int i, int j, int k) {
-                    const long long q = lin(i, j, k, L.sy, L.sz);
-                    x[q] = fmaf(alpha, p[q], x[q]);
-                    rs[q] = fmaf(-alpha, ap[q], rs[q]);
-                });
-                __syncthreads();
-                const double t2 = t32_dot(L, rs, rs, sw);
-                if (sqrt(t2 / r0) < D.tol) break;
-                const float beta = (float)(t2 / t1);
-                for_cells(L.nx, L.ny, L.nz, [&](int i, int j, int k) {
-                    const long long q = lin(i, j, k, L.sy, L.sz);
-                    p[q] = fmaf(beta, p[q], rs[q]);
-                });
-                __syncthreads();
-            }
-            iters = it;
-        }
+        const int iters = coarse_solve_f64(C, D.cx64, D.cb64, D.cp64, D.cap64, D.crr64, D.coarse_solver,
+                                           D.coarse_maxit, D.tol, D.omega64, D.omw64, sw);
+        for_cells(L.nx, L.ny, L.nz, [&](int i, int j, int k) {
+            x[lin(i, j, k, L.sy, L.sz)] = (float)D.cx64[lin(i, j, k, C.sy, C.sz)];
+        });
         if (threadIdx.x == 0 && D.iters_out) *D.iters_out = iters;
         __syncthreads();
     }
@@ -421,23 +411,26 @@ dim3 grid3m(int nxt, int ny, int nz, const Launch &ln)
 struct MixedState {
     std::vector<float> tables_host;
     float *tables = nullptr;
+    double *diag64 = nullptr;        // per level: dyy (ny+2) and dzz (nz+2) for the outer residual
+    std::vector<const double *> dyy, dzz;
     std::vector<LevelK<float>> K;
     std::vector<XferK<float>> X;
-    std::vector<float *> e, b;       // e[l], b[l]; b[0] is the FP32 outer residual
-    float *cp = nullptr, *cap = nullptr, *crr = nullptr;
+    std::vector<float *> alloc;      // raw allocations
+    std::vector<float *> e[2], b;    // e[buf][l] (two buffers for out-of-place sweeps), b[l]
+    std::vector<int> cur;            // current buffer of e at each level
+    std::vector<bool> fused;         // level uses the fused out-of-place smoother
     TailDesc<float> tail_host;
     TailDesc<float> *d_tail = nullptr;
     int inner = 2;
     ~MixedState()
     {
         cudaFree(tables);
-        for (auto p : e) cudaFree(p);
-        for (auto p : b) cudaFree(p);
-        cudaFree(cp);
-        cudaFree(cap);
-        cudaFree(crr);
+        cudaFree(diag64);
+        for (auto p : alloc) cudaFree(p);
         cudaFree(d_tail);
     }
+    float *E(int l) const { return e[cur[l]][l]; }
+    float *Eother(int l) const { return e[1 - cur[l]][l]; }
 };
 
 #define PMG_TRY_M(expr)                \
@@ -447,6 +440,25 @@ struct MixedState {
     } while (0)
 
 static int mstatus(cudaError_t e, const char *what) { return cuda_status(e, what); }
+
+// FP32 arrays: row pitch a multiple of 4 floats with room for the fused smoother's
+// aligned 16-byte copies (columns -3 .. pitch-4), data pointer = allocation + 3 so that
+// column 1 is 16-byte aligned.
+static int alloc_f32(MixedState *m, int nx, int ny, int nz, int *pitch, long long *plane, float **data)
+{
+    const int tiles = (nx + 63) / 64;
+    const int p = 64 * tiles + 8;
+    const long long pl = (long long)p * (ny + 2);
+    const size_t n = (size_t)pl * (size_t)(nz + 2) + 8;
+    float *a = nullptr;
+    PMG_TRY_M(mstatus(cudaMalloc(&a, n * sizeof(float)), "mixed level allocation"));
+    PMG_TRY_M(mstatus(cudaMemset(a, 0, n * sizeof(float)), "mixed level init"));
+    m->alloc.push_back(a);
+    *pitch = p;
+    *plane = pl;
+    *data = a + 3;
+    return PMG_OK;
+}
 
 int Ctx::setup_mixed()
 {
@@ -465,38 +477,51 @@ int Ctx::setup_mixed()
     PMG_TRY_M(mstatus(cudaMemcpy(m->tables, m->tables_host.data(), m->tables_host.size() * sizeof(float),
                                  cudaMemcpyHostToDevice),
                       "mixed tables"));
+    // FP64 per-axis diagonal sums of the finest level (outer residual)
+    {
+        const Level &S = lv[0];
+        std::vector<double> h((size_t)S.n[1] + 2 + (size_t)S.n[2] + 2, 0.0);
+        for (int j = 1; j <= S.n[1]; ++j) h[j] = 1.0 / (S.dm[1][j] * S.dg[1][j]) + 1.0 / (S.dm[1][j] * S.dg[1][j + 1]);
+        for (int k = 1; k <= S.n[2]; ++k)
+            h[S.n[1] + 2 + k] = 1.0 / (S.dm[2][k] * S.dg[2][k]) + 1.0 / (S.dm[2][k] * S.dg[2][k + 1]);
+        PMG_TRY_M(mstatus(cudaMalloc(&m->diag64, h.size() * sizeof(double)), "mixed tables"));
+        PMG_TRY_M(mstatus(cudaMemcpy(m->diag64, h.data(), h.size() * sizeof(double), cudaMemcpyHostToDevice),
+                          "mixed tables"));
+        m->dyy.push_back(m->diag64);
+        m->dzz.push_back(m->diag64 + S.n[1] + 2);
+    }
     auto F = [&](const double *p) { return (const float *)(m->tables + (p - d_tables)); };
     m->K.resize((size_t)nl + 1);
     m->X.resize((size_t)nl);
+    m->e[0].assign((size_t)nl + 1, nullptr);
+    m->e[1].assign((size_t)nl + 1, nullptr);
+    m->b.assign((size_t)nl + 1, nullptr);
+    m->cur.assign((size_t)nl + 1, 0);
+    m->fused.assign((size_t)nl + 1, false);
     for (int l = 0; l <= nl; ++l) {
         const LevelK<double> &k = K[l];
         LevelK<float> &f = m->K[l];
-        f.nx = k.nx; f.ny = k.ny; f.nz = k.nz; f.sy = k.sy; f.sz = k.sz;
+        int pitch = 0;
+        long long plane = 0;
+        PMG_TRY_M(alloc_f32(m, k.nx, k.ny, k.nz, &pitch, &plane, &m->e[0][l]));
+        PMG_TRY_M(alloc_f32(m, k.nx, k.ny, k.nz, &pitch, &plane, &m->e[1][l]));
+        PMG_TRY_M(alloc_f32(m, k.nx, k.ny, k.nz, &pitch, &plane, &m->b[l]));
+        f.nx = k.nx; f.ny = k.ny; f.nz = k.nz; f.sy = pitch; f.sz = plane;
         f.cxm = F(k.cxm); f.cxp = F(k.cxp); f.sx = F(k.sx);
         f.cym = F(k.cym); f.cyp = F(k.cyp); f.czm = F(k.czm); f.czp = F(k.czp);
-        if (l < nl) {
-            const XferK<double> &x = X[l];
-            XferK<float> &y = m->X[l];
-            y.ncx = x.ncx; y.ncy = x.ncy; y.ncz = x.ncz; y.csy = x.csy; y.csz = x.csz;
-            y.fsy = x.fsy; y.fsz = x.fsz; y.stx = x.stx; y.sty = x.sty; y.stz = x.stz;
-            y.wx = F(x.wx); y.wy = F(x.wy); y.wz = F(x.wz);
-            y.pxp = F(x.pxp); y.pxn = F(x.pxn); y.pyp = F(x.pyp); y.pyn = F(x.pyn);
-            y.pzp = F(x.pzp); y.pzn = F(x.pzn);
-        }
+        m->fused[l] = l < tail_l0 && rb32_fused_layout_ok(f, m->e[0][l], m->b[l]) &&
+                      rb32_fused_layout_ok(f, m->e[1][l], m->b[l]);
     }
-    m->e.assign((size_t)nl + 1, nullptr);
-    m->b.assign((size_t)nl + 1, nullptr);
-    for (int l = 0; l <= nl; ++l) {
-        const size_t bytes = lv[l].total * sizeof(float);
-        PMG_TRY_M(mstatus(cudaMalloc(&m->e[l], bytes), "mixed level allocation"));
-        PMG_TRY_M(mstatus(cudaMalloc(&m->b[l], bytes), "mixed level allocation"));
-        PMG_TRY_M(mstatus(cudaMemset(m->e[l], 0, bytes), "mixed level init"));
-        PMG_TRY_M(mstatus(cudaMemset(m->b[l], 0, bytes), "mixed level init"));
-    }
-    const size_t cb = lv[nl].total * sizeof(float);
-    for (float **p : {&m->cp, &m->cap, &m->crr}) {
-        PMG_TRY_M(mstatus(cudaMalloc(p, cb), "mixed coarse scratch"));
-        PMG_TRY_M(mstatus(cudaMemset(*p, 0, cb), "mixed coarse scratch"));
+    for (int l = 0; l < nl; ++l) {
+        const XferK<double> &x = X[l];
+        XferK<float> &y = m->X[l];
+        y.ncx = x.ncx; y.ncy = x.ncy; y.ncz = x.ncz;
+        y.csy = m->K[l + 1].sy; y.csz = m->K[l + 1].sz;
+        y.fsy = m->K[l].sy; y.fsz = m->K[l].sz;
+        y.stx = x.stx; y.sty = x.sty; y.stz = x.stz;
+        y.wx = F(x.wx); y.wy = F(x.wy); y.wz = F(x.wz);
+        y.pxp = F(x.pxp); y.pxn = F(x.pxn); y.pyp = F(x.pyp); y.pyn = F(x.pyn);
+        y.pzp = F(x.pzp); y.pzn = F(x.pzn);
     }
     PMG_TRY_M(mstatus(cudaMalloc(&m->d_tail, sizeof(TailDesc<float>)), "mixed tail descriptor"));
     return PMG_OK;
@@ -515,17 +540,15 @@ int Ctx::upload_tail32(int maxit, double omega, double tol)
     D.omega = (float)omega;
     D.omw = (float)(1.0 - omega);
     D.tol = tol;
-    D.p = m->cp;
-    D.ap = m->cap;
-    D.rr = m->crr;
     D.iters_out = d_iscal + 2;
     for (int l = 0; l <= nl; ++l) {
         D.L[l] = m->K[l];
         if (l < nl) D.X[l] = m->X[l];
-        D.x[l] = m->e[l];
+        D.x[l] = m->e[0][l];   // the tail works in place on buffer 0
         D.b[l] = m->b[l];
         D.r[l] = nullptr;
     }
+    fill_coarse64(D.C64, D.cx64, D.cb64, D.cp64, D.cap64, D.crr64, D.omega64, D.omw64, omega);
     return mstatus(cudaMemcpyAsync(m->d_tail, &D, sizeof(D), cudaMemcpyHostToDevice, stream), "tail upload");
 }
 
@@ -537,34 +560,43 @@ int Ctx::vcycle32(int maxit, double omega, bool zero_start)
     const dim3 bl(kBX, kBY, 1);
     const double N = (double)m->K[0].nx * m->K[0].ny * m->K[0].nz;
     long long nlaunch = 0;
-    auto sweeps = [&](int l, bool zs) {
+    auto sweeps = [&](int l, bool zs) -> int {
         const LevelK<float> &L = m->K[l];
-        const dim3 gc = grid3m((L.nx + 1) / 2, L.ny, L.nz, launch[l]), gf = grid3m(L.nx, L.ny, L.nz, launch[l]);
         const int pi = l == 0 ? prof.begin(stream) : -1;
-        for (int it = 0; it < maxit; ++it)
-            for (int c = 0; c < 2; ++c) {
-                if (zs && it == 0 && c == 0)
-                    k_rbgs32<true><<<gf, bl, 0, stream>>>(L, m->e[l], m->b[l], om, omw, c);
-                else
-                    k_rbgs32<false><<<gc, bl, 0, stream>>>(L, m->e[l], m->b[l], om, omw, c);
-                ++nlaunch;
+        if (m->fused[l]) {
+            for (int it = 0; it < maxit; ++it) {
+                PMG_TRY_M(rb32_fused(L, launch[l], m->E(l), m->Eother(l), m->b[l], om, omw, zs && it == 0, stream));
+                m->cur[l] = 1 - m->cur[l];
             }
-        prof.end(pi, PC_SMOOTH32, 2 * maxit, 8.0 * N, stream);
-        if (zs && maxit == 0) cudaMemsetAsync(m->e[l], 0, lv[l].total * sizeof(float), stream);
+            prof.end(pi, PC_SMOOTH32, maxit, 12.0 * N, stream);
+        } else {
+            const dim3 gc = grid3m((L.nx + 1) / 2, L.ny, L.nz, launch[l]), gf = grid3m(L.nx, L.ny, L.nz, launch[l]);
+            for (int it = 0; it < maxit; ++it)
+                for (int c = 0; c < 2; ++c) {
+                    if (zs && it == 0 && c == 0)
+                        k_rbgs32<true><<<gf, bl, 0, stream>>>(L, m->E(l), m->b[l], om, omw, c);
+                    else
+                        k_rbgs32<false><<<gc, bl, 0, stream>>>(L, m->E(l), m->b[l], om, omw, c);
+                    ++nlaunch;
+                }
+            prof.end(pi, PC_SMOOTH32, 2 * maxit, 8.0 * N, stream);
+        }
+        if (zs && maxit == 0) cudaMemsetAsync(m->E(l) - 3, 0, (size_t)(L.sz * (L.nz + 2) + 8) * sizeof(float), stream);
+        return PMG_OK;
     };
-    sweeps(0, zero_start);
+    PMG_TRY_M(sweeps(0, zero_start));
     {
         const XferK<float> &X0 = m->X[0];
         const int pi = prof.begin(stream);
-        k_resrestrict32<<<grid3m(X0.ncx, X0.ncy, X0.ncz, launch[1]), bl, 0, stream>>>(m->K[0], X0, m->e[0], m->b[0],
+        k_resrestrict32<<<grid3m(X0.ncx, X0.ncy, X0.ncz, launch[1]), bl, 0, stream>>>(m->K[0], X0, m->E(0), m->b[0],
                                                                                      m->b[1]);
         prof.end(pi, PC_RESRESTRICT32, 1, 8.5 * N, stream);
         ++nlaunch;
     }
     for (int l = 1; l < tail_l0; ++l) {
-        sweeps(l, true);
+        PMG_TRY_M(sweeps(l, true));
         const XferK<float> &Xl = m->X[l];
-        k_resrestrict32<<<grid3m(Xl.ncx, Xl.ncy, Xl.ncz, launch[l + 1]), bl, 0, stream>>>(m->K[l], Xl, m->e[l],
+        k_resrestrict32<<<grid3m(Xl.ncx, Xl.ncy, Xl.ncz, launch[l + 1]), bl, 0, stream>>>(m->K[l], Xl, m->E(l),
                                                                                          m->b[l], m->b[l + 1]);
         ++nlaunch;
     }
@@ -577,10 +609,10 @@ int Ctx::vcycle32(int maxit, double omega, bool zero_start)
     for (int l = tail_l0 - 1; l >= 0; --l) {
         const XferK<float> &Xl = m->X[l];
         const int pi = l == 0 ? prof.begin(stream) : -1;
-        k_prolong_add32<<<grid3m(Xl.ncx, Xl.ncy, Xl.ncz, launch[l + 1]), bl, 0, stream>>>(Xl, m->e[l + 1], m->e[l]);
+        k_prolong_add32<<<grid3m(Xl.ncx, Xl.ncy, Xl.ncz, launch[l + 1]), bl, 0, stream>>>(Xl, m->E(l + 1), m->E(l));
         prof.end(pi, PC_PROLONG32, 1, 8.5 * N, stream);
         ++nlaunch;
-        sweeps(l, false);
+        PMG_TRY_M(sweeps(l, false));
     }
     count_launches(nlaunch);
     return cuda_status(cudaGetLastError(), "fp32 v-cycle");
@@ -589,9 +621,10 @@ int Ctx::vcycle32(int maxit, double omega, bool zero_start)
 int Ctx::outer_residual(double *sol, double *rsd, const double *rhs, int slot)
 {
     const LevelK<double> &L = K[0];
-    const dim3 g = grid3m(L.nx, L.ny, L.nz, launch[0]), bl(kBX, kBY, 1);
+    const dim3 g = grid3m((L.nx + kOuterVec - 1) / kOuterVec, L.ny, L.nz, launch[0]), bl(kBX, kBY, 1);
     const int pi = prof.begin(stream);
-    k_outer_residual<<<g, bl, 0, stream>>>(L, sol, rhs, rsd, mixed->b[0], d_partials);
+    k_outer_residual<<<g, bl, 0, stream>>>(L, mixed->dyy[0], mixed->dzz[0], sol, rhs, rsd, mixed->b[0],
+                                           mixed->K[0].sy, mixed->K[0].sz, d_partials);
     prof.end(pi, PC_OUTER_RES, 1, 28.0 * (double)L.nx * L.ny * L.nz, stream);
     count_launches(1);
     PMG_TRY_M(cuda_status(cudaGetLastError(), "outer residual"));
@@ -618,7 +651,7 @@ int Ctx::solve_mixed(double *sol, double *rsd, const double *rhs, int maxit, dou
         for (int q = 0; q < m->inner; ++q) PMG_TRY_M(vcycle32(maxit, omega, q == 0));
         inner_total += m->inner;
         const int pi = prof.begin(stream);
-        k_add_correction<<<g, bl, 0, stream>>>(L, sol, m->e[0]);
+        k_add_correction<<<g, bl, 0, stream>>>(L, sol, m->E(0), m->K[0].sy, m->K[0].sz);
         prof.end(pi, PC_ADDCORR, 1, 20.0 * (double)L.nx * L.ny * L.nz, stream);
         count_launches(1);
         PMG_TRY_M(outer_residual(sol, rsd, rhs, 1));
@@ -660,6 +693,13 @@ int Ctx::solve_mixed(double *sol, double *rsd, const double *rhs, int maxit, dou
         rep->inner_cycles = inner_total;
     }
     return PMG_OK;
+}
+
+int convert_selftest(const double *in64, float *out32, const float *in32, double *out64, int n, cudaStream_t s)
+{
+    k_convert_test<<<std::max(1, std::min((n + 255) / 256, 4096)), 256, 0, s>>>(in64, out32, in32, out64, n);
+    count_launches(1);
+    return cuda_status(cudaGetLastError(), "conversion self-test");
 }
 
 void Ctx::destroy_mixed()
