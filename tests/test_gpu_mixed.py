@@ -97,7 +97,7 @@ def test_mixed_faster_cycles_than_fp64_history():
     assert rep.cycles <= (ncyc + 1) // 2 + 1
 
 
-@pytest.mark.parametrize("n3,levels", [((100, 36, 20), 2), ((72, 40, 24), 3), ((130, 66, 34), 1 + 1)])
+@pytest.mark.parametrize("n3,levels", [((100, 36, 20), 2), ((72, 40, 24), 3), ((130, 68, 36), 2)])
 def test_mixed_uneven_tiles(n3, levels):
     """Sizes that are not multiples of the fused smoother's 64 x 16 tile, odd sizes at the
     coarse levels, a stretched mesh and a non-zero Dirichlet face."""
