@@ -236,9 +236,11 @@ def run_ours(args):
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
     barrier()
+    torch.cuda.nvtx.range_push("timed")
     e0.record(stream)
     reps = [step() for _ in range(args.steps)]
     e1.record(stream)
+    torch.cuda.nvtx.range_pop()
     barrier()
     launches = pmg.launch_count() - l0
     ms = e0.elapsed_time(e1) / args.steps

@@ -455,6 +455,13 @@ int Ctx::build(const pmg_config_t *c, cudaStream_t s)
     }
     // A level too large for one CTA is kept on the grid kernels.
     while (tail_l0 <= nl && lv[tail_l0].total > kTailMaxCells) ++tail_l0;
+    // Tail block size: about two cells per thread at the largest tail level (barriers of
+    // a 1024-thread CTA dominate the coarsest solve of a few cells).
+    {
+        long long cells = 1;
+        for (int l = tail_l0; l <= nl; ++l) cells = std::max(cells, (long long)lv[l].n[0] * lv[l].n[1] * lv[l].n[2]);
+        tail_threads = (int)std::min<long long>(1024, std::max<long long>(64, ((cells / 2 + 31) / 32) * 32));
+    }
 
     // ---- device arrays -------------------------------------------------------------
     size_t max_part = 1;
@@ -611,7 +618,7 @@ int Ctx::vcycle_f64(double *sol, double *rsd, const double *rhs, int maxit, doub
     }
     if (tail_l0 <= nl) {
         pi = prof.begin(stream);
-        PMG_TRY(f64_tail(d_tail, stream));
+        PMG_TRY(f64_tail(d_tail, tail_threads, stream));
         prof.end(pi, PC_TAIL64, 1, 0.0, stream);
         if (coarse_iters) {
             int h = 0;

@@ -62,6 +62,7 @@ struct Ctx {
     std::vector<XferK<double>> X;
     std::vector<Launch> launch;
     int tail_l0 = 0;
+    int tail_threads = 1024;   // block size of the single-CTA tail kernels
     TailDesc<double> tail_host;
     TailDesc<double> *d_tail = nullptr;
     double *d_partials = nullptr;

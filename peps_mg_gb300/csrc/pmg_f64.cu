@@ -351,9 +351,9 @@ int zero_ghosts_f64(double *a, int nx, int ny, int nz, cudaStream_t s)
     return cuda_status(cudaGetLastError(), "zero ghosts");
 }
 
-int f64_tail(const TailDesc<double> *dev_desc, cudaStream_t s)
+int f64_tail(const TailDesc<double> *dev_desc, int threads, cudaStream_t s)
 {
-    k_tail_f64<<<1, kTailThreads, 0, s>>>(dev_desc);
+    k_tail_f64<<<1, threads, 0, s>>>(dev_desc);
     count_launches(1);
     return cuda_status(cudaGetLastError(), "coarse tail");
 }

@@ -55,7 +55,7 @@ int f64_restrict(const XferK<double> &X, const Launch &ln, const double *vf, dou
 int f64_prolong(const XferK<double> &X, const Launch &ln, const double *vc, double *vf, bool add,
                 cudaStream_t s);
 int zero_ghosts_f64(double *a, int nx, int ny, int nz, cudaStream_t s);
-int f64_tail(const TailDesc<double> *dev_desc, cudaStream_t s);
+int f64_tail(const TailDesc<double> *dev_desc, int threads, cudaStream_t s);
 // CG building blocks on device scalars (src/cg_poisson_matrix.f90:99-138)
 int f64_copy_interior(const LevelK<double> &L, double *dst, const double *src, cudaStream_t s);
 int f64_cg_scalar(const double *num, const double *den, double *out, cudaStream_t s);
@@ -72,8 +72,13 @@ int f64_check(const double *num, const double *den, double tol, int le, int iter
 // One out-of-place red-black iteration e_out = RB(e_in) of a whole level (zero_in: e_in
 // is zero and is not read).  Needs the padded FP32 layout checked by rb32_fused_layout_ok.
 bool rb32_fused_layout_ok(const LevelK<float> &L, const void *e, const void *b);
+// variant: 0 = 64 x 16 tiles, 1 = 64 x 8, 2 = 64 x 12; kchunk: planes per work item
+// (0 = automatic).
 int rb32_fused(const LevelK<float> &L, const Launch &ln, const float *ein, float *eout, const float *b, float omega,
-               float omw, bool zero_in, cudaStream_t s);
+               float omw, bool zero_in, cudaStream_t s, int variant = 0, int kchunk = 0);
+// Picks the fastest tile variant and k-chunk for a level (process-wide cache).
+int tune_smoother(const LevelK<float> &L, const Launch &ln, float *e0, float *e1, const float *b, cudaStream_t s,
+                  int *variant, int *kchunk);
 // Integer-pipe precision conversions used by the outer kernels (self-test hook).
 int convert_selftest(const double *in64, float *out32, const float *in32, double *out64, int n, cudaStream_t s);
 

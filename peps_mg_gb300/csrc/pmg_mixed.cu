@@ -419,6 +419,7 @@ struct MixedState {
     std::vector<float *> e[2], b;    // e[buf][l] (two buffers for out-of-place sweeps), b[l]
     std::vector<int> cur;            // current buffer of e at each level
     std::vector<bool> fused;         // level uses the fused out-of-place smoother
+    std::vector<int> variant, kchunk;  // autotuned tile variant and k-chunk of the fused smoother
     TailDesc<float> tail_host;
     TailDesc<float> *d_tail = nullptr;
     int inner = 2;
@@ -498,6 +499,8 @@ int Ctx::setup_mixed()
     m->b.assign((size_t)nl + 1, nullptr);
     m->cur.assign((size_t)nl + 1, 0);
     m->fused.assign((size_t)nl + 1, false);
+    m->variant.assign((size_t)nl + 1, 0);
+    m->kchunk.assign((size_t)nl + 1, 0);
     for (int l = 0; l <= nl; ++l) {
         const LevelK<double> &k = K[l];
         LevelK<float> &f = m->K[l];
@@ -524,6 +527,9 @@ int Ctx::setup_mixed()
         y.pzp = F(x.pzp); y.pzn = F(x.pzn);
     }
     PMG_TRY_M(mstatus(cudaMalloc(&m->d_tail, sizeof(TailDesc<float>)), "mixed tail descriptor"));
+    for (int l = 0; l < tail_l0; ++l)
+        if (m->fused[l]) PMG_TRY_M(tune_smoother(m->K[l], launch[l], m->e[0][l], m->e[1][l], m->b[l], stream,
+                                                 &m->variant[l], &m->kchunk[l]));
     return PMG_OK;
 }
 
@@ -565,7 +571,8 @@ int Ctx::vcycle32(int maxit, double omega, bool zero_start)
         const int pi = l == 0 ? prof.begin(stream) : -1;
         if (m->fused[l]) {
             for (int it = 0; it < maxit; ++it) {
-                PMG_TRY_M(rb32_fused(L, launch[l], m->E(l), m->Eother(l), m->b[l], om, omw, zs && it == 0, stream));
+                PMG_TRY_M(rb32_fused(L, launch[l], m->E(l), m->Eother(l), m->b[l], om, omw, zs && it == 0, stream,
+                                     m->variant[l], m->kchunk[l]));
                 m->cur[l] = 1 - m->cur[l];
             }
             prof.end(pi, PC_SMOOTH32, maxit, 12.0 * N, stream);
@@ -602,7 +609,7 @@ int Ctx::vcycle32(int maxit, double omega, bool zero_start)
     }
     {
         const int pi = prof.begin(stream);
-        k_tail32<<<1, kTail32Threads, 0, stream>>>(m->d_tail);
+        k_tail32<<<1, tail_threads, 0, stream>>>(m->d_tail);
         prof.end(pi, PC_TAIL32, 1, 0.0, stream);
         ++nlaunch;
     }

@@ -33,37 +33,47 @@ __device__ void tail_rbgs(const LevelK<double> &L, double *x, const double *b, i
 }
 
 // r = b - A x; returns sum(r^2) over the block (fixed order) when NORM.
-template <bool NORM>
-__device__ double tail_residual(const LevelK<double> &L, double *r, const double *x, const double *b, double *sw)
-{
-    const long long n = (long long)L.nx * L.ny * L.nz;
-    double acc = 0.0;
-    for (long long q = threadIdx.x; q < n; q += blockDim.x) {
-        const int i = (int)(q % L.nx) + 1;
-        const long long rr = q / L.nx;
-        const int j = (int)(rr % L.ny) + 1, k = (int)(rr / L.ny) + 1;
-        const long long p = lin(i, j, k, L.sy, L.sz);
-        const double v = __dsub_rn(b[p], ax_cell_f64(L, x, i, j, k));
-        r[p] = v;
-        if (NORM) acc = __dadd_rn(acc, __dmul_rn(v, v));
-    }
-    __syncthreads();
-    if (NORM) return block_sum(acc, sw);
-    return 0.0;
-}
-
+// Sum of x*y over the interior in an order fixed by the level alone: 64 lanes (threads
+// 0..63, blocks have at least 64 threads) each accumulate the cells q = lane (mod 64) in
+// increasing q, then the lanes are combined by a fixed tree.  The result therefore does
+// not depend on the block size the tail runs with.
 __device__ double tail_dot(const LevelK<double> &L, const double *x, const double *y, double *sw)
 {
     const long long n = (long long)L.nx * L.ny * L.nz;
     double acc = 0.0;
+    if (threadIdx.x < 64) {
+        for (long long q = threadIdx.x; q < n; q += 64) {
+            const int i = (int)(q % L.nx) + 1;
+            const long long rr = q / L.nx;
+            const int j = (int)(rr % L.ny) + 1, k = (int)(rr / L.ny) + 1;
+            const long long p = lin(i, j, k, L.sy, L.sz);
+            acc = __dadd_rn(acc, __dmul_rn(x[p], y[p]));
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) acc = __dadd_rn(acc, __shfl_down_sync(0xffffffffu, acc, o));
+        if ((threadIdx.x & 31) == 0) sw[threadIdx.x >> 5] = acc;
+    }
+    __syncthreads();
+    const double s = __dadd_rn(sw[0], sw[1]);
+    __syncthreads();
+    return s;
+}
+
+// r = b - A x on the interior; with NORM also returns sum(r^2) (tail_dot order).
+template <bool NORM>
+__device__ double tail_residual(const LevelK<double> &L, double *r, const double *x, const double *b, double *sw)
+{
+    const long long n = (long long)L.nx * L.ny * L.nz;
     for (long long q = threadIdx.x; q < n; q += blockDim.x) {
         const int i = (int)(q % L.nx) + 1;
         const long long rr = q / L.nx;
         const int j = (int)(rr % L.ny) + 1, k = (int)(rr / L.ny) + 1;
         const long long p = lin(i, j, k, L.sy, L.sz);
-        acc = __dadd_rn(acc, __dmul_rn(x[p], y[p]));
+        r[p] = __dsub_rn(b[p], ax_cell_f64(L, x, i, j, k));
     }
-    return block_sum(acc, sw);
+    __syncthreads();
+    if (NORM) return tail_dot(L, r, r, sw);
+    return 0.0;
 }
 
 __device__ void tail_mvmul(const LevelK<double> &L, double *y, const double *x)
