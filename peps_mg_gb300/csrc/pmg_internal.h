@@ -72,7 +72,7 @@ int f64_check(const double *num, const double *den, double tol, int le, int iter
 // One out-of-place red-black iteration e_out = RB(e_in) of a whole level (zero_in: e_in
 // is zero and is not read).  Needs the padded FP32 layout checked by rb32_fused_layout_ok.
 bool rb32_fused_layout_ok(const LevelK<float> &L, const void *e, const void *b);
-// variant: 0 = 60 x 14 tiles (512 threads), 1 = 60 x 6 (256), 2 = 60 x 30 (1024);
+// variant: 0 = 60 x 14 tiles (512 threads), 1 = 60 x 6 (256), 2 = 60 x 10 (384);
 // kchunk: planes per work item (0 = automatic).
 int rb32_fused(const LevelK<float> &L, const Launch &ln, const float *ein, float *eout, const float *b, float omega,
                float omw, bool zero_in, cudaStream_t s, int variant = 0, int kchunk = 0);

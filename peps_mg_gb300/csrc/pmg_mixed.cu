@@ -67,42 +67,25 @@ __device__ __forceinline__ float resid32(const LevelK<float> &L, const float *x,
     return b[p] - fmaf(diag32(L, i, j, k), x[p], nbsum32(L, x, p, i, j, k));
 }
 
-// Restriction weights of one coarse cell (src/multigrid.f90:1474-1482) applied to
-// values v[0..7] in the reference's term order.
-__device__ __forceinline__ float restrict_combine32(const XferK<float> &X, int ip, int iz, int jp, int jz, int kp,
-                                                    int kz, const float v[8])
-{
-    const float xz = X.wx[iz], xp = X.wx[ip], yz = X.wy[jz], yp = X.wy[jp], zz = X.wz[kz], zp = X.wz[kp];
-    const float w[8] = {xz * yz * zz, xp * yz * zz, xz * yp * zz, xp * yp * zz,
-                        xz * yz * zp, xp * yz * zp, xz * yp * zp, xp * yp * zp};
-    float vol = 0.f, s = 0.f;
-#pragma unroll
-    for (int q = 0; q < 8; ++q) {
-        vol += w[q];
-        s = fmaf(w[q], v[q], s);
-    }
-    return __fdividef(s, vol);
-}
-
 // Fused residual + restriction: b_c(i,j,k) = R (b_f - A_f e_f) without storing the
-// fine residual (src/multigrid.f90:1932-1933 and :1939-1940).
+// fine residual (src/multigrid.f90:1932-1933 and :1939-1940); the eight children in the
+// reference's term order (src/multigrid.f90:1474-1491), accumulated one at a time.
 __device__ __forceinline__ float resrestrict_cell32(const LevelK<float> &F, const XferK<float> &X, const float *e,
                                                     const float *b, int i, int j, int k)
 {
     const int ip = i * X.stx, iz = ip - (X.stx - 1);
     const int jp = j * X.sty, jz = jp - (X.sty - 1);
     const int kp = k * X.stz, kz = kp - (X.stz - 1);
-    // children in the reference's term order: (p,p,p) (z,p,p) (p,z,p) (z,z,p) (p,p,z) (z,p,z) (p,z,z) (z,z,z)
-    float v[8];
-    v[0] = resid32(F, e, b, ip, jp, kp);
-    v[1] = resid32(F, e, b, iz, jp, kp);
-    v[2] = resid32(F, e, b, ip, jz, kp);
-    v[3] = resid32(F, e, b, iz, jz, kp);
-    v[4] = resid32(F, e, b, ip, jp, kz);
-    v[5] = resid32(F, e, b, iz, jp, kz);
-    v[6] = resid32(F, e, b, ip, jz, kz);
-    v[7] = resid32(F, e, b, iz, jz, kz);
-    return restrict_combine32(X, ip, iz, jp, jz, kp, kz, v);
+    const float xz = X.wx[iz], xp = X.wx[ip], yz = X.wy[jz], yp = X.wy[jp], zz = X.wz[kz], zp = X.wz[kp];
+    float vol = 0.f, s = 0.f;
+#pragma unroll
+    for (int c = 0; c < 8; ++c) {
+        const int fi = (c & 1) ? iz : ip, fj = (c & 2) ? jz : jp, fk = (c & 4) ? kz : kp;
+        const float wv = ((c & 1) ? xp : xz) * ((c & 2) ? yp : yz) * ((c & 4) ? zp : zz);
+        vol += wv;
+        s = fmaf(wv, resid32(F, e, b, fi, fj, fk), s);
+    }
+    return __fdividef(s, vol);
 }
 
 __device__ __forceinline__ float prolong_child32(float ax, float bx, float ay, float by, float az, float bz,
@@ -190,7 +173,7 @@ __global__ void __launch_bounds__(kBX *kBY) k_rbgs32(LevelK<float> L, float *__r
         }
 }
 
-__global__ void __launch_bounds__(kBX *kBY) k_resrestrict32(LevelK<float> F, XferK<float> X,
+__global__ void __launch_bounds__(kBX *kBY, 4) k_resrestrict32(LevelK<float> F, XferK<float> X,
                                                             const float *__restrict__ e, const float *__restrict__ b,
                                                             float *__restrict__ bc)
 {
@@ -200,13 +183,69 @@ __global__ void __launch_bounds__(kBX *kBY) k_resrestrict32(LevelK<float> F, Xfe
                 bc[lin(i, j, k, X.csy, X.csz)] = resrestrict_cell32(F, X, e, b, i, j, k);
 }
 
-__global__ void __launch_bounds__(kBX *kBY) k_prolong_add32(XferK<float> X, const float *__restrict__ vc,
-                                                            float *__restrict__ vf)
+// Coarse index, neighbour and the two 1-D weights of fine index f along one axis
+// (stride 2: odd f is the low child (z_f), even f the high child (p_f); stride 1: the
+// high child, src/multigrid.f90:1594-1649).
+__device__ __forceinline__ void side_weights(int st, int f, const float *pp, const float *pn, int *c, int *nb,
+                                             float *wa, float *wb)
 {
-    for (int k = blockIdx.z + 1; k <= X.ncz; k += gridDim.z)
-        for (int j = blockIdx.y * blockDim.y + threadIdx.y + 1; j <= X.ncy; j += gridDim.y * blockDim.y)
-            for (int i = blockIdx.x * blockDim.x + threadIdx.x + 1; i <= X.ncx; i += gridDim.x * blockDim.x)
-                prolong_add_cell32(X, vc, vf, i, j, k);
+    if (st == 2) {
+        const int cc = (f + 1) >> 1;
+        *c = cc;
+        if (f & 1) {
+            *nb = cc - 1;
+            *wa = pp[f];
+            *wb = pp[f + 1];
+        } else {
+            *nb = cc + 1;
+            *wa = pn[f];
+            *wb = pn[f - 1];
+        }
+    } else {
+        *c = f;
+        *nb = f;
+        *wa = pn[f];
+        *wb = pn[f];
+    }
+}
+
+// e_f += P e_c with one thread per fine x-pair (the two x-children of a coarse cell share
+// its coarse values), or per fine cell along an x-axis that is no longer coarsened.
+__global__ void __launch_bounds__(kBX *kBY) k_prolong_add32(XferK<float> X, int nfy, int nfz,
+                                                            const float *__restrict__ vc, float *__restrict__ vf)
+{
+    for (int kf = blockIdx.z + 1; kf <= nfz; kf += gridDim.z) {
+        int kc, kn;
+        float az, bz;
+        side_weights(X.stz, kf, X.pzp, X.pzn, &kc, &kn, &az, &bz);
+        for (int jf = blockIdx.y * blockDim.y + threadIdx.y + 1; jf <= nfy; jf += gridDim.y * blockDim.y) {
+            int jc, jn;
+            float ay, by;
+            side_weights(X.sty, jf, X.pyp, X.pyn, &jc, &jn, &ay, &by);
+            const float *r00 = vc + lin(0, jc, kc, X.csy, X.csz), *rn0 = vc + lin(0, jn, kc, X.csy, X.csz);
+            const float *r0n = vc + lin(0, jc, kn, X.csy, X.csz), *rnn = vc + lin(0, jn, kn, X.csy, X.csz);
+            for (int ic = blockIdx.x * blockDim.x + threadIdx.x + 1; ic <= X.ncx; ic += gridDim.x * blockDim.x) {
+                const float c000 = __ldg(r00 + ic), c0n0 = __ldg(rn0 + ic), c00n = __ldg(r0n + ic),
+                            c0nn = __ldg(rnn + ic);
+                if (X.stx == 2) {
+                    const int iz = 2 * ic - 1, ip = 2 * ic;
+                    const float lo = prolong_child32(X.pxp[iz], X.pxp[ip], ay, by, az, bz, c000, __ldg(r00 + ic - 1),
+                                                     c0n0, c00n, __ldg(rn0 + ic - 1), __ldg(r0n + ic - 1), c0nn,
+                                                     __ldg(rnn + ic - 1));
+                    const float hi = prolong_child32(X.pxn[ip], X.pxn[iz], ay, by, az, bz, c000, __ldg(r00 + ic + 1),
+                                                     c0n0, c00n, __ldg(rn0 + ic + 1), __ldg(r0n + ic + 1), c0nn,
+                                                     __ldg(rnn + ic + 1));
+                    float *q = vf + lin(iz, jf, kf, X.fsy, X.fsz);
+                    q[0] += lo;
+                    q[1] += hi;
+                } else {
+                    const float wx = X.pxn[ic];
+                    vf[lin(ic, jf, kf, X.fsy, X.fsz)] +=
+                        prolong_child32(wx, wx, ay, by, az, bz, c000, c000, c0n0, c00n, c0n0, c00n, c0nn, c0nn);
+                }
+            }
+        }
+    }
 }
 
 // ---------------------------------------------------------------------------------
@@ -616,7 +655,11 @@ int Ctx::vcycle32(int maxit, double omega, bool zero_start)
     for (int l = tail_l0 - 1; l >= 0; --l) {
         const XferK<float> &Xl = m->X[l];
         const int pi = l == 0 ? prof.begin(stream) : -1;
-        k_prolong_add32<<<grid3m(Xl.ncx, Xl.ncy, Xl.ncz, launch[l + 1]), bl, 0, stream>>>(Xl, m->E(l + 1), m->E(l));
+        {
+            const LevelK<float> &Lf = m->K[l];
+            k_prolong_add32<<<grid3m(Xl.ncx, Lf.ny, Lf.nz, launch[l]), bl, 0, stream>>>(Xl, Lf.ny, Lf.nz,
+                                                                                      m->E(l + 1), m->E(l));
+        }
         prof.end(pi, PC_PROLONG32, 1, 8.5 * N, stream);
         ++nlaunch;
         PMG_TRY_M(sweeps(l, false));

@@ -3,7 +3,7 @@
 //
 // A launch performs one RBGS iteration of a whole level, out of place.  Work items are
 // (60 x TY tile) x (chunk of k planes); a persistent grid of resident CTAs walks them
-// chunk-major.  TY is 6, 14 or 30 (CTAs of 256, 512 or 1024 threads); the autotuner
+// chunk-major.  TY is 6, 10 or 14 (CTAs of 256, 384 or 512 threads); the autotuner
 // times every (TY, k-chunk) candidate on the level's own buffers and keeps the fastest.
 #include <cuda_runtime.h>
 
@@ -26,7 +26,7 @@ namespace {
         if (_rc != PMG_OK) return _rc; \
     } while (0)
 
-template <int TY, bool ZERO_IN>
+template <int TY, bool ZERO_IN, bool OMEGA1>
 __global__ void __launch_bounds__(rb_threads<TY>()) k_rb32_fused(LevelK<float> L, const float *__restrict__ ein,
                                                                  float *__restrict__ eout, const float *__restrict__ b,
                                                                  float omega, float omw, int kchunk, int ntx, int nty,
@@ -38,7 +38,7 @@ __global__ void __launch_bounds__(rb_threads<TY>()) k_rb32_fused(LevelK<float> L
         const int by = rem / ntx, bx = rem % ntx;
         const int k0 = 1 + kchunk * bz;
         const int k1 = min(L.nz, k0 + kchunk - 1);
-        rb32_item<TY, ZERO_IN>(S, L, ein, eout, b, omega, omw, bx, by, k0, k1);
+        rb32_item<TY, ZERO_IN, OMEGA1>(S, L, ein, eout, b, omega, omw, bx, by, k0, k1);
     }
 }
 
@@ -49,7 +49,8 @@ int slots_for(int *slots)
     static int per = 0, sms = 0;
     static cudaError_t err = cudaSuccess;
     std::call_once(once, [] {
-        err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_rb32_fused<TY, false>, rb_threads<TY>(), 0);
+        err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_rb32_fused<TY, false, false>, rb_threads<TY>(),
+                                                            0);
         int dev = 0;
         if (err == cudaSuccess) err = cudaGetDevice(&dev);
         if (err == cudaSuccess) err = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
@@ -76,12 +77,19 @@ int launch_ty(const LevelK<float> &L, const Launch &ln, const float *ein, float 
     const int chunks = (L.nz + kchunk - 1) / kchunk;
     const int nitems = ntx * nty * chunks;
     const int grid = std::max(1, std::min(nitems, slots));
-    if (zero_in)
-        k_rb32_fused<TY, true><<<grid, rb_threads<TY>(), 0, s>>>(L, ein, eout, b, omega, omw, kchunk, ntx, nty,
-                                                                 nitems);
+    const bool one = omega == 1.f;
+    if (zero_in && one)
+        k_rb32_fused<TY, true, true><<<grid, rb_threads<TY>(), 0, s>>>(L, ein, eout, b, omega, omw, kchunk, ntx, nty,
+                                                                       nitems);
+    else if (zero_in)
+        k_rb32_fused<TY, true, false><<<grid, rb_threads<TY>(), 0, s>>>(L, ein, eout, b, omega, omw, kchunk, ntx,
+                                                                        nty, nitems);
+    else if (one)
+        k_rb32_fused<TY, false, true><<<grid, rb_threads<TY>(), 0, s>>>(L, ein, eout, b, omega, omw, kchunk, ntx,
+                                                                        nty, nitems);
     else
-        k_rb32_fused<TY, false><<<grid, rb_threads<TY>(), 0, s>>>(L, ein, eout, b, omega, omw, kchunk, ntx, nty,
-                                                                  nitems);
+        k_rb32_fused<TY, false, false><<<grid, rb_threads<TY>(), 0, s>>>(L, ein, eout, b, omega, omw, kchunk, ntx,
+                                                                         nty, nitems);
     count_launches(1);
     return cuda_status(cudaGetLastError(), "fused fp32 smoother");
 }
@@ -93,7 +101,7 @@ int rb32_fused(const LevelK<float> &L, const Launch &ln, const float *ein, float
 {
     switch (variant) {
     case 1: return launch_ty<6>(L, ln, ein, eout, b, omega, omw, zero_in, kchunk, s);
-    case 2: return launch_ty<30>(L, ln, ein, eout, b, omega, omw, zero_in, kchunk, s);
+    case 2: return launch_ty<10>(L, ln, ein, eout, b, omega, omw, zero_in, kchunk, s);
     default: return launch_ty<14>(L, ln, ein, eout, b, omega, omw, zero_in, kchunk, s);
     }
 }

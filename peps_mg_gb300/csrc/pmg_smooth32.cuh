@@ -15,6 +15,11 @@
 // stored with one 8-byte store.  Global loads run three planes ahead in registers.
 // DRAM traffic per iteration: e_in read once, b read once, e_out written once (12 B per
 // cell; 8 B when e_in = 0, which is not read).
+//
+// The plane loop is unrolled by the six-plane register window (fixed register roles),
+// and the colour of the pair's first-colour cell is a template parameter of each
+// unrolled step, so the per-cell work is a handful of FMAs, two shuffles, two shared
+// loads and one reciprocal.
 #pragma once
 
 #include "pmg_common.cuh"
@@ -35,27 +40,22 @@ struct RbSmem {
 
 namespace rbdetail {
 
-// pair (a, a+1) of plane k, row j, columns valid in [0, nx+1], rows in [0, ny+1], planes in
-// [0, nz+1]; elsewhere 0
-__device__ __forceinline__ float2 load_pair(const float *__restrict__ p, int a, int j, int k, int nx, int ny, int nz,
-                                            int sy, long long sz)
+// pair load; mode bit 0: first cell valid, bit 1: second cell valid
+__device__ __forceinline__ float2 ld2(const float *q, int mode)
 {
+    if (mode == 3) return __ldg(reinterpret_cast<const float2 *>(q));
     float2 v = make_float2(0.f, 0.f);
-    if (j < 0 || j > ny + 1 || k < 0 || k > nz + 1) return v;
-    const float *q = p + (long long)a + (long long)sy * j + sz * k;
-    if (a >= 0 && a + 1 <= nx + 1) {
-        v = __ldg(reinterpret_cast<const float2 *>(q));
-    } else {
-        if (a >= 0 && a <= nx + 1) v.x = __ldg(q);
-        if (a + 1 >= 0 && a + 1 <= nx + 1) v.y = __ldg(q + 1);
-    }
+    if (mode & 1) v.x = __ldg(q);
+    if (mode & 2) v.y = __ldg(q + 1);
     return v;
 }
 
-__device__ __forceinline__ float comp(const float2 &v, int q) { return q ? v.y : v.x; }
-__device__ __forceinline__ void setc(float2 &v, int q, float x)
+template <int Q>
+__device__ __forceinline__ float cq(const float2 &v) { return Q ? v.y : v.x; }
+template <int Q>
+__device__ __forceinline__ void sq(float2 &v, float x)
 {
-    if (q)
+    if (Q)
         v.y = x;
     else
         v.x = x;
@@ -63,150 +63,209 @@ __device__ __forceinline__ void setc(float2 &v, int q, float x)
 
 }  // namespace rbdetail
 
-template <int TY, bool ZERO_IN>
-__device__ void rb32_item(RbSmem<TY> &S, const LevelK<float> &L, const float *__restrict__ ein,
-                          float *__restrict__ eout, const float *__restrict__ b, float omega, float omw, int bx,
-                          int by, int k0, int k1)
+template <int TY, bool ZERO_IN, bool OMEGA1>
+struct RbItem {
+    // per-thread constants of the item
+    const float *czm_t, *czp_t;      // z coefficient tables
+    int nz, k0, k1, lane, r, ro;
+    int cmode;                       // column validity of the lane's pair (ld2 mode)
+    bool row_e, row_in, has_outer, store_lane;
+    bool need0, need1;               // the lane updates the first-colour cell when it is cell 0 / 1
+    bool st_full;                    // the final pair is stored whole (else only its first cell)
+    const float *pe, *po, *pb;       // e_in row, outer row, b row at plane 0
+    float *pw;                       // e_out row at plane 0
+    long long sz;
+    float omega, omw;
+    float dxc[2], cxm[2], cxp[2], cym, cyp, dy;
+    float2 E[6], O[6], B[6];         // planes t-2 .. t+3 at window positions (P .. P+5) % 6
+
+    __device__ __forceinline__ float2 LE(int k) const
+    {
+        if (ZERO_IN || !row_e || k < 0 || k > nz + 1) return make_float2(0.f, 0.f);
+        return rbdetail::ld2(pe + sz * k, cmode);
+    }
+    __device__ __forceinline__ float2 LO(int k) const
+    {
+        if (ZERO_IN || !has_outer || k < 0 || k > nz + 1) return make_float2(0.f, 0.f);
+        return rbdetail::ld2(po + sz * k, cmode);
+    }
+    __device__ __forceinline__ float2 LB(int k) const
+    {
+        if (!row_in || k < 1 || k > nz) return make_float2(0.f, 0.f);
+        return rbdetail::ld2(pb + sz * k, cmode);
+    }
+
+    __device__ __forceinline__ float upd(float old, float bb, float s, float c0) const
+    {
+        if (OMEGA1) return __fdividef(bb - s, c0);
+        return fmaf(omw, old, __fdividef(omega * (bb - s), c0));
+    }
+
+    // One step: first colour on plane t, second colour on plane t-1.  P = window position
+    // of plane t-2; Q = index within the pair of the first-colour cell on plane t (and of
+    // the second-colour cell on plane t-1).
+    template <int P, int Q>
+    __device__ __forceinline__ void step(RbSmem<TY> &S, int t)
+    {
+        using namespace rbdetail;
+        constexpr int im2 = P % 6, im1 = (P + 1) % 6, i00 = (P + 2) % 6, ip1 = (P + 3) % 6, ip3 = (P + 5) % 6;
+        E[ip3] = LE(t + 3);
+        O[ip3] = LO(t + 3);
+        B[ip3] = LB(t + 3);
+        {
+            float(*St)[RB_SW] = S.s[t & 3];
+            const float up = __shfl_up_sync(0xffffffffu, E[i00].y, 1);
+            const float dn = __shfl_down_sync(0xffffffffu, E[i00].x, 1);
+            if ((Q ? need1 : need0) && t >= 1 && t <= nz) {
+                // only second-colour words of the neighbouring rows are read here
+                const float yl = St[r - 1][2 * lane + Q];
+                const float yr = St[r + 1][2 * lane + Q];
+                const float czm = czm_t[t], czp = czp_t[t];
+                const float left = Q ? E[i00].x : up;
+                const float right = Q ? dn : E[i00].y;
+                float s = cxm[Q] * left;
+                s = fmaf(cxp[Q], right, s);
+                s = fmaf(cym, yl, s);
+                s = fmaf(cyp, yr, s);
+                s = fmaf(czm, cq<Q>(E[im1]), s);
+                s = fmaf(czp, cq<Q>(E[ip1]), s);
+                const float c0 = -(dxc[Q] + (dy + (czm + czp)));
+                const float v = upd(cq<Q>(E[i00]), cq<Q>(B[i00]), s, c0);
+                sq<Q>(E[i00], v);
+                St[r][2 * lane + Q] = v;
+            }
+            float(*Sn)[RB_SW] = S.s[(t + 1) & 3];
+            *reinterpret_cast<float2 *>(&Sn[r][2 * lane]) = E[ip1];
+            if (has_outer) *reinterpret_cast<float2 *>(&Sn[ro][2 * lane]) = O[ip1];
+        }
+        __syncthreads();
+        {
+            const int s1 = t - 1;
+            const float up = __shfl_up_sync(0xffffffffu, E[im1].y, 1);
+            const float dn = __shfl_down_sync(0xffffffffu, E[im1].x, 1);
+            if (store_lane && s1 >= k0 && s1 <= k1) {
+                if (Q == 0 || st_full) {
+                    float(*Ss)[RB_SW] = S.s[s1 & 3];
+                    const float yl = Ss[r - 1][2 * lane + Q];
+                    const float yr = Ss[r + 1][2 * lane + Q];
+                    const float czm = czm_t[s1], czp = czp_t[s1];
+                    const float left = Q ? E[im1].x : up;
+                    const float right = Q ? dn : E[im1].y;
+                    float s = cxm[Q] * left;
+                    s = fmaf(cxp[Q], right, s);
+                    s = fmaf(cym, yl, s);
+                    s = fmaf(cyp, yr, s);
+                    s = fmaf(czm, cq<Q>(E[im2]), s);
+                    s = fmaf(czp, cq<Q>(E[i00]), s);
+                    const float c0 = -(dxc[Q] + (dy + (czm + czp)));
+                    const float v = upd(cq<Q>(E[im1]), cq<Q>(B[im1]), s, c0);
+                    sq<Q>(E[im1], v);
+                }
+                float *g = pw + sz * s1;
+                if (st_full)
+                    *reinterpret_cast<float2 *>(g) = E[im1];
+                else
+                    g[0] = E[im1].x;
+            }
+        }
+    }
+
+    template <int Q0>
+    __device__ __forceinline__ void run(RbSmem<TY> &S)
+    {
+        int t = k0 - 1;
+        for (; t + 5 <= k1 + 1; t += 6) {
+            step<0, Q0>(S, t);
+            step<1, 1 - Q0>(S, t + 1);
+            step<2, Q0>(S, t + 2);
+            step<3, 1 - Q0>(S, t + 3);
+            step<4, Q0>(S, t + 4);
+            step<5, 1 - Q0>(S, t + 5);
+        }
+        if (t <= k1 + 1) step<0, Q0>(S, t++);
+        if (t <= k1 + 1) step<1, 1 - Q0>(S, t++);
+        if (t <= k1 + 1) step<2, Q0>(S, t++);
+        if (t <= k1 + 1) step<3, 1 - Q0>(S, t++);
+        if (t <= k1 + 1) step<4, Q0>(S, t++);
+    }
+};
+
+template <int TY, bool ZERO_IN, bool OMEGA1>
+__device__ __forceinline__ void rb32_item(RbSmem<TY> &S, const LevelK<float> &L, const float *__restrict__ ein,
+                                          float *__restrict__ eout, const float *__restrict__ b, float omega,
+                                          float omw, int bx, int by, int k0, int k1)
 {
-    using namespace rbdetail;
+    RbItem<TY, ZERO_IN, OMEGA1> I;
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const int i0 = 1 + RB_TX * bx, j0 = 1 + TY * by;
-    const int nx = L.nx, ny = L.ny, nz = L.nz;
-    const int sy = L.sy;
-    const long long sz = L.sz;
-    const int a = i0 - 2 + 2 * lane;           // first cell of the lane's pair
-    const int j = j0 - 1 + w;                  // the warp's row
-    const int r = w + 1;                       // its shared row
-    const bool row_in = j >= 1 && j <= ny;
-    const bool tile_row = w >= 1 && w <= TY;
-    // the outer rows j0-2 and j0+TY+1 are deposited by the first and the last warp
-    const bool has_outer = (w == 0) || (w == TY + 1);
+    const int nx = L.nx, ny = L.ny;
+    const int a = i0 - 2 + 2 * lane;
+    const int j = j0 - 1 + w;
+    I.czm_t = L.czm;
+    I.czp_t = L.czp;
+    I.nz = L.nz;
+    I.k0 = k0;
+    I.k1 = k1;
+    I.lane = lane;
+    I.r = w + 1;
+    I.sz = L.sz;
+    I.omega = omega;
+    I.omw = omw;
+    I.cmode = (a >= 0 && a <= nx + 1 ? 1 : 0) | (a + 1 >= 0 && a + 1 <= nx + 1 ? 2 : 0);
+    I.row_e = j >= 0 && j <= ny + 1;
+    I.row_in = j >= 1 && j <= ny;
     const int jo = w == 0 ? j0 - 2 : j0 + TY + 1;
-    const int ro = w == 0 ? 0 : TY + 3;
-
-    // per-lane x-coefficients (both cells of the pair) and per-warp y-coefficients
-    float dxc[2], cxm[2], cxp[2];
+    I.ro = w == 0 ? 0 : TY + 3;
+    I.has_outer = (w == 0 || w == TY + 1) && jo >= 0 && jo <= ny + 1;
+    // a lane updates the first-colour cell of its pair when it is interior and in the tile
+    // or the ring cell beside it (lane 0: its second cell, lane 31: its first cell)
+    const bool in0 = a >= 1 && a <= nx, in1 = a + 1 >= 1 && a + 1 <= nx;
+    const bool mid = lane >= 1 && lane <= 30;
+    I.need0 = I.row_in && in0 && (mid || lane == 31);
+    I.need1 = I.row_in && in1 && (mid || lane == 0);
+    I.store_lane = (w >= 1 && w <= TY) && I.row_in && mid && a <= nx;
+    I.st_full = a + 1 <= nx;
+    const long long rowoff = (long long)a + (long long)L.sy * j;
+    I.pe = ein + rowoff;
+    I.pb = b + rowoff;
+    I.pw = eout + rowoff;
+    I.po = ein + (long long)a + (long long)L.sy * jo;
 #pragma unroll
     for (int q = 0; q < 2; ++q) {
         const int i = a + q;
         const bool in = i >= 1 && i <= nx;
-        dxc[q] = in ? L.sx[i] : 0.f;
-        cxm[q] = in ? L.cxm[i] : 0.f;
-        cxp[q] = in ? L.cxp[i] : 0.f;
+        I.dxc[q] = in ? L.sx[i] : 0.f;
+        I.cxm[q] = in ? L.cxm[i] : 0.f;
+        I.cxp[q] = in ? L.cxp[i] : 0.f;
     }
-    const float cym = row_in ? L.cym[j] : 0.f, cyp = row_in ? L.cyp[j] : 0.f;
-    const float dy = cym + cyp;
+    I.cym = I.row_in ? L.cym[j] : 0.f;
+    I.cyp = I.row_in ? L.cyp[j] : 0.f;
+    I.dy = I.cym + I.cyp;
 
-    auto LE = [&](int k) -> float2 {
-        if (ZERO_IN) return make_float2(0.f, 0.f);
-        return load_pair(ein, a, j, k, nx, ny, nz, sy, sz);
-    };
-    auto LO = [&](int k) -> float2 {
-        if (ZERO_IN || !has_outer) return make_float2(0.f, 0.f);
-        return load_pair(ein, a, jo, k, nx, ny, nz, sy, sz);
-    };
-    auto LB = [&](int k) -> float2 {
-        if (k < 1 || k > nz || !row_in) return make_float2(0.f, 0.f);
-        return load_pair(b, a, j, k, nx, ny, nz, sy, sz);
-    };
-
-    // register window at the start of step t: E[0..5] = planes t-2 .. t+3
-    float2 Em2 = make_float2(0.f, 0.f);
-    float2 Em1 = LE(k0 - 2), E0 = LE(k0 - 1), Ep1 = LE(k0), Ep2 = LE(k0 + 1), Ep3;
-    float2 Op1 = LO(k0), Op2 = LO(k0 + 1), Op3;
-    float2 Bm1 = make_float2(0.f, 0.f), B0 = LB(k0 - 1), Bp1 = LB(k0), Bp2 = LB(k0 + 1), Bp3;
-    // plane k0-1 in the shared ring
+    // window at the first step t = k0 - 1: positions 0..5 = planes k0-3 .. k0+2
+    I.E[0] = make_float2(0.f, 0.f);
+    I.E[1] = I.LE(k0 - 2);
+    I.E[2] = I.LE(k0 - 1);
+    I.E[3] = I.LE(k0);
+    I.E[4] = I.LE(k0 + 1);
+    I.O[3] = I.LO(k0);
+    I.O[4] = I.LO(k0 + 1);
+    I.B[1] = make_float2(0.f, 0.f);
+    I.B[2] = I.LB(k0 - 1);
+    I.B[3] = I.LB(k0);
+    I.B[4] = I.LB(k0 + 1);
     {
-        const float2 o0 = LO(k0 - 1);
-        *reinterpret_cast<float2 *>(&S.s[(k0 - 1) & 3][r][2 * lane]) = E0;
-        if (has_outer) *reinterpret_cast<float2 *>(&S.s[(k0 - 1) & 3][ro][2 * lane]) = o0;
+        const float2 o0 = I.LO(k0 - 1);
+        *reinterpret_cast<float2 *>(&S.s[(k0 - 1) & 3][I.r][2 * lane]) = I.E[2];
+        if (I.has_outer) *reinterpret_cast<float2 *>(&S.s[(k0 - 1) & 3][I.ro][2 * lane]) = o0;
     }
     __syncthreads();
-
-    for (int t = k0 - 1; t <= k1 + 1; ++t) {
-        Ep3 = LE(t + 3);
-        Op3 = LO(t + 3);
-        Bp3 = LB(t + 3);
-        float(*St)[RB_SW] = S.s[t & 3];
-
-        // ---- A: first colour on plane t (tile and ring) --------------------------------
-        {
-            const int q = (j + t) & 1;                       // first-colour cell of the pair
-            const float up = __shfl_up_sync(0xffffffffu, E0.y, 1);
-            const float dn = __shfl_down_sync(0xffffffffu, E0.x, 1);
-            const int i = a + q;
-            const bool need = (lane >= 1 && lane <= 30) || (lane == 0 && q == 1) || (lane == 31 && q == 0);
-            if (need && row_in && i >= 1 && i <= nx && t >= 1 && t <= nz) {
-                // only the second-colour words of the neighbouring rows are read (the
-                // first-colour words of those rows are being written in this phase)
-                const float yl = St[r - 1][2 * lane + q];
-                const float yr = St[r + 1][2 * lane + q];
-                const float left = q ? E0.x : up;
-                const float right = q ? dn : E0.y;
-                const float czm = L.czm[t], czp = L.czp[t];
-                float s = cxm[q] * left;
-                s = fmaf(cxp[q], right, s);
-                s = fmaf(cym, yl, s);
-                s = fmaf(cyp, yr, s);
-                s = fmaf(czm, comp(Em1, q), s);
-                s = fmaf(czp, comp(Ep1, q), s);
-                const float c0 = -((dxc[q] + dy) + (czm + czp));
-                const float v = fmaf(omw, comp(E0, q), __fdividef(omega * (comp(B0, q) - s), c0));
-                setc(E0, q, v);
-                St[r][2 * lane + q] = v;
-            }
-            // the next plane's old values for the y-neighbours of step t+1
-            float(*Sn)[RB_SW] = S.s[(t + 1) & 3];
-            *reinterpret_cast<float2 *>(&Sn[r][2 * lane]) = Ep1;
-            if (has_outer) *reinterpret_cast<float2 *>(&Sn[ro][2 * lane]) = Op1;
-        }
-        __syncthreads();
-
-        // ---- C: second colour on plane t-1 (tile), store the final pair -----------------
-        const int s1 = t - 1;
-        {
-            const int qb = 1 - ((j + s1) & 1);               // second-colour cell of the pair
-            const float up = __shfl_up_sync(0xffffffffu, Em1.y, 1);
-            const float dn = __shfl_down_sync(0xffffffffu, Em1.x, 1);
-            if (s1 >= k0 && s1 <= k1 && tile_row && row_in && lane >= 1 && lane <= 30 && a <= nx) {
-                const int i = a + qb;
-                if (i <= nx) {
-                    float(*Ss)[RB_SW] = S.s[s1 & 3];
-                    const float2 yl = *reinterpret_cast<const float2 *>(&Ss[r - 1][2 * lane]);
-                    const float2 yr = *reinterpret_cast<const float2 *>(&Ss[r + 1][2 * lane]);
-                    const float left = qb ? Em1.x : up;
-                    const float right = qb ? dn : Em1.y;
-                    const float czm = L.czm[s1], czp = L.czp[s1];
-                    float s = cxm[qb] * left;
-                    s = fmaf(cxp[qb], right, s);
-                    s = fmaf(cym, comp(yl, qb), s);
-                    s = fmaf(cyp, comp(yr, qb), s);
-                    s = fmaf(czm, comp(Em2, qb), s);
-                    s = fmaf(czp, comp(E0, qb), s);
-                    const float c0 = -((dxc[qb] + dy) + (czm + czp));
-                    const float v = fmaf(omw, comp(Em1, qb), __fdividef(omega * (comp(Bm1, qb) - s), c0));
-                    setc(Em1, qb, v);
-                }
-                float *g = eout + (long long)a + (long long)sy * j + sz * s1;
-                if (a + 1 <= nx)
-                    *reinterpret_cast<float2 *>(g) = Em1;
-                else
-                    g[0] = Em1.x;
-            }
-        }
-        // rotate the register window
-        Em2 = Em1;
-        Em1 = E0;
-        E0 = Ep1;
-        Ep1 = Ep2;
-        Ep2 = Ep3;
-        Op1 = Op2;
-        Op2 = Op3;
-        Bm1 = B0;
-        B0 = Bp1;
-        Bp1 = Bp2;
-        Bp2 = Bp3;
-    }
+    // the pair's first cell a is odd, so it carries the first colour on plane k when j + k
+    // is even ((i + j + k) odd, src/rbgs_poisson_matrix.f90:242)
+    if (((j + k0 - 1) & 1) == 0)
+        I.template run<0>(S);
+    else
+        I.template run<1>(S);
     __syncthreads();
 }
 
