@@ -21,6 +21,7 @@
 
 #include "pmg_ctx.h"
 #include "pmg_tail64.cuh"
+#include "pmg_smooth32.cuh"
 
 namespace pmg {
 
@@ -481,22 +482,26 @@ struct MixedState {
 
 static int mstatus(cudaError_t e, const char *what) { return cuda_status(e, what); }
 
-// FP32 arrays: row pitch a multiple of 4 floats with room for the fused smoother's
-// aligned 16-byte copies (columns -3 .. pitch-4), data pointer = allocation + 3 so that
-// column 1 is 16-byte aligned.
+// FP32 arrays of the mixed V-cycle.  Besides the (0:nx+1,0:ny+1,0:nz+1) cells every array
+// carries zero padding that the fused smoother reads without bounds checks: columns
+// -3 .. pitch-4 (pitch >= 60*ceil(nx/60)+8 and >= 64*ceil(nx/64)+8, even), rows -1 ..
+// ny+1+RB_PAD_ROWS, planes -1 .. nz+1+RB_PAD_PLANES.  The data pointer (cell (0,0,0)) sits
+// an odd number of floats past the 256-byte aligned allocation, so the pair of cells
+// (i, i+1) with i odd is 8-byte aligned.  Padding is never written.
 static int alloc_f32(MixedState *m, int nx, int ny, int nz, int *pitch, long long *plane, float **data)
 {
-    const int tiles = (nx + 63) / 64;
-    const int p = 64 * tiles + 8;
-    const long long pl = (long long)p * (ny + 2);
-    const size_t n = (size_t)pl * (size_t)(nz + 2) + 8;
+    int p = std::max(64 * ((nx + 63) / 64) + 8, RB_TX * ((nx + RB_TX - 1) / RB_TX) + 8);
+    p += p & 1;
+    const long long rows = (long long)ny + 2 + 1 + RB_PAD_ROWS;
+    const long long pl = (long long)p * rows;
+    const size_t n = (size_t)pl * (size_t)(nz + 2 + 1 + RB_PAD_PLANES) + 8;
     float *a = nullptr;
     PMG_TRY_M(mstatus(cudaMalloc(&a, n * sizeof(float)), "mixed level allocation"));
     PMG_TRY_M(mstatus(cudaMemset(a, 0, n * sizeof(float)), "mixed level init"));
     m->alloc.push_back(a);
     *pitch = p;
     *plane = pl;
-    *data = a + 3;
+    *data = a + 3 + p + pl;     // skip 3 columns, one row and one plane of padding
     return PMG_OK;
 }
 
@@ -627,7 +632,7 @@ int Ctx::vcycle32(int maxit, double omega, bool zero_start)
                 }
             prof.end(pi, PC_SMOOTH32, 2 * maxit, 8.0 * N, stream);
         }
-        if (zs && maxit == 0) cudaMemsetAsync(m->E(l) - 3, 0, (size_t)(L.sz * (L.nz + 2) + 8) * sizeof(float), stream);
+        if (zs && maxit == 0) cudaMemsetAsync(m->E(l), 0, (size_t)(L.sz * (L.nz + 2)) * sizeof(float), stream);
         return PMG_OK;
     };
     PMG_TRY_M(sweeps(0, zero_start));

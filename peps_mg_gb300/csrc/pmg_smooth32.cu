@@ -26,8 +26,12 @@ namespace {
         if (_rc != PMG_OK) return _rc; \
     } while (0)
 
+// blocks per SM the register budget is sized for
+template <int TY>
+constexpr int rb_min_blocks() { return TY <= 6 ? 3 : TY <= 10 ? 2 : 1; }
+
 template <int TY, bool ZERO_IN, bool OMEGA1>
-__global__ void __launch_bounds__(rb_threads<TY>()) k_rb32_fused(LevelK<float> L, const float *__restrict__ ein,
+__global__ void __launch_bounds__(rb_threads<TY>(), rb_min_blocks<TY>()) k_rb32_fused(LevelK<float> L, const float *__restrict__ ein,
                                                                  float *__restrict__ eout, const float *__restrict__ b,
                                                                  float omega, float omw, int kchunk, int ntx, int nty,
                                                                  int nitems)
@@ -73,7 +77,7 @@ int launch_ty(const LevelK<float> &L, const Launch &ln, const float *ein, float 
         kchunk = std::max(16, (L.nz + want - 1) / want);
     }
     if (ln.collapse[2]) kchunk = L.nz;
-    kchunk = std::max(1, std::min(kchunk, L.nz));
+    kchunk = std::max(1, std::min(std::min(kchunk, L.nz), RB_ZC - 3));
     const int chunks = (L.nz + kchunk - 1) / kchunk;
     const int nitems = ntx * nty * chunks;
     const int grid = std::max(1, std::min(nitems, slots));
@@ -109,9 +113,12 @@ int rb32_fused(const LevelK<float> &L, const Launch &ln, const float *ein, float
 bool rb32_fused_layout_ok(const LevelK<float> &L, const void *e, const void *b)
 {
     // 8-byte pair loads and stores at odd cell indices: data pointers at an odd float
-    // offset from an 8-byte boundary and even pitches
+    // offset from an 8-byte boundary, even pitches, room for the tiles' columns and
+    // 32-bit plane offsets
     const auto ae = reinterpret_cast<uintptr_t>(e), ab = reinterpret_cast<uintptr_t>(b);
-    return L.sy % 2 == 0 && L.sz % 2 == 0 && (ae + 4) % 8 == 0 && (ab + 4) % 8 == 0;
+    const int ntx = (L.nx + RB_TX - 1) / RB_TX;
+    return L.sy % 2 == 0 && L.sz % 2 == 0 && (ae + 4) % 8 == 0 && (ab + 4) % 8 == 0 &&
+           L.sy >= RB_TX * ntx + 8 && L.sz * (long long)(L.nz + 6) < (1LL << 31);
 }
 
 int tune_smoother(const LevelK<float> &L, const Launch &ln, float *e0, float *e1, const float *b, cudaStream_t s,

@@ -29,6 +29,10 @@ namespace pmg {
 constexpr int RB_TX = 60;        // tile columns
 constexpr int RB_SW = 64;        // shared row width (one pair per lane)
 constexpr int RB_NS = 4;         // shared plane slots
+constexpr int RB_TYMAX = 14;     // tallest tile
+constexpr int RB_PAD_ROWS = RB_TYMAX + 2;   // zero rows above ny+1 read by the last tile row
+constexpr int RB_PAD_PLANES = 3;            // zero planes above nz+1 read ahead by the last chunk
+constexpr int RB_ZC = 128;       // z coefficients staged per item (planes k0-1 .. k0+RB_ZC-2)
 
 template <int TY>
 constexpr int rb_threads() { return (TY + 2) * 32; }
@@ -36,19 +40,13 @@ constexpr int rb_threads() { return (TY + 2) * 32; }
 template <int TY>
 struct RbSmem {
     float s[RB_NS][TY + 4][RB_SW];   // rows j0-2 .. j0+TY+1
+    float2 zc[RB_ZC];                // (czm, czp) of planes k0-1 ..
 };
 
 namespace rbdetail {
 
-// pair load; mode bit 0: first cell valid, bit 1: second cell valid
-__device__ __forceinline__ float2 ld2(const float *q, int mode)
-{
-    if (mode == 3) return __ldg(reinterpret_cast<const float2 *>(q));
-    float2 v = make_float2(0.f, 0.f);
-    if (mode & 1) v.x = __ldg(q);
-    if (mode & 2) v.y = __ldg(q + 1);
-    return v;
-}
+// pair load (8-byte aligned; padding makes every pair the kernel reads addressable)
+__device__ __forceinline__ float2 ld2(const float *q) { return __ldg(reinterpret_cast<const float2 *>(q)); }
 
 template <int Q>
 __device__ __forceinline__ float cq(const float2 &v) { return Q ? v.y : v.x; }
@@ -66,34 +64,29 @@ __device__ __forceinline__ void sq(float2 &v, float x)
 template <int TY, bool ZERO_IN, bool OMEGA1>
 struct RbItem {
     // per-thread constants of the item
-    const float *czm_t, *czp_t;      // z coefficient tables
-    int nz, k0, k1, lane, r, ro;
-    int cmode;                       // column validity of the lane's pair (ld2 mode)
-    bool row_e, row_in, has_outer, store_lane;
+    const float2 *zc;                // staged (czm, czp), index t - (k0 - 1)
+    int nz, k0, k1, lane, r, ro, sz32;
+    bool has_outer, store_lane;
     bool need0, need1;               // the lane updates the first-colour cell when it is cell 0 / 1
     bool st_full;                    // the final pair is stored whole (else only its first cell)
     const float *pe, *po, *pb;       // e_in row, outer row, b row at plane 0
     float *pw;                       // e_out row at plane 0
-    long long sz;
     float omega, omw;
     float dxc[2], cxm[2], cxp[2], cym, cyp, dy;
-    float2 E[6], O[6], B[6];         // planes t-2 .. t+3 at window positions (P .. P+5) % 6
+    float2 E[6], B[6];               // planes t-2 .. t+3 at window positions (P .. P+5) % 6
+    float2 O[3];                     // outer row, planes t+1 .. t+3 at positions (P .. P+2) % 3
 
     __device__ __forceinline__ float2 LE(int k) const
     {
-        if (ZERO_IN || !row_e || k < 0 || k > nz + 1) return make_float2(0.f, 0.f);
-        return rbdetail::ld2(pe + sz * k, cmode);
+        if (ZERO_IN) return make_float2(0.f, 0.f);
+        return rbdetail::ld2(pe + sz32 * k);
     }
     __device__ __forceinline__ float2 LO(int k) const
     {
-        if (ZERO_IN || !has_outer || k < 0 || k > nz + 1) return make_float2(0.f, 0.f);
-        return rbdetail::ld2(po + sz * k, cmode);
+        if (ZERO_IN || !has_outer) return make_float2(0.f, 0.f);
+        return rbdetail::ld2(po + sz32 * k);
     }
-    __device__ __forceinline__ float2 LB(int k) const
-    {
-        if (!row_in || k < 1 || k > nz) return make_float2(0.f, 0.f);
-        return rbdetail::ld2(pb + sz * k, cmode);
-    }
+    __device__ __forceinline__ float2 LB(int k) const { return rbdetail::ld2(pb + sz32 * k); }
 
     __device__ __forceinline__ float upd(float old, float bb, float s, float c0) const
     {
@@ -109,8 +102,9 @@ struct RbItem {
     {
         using namespace rbdetail;
         constexpr int im2 = P % 6, im1 = (P + 1) % 6, i00 = (P + 2) % 6, ip1 = (P + 3) % 6, ip3 = (P + 5) % 6;
+        constexpr int o1 = P % 3, o3 = (P + 2) % 3;
         E[ip3] = LE(t + 3);
-        O[ip3] = LO(t + 3);
+        O[o3] = LO(t + 3);
         B[ip3] = LB(t + 3);
         {
             float(*St)[RB_SW] = S.s[t & 3];
@@ -120,7 +114,8 @@ struct RbItem {
                 // only second-colour words of the neighbouring rows are read here
                 const float yl = St[r - 1][2 * lane + Q];
                 const float yr = St[r + 1][2 * lane + Q];
-                const float czm = czm_t[t], czp = czp_t[t];
+                const float2 cz = zc[t - k0 + 1];
+                const float czm = cz.x, czp = cz.y;
                 const float left = Q ? E[i00].x : up;
                 const float right = Q ? dn : E[i00].y;
                 float s = cxm[Q] * left;
@@ -136,7 +131,7 @@ struct RbItem {
             }
             float(*Sn)[RB_SW] = S.s[(t + 1) & 3];
             *reinterpret_cast<float2 *>(&Sn[r][2 * lane]) = E[ip1];
-            if (has_outer) *reinterpret_cast<float2 *>(&Sn[ro][2 * lane]) = O[ip1];
+            if (has_outer) *reinterpret_cast<float2 *>(&Sn[ro][2 * lane]) = O[o1];
         }
         __syncthreads();
         {
@@ -148,7 +143,8 @@ struct RbItem {
                     float(*Ss)[RB_SW] = S.s[s1 & 3];
                     const float yl = Ss[r - 1][2 * lane + Q];
                     const float yr = Ss[r + 1][2 * lane + Q];
-                    const float czm = czm_t[s1], czp = czp_t[s1];
+                    const float2 cz = zc[s1 - k0 + 1];
+                    const float czm = cz.x, czp = cz.y;
                     const float left = Q ? E[im1].x : up;
                     const float right = Q ? dn : E[im1].y;
                     float s = cxm[Q] * left;
@@ -161,7 +157,7 @@ struct RbItem {
                     const float v = upd(cq<Q>(E[im1]), cq<Q>(B[im1]), s, c0);
                     sq<Q>(E[im1], v);
                 }
-                float *g = pw + sz * s1;
+                float *g = pw + sz32 * s1;
                 if (st_full)
                     *reinterpret_cast<float2 *>(g) = E[im1];
                 else
@@ -201,29 +197,30 @@ __device__ __forceinline__ void rb32_item(RbSmem<TY> &S, const LevelK<float> &L,
     const int nx = L.nx, ny = L.ny;
     const int a = i0 - 2 + 2 * lane;
     const int j = j0 - 1 + w;
-    I.czm_t = L.czm;
-    I.czp_t = L.czp;
+    for (int q = threadIdx.x; q < k1 - k0 + 3; q += blockDim.x) {
+        const int k = k0 - 1 + q;
+        S.zc[q] = (k >= 1 && k <= L.nz) ? make_float2(L.czm[k], L.czp[k]) : make_float2(0.f, 0.f);
+    }
+    I.zc = S.zc;
     I.nz = L.nz;
     I.k0 = k0;
     I.k1 = k1;
     I.lane = lane;
     I.r = w + 1;
-    I.sz = L.sz;
+    I.sz32 = (int)L.sz;
     I.omega = omega;
     I.omw = omw;
-    I.cmode = (a >= 0 && a <= nx + 1 ? 1 : 0) | (a + 1 >= 0 && a + 1 <= nx + 1 ? 2 : 0);
-    I.row_e = j >= 0 && j <= ny + 1;
-    I.row_in = j >= 1 && j <= ny;
+    const bool row_in = j >= 1 && j <= ny;
     const int jo = w == 0 ? j0 - 2 : j0 + TY + 1;
     I.ro = w == 0 ? 0 : TY + 3;
-    I.has_outer = (w == 0 || w == TY + 1) && jo >= 0 && jo <= ny + 1;
+    I.has_outer = (w == 0 || w == TY + 1);
     // a lane updates the first-colour cell of its pair when it is interior and in the tile
     // or the ring cell beside it (lane 0: its second cell, lane 31: its first cell)
     const bool in0 = a >= 1 && a <= nx, in1 = a + 1 >= 1 && a + 1 <= nx;
     const bool mid = lane >= 1 && lane <= 30;
-    I.need0 = I.row_in && in0 && (mid || lane == 31);
-    I.need1 = I.row_in && in1 && (mid || lane == 0);
-    I.store_lane = (w >= 1 && w <= TY) && I.row_in && mid && a <= nx;
+    I.need0 = row_in && in0 && (mid || lane == 31);
+    I.need1 = row_in && in1 && (mid || lane == 0);
+    I.store_lane = (w >= 1 && w <= TY) && row_in && mid && a <= nx;
     I.st_full = a + 1 <= nx;
     const long long rowoff = (long long)a + (long long)L.sy * j;
     I.pe = ein + rowoff;
@@ -238,8 +235,8 @@ __device__ __forceinline__ void rb32_item(RbSmem<TY> &S, const LevelK<float> &L,
         I.cxm[q] = in ? L.cxm[i] : 0.f;
         I.cxp[q] = in ? L.cxp[i] : 0.f;
     }
-    I.cym = I.row_in ? L.cym[j] : 0.f;
-    I.cyp = I.row_in ? L.cyp[j] : 0.f;
+    I.cym = row_in ? L.cym[j] : 0.f;
+    I.cyp = row_in ? L.cyp[j] : 0.f;
     I.dy = I.cym + I.cyp;
 
     // window at the first step t = k0 - 1: positions 0..5 = planes k0-3 .. k0+2
@@ -248,8 +245,8 @@ __device__ __forceinline__ void rb32_item(RbSmem<TY> &S, const LevelK<float> &L,
     I.E[2] = I.LE(k0 - 1);
     I.E[3] = I.LE(k0);
     I.E[4] = I.LE(k0 + 1);
-    I.O[3] = I.LO(k0);
-    I.O[4] = I.LO(k0 + 1);
+    I.O[0] = I.LO(k0);
+    I.O[1] = I.LO(k0 + 1);
     I.B[1] = make_float2(0.f, 0.f);
     I.B[2] = I.LB(k0 - 1);
     I.B[3] = I.LB(k0);
