@@ -138,6 +138,40 @@ int pmg_prolongation(pmg_ctx *ctx, int level, double *val_f, const double *val_c
  * src/multigrid.f90:1957-1958 (interior; the reference's ghost add is of zeros). */
 int pmg_prolong_add(pmg_ctx *ctx, int level, double *x_f, const double *x_c);
 
+/* ---- Adjoint (no counterpart in the reference) ------------------------------------- */
+/* Gradients of a loss L(u) of the last solution u of this context with respect to the
+ * right-hand side and the six Dirichlet face values, given dLdu = dL/du (device array of
+ * the finest level; ghost entries ignored):
+ *   dLdb    = A^{-T} dLdu on the interior, 0 on the ghosts       (device array)
+ *   dLdg[f] = -sum over the cells next to face f of c_f * dLdb   (host, 6 doubles, order
+ *             x-, x+, y-, y+, z-, z+; each face's ghost layer is one scalar value)
+ * A^T = V A V^{-1} with V = diag(dxm dym dzm), so the transposed system is solved by this
+ * context's own V-cycle (FP64 or mixed) with zero ghost values; only the finest-level
+ * right-hand side and solution of that solve are held.  report may be NULL. */
+int pmg_adjoint(pmg_ctx *ctx, const double *dLdu, double *dLdb, double dLdg[6], int maxiteration, double tolerance,
+                double omega_sor, pmg_report_t *report);
+
+/* ---- Batched solver (no counterpart in the reference) ------------------------------ */
+/* Many independent problems of uneven sizes, each with its own hierarchy (the CGS level
+ * rules with as many levels as its sizes allow), solved together in mixed precision:
+ * every V-cycle operation at a depth is one persistent launch over all problems, one
+ * outer correction is captured in a CUDA graph, smoother tiles are autotuned per depth.
+ * dims: 3 ints per problem.  meshes: NULL (uniform meshes of the unit cube) or 6 host
+ * pointers per problem (dxm, dxg, dym, dyg, dzm, dzg, each n+2 values; NULL entries mean
+ * uniform).  sol and rhs are packed device arrays: problem p occupies elements
+ * offsets[p] .. offsets[p+1]-1 in the usual (0:n+1)^3 Fortran layout
+ * (pmg_batch_layout). */
+typedef struct pmg_batch pmg_batch;
+int pmg_batch_create(pmg_batch **batch, int n_problems, const int *dims, const double *const *meshes,
+                     int mixed_inner_cycles, void *stream);
+int pmg_batch_layout(const pmg_batch *batch, long long *offsets, int *levels);
+/* Solves until every problem reaches sqrt(|r|^2/|r0|^2) < tolerance or max_cycles outer
+ * corrections ran; cycles/ratio (per problem, may be NULL) receive the corrections used
+ * and the final ratio; elapsed_ms (may be NULL) the device time.  Synchronous. */
+int pmg_batch_solve(pmg_batch *batch, double *sol, const double *rhs, int maxiteration, double tolerance,
+                    double omega_sor, int max_cycles, int *cycles, double *ratio, float *elapsed_ms);
+int pmg_batch_destroy(pmg_batch *batch);
+
 /* ---- Telemetry (no counterpart in the reference; it only prints MPI_Wtime) ------ */
 /* Kernel classes of pmg_profile_read (finest-level launches only). */
 #define PMG_PROF_SMOOTH32 0       /* FP32 RBGS half-sweep                    */

@@ -3,10 +3,12 @@ equation on cell-centred, non-uniform Cartesian grids; a drop-in for the solve p
 PEPS_MG (multigrid_create / multigrid_solve_vcycle / multigrid_destroy).
 """
 from . import geometry  # noqa: F401
+from .autograd import PoissonSolve  # noqa: F401
+from .batch import BatchSolver  # noqa: F401
 from ._lib import (PMG_CGA, PMG_CGPSA, PMG_CGS, PMG_COARSE_CG, PMG_COARSE_RBGS, PMG_FP64,  # noqa: F401
                    PMG_MIXED, PmgError, load)
 from .multigrid import (PROF_CLASSES, Multigrid, SolveReport, launch_count, level_sizes, multigrid_create, multigrid_destroy,  # noqa: F401
                         multigrid_solve_vcycle)
 
 __all__ = ["Multigrid", "SolveReport", "PmgError", "multigrid_create", "multigrid_solve_vcycle",
-           "multigrid_destroy", "level_sizes", "geometry", "load"]
+           "multigrid_destroy", "level_sizes", "geometry", "load", "BatchSolver", "PoissonSolve"]

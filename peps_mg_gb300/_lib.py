@@ -55,6 +55,13 @@ _SIGS = {
     "pmg_restriction": [c_void_p, c_int, c_void_p, c_void_p],
     "pmg_prolongation": [c_void_p, c_int, c_void_p, c_void_p],
     "pmg_prolong_add": [c_void_p, c_int, c_void_p, c_void_p],
+    "pmg_adjoint": [c_void_p, c_void_p, c_void_p, ctypes.POINTER(c_double), c_int, c_double, c_double,
+                    ctypes.POINTER(PmgReport)],
+    "pmg_batch_create": [ctypes.POINTER(c_void_p), c_int, ctypes.POINTER(c_int), c_void_p, c_int, c_void_p],
+    "pmg_batch_layout": [c_void_p, ctypes.POINTER(ctypes.c_longlong), ctypes.POINTER(c_int)],
+    "pmg_batch_solve": [c_void_p, c_void_p, c_void_p, c_int, c_double, c_double, c_int, ctypes.POINTER(c_int),
+                        ctypes.POINTER(c_double), ctypes.POINTER(c_float)],
+    "pmg_batch_destroy": [c_void_p],
     "pmg_profile": [c_void_p, c_int],
     "pmg_profile_read": [c_void_p, c_int, ctypes.POINTER(c_double), ctypes.POINTER(ctypes.c_longlong),
                          ctypes.POINTER(c_double)],

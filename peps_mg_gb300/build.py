@@ -26,6 +26,8 @@ UNITS = {
     "pmg_f64.cu": ["--fmad=false"],
     "pmg_mixed.cu": ["--fmad=true"],
     "pmg_smooth32.cu": ["--fmad=true"],
+    "pmg_batch.cu": ["--fmad=true"],
+    "pmg_adjoint.cu": ["--fmad=false"],
 }
 
 

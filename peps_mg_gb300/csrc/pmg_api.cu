@@ -516,6 +516,11 @@ Ctx::~Ctx()
     cudaFree(stage_rsd);
     cudaFree(stage_rhs);
     for (auto &v : scratch_levels) cudaFree(v);
+    cudaFree(adj_rhs);
+    cudaFree(adj_sol);
+    cudaFree(adj_rsd);
+    cudaFree(adj_vol);
+    cudaFree(adj_faces);
     if (ev0) cudaEventDestroy(ev0);
     if (ev1) cudaEventDestroy(ev1);
     destroy_mixed();
@@ -708,6 +713,11 @@ int Ctx::level_scratch(int l, double **bufs, int count)
     const size_t need = lv[l].total * (size_t)count;
     if (scratch_cap < need) {
         for (auto &v : scratch_levels) cudaFree(v);
+    cudaFree(adj_rhs);
+    cudaFree(adj_sol);
+    cudaFree(adj_rsd);
+    cudaFree(adj_vol);
+    cudaFree(adj_faces);
         scratch_levels.clear();
         double *p = nullptr;
         PMG_CUDA(cudaMalloc(&p, need * sizeof(double)), "scratch allocation");
@@ -1048,6 +1058,71 @@ int pmg_prolong_add(pmg_ctx *ctx, int level, double *x_f, const double *x_c)
         return PMG_EINVAL;
     }
     return pmg::f64_prolong(c.X[level], c.launch[level + 1], x_c, x_f, true, c.stream);
+}
+
+int pmg_adjoint(pmg_ctx *ctx, const double *dLdu, double *dLdb, double dLdg[6], int maxiteration, double tolerance,
+                double omega_sor, pmg_report_t *report)
+{
+    PMG_TRY(check_ctx_level(ctx, 0));
+    if (!dLdu || !dLdb || maxiteration < 0) {
+        pmg::set_error("dLdu and dLdb are required");
+        return PMG_EINVAL;
+    }
+    cudaPointerAttributes a1, a2;
+    if (cudaPointerGetAttributes(&a1, dLdu) != cudaSuccess || cudaPointerGetAttributes(&a2, dLdb) != cudaSuccess ||
+        a1.type != cudaMemoryTypeDevice || a2.type != cudaMemoryTypeDevice) {
+        cudaGetLastError();
+        pmg::set_error("pmg_adjoint takes device arrays");
+        return PMG_EINVAL;
+    }
+    return ctx->impl.adjoint(dLdu, dLdb, dLdg, maxiteration, tolerance, omega_sor, report);
+}
+
+struct pmg_batch {
+    pmg::Batch *impl;
+};
+
+int pmg_batch_create(pmg_batch **batch, int n_problems, const int *dims, const double *const *meshes,
+                     int mixed_inner_cycles, void *stream)
+{
+    if (!batch) {
+        pmg::set_error("batch is required");
+        return PMG_EINVAL;
+    }
+    *batch = nullptr;
+    pmg::Batch *b = nullptr;
+    const int rc = pmg::batch_create(&b, n_problems, dims, meshes, mixed_inner_cycles, (cudaStream_t)stream);
+    if (rc != PMG_OK) return rc;
+    pmg_batch *h = new (std::nothrow) pmg_batch{b};
+    if (!h) {
+        pmg::batch_destroy(b);
+        return PMG_ENOMEM;
+    }
+    *batch = h;
+    return PMG_OK;
+}
+
+int pmg_batch_layout(const pmg_batch *batch, long long *offsets, int *levels)
+{
+    if (!batch) return PMG_EINVAL;
+    pmg::batch_layout(*batch->impl, offsets, levels);
+    return PMG_OK;
+}
+
+int pmg_batch_solve(pmg_batch *batch, double *sol, const double *rhs, int maxiteration, double tolerance,
+                    double omega_sor, int max_cycles, int *cycles, double *ratio, float *elapsed_ms)
+{
+    if (!batch) return PMG_EINVAL;
+    return pmg::batch_solve(*batch->impl, sol, rhs, maxiteration, tolerance, omega_sor, max_cycles, cycles, ratio,
+                            elapsed_ms);
+}
+
+int pmg_batch_destroy(pmg_batch *batch)
+{
+    if (!batch) return PMG_OK;
+    pmg::batch_destroy(batch->impl);
+    delete batch;
+    return PMG_OK;
 }
 
 int pmg_profile(pmg_ctx *ctx, int enable)

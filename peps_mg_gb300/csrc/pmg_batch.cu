@@ -1,0 +1,674 @@
+// pmg_batch.cu -- many independent Poisson problems of uneven sizes solved together.
+//
+// Every problem has its own hierarchy (the CGS level rules with as many levels as its
+// sizes allow, uniform or given meshes) and is solved in mixed precision: FP32 V-cycles
+// inside FP64 defect correction, exactly the per-problem algorithm of pmg_mixed.cu.  The
+// batch runs depth by depth: each operation of the V-cycle at depth d is ONE persistent
+// launch over a work list of (problem, tile) items gathered from every problem that has
+// that depth; the coarsest-level solves are one launch with one CTA per problem.  One
+// outer correction -- the FP32 V-cycles, the FP64 correction, the FP64 residual, the
+// per-problem norms and convergence test -- is captured once in a CUDA graph and then
+// replayed.  Converged problems skip their work items, so their results stay those of
+// the correction at which they converged.
+//
+// The smoother's tile shape (64 x 8, 64 x 12 or 64 x 16) is chosen per depth by timing
+// the batch's own work lists (autotuning at the first solve).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <memory>
+#include <new>
+#include <vector>
+
+#include "pmg_cell32.cuh"
+#include "pmg_ctx.h"
+#include "pmg_mixed.h"
+#include "pmg_smooth32.cuh"
+
+#define PMG_TRY_B(expr)                \
+    do {                               \
+        int _rc = (expr);              \
+        if (_rc != PMG_OK) return _rc; \
+    } while (0)
+
+namespace pmg {
+
+namespace {
+
+constexpr int NTB = 256;
+
+// per (depth, problem) descriptor
+struct BLevel {
+    LevelK<float> L;
+    XferK<float> X;        // transfer to depth + 1 (valid when depth < nl)
+    float *e[2];
+    float *b;
+    int nl;                // coarsest depth of the problem
+    int kchunk;
+};
+
+// per problem, finest level
+struct BOuter {
+    LevelK<double> L;
+    const double *dyy, *dzz;
+    double *sol, *rsd;
+    const double *rhs;
+    int sy32;
+    long long sz32;
+    float *r32;
+    float *e0;             // the depth-0 correction buffer the V-cycle leaves its result in
+};
+
+struct Item {
+    int p, bx, by, k0;     // problem, tile, first plane (smoother) or plane (others)
+};
+
+// ---- smoother ----------------------------------------------------------------------------
+template <int TY, bool ZERO_IN, bool OMEGA1>
+__global__ void __launch_bounds__(rb_threads<TY>()) k_batch_rb32(const BLevel *__restrict__ lv,
+                                                                 const Item *__restrict__ items, int nitems, int which,
+                                                                 float omega, float omw, const int *__restrict__ done)
+{
+    __shared__ __align__(16) RbSmem<TY> S;
+    for (int it = blockIdx.x; it < nitems; it += gridDim.x) {
+        const Item w = items[it];
+        if (done[w.p]) continue;
+        const BLevel &D = lv[w.p];
+        const LevelK<float> L = D.L;
+        const int k1 = min(L.nz, w.k0 + D.kchunk - 1);
+        rb32_item<TY, ZERO_IN, OMEGA1>(S, L, D.e[which], D.e[1 - which], D.b, omega, omw, w.bx, w.by, w.k0, k1);
+    }
+}
+
+// ---- residual + restriction into depth d+1: one item per coarse plane ---------------------
+__global__ void __launch_bounds__(NTB) k_batch_resrestrict(const BLevel *__restrict__ lvd,
+                                                           const BLevel *__restrict__ lvc, const Item *__restrict__ items,
+                                                           int nitems, int which, const int *__restrict__ done)
+{
+    for (int it = blockIdx.x; it < nitems; it += gridDim.x) {
+        const Item w = items[it];
+        if (done[w.p]) continue;
+        const BLevel &D = lvd[w.p];
+        const XferK<float> X = D.X;
+        const LevelK<float> L = D.L;
+        const float *e = D.e[which];
+        float *bc = lvc[w.p].b;
+        const int k = w.k0;
+        for (int q = threadIdx.x; q < X.ncx * X.ncy; q += NTB) {
+            const int i = q % X.ncx + 1, j = q / X.ncx + 1;
+            bc[lin(i, j, k, X.csy, X.csz)] = resrestrict_cell32(L, X, e, D.b, i, j, k);
+        }
+    }
+}
+
+// ---- prolongation + correction from depth d+1 into depth d ---------------------------------
+__global__ void __launch_bounds__(NTB) k_batch_prolong(const BLevel *__restrict__ lvd, const BLevel *__restrict__ lvc,
+                                                       const Item *__restrict__ items, int nitems, int which,
+                                                       int which_c, int d, const int *__restrict__ done)
+{
+    for (int it = blockIdx.x; it < nitems; it += gridDim.x) {
+        const Item w = items[it];
+        if (done[w.p]) continue;
+        const BLevel &D = lvd[w.p];
+        const XferK<float> X = D.X;
+        // the coarsest depth of a problem is solved in place in buffer 0
+        const float *ec = (d + 1 == D.nl) ? lvc[w.p].e[0] : lvc[w.p].e[which_c];
+        float *e = D.e[which];
+        const int k = w.k0;
+        for (int q = threadIdx.x; q < X.ncx * X.ncy; q += NTB) {
+            const int i = q % X.ncx + 1, j = q / X.ncx + 1;
+            prolong_add_cell32(X, ec, e, i, j, k);
+        }
+    }
+}
+
+// ---- outer FP64 kernels: one item per fine plane ------------------------------------------
+__global__ void __launch_bounds__(NTB) k_batch_outer_residual(const BOuter *__restrict__ po,
+                                                              const Item *__restrict__ items, int nitems,
+                                                              double *__restrict__ partials,
+                                                              const int *__restrict__ done)
+{
+    __shared__ double sw[NTB / 32];
+    for (int it = blockIdx.x; it < nitems; it += gridDim.x) {
+        const Item w = items[it];
+        if (done[w.p]) continue;       // uniform over the block
+        const BOuter &O = po[w.p];
+        const LevelK<double> L = O.L;
+        const int k = w.k0;
+        const double dz = O.dzz[k];
+        double acc = 0.0;
+        for (int q = threadIdx.x; q < L.nx * L.ny; q += NTB) {
+            const int i = q % L.nx + 1, j = q / L.nx + 1;
+            const long long p = lin(i, j, k, L.sy, L.sz);
+            const double v = outer_residual_cell(L, O.dyy[j] + dz, O.sol, O.rhs, i, j, k, p);
+            O.rsd[p] = v;
+            O.r32[lin(i, j, k, O.sy32, O.sz32)] = f64_to_f32_rn(v);
+            acc = fma(v, v, acc);
+        }
+        const double s = block_sum(acc, sw);
+        if (threadIdx.x == 0) partials[it] = s;
+    }
+}
+
+__global__ void __launch_bounds__(NTB) k_batch_add_correction(const BOuter *__restrict__ po,
+                                                              const Item *__restrict__ items, int nitems,
+                                                              const int *__restrict__ done)
+{
+    for (int it = blockIdx.x; it < nitems; it += gridDim.x) {
+        const Item w = items[it];
+        if (done[w.p]) continue;
+        const BOuter &O = po[w.p];
+        const LevelK<double> L = O.L;
+        const int k = w.k0;
+        for (int q = threadIdx.x; q < L.nx * L.ny; q += NTB) {
+            const int i = q % L.nx + 1, j = q / L.nx + 1;
+            const long long p = lin(i, j, k, L.sy, L.sz);
+            O.sol[p] = O.sol[p] + f32_to_f64(O.e0[lin(i, j, k, O.sy32, O.sz32)]);
+        }
+    }
+}
+
+// per problem: norm = sum of its items' partials in item order; first = 1 stores res0,
+// else the ratio test of src/multigrid.f90:1973 updates done/cycles/ratio.
+__global__ void __launch_bounds__(NTB) k_batch_norms(const double *__restrict__ partials,
+                                                     const int *__restrict__ first_item, double *__restrict__ res0,
+                                                     double *__restrict__ ratio, int *__restrict__ done,
+                                                     int *__restrict__ cycles, int *__restrict__ ndone, double tol,
+                                                     int first)
+{
+    __shared__ double sw[NTB / 32];
+    const int p = blockIdx.x;
+    if (!first && done[p]) return;
+    double acc = 0.0;
+    for (int q = first_item[p] + threadIdx.x; q < first_item[p + 1]; q += NTB) acc += partials[q];
+    const double s = block_sum(acc, sw);
+    if (threadIdx.x == 0) {
+        if (first) {
+            res0[p] = s;
+            ratio[p] = 1.0;
+            cycles[p] = 0;
+            done[p] = 0;
+        } else {
+            const double r = sqrt(s / res0[p]);
+            ratio[p] = r;
+            cycles[p] += 1;
+            if (r < tol || !(r == r)) {
+                done[p] = 1;
+                atomicAdd(ndone, 1);
+            }
+        }
+    }
+}
+
+
+}  // namespace
+
+// ---------------------------------------------------------------------------------------
+// Batch object
+// ---------------------------------------------------------------------------------------
+struct Batch {
+    cudaStream_t stream = nullptr;
+    int n = 0, dmax = 0;
+    std::vector<std::unique_ptr<Ctx>> probs;
+    std::vector<long long> offset;          // element offsets of each problem in the packed arrays
+    long long total = 0;
+    // descriptors
+    BLevel *d_lv = nullptr;                 // [(dmax+1) * n]
+    BOuter *d_outer = nullptr;
+    std::vector<BOuter> h_outer;
+    // work lists
+    struct List {
+        Item *d = nullptr;
+        int n = 0;
+    };
+    std::vector<List> smooth[3];            // [variant][depth]
+    std::vector<List> xfer;                 // [depth]: coarse planes of depth+1 for problems with nl > depth
+    List outer;                             // fine planes
+    std::vector<int> first_item;            // per problem range in `outer`
+    int *d_first = nullptr;
+    double *d_partials = nullptr, *d_res0 = nullptr, *d_ratio = nullptr;
+    int *d_done = nullptr, *d_cycles = nullptr, *d_ndone = nullptr;
+    double *rsd = nullptr;                  // packed FP64 residual
+    const TailDesc<float> **d_tails = nullptr;
+    int tail_threads = 64;
+    std::vector<int> variant;               // chosen smoother variant per depth
+    int slots[3] = {0, 0, 0};
+    cudaGraphExec_t graph = nullptr;
+    int graph_maxit = -1;
+    double graph_omega = 0.0, graph_tol = 0.0;
+    int inner = 2;
+    ~Batch();
+};
+
+Batch::~Batch()
+{
+    if (graph) cudaGraphExecDestroy(graph);
+    cudaFree(d_lv);
+    cudaFree(d_outer);
+    for (auto &v : smooth)
+        for (auto &l : v) cudaFree(l.d);
+    for (auto &l : xfer) cudaFree(l.d);
+    cudaFree(outer.d);
+    cudaFree(d_first);
+    cudaFree(d_partials);
+    cudaFree(d_res0);
+    cudaFree(d_ratio);
+    cudaFree(d_done);
+    cudaFree(d_cycles);
+    cudaFree(d_ndone);
+    cudaFree(rsd);
+    cudaFree(d_tails);
+}
+
+}  // namespace pmg
+
+// ---------------------------------------------------------------------------------------
+// Creation, scheduling, graph and solve
+// ---------------------------------------------------------------------------------------
+namespace pmg {
+
+namespace {
+
+int v2(int n)
+{
+    int c = 0;
+    while (n > 0 && n % 2 == 0) {
+        n /= 2;
+        ++c;
+    }
+    return c;
+}
+
+template <typename T>
+int upload(const std::vector<T> &h, T **d)
+{
+    if (h.empty()) return PMG_OK;
+    int rc = cuda_status(cudaMalloc(d, h.size() * sizeof(T)), "batch allocation");
+    if (rc != PMG_OK) return rc;
+    return cuda_status(cudaMemcpy(*d, h.data(), h.size() * sizeof(T), cudaMemcpyHostToDevice), "batch upload");
+}
+
+constexpr int kTY[3] = {14, 6, 10};   // tile heights of the smoother variants (as pmg_smooth32.cu)
+
+template <int TY>
+int setup_variant(int *slots)
+{
+    int per = 0, dev = 0, sms = 0;
+    int rc = cuda_status(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_batch_rb32<TY, false, false>,
+                                                                       rb_threads<TY>(), 0),
+                         "batch smoother occupancy");
+    if (rc != PMG_OK) return rc;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    *slots = std::max(1, per) * std::max(1, sms);
+    return PMG_OK;
+}
+
+template <int TY>
+void launch_batch_rb(const Batch &B, int d, const Batch::List &Ls, int slots, int which, float om, float omw, bool zs)
+{
+    const int grid = std::max(1, std::min(Ls.n, slots));
+    const BLevel *lv = B.d_lv + (size_t)d * B.n;
+    const bool one = om == 1.f;
+    const int nt = rb_threads<TY>();
+    if (zs && one)
+        k_batch_rb32<TY, true, true><<<grid, nt, 0, B.stream>>>(lv, Ls.d, Ls.n, which, om, omw, B.d_done);
+    else if (zs)
+        k_batch_rb32<TY, true, false><<<grid, nt, 0, B.stream>>>(lv, Ls.d, Ls.n, which, om, omw, B.d_done);
+    else if (one)
+        k_batch_rb32<TY, false, true><<<grid, nt, 0, B.stream>>>(lv, Ls.d, Ls.n, which, om, omw, B.d_done);
+    else
+        k_batch_rb32<TY, false, false><<<grid, nt, 0, B.stream>>>(lv, Ls.d, Ls.n, which, om, omw, B.d_done);
+}
+
+void launch_rb(const Batch &B, int v, int d, int which, float om, float omw, bool zs)
+{
+    const Batch::List &Ls = B.smooth[v][d];
+    if (!Ls.n) return;
+    if (v == 0)
+        launch_batch_rb<14>(B, d, Ls, B.slots[0], which, om, omw, zs);
+    else if (v == 1)
+        launch_batch_rb<6>(B, d, Ls, B.slots[1], which, om, omw, zs);
+    else
+        launch_batch_rb<10>(B, d, Ls, B.slots[2], which, om, omw, zs);
+    count_launches(1);
+}
+
+int grid_for(int items) { return std::max(1, std::min(items, 8 * 152)); }
+
+}  // namespace
+
+int batch_create(Batch **out, int n, const int *dims, const double *const *meshes, int inner, cudaStream_t user)
+{
+    (void)user;
+    *out = nullptr;
+    if (n <= 0 || !dims) {
+        set_error("batch needs at least one problem and its sizes");
+        return PMG_EINVAL;
+    }
+    std::unique_ptr<Batch> B(new (std::nothrow) Batch());
+    if (!B) return PMG_ENOMEM;
+    B->n = n;
+    B->inner = inner > 0 ? inner : 2;
+    PMG_TRY_B(cuda_status(cudaStreamCreateWithFlags(&B->stream, cudaStreamNonBlocking), "batch stream"));
+    B->offset.assign((size_t)n + 1, 0);
+    for (int p = 0; p < n; ++p) {
+        const int nx = dims[3 * p], ny = dims[3 * p + 1], nz = dims[3 * p + 2];
+        if (nx < 1 || ny < 1 || nz < 1) {
+            set_error("batch problem sizes must be positive");
+            return PMG_EINVAL;
+        }
+        const int nl = std::max(v2(nx), std::max(v2(ny), v2(nz)));
+        if (nl < 2) {
+            set_error("every batch problem needs at least two coarsening levels (an axis divisible by 4)");
+            return PMG_EINVAL;
+        }
+        std::vector<double> ax[3][3];
+        const double *mp[9];
+        const int nn[3] = {nx, ny, nz};
+        for (int d = 0; d < 3; ++d) {
+            if (meshes && meshes[6 * p + 2 * d] && meshes[6 * p + 2 * d + 1]) {
+                mp[3 * d] = meshes[6 * p + 2 * d];
+                mp[3 * d + 1] = meshes[6 * p + 2 * d + 1];
+                mp[3 * d + 2] = nullptr;
+            } else {
+                // uniform mesh of the unit interval (src/geometry.f90:180-189)
+                auto &dm = ax[d][0], &dg = ax[d][1], &xg = ax[d][2];
+                const int m = nn[d];
+                dm.assign((size_t)m + 2, 0.0);
+                dg.assign((size_t)m + 2, 0.0);
+                xg.assign((size_t)m + 2, 0.0);
+                for (int i = 1; i <= m; ++i) {
+                    dm[i] = 1.0 / (double)m;
+                    dg[i] = 0.5 * (dm[i] + dm[i - 1]);
+                    xg[i] = xg[i - 1] + dg[i];
+                }
+                dg[m + 1] = 0.5 * (dm[m + 1] + dm[m]);
+                xg[m + 1] = xg[m] + dg[m + 1];
+                mp[3 * d] = dm.data();
+                mp[3 * d + 1] = dg.data();
+                mp[3 * d + 2] = xg.data();
+            }
+        }
+        pmg_config_t cfg;
+        std::memset(&cfg, 0, sizeof(cfg));
+        cfg.nx = nx; cfg.ny = ny; cfg.nz = nz;
+        cfg.dxm = mp[0]; cfg.dxg = mp[1]; cfg.xg = mp[2];
+        cfg.dym = mp[3]; cfg.dyg = mp[4]; cfg.yg = mp[5];
+        cfg.dzm = mp[6]; cfg.dzg = mp[7]; cfg.zg = mp[8];
+        cfg.number_of_levels = nl;
+        cfg.number_of_vcycles = 1;
+        cfg.aggregation_method = PMG_CGS;
+        cfg.coarse_solver = PMG_COARSE_RBGS;
+        cfg.precision = PMG_MIXED;
+        cfg.mixed_inner_cycles = B->inner;
+        std::unique_ptr<Ctx> c(new (std::nothrow) Ctx());
+        if (!c) return PMG_ENOMEM;
+        c->autotune = false;
+        PMG_TRY_B(c->build(&cfg, B->stream));
+        PMG_TRY_B(c->setup_mixed());
+        B->dmax = std::max(B->dmax, c->nl);
+        B->offset[p + 1] = B->offset[p] + (long long)c->lv[0].total;
+        B->tail_threads = std::max(B->tail_threads, c->tail_threads);
+        B->probs.push_back(std::move(c));
+    }
+    B->total = B->offset[n];
+    const int D = B->dmax;
+    // descriptors
+    std::vector<BLevel> lv((size_t)(D + 1) * n);
+    std::memset(lv.data(), 0, lv.size() * sizeof(BLevel));
+    for (int p = 0; p < n; ++p) {
+        Ctx &c = *B->probs[p];
+        MixedState *m = c.mixed;
+        for (int d = 0; d <= c.nl; ++d) {
+            BLevel &x = lv[(size_t)d * n + p];
+            x.L = m->K[d];
+            if (d < c.nl) x.X = m->X[d];
+            x.e[0] = m->e[0][d];
+            x.e[1] = m->e[1][d];
+            x.b = m->b[d];
+            if (!rb32_fused_layout_ok(x.L, x.e[0], x.b) || !rb32_fused_layout_ok(x.L, x.e[1], x.b)) {
+                set_error("batch problem too large for the fused smoother layout");
+                return PMG_EINVAL;
+            }
+            x.nl = c.nl;
+            x.kchunk = std::min(x.L.nz, 32);
+        }
+    }
+    PMG_TRY_B(upload(lv, &B->d_lv));
+    // work lists
+    for (int v = 0; v < 3; ++v) {
+        B->smooth[v].resize((size_t)D);
+        for (int d = 0; d < D; ++d) {
+            std::vector<Item> it;
+            for (int p = 0; p < n; ++p) {
+                if (B->probs[p]->nl <= d) continue;
+                const BLevel &x = lv[(size_t)d * n + p];
+                const int ntx = (x.L.nx + RB_TX - 1) / RB_TX, nty = (x.L.ny + kTY[v] - 1) / kTY[v];
+                for (int k0 = 1; k0 <= x.L.nz; k0 += x.kchunk)
+                    for (int by = 0; by < nty; ++by)
+                        for (int bx = 0; bx < ntx; ++bx) it.push_back({p, bx, by, k0});
+            }
+            B->smooth[v][d].n = (int)it.size();
+            PMG_TRY_B(upload(it, &B->smooth[v][d].d));
+        }
+    }
+    B->xfer.resize((size_t)D);
+    for (int d = 0; d < D; ++d) {
+        std::vector<Item> it;
+        for (int p = 0; p < n; ++p) {
+            if (B->probs[p]->nl <= d) continue;
+            const int ncz = lv[(size_t)(d + 1) * n + p].L.nz;
+            for (int k = 1; k <= ncz; ++k) it.push_back({p, 0, 0, k});
+        }
+        B->xfer[d].n = (int)it.size();
+        PMG_TRY_B(upload(it, &B->xfer[d].d));
+    }
+    {
+        std::vector<Item> it;
+        B->first_item.assign((size_t)n + 1, 0);
+        for (int p = 0; p < n; ++p) {
+            B->first_item[p] = (int)it.size();
+            for (int k = 1; k <= B->probs[p]->lv[0].n[2]; ++k) it.push_back({p, 0, 0, k});
+        }
+        B->first_item[n] = (int)it.size();
+        B->outer.n = (int)it.size();
+        PMG_TRY_B(upload(it, &B->outer.d));
+        PMG_TRY_B(upload(B->first_item, &B->d_first));
+    }
+    PMG_TRY_B(cuda_status(cudaMalloc(&B->d_partials, (size_t)B->outer.n * sizeof(double)), "batch allocation"));
+    PMG_TRY_B(cuda_status(cudaMalloc(&B->d_res0, n * sizeof(double)), "batch allocation"));
+    PMG_TRY_B(cuda_status(cudaMalloc(&B->d_ratio, n * sizeof(double)), "batch allocation"));
+    PMG_TRY_B(cuda_status(cudaMalloc(&B->d_done, n * sizeof(int)), "batch allocation"));
+    PMG_TRY_B(cuda_status(cudaMemset(B->d_done, 0, n * sizeof(int)), "batch init"));
+    PMG_TRY_B(cuda_status(cudaMalloc(&B->d_cycles, n * sizeof(int)), "batch allocation"));
+    PMG_TRY_B(cuda_status(cudaMalloc(&B->d_ndone, sizeof(int)), "batch allocation"));
+    PMG_TRY_B(cuda_status(cudaMalloc(&B->rsd, (size_t)B->total * sizeof(double)), "batch allocation"));
+    PMG_TRY_B(cuda_status(cudaMemset(B->rsd, 0, (size_t)B->total * sizeof(double)), "batch init"));
+    {
+        std::vector<const TailDesc<float> *> t((size_t)n);
+        for (int p = 0; p < n; ++p) t[p] = B->probs[p]->mixed->d_tail;
+        PMG_TRY_B(upload(t, &B->d_tails));
+    }
+    PMG_TRY_B(setup_variant<14>(&B->slots[0]));
+    PMG_TRY_B(setup_variant<6>(&B->slots[1]));
+    PMG_TRY_B(setup_variant<10>(&B->slots[2]));
+    B->variant.assign((size_t)D, -1);
+    B->h_outer.resize((size_t)n);
+    *out = B.release();
+    return PMG_OK;
+}
+
+// Times the three tile variants on each depth's work list; keeps the fastest.
+static int batch_autotune(Batch &B)
+{
+    cudaEvent_t a, z;
+    PMG_TRY_B(cuda_status(cudaEventCreate(&a), "batch tuner"));
+    PMG_TRY_B(cuda_status(cudaEventCreate(&z), "batch tuner"));
+    for (int d = 0; d < B.dmax; ++d) {
+        float best = 1e30f;
+        int bv = 0;
+        for (int v = 0; v < 3; ++v) {
+            if (!B.smooth[v][d].n) continue;
+            launch_rb(B, v, d, 0, 1.f, 0.f, false);
+            cudaEventRecord(a, B.stream);
+            for (int r = 0; r < 3; ++r) launch_rb(B, v, d, 0, 1.f, 0.f, false);
+            cudaEventRecord(z, B.stream);
+            cudaEventSynchronize(z);
+            float ms = 0.f;
+            cudaEventElapsedTime(&ms, a, z);
+            if (ms < best) {
+                best = ms;
+                bv = v;
+            }
+        }
+        B.variant[d] = bv;
+    }
+    cudaEventDestroy(a);
+    cudaEventDestroy(z);
+    return cuda_status(cudaGetLastError(), "batch autotuning");
+}
+
+// One FP32 V-cycle on every unconverged problem.
+static void batch_vcycle(Batch &B, int maxit, float om, float omw, bool zero_start)
+{
+    const int D = B.dmax, n = B.n;
+    std::vector<int> par((size_t)D + 1, 0);
+    auto smooth = [&](int d, bool zs) {
+        for (int it = 0; it < maxit; ++it) {
+            launch_rb(B, B.variant[d], d, par[d], om, omw, zs && it == 0);
+            par[d] ^= 1;
+        }
+    };
+    for (int d = 0; d < D; ++d) {
+        smooth(d, d > 0 || zero_start);
+        const Batch::List &X = B.xfer[d];
+        if (X.n) {
+            k_batch_resrestrict<<<grid_for(X.n), NTB, 0, B.stream>>>(B.d_lv + (size_t)d * n, B.d_lv + (size_t)(d + 1) * n,
+                                                                     X.d, X.n, par[d], B.d_done);
+            count_launches(1);
+        }
+    }
+    batch_tail32(B.d_tails, n, B.d_done, B.tail_threads, B.stream);
+    for (int d = D - 1; d >= 0; --d) {
+        const Batch::List &X = B.xfer[d];
+        if (X.n) {
+            k_batch_prolong<<<grid_for(X.n), NTB, 0, B.stream>>>(B.d_lv + (size_t)d * n, B.d_lv + (size_t)(d + 1) * n,
+                                                                 X.d, X.n, par[d], par[d + 1], d, B.d_done);
+            count_launches(1);
+        }
+        smooth(d, false);
+    }
+}
+
+static void batch_outer(Batch &B, bool first, double tol)
+{
+    const int n = B.n;
+    if (!first) {
+        k_batch_add_correction<<<grid_for(B.outer.n), NTB, 0, B.stream>>>(B.d_outer, B.outer.d, B.outer.n, B.d_done);
+        count_launches(1);
+    }
+    k_batch_outer_residual<<<grid_for(B.outer.n), NTB, 0, B.stream>>>(B.d_outer, B.outer.d, B.outer.n, B.d_partials,
+                                                                      B.d_done);
+    k_batch_norms<<<n, NTB, 0, B.stream>>>(B.d_partials, B.d_first, B.d_res0, B.d_ratio, B.d_done, B.d_cycles,
+                                           B.d_ndone, tol, first ? 1 : 0);
+    count_launches(2);
+}
+
+int batch_solve(Batch &B, double *sol, const double *rhs, int maxit, double tol, double omega, int max_cycles,
+                int *cycles, double *ratio, float *elapsed_ms)
+{
+    const int n = B.n;
+    if (!sol || !rhs || maxit < 0 || max_cycles < 0) {
+        set_error("invalid batch solve arguments");
+        return PMG_EINVAL;
+    }
+    cudaEvent_t e0, e1;
+    PMG_TRY_B(cuda_status(cudaEventCreate(&e0), "batch event"));
+    PMG_TRY_B(cuda_status(cudaEventCreate(&e1), "batch event"));
+    // the caller's work on the legacy stream (its inputs) comes first
+    PMG_TRY_B(cuda_status(cudaEventRecord(e0, 0), "batch event"));
+    PMG_TRY_B(cuda_status(cudaStreamWaitEvent(B.stream, e0, 0), "batch event"));
+    PMG_TRY_B(cuda_status(cudaEventRecord(e0, B.stream), "batch event"));
+    // per-problem outer descriptors (the caller's packed arrays)
+    bool changed = false;
+    for (int p = 0; p < n; ++p) {
+        Ctx &c = *B.probs[p];
+        BOuter o;
+        std::memset(&o, 0, sizeof(o));
+        o.L = c.K[0];
+        o.dyy = c.mixed->dyy[0];
+        o.dzz = c.mixed->dzz[0];
+        o.sy32 = c.mixed->K[0].sy;
+        o.sz32 = c.mixed->K[0].sz;
+        o.r32 = c.mixed->b[0];
+        o.e0 = c.mixed->e[0][0];
+        o.sol = sol + B.offset[p];
+        o.rhs = rhs + B.offset[p];
+        o.rsd = B.rsd + B.offset[p];
+        if (std::memcmp(&o, &B.h_outer[p], sizeof(BOuter)) != 0) changed = true;
+        B.h_outer[p] = o;
+        PMG_TRY_B(c.upload_tail32(maxit, omega, tol));
+    }
+    if (!B.d_outer) PMG_TRY_B(cuda_status(cudaMalloc(&B.d_outer, n * sizeof(BOuter)), "batch allocation"));
+    PMG_TRY_B(cuda_status(cudaMemcpyAsync(B.d_outer, B.h_outer.data(), n * sizeof(BOuter), cudaMemcpyHostToDevice,
+                                          B.stream), "batch upload"));
+    if (B.variant[0] < 0) PMG_TRY_B(batch_autotune(B));
+    PMG_TRY_B(cuda_status(cudaMemsetAsync(B.d_ndone, 0, sizeof(int), B.stream), "batch init"));
+    PMG_TRY_B(cuda_status(cudaMemsetAsync(B.d_done, 0, n * sizeof(int), B.stream), "batch init"));
+    batch_outer(B, true, tol);
+    const float om = (float)omega, omw = (float)(1.0 - omega);
+    if (!B.graph || B.graph_maxit != maxit || B.graph_omega != omega || B.graph_tol != tol || changed) {
+        if (B.graph) cudaGraphExecDestroy(B.graph);
+        B.graph = nullptr;
+        cudaGraph_t g;
+        PMG_TRY_B(cuda_status(cudaStreamBeginCapture(B.stream, cudaStreamCaptureModeThreadLocal), "graph capture"));
+        for (int q = 0; q < B.inner; ++q) batch_vcycle(B, maxit, om, omw, q == 0);
+        batch_outer(B, false, tol);
+        PMG_TRY_B(cuda_status(cudaStreamEndCapture(B.stream, &g), "graph capture"));
+        const cudaError_t ie = cudaGraphInstantiate(&B.graph, g, 0);
+        cudaGraphDestroy(g);
+        PMG_TRY_B(cuda_status(ie, "graph instantiate"));
+        B.graph_maxit = maxit;
+        B.graph_omega = omega;
+        B.graph_tol = tol;
+    }
+    int ndone = 0;
+    for (int c = 0; c < max_cycles && ndone < n; ++c) {
+        PMG_TRY_B(cuda_status(cudaGraphLaunch(B.graph, B.stream), "graph launch"));
+        PMG_TRY_B(cuda_status(cudaMemcpyAsync(&ndone, B.d_ndone, sizeof(int), cudaMemcpyDeviceToHost, B.stream),
+                              "batch progress"));
+        PMG_TRY_B(cuda_status(cudaStreamSynchronize(B.stream), "batch sync"));
+    }
+    PMG_TRY_B(cuda_status(cudaEventRecord(e1, B.stream), "batch event"));
+    PMG_TRY_B(cuda_status(cudaEventSynchronize(e1), "batch event"));
+    if (elapsed_ms) cudaEventElapsedTime(elapsed_ms, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (cycles) PMG_TRY_B(cuda_status(cudaMemcpy(cycles, B.d_cycles, n * sizeof(int), cudaMemcpyDeviceToHost), "copy"));
+    if (ratio) PMG_TRY_B(cuda_status(cudaMemcpy(ratio, B.d_ratio, n * sizeof(double), cudaMemcpyDeviceToHost), "copy"));
+    return PMG_OK;
+}
+
+void batch_destroy(Batch *B)
+{
+    if (!B) return;
+    cudaStreamSynchronize(B->stream);
+    cudaStream_t s = B->stream;
+    delete B;
+    if (s) cudaStreamDestroy(s);
+}
+
+void batch_layout(const Batch &B, long long *offsets, int *levels)
+{
+    for (int p = 0; p <= B.n; ++p)
+        if (offsets) offsets[p] = B.offset[p];
+    for (int p = 0; p < B.n; ++p)
+        if (levels) levels[p] = B.probs[p]->nl;
+}
+
+int batch_size(const Batch &B) { return B.n; }
+
+}  // namespace pmg

@@ -76,6 +76,9 @@ struct Ctx {
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     MixedState *mixed = nullptr;
     Profiler prof;
+    bool autotune = true;       // tune the fused smoother per level in setup_mixed
+    // adjoint scratch (finest level)
+    double *adj_rhs = nullptr, *adj_sol = nullptr, *adj_rsd = nullptr, *adj_vol = nullptr, *adj_faces = nullptr;
 
     int build(const pmg_config_t *c, cudaStream_t s);
     ~Ctx();
@@ -103,6 +106,7 @@ struct Ctx {
     int rbgs_solver_dev(int l, double *x, const double *b, int maxit, double tol, double omega, int *iters,
                         double *ratio_out);
     int cg_dev(int l, double *x, const double *b, int maxit, double tol, bool check, int *iters, double *ratio_out);
+    int adjoint(const double *dLdu, double *dLdb, double *dLdg, int maxit, double tol, double omega, pmg_report_t *rep);
 };
 
 }  // namespace pmg

@@ -82,6 +82,18 @@ int tune_smoother(const LevelK<float> &L, const Launch &ln, float *e0, float *e1
 // Integer-pipe precision conversions used by the outer kernels (self-test hook).
 int convert_selftest(const double *in64, float *out32, const float *in32, double *out64, int n, cudaStream_t s);
 
+// Coarse tails of a batch: one CTA per problem (pmg_mixed.cu).
+int batch_tail32(const TailDesc<float> *const *descs, int n, const int *done, int threads, cudaStream_t s);
+
+// ---- batched solver, pmg_batch.cu ---------------------------------------------------
+struct Batch;
+int batch_create(Batch **out, int n, const int *dims, const double *const *meshes, int inner, cudaStream_t user);
+int batch_solve(Batch &B, double *sol, const double *rhs, int maxit, double tol, double omega, int max_cycles,
+                int *cycles, double *ratio, float *elapsed_ms);
+void batch_destroy(Batch *B);
+void batch_layout(const Batch &B, long long *offsets, int *levels);
+int batch_size(const Batch &B);
+
 // Fixed launch shapes (shared with the host driver for partial-sum sizing).
 void grid_for_cells(const LevelK<double> &L, const Launch &ln, dim3 *grid, dim3 *block);
 

@@ -19,8 +19,9 @@
 #include <cstring>
 #include <vector>
 
+#include "pmg_cell32.cuh"
 #include "pmg_ctx.h"
-#include "pmg_tail64.cuh"
+#include "pmg_mixed.h"
 #include "pmg_smooth32.cuh"
 
 namespace pmg {
@@ -33,120 +34,6 @@ constexpr int kMaxGridZ = 65535;
 
 __device__ __forceinline__ int tid2() { return threadIdx.x + blockDim.x * threadIdx.y; }
 __device__ __forceinline__ int blin() { return blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z); }
-
-// ---------------------------------------------------------------------------------
-// FP32 per-cell arithmetic
-// ---------------------------------------------------------------------------------
-__device__ __forceinline__ float diag32(const LevelK<float> &L, int i, int j, int k)
-{
-    return -((L.sx[i] + (L.cym[j] + L.cyp[j])) + (L.czm[k] + L.czp[k]));
-}
-
-__device__ __forceinline__ float nbsum32(const LevelK<float> &L, const float *x, long long p, int i, int j, int k)
-{
-    float t = L.cxm[i] * x[p - 1];
-    t = fmaf(L.cxp[i], x[p + 1], t);
-    t = fmaf(L.cym[j], x[p - L.sy], t);
-    t = fmaf(L.cyp[j], x[p + L.sy], t);
-    t = fmaf(L.czm[k], x[p - L.sz], t);
-    t = fmaf(L.czp[k], x[p + L.sz], t);
-    return t;
-}
-
-__device__ __forceinline__ float rbgs32(const LevelK<float> &L, const float *x, const float *b, int i, int j, int k,
-                                        float omega, float omw)
-{
-    const long long p = lin(i, j, k, L.sy, L.sz);
-    const float t = nbsum32(L, x, p, i, j, k);
-    const float c0 = diag32(L, i, j, k);
-    return fmaf(omw, x[p], __fdividef(omega * (b[p] - t), c0));
-}
-
-__device__ __forceinline__ float resid32(const LevelK<float> &L, const float *x, const float *b, int i, int j, int k)
-{
-    const long long p = lin(i, j, k, L.sy, L.sz);
-    return b[p] - fmaf(diag32(L, i, j, k), x[p], nbsum32(L, x, p, i, j, k));
-}
-
-// Fused residual + restriction: b_c(i,j,k) = R (b_f - A_f e_f) without storing the
-// fine residual (src/multigrid.f90:1932-1933 and :1939-1940); the eight children in the
-// reference's term order (src/multigrid.f90:1474-1491), accumulated one at a time.
-__device__ __forceinline__ float resrestrict_cell32(const LevelK<float> &F, const XferK<float> &X, const float *e,
-                                                    const float *b, int i, int j, int k)
-{
-    const int ip = i * X.stx, iz = ip - (X.stx - 1);
-    const int jp = j * X.sty, jz = jp - (X.sty - 1);
-    const int kp = k * X.stz, kz = kp - (X.stz - 1);
-    const float xz = X.wx[iz], xp = X.wx[ip], yz = X.wy[jz], yp = X.wy[jp], zz = X.wz[kz], zp = X.wz[kp];
-    float vol = 0.f, s = 0.f;
-#pragma unroll
-    for (int c = 0; c < 8; ++c) {
-        const int fi = (c & 1) ? iz : ip, fj = (c & 2) ? jz : jp, fk = (c & 4) ? kz : kp;
-        const float wv = ((c & 1) ? xp : xz) * ((c & 2) ? yp : yz) * ((c & 4) ? zp : zz);
-        vol += wv;
-        s = fmaf(wv, resid32(F, e, b, fi, fj, fk), s);
-    }
-    return __fdividef(s, vol);
-}
-
-__device__ __forceinline__ float prolong_child32(float ax, float bx, float ay, float by, float az, float bz,
-                                                 float v000, float v100, float v010, float v001, float v110,
-                                                 float v101, float v011, float v111)
-{
-    const float axy = ax * ay, bxy = bx * ay, axby = ax * by, bxby = bx * by;
-    float t = axy * az * v000;
-    t = fmaf(bxy * az, v100, t);
-    t = fmaf(axby * az, v010, t);
-    t = fmaf(axy * bz, v001, t);
-    t = fmaf(bxby * az, v110, t);
-    t = fmaf(bxy * bz, v101, t);
-    t = fmaf(axby * bz, v011, t);
-    t = fmaf(bxby * bz, v111, t);
-    return __fdividef(t, (ax + bx) * (ay + by) * (az + bz));
-}
-
-// e_f += P e_c for the children of one coarse cell (src/multigrid.f90:1652-1758 and
-// the correction x = x + r of :1958).
-__device__ __forceinline__ void prolong_add_cell32(const XferK<float> &X, const float *vc, float *vf, int i, int j,
-                                                   int k)
-{
-    const int ox = X.stx - 1, oy = X.sty - 1, oz = X.stz - 1;
-    const int ip = i * X.stx, iz = ip - ox;
-    const int jp = j * X.sty, jz = jp - oy;
-    const int kp = k * X.stz, kz = kp - oz;
-    const int csy = X.csy;
-    const long long csz = X.csz;
-    auto V = [&](int a, int b, int c) { return vc[lin(a, b, c, csy, csz)]; };
-#pragma unroll
-    for (int sk = 0; sk < 2; ++sk) {
-        if (sk == 0 && oz == 0) continue;
-        const float az = sk ? X.pzn[kp] : X.pzp[kz];
-        const float bz = sk ? X.pzn[kz] : X.pzp[kp];
-        const int kn = sk ? k + oz : k - oz;
-        const int kf = sk ? kp : kz;
-#pragma unroll
-        for (int sj = 0; sj < 2; ++sj) {
-            if (sj == 0 && oy == 0) continue;
-            const float ay = sj ? X.pyn[jp] : X.pyp[jz];
-            const float by = sj ? X.pyn[jz] : X.pyp[jp];
-            const int jn = sj ? j + oy : j - oy;
-            const int jf = sj ? jp : jz;
-#pragma unroll
-            for (int si = 0; si < 2; ++si) {
-                if (si == 0 && ox == 0) continue;
-                const float ax = si ? X.pxn[ip] : X.pxp[iz];
-                const float bx = si ? X.pxn[iz] : X.pxp[ip];
-                const int in = si ? i + ox : i - ox;
-                const int ifn = si ? ip : iz;
-                const float v = prolong_child32(ax, bx, ay, by, az, bz, V(i, j, k), V(in, j, k), V(i, jn, k),
-                                                V(i, j, kn), V(in, jn, k), V(in, j, kn), V(i, jn, kn),
-                                                V(in, jn, kn));
-                const long long q = lin(ifn, jf, kf, X.fsy, X.fsz);
-                vf[q] += v;
-            }
-        }
-    }
-}
 
 // ---------------------------------------------------------------------------------
 // FP32 grid kernels
@@ -182,32 +69,6 @@ __global__ void __launch_bounds__(kBX *kBY, 4) k_resrestrict32(LevelK<float> F, 
         for (int j = blockIdx.y * blockDim.y + threadIdx.y + 1; j <= X.ncy; j += gridDim.y * blockDim.y)
             for (int i = blockIdx.x * blockDim.x + threadIdx.x + 1; i <= X.ncx; i += gridDim.x * blockDim.x)
                 bc[lin(i, j, k, X.csy, X.csz)] = resrestrict_cell32(F, X, e, b, i, j, k);
-}
-
-// Coarse index, neighbour and the two 1-D weights of fine index f along one axis
-// (stride 2: odd f is the low child (z_f), even f the high child (p_f); stride 1: the
-// high child, src/multigrid.f90:1594-1649).
-__device__ __forceinline__ void side_weights(int st, int f, const float *pp, const float *pn, int *c, int *nb,
-                                             float *wa, float *wb)
-{
-    if (st == 2) {
-        const int cc = (f + 1) >> 1;
-        *c = cc;
-        if (f & 1) {
-            *nb = cc - 1;
-            *wa = pp[f];
-            *wb = pp[f + 1];
-        } else {
-            *nb = cc + 1;
-            *wa = pn[f];
-            *wb = pn[f - 1];
-        }
-    } else {
-        *c = f;
-        *nb = f;
-        *wa = pn[f];
-        *wb = pn[f];
-    }
 }
 
 // e_f += P e_c with one thread per fine x-pair (the two x-children of a coarse cell share
@@ -252,40 +113,6 @@ __global__ void __launch_bounds__(kBX *kBY) k_prolong_add32(XferK<float> X, int 
 // ---------------------------------------------------------------------------------
 // FP64 outer kernels
 // ---------------------------------------------------------------------------------
-// Round-to-nearest-even double -> float, from the IEEE-754 encodings, on the integer
-// pipe (the FP64 pipe is the bottleneck of the outer kernels).  Results that are not
-// normal floats (zero, subnormal, overflow, NaN) use the hardware conversion.
-__device__ __forceinline__ float f64_to_f32_rn(double v)
-{
-    const unsigned long long bits = (unsigned long long)__double_as_longlong(v);
-    const int e = (int)((bits >> 52) & 0x7ff) - 1023;
-    if (e < -126 || e > 127) return __double2float_rn(v);
-    const unsigned long long m = bits & 0xFFFFFFFFFFFFFull;
-    const unsigned hi = (unsigned)(m >> 29);
-    const unsigned long long rem = m & 0x1FFFFFFFull;
-    unsigned f = ((unsigned)(e + 127) << 23) | hi;
-    if (rem > 0x10000000ull || (rem == 0x10000000ull && (hi & 1u))) f += 1u;   // carry may reach the exponent
-    f |= (unsigned)(bits >> 32) & 0x80000000u;
-    return __uint_as_float(f);
-}
-
-// Exact float -> double from the encodings (integer pipe); subnormal, Inf and NaN
-// inputs use the hardware conversion.
-__device__ __forceinline__ double f32_to_f64(float f)
-{
-    const unsigned u = __float_as_uint(f);
-    const unsigned e = (u >> 23) & 0xffu;
-    const unsigned long long sign = (unsigned long long)(u & 0x80000000u) << 32;
-    if (e == 0u) {
-        if ((u & 0x7fffffu) == 0u) return __longlong_as_double((long long)sign);
-        return (double)f;
-    }
-    if (e == 255u) return (double)f;
-    const unsigned long long bits = sign | ((unsigned long long)(e + 896u) << 52) |
-                                    ((unsigned long long)(u & 0x7fffffu) << 29);
-    return __longlong_as_double((long long)bits);
-}
-
 // r = b - A x in FP64 (FMA form: r = b + d x - sum c x_nb with d = -c0, the diagonal
 // from the per-axis sums dxx = cxm+cxp, dyy, dzz), stored both as the FP64 residual and
 // as the FP32 right-hand side of the inner system, with the per-block sum of r^2.
@@ -310,14 +137,7 @@ __global__ void __launch_bounds__(kBX *kBY) k_outer_residual(LevelK<double> L, c
                     const int i = i0 + u * kBX;
                     if (i > L.nx) break;
                     const long long p = lin(i, j, k, L.sy, L.sz);
-                    const double d = L.sx[i] + dyz;
-                    double v = fma(d, x[p], b[p]);
-                    v = fma(-L.cxm[i], x[p - 1], v);
-                    v = fma(-L.cxp[i], x[p + 1], v);
-                    v = fma(-L.cym[j], x[p - L.sy], v);
-                    v = fma(-L.cyp[j], x[p + L.sy], v);
-                    v = fma(-L.czm[k], x[p - L.sz], v);
-                    v = fma(-L.czp[k], x[p + L.sz], v);
+                    const double v = outer_residual_cell(L, dyz, x, b, i, j, k, p);
                     r[p] = v;
                     r32[lin(i, j, k, sy32, sz32)] = f64_to_f32_rn(v);
                     acc = fma(v, v, acc);
@@ -355,86 +175,19 @@ __global__ void k_convert_test(const double *in64, float *out32, const float *in
 // FP32 single-CTA coarse tail (same sequence as the FP64 tail in pmg_f64.cu); the
 // coarsest solver's dot products and its convergence test are FP64.
 // ---------------------------------------------------------------------------------
-template <typename F>
-__device__ __forceinline__ void for_cells(int nx, int ny, int nz, F f)
-{
-    const long long n = (long long)nx * ny * nz;
-    for (long long q = threadIdx.x; q < n; q += blockDim.x) {
-        const int i = (int)(q % nx) + 1;
-        const long long rr = q / nx;
-        f(i, (int)(rr % ny) + 1, (int)(rr / ny) + 1);
-    }
-}
-
-__device__ void t32_sweeps(const LevelK<float> &L, float *x, const float *b, int iters, float omega, float omw,
-                           bool zero_start)
-{
-    const int hx = (L.nx + 1) / 2;
-    const long long nq = (long long)hx * L.ny * L.nz;
-    for (int it = 0; it < iters; ++it)
-        for (int colour = 0; colour < 2; ++colour) {
-            if (zero_start && it == 0 && colour == 0) {
-                for_cells(L.nx, L.ny, L.nz, [&](int i, int j, int k) {
-                    const long long p = lin(i, j, k, L.sy, L.sz);
-                    x[p] = ((i + j + k) & 1) ? __fdividef(omega * b[p], diag32(L, i, j, k)) : 0.f;
-                });
-            } else {
-                for (long long q = threadIdx.x; q < nq; q += blockDim.x) {
-                    const int t = (int)(q % hx);
-                    const long long rr = q / hx;
-                    const int j = (int)(rr % L.ny) + 1, k = (int)(rr / L.ny) + 1;
-                    const int i = 2 * t + 1 + ((j + k + colour) & 1);
-                    if (i <= L.nx) x[lin(i, j, k, L.sy, L.sz)] = rbgs32(L, x, b, i, j, k, omega, omw);
-                }
-            }
-            __syncthreads();
-        }
-}
-
 __global__ void __launch_bounds__(kTail32Threads) k_tail32(const TailDesc<float> *__restrict__ Dp)
 {
     __shared__ double sw[kTail32Threads / 32];
-    const TailDesc<float> &D = *Dp;
-    const float omega = D.omega, omw = D.omw;
-    for (int l = D.l0; l < D.nl; ++l) {
-        const LevelK<float> L = D.L[l];
-        const XferK<float> X = D.X[l];
-        float *x = D.x[l], *bc = D.b[l + 1];
-        const float *b = D.b[l];
-        t32_sweeps(L, x, b, D.maxit, omega, omw, true);
-        for_cells(X.ncx, X.ncy, X.ncz, [&](int i, int j, int k) {
-            bc[lin(i, j, k, X.csy, X.csz)] = resrestrict_cell32(L, X, x, b, i, j, k);
-        });
-        __syncthreads();
-    }
-    // coarsest level: solved in FP64 (b converted up, x converted down), so its
-    // convergence test against the FP64 tolerance is attainable
-    {
-        const LevelK<float> L = D.L[D.nl];
-        const LevelK<double> &C = D.C64;
-        float *x = D.x[D.nl];
-        const float *b = D.b[D.nl];
-        for_cells(L.nx, L.ny, L.nz, [&](int i, int j, int k) {
-            D.cb64[lin(i, j, k, C.sy, C.sz)] = (double)b[lin(i, j, k, L.sy, L.sz)];
-        });
-        __syncthreads();
-        const int iters = coarse_solve_f64(C, D.cx64, D.cb64, D.cp64, D.cap64, D.crr64, D.coarse_solver,
-                                           D.coarse_maxit, D.tol, D.omega64, D.omw64, sw);
-        for_cells(L.nx, L.ny, L.nz, [&](int i, int j, int k) {
-            x[lin(i, j, k, L.sy, L.sz)] = (float)D.cx64[lin(i, j, k, C.sy, C.sz)];
-        });
-        if (threadIdx.x == 0 && D.iters_out) *D.iters_out = iters;
-        __syncthreads();
-    }
-    for (int l = D.nl - 1; l >= D.l0; --l) {
-        const LevelK<float> L = D.L[l];
-        const XferK<float> X = D.X[l];
-        float *x = D.x[l], *xc = D.x[l + 1];
-        const float *b = D.b[l];
-        for_cells(X.ncx, X.ncy, X.ncz, [&](int i, int j, int k) { prolong_add_cell32(X, xc, x, i, j, k); });
-        __syncthreads();
-        t32_sweeps(L, x, b, D.maxit, omega, omw, false);
-    }
+    tail32_body(*Dp, sw);
+}
+
+// One CTA per problem: the coarse tails of a batch (problems marked done are skipped).
+__global__ void __launch_bounds__(kTail32Threads) k_batch_tail32(const TailDesc<float> *const *__restrict__ descs,
+                                                                 const int *__restrict__ done)
+{
+    __shared__ double sw[kTail32Threads / 32];
+    if (done[blockIdx.x]) return;
+    tail32_body(*descs[blockIdx.x], sw);
 }
 
 dim3 grid3m(int nxt, int ny, int nz, const Launch &ln)
@@ -447,32 +200,6 @@ dim3 grid3m(int nxt, int ny, int nz, const Launch &ln)
 }
 
 }  // namespace
-
-struct MixedState {
-    std::vector<float> tables_host;
-    float *tables = nullptr;
-    double *diag64 = nullptr;        // per level: dyy (ny+2) and dzz (nz+2) for the outer residual
-    std::vector<const double *> dyy, dzz;
-    std::vector<LevelK<float>> K;
-    std::vector<XferK<float>> X;
-    std::vector<float *> alloc;      // raw allocations
-    std::vector<float *> e[2], b;    // e[buf][l] (two buffers for out-of-place sweeps), b[l]
-    std::vector<int> cur;            // current buffer of e at each level
-    std::vector<bool> fused;         // level uses the fused out-of-place smoother
-    std::vector<int> variant, kchunk;  // autotuned tile variant and k-chunk of the fused smoother
-    TailDesc<float> tail_host;
-    TailDesc<float> *d_tail = nullptr;
-    int inner = 2;
-    ~MixedState()
-    {
-        cudaFree(tables);
-        cudaFree(diag64);
-        for (auto p : alloc) cudaFree(p);
-        cudaFree(d_tail);
-    }
-    float *E(int l) const { return e[cur[l]][l]; }
-    float *Eother(int l) const { return e[1 - cur[l]][l]; }
-};
 
 #define PMG_TRY_M(expr)                \
     do {                               \
@@ -572,7 +299,7 @@ int Ctx::setup_mixed()
     }
     PMG_TRY_M(mstatus(cudaMalloc(&m->d_tail, sizeof(TailDesc<float>)), "mixed tail descriptor"));
     for (int l = 0; l < tail_l0; ++l)
-        if (m->fused[l]) PMG_TRY_M(tune_smoother(m->K[l], launch[l], m->e[0][l], m->e[1][l], m->b[l], stream,
+        if (m->fused[l] && autotune) PMG_TRY_M(tune_smoother(m->K[l], launch[l], m->e[0][l], m->e[1][l], m->b[l], stream,
                                                  &m->variant[l], &m->kchunk[l]));
     return PMG_OK;
 }
@@ -755,6 +482,13 @@ int convert_selftest(const double *in64, float *out32, const float *in32, double
     k_convert_test<<<std::max(1, std::min((n + 255) / 256, 4096)), 256, 0, s>>>(in64, out32, in32, out64, n);
     count_launches(1);
     return cuda_status(cudaGetLastError(), "conversion self-test");
+}
+
+int batch_tail32(const TailDesc<float> *const *descs, int n, const int *done, int threads, cudaStream_t s)
+{
+    k_batch_tail32<<<n, threads, 0, s>>>(descs, done);
+    count_launches(1);
+    return cuda_status(cudaGetLastError(), "batch coarse tails");
 }
 
 void Ctx::destroy_mixed()

@@ -1,0 +1,37 @@
+// pmg_mixed.h -- state of the mixed-precision V-cycle of one problem (FP32 hierarchy).
+#pragma once
+
+#include <vector>
+
+#include "pmg_internal.h"
+
+namespace pmg {
+
+struct MixedState {
+    std::vector<float> tables_host;
+    float *tables = nullptr;
+    double *diag64 = nullptr;        // per level: dyy (ny+2) and dzz (nz+2) for the outer residual
+    std::vector<const double *> dyy, dzz;
+    std::vector<LevelK<float>> K;
+    std::vector<XferK<float>> X;
+    std::vector<float *> alloc;      // raw allocations
+    std::vector<float *> e[2], b;    // e[buf][l] (two buffers for out-of-place sweeps), b[l]
+    std::vector<int> cur;            // current buffer of e at each level
+    std::vector<bool> fused;         // level uses the fused out-of-place smoother
+    std::vector<int> variant, kchunk;  // autotuned tile variant and k-chunk of the fused smoother
+    TailDesc<float> tail_host;
+    TailDesc<float> *d_tail = nullptr;
+    int inner = 2;
+    ~MixedState()
+    {
+        cudaFree(tables);
+        cudaFree(diag64);
+        for (auto p : alloc) cudaFree(p);
+        cudaFree(d_tail);
+    }
+    float *E(int l) const { return e[cur[l]][l]; }
+    float *Eother(int l) const { return e[1 - cur[l]][l]; }
+};
+
+
+}  // namespace pmg

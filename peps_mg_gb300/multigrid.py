@@ -235,6 +235,24 @@ class Multigrid:
     def sync(self):
         check(self._lib.pmg_sync(self._h), "sync")
 
+    # -- adjoint --------------------------------------------------------------------------
+    def adjoint(self, dLdu, dLdb, maxiteration, tolerance, omega_sor):
+        """Gradients of a loss of the solution (pmg_adjoint): fills dLdb (device array of
+        the finest level) and returns (SolveReport of the transposed solve, dL/dg[6])."""
+        g = (ctypes.c_double * 6)()
+        hist = np.zeros(3 * max(self.number_of_vcycles, 1))
+        citers = np.zeros(max(self.number_of_vcycles, 1), dtype=np.int32)
+        rep = PmgReport()
+        rep.history = hist.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+        rep.coarse_iterations = citers.ctypes.data_as(ctypes.POINTER(ctypes.c_int))
+        rc = self._lib.pmg_adjoint(self._h, self._dev(dLdu, 0, "dLdu"), self._dev(dLdb, 0, "dLdb"), g,
+                                   int(maxiteration), float(tolerance), float(omega_sor), ctypes.byref(rep))
+        check(rc, "adjoint")
+        out = SolveReport(rep.cycles, bool(rep.converged), rep.res0, rep.final_ratio,
+                          hist[:3 * rep.cycles].reshape(rep.cycles, 3).copy(), citers[:rep.cycles].copy(),
+                          rep.elapsed_ms, rep.inner_cycles)
+        return out, np.array(g[:])
+
     # -- telemetry ----------------------------------------------------------------------------
     def profile(self, enable=True):
         """Enable (and reset) or disable CUDA-event timing of the finest-level launches."""

@@ -1,0 +1,72 @@
+"""Batched solver: every problem of an uneven batch converges, agrees with the single-
+problem mixed solver, and (for a sample) with the FP64 oracle."""
+import numpy as np
+import pytest
+
+torch = pytest.importorskip("torch")
+pytestmark = pytest.mark.gpu
+
+import peps_mg_gb300 as pmg  # noqa: E402
+from oracle import oracle as O  # noqa: E402
+from peps_mg_gb300.batch import BatchSolver  # noqa: E402
+from tests.helpers import from_dev, rel, to_dev  # noqa: E402
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _need_gpu():
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+
+
+def batch_dims(count, sizes, seed=4):
+    rng = np.random.Generator(np.random.PCG64(seed))
+    return rng.choice(sizes, size=(count, 3))
+
+
+def fill(bs, seed=4):
+    rng = np.random.Generator(np.random.PCG64(seed + 100))
+    rhs = bs.field()
+    for p in range(bs.n):
+        v = bs.view(rhs, p)
+        nz, ny, nx = (s - 2 for s in v.shape)
+        v[1:-1, 1:-1, 1:-1] = torch.from_numpy(rng.uniform(-1, 1, (nz, ny, nx))).cuda()
+    return rhs
+
+
+def test_batch_matches_single_problem_solves():
+    dims = batch_dims(12, [8, 12, 16, 24, 32, 48])
+    with BatchSolver(dims) as bs:
+        rhs = fill(bs)
+        sol = bs.field()
+        cycles, ratio, ms = bs.solve(sol, rhs, 2, 1e-10, 1.0, max_cycles=60)
+        assert np.all(ratio < 1e-10), ratio
+        for p in range(bs.n):
+            nx, ny, nz = (int(v) for v in dims[p])
+            mesh = [pmg.geometry.uniform_axis(m, 0.0, 1.0) for m in (nx, ny, nz)]
+            with pmg.Multigrid(mesh, int(bs.levels[p]), 60, "cgs", precision="mixed") as mg:
+                s1 = torch.zeros_like(bs.view(rhs, p))
+                r1 = torch.zeros_like(s1)
+                rep = mg.solve_vcycle(s1, r1, bs.view(rhs, p).contiguous(), 2, 1e-10, 1.0)
+            assert abs(rep.cycles - cycles[p]) <= 1
+            assert rel(from_dev(bs.view(sol, p)), from_dev(s1)) < 1e-8
+
+
+def test_batch_against_fp64_oracle_sample():
+    dims = batch_dims(6, [16, 24, 32], seed=11)
+    with BatchSolver(dims) as bs:
+        rhs = fill(bs, seed=11)
+        sol = bs.field()
+        cycles, ratio, _ = bs.solve(sol, rhs, 2, 1e-10, 1.0, max_cycles=60)
+        assert np.all(ratio < 1e-10)
+        for p in (0, 3, 5):
+            nx, ny, nz = (int(v) for v in dims[p])
+            mesh = [pmg.geometry.uniform_axis(m, 0.0, 1.0) for m in (nx, ny, nz)]
+            omg = O.OracleMG(mesh, int(bs.levels[p]), 100, 0)
+            ref, rr = O.field(nx, ny, nz), O.field(nx, ny, nz)
+            omg.solve(ref, rr, from_dev(bs.view(rhs, p)), 2, 1e-10, 1.0)
+            assert rel(from_dev(bs.view(sol, p)), ref) < 1e-8
+
+
+def test_batch_rejects_bad_sizes():
+    with pytest.raises(pmg.PmgError):
+        BatchSolver([[9, 9, 9]])
