@@ -43,8 +43,8 @@ def _lib(omp=False):
 
 
 def P(a):
-    """Pointer to a contiguous float64 numpy array."""
-    assert a.dtype == np.float64 and (a.flags.f_contiguous or a.flags.c_contiguous)
+    """Pointer to a Fortran-ordered (column-major) contiguous float64 numpy array."""
+    assert a.dtype == np.float64 and a.flags.f_contiguous, "oracle arrays must be float64 in Fortran order"
     return a.ctypes.data_as(_dp)
 
 
