@@ -172,6 +172,26 @@ int pmg_batch_solve(pmg_batch *batch, double *sol, const double *rhs, int maxite
                     double omega_sor, int max_cycles, int *cycles, double *ratio, float *elapsed_ms);
 int pmg_batch_destroy(pmg_batch *batch);
 
+/* ---- Dot product without device allocation (no counterpart in the reference) ------ */
+/* For host codes that must not have a library call cudaMalloc: one whose device memory
+ * is handed to its own allocator at start-up, or one calling from inside its iteration
+ * loop, where cudaMalloc/cudaFree would synchronise the whole device.  Such a caller keeps
+ * its own CG loop around vv_dot_3d_matrix (src/poisson_matrix_operator.f90:40) and has no
+ * pmg_ctx (creating one allocates the level hierarchy).
+ *   *result = sum over the interior cells of x(i,j,k) * y(i,j,k)
+ * x, y: device arrays in the (0:nx+1, 0:ny+1, 0:nz+1) layout; stream: a cudaStream_t
+ * (NULL = the default stream).  The value equals pmg_vv_dot's on the same arrays to
+ * within FP64 rounding (bit for bit when nz * ceil(nx/32) * ceil(ny/8) <= 16384).
+ * Nothing is allocated: the partial sums live in a static 128 KiB device array that every
+ * GPU loading this library holds until the process exits.  Limit: ceil(nx/32) *
+ * ceil(ny/8) <= 16384 (e.g. planes up to 2048 x 2048); larger planes return PMG_EINVAL
+ * with a message in pmg_last_error.  The first call on each device does a one-time
+ * set-up on that device (it looks up the array's address and clears it); make that
+ * first call before any stream capture.  All calls on one device share the array, so
+ * calls that overlap in time (from several host threads, or on several streams at once)
+ * race: serialise them.  Synchronous: returns after *result is written. */
+int pmg_vv_dot_static(const double *x, const double *y, int nx, int ny, int nz, void *stream, double *result);
+
 /* ---- Telemetry (no counterpart in the reference; it only prints MPI_Wtime) ------ */
 /* Kernel classes of pmg_profile_read (finest-level launches only). */
 #define PMG_PROF_SMOOTH32 0       /* FP32 RBGS half-sweep                    */

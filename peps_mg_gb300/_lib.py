@@ -62,6 +62,7 @@ _SIGS = {
     "pmg_batch_solve": [c_void_p, c_void_p, c_void_p, c_int, c_double, c_double, c_int, ctypes.POINTER(c_int),
                         ctypes.POINTER(c_double), ctypes.POINTER(c_float)],
     "pmg_batch_destroy": [c_void_p],
+    "pmg_vv_dot_static": [c_void_p, c_void_p, c_int, c_int, c_int, c_void_p, ctypes.POINTER(c_double)],
     "pmg_profile": [c_void_p, c_int],
     "pmg_profile_read": [c_void_p, c_int, ctypes.POINTER(c_double), ctypes.POINTER(ctypes.c_longlong),
                          ctypes.POINTER(c_double)],

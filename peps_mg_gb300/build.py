@@ -28,6 +28,7 @@ UNITS = {
     "pmg_smooth32.cu": ["--fmad=true"],
     "pmg_batch.cu": ["--fmad=true"],
     "pmg_adjoint.cu": ["--fmad=false"],
+    "pmg_dot_static.cu": ["--fmad=false"],
 }
 
 
