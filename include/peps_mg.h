@@ -218,6 +218,18 @@ int pmg_launch_count(long long *count);
  * out64[q] = (double)in32[q]; device pointers, synchronous. */
 int pmg_selftest_convert(const double *in64, float *out32, const float *in32, double *out64, int n);
 
+/* Self-test of the fused FP32 smoother of a mixed-precision context (no counterpart in the
+ * reference): e_out = one red-black iteration (src/rbgs_poisson_matrix.f90:235-273) of
+ * e_in for right-hand side b on `level`, computed in FP32 by the fused kernel.
+ * impl: 0 = TMA-fed kernel, 1 = register-window kernel; variant 0/1/2 = tiles 60 x 14 /
+ * 60 x 6 / 60 x 10; kchunk: planes per work item (0 = automatic); zero_in: treat e_in as
+ * zero.  Host arrays of the level's (0:nx+1,0:ny+1,0:nz+1) Fortran layout (ghosts of
+ * e_in and b must be zero); e_out receives every cell.  PMG_EINVAL when the level has no
+ * fused smoother or impl 0 is unavailable for it.  Synchronous; overwrites the context's
+ * FP32 work arrays of that level. */
+int pmg_selftest_smooth32(pmg_ctx *ctx, int level, int impl, int variant, int kchunk, int zero_in, double omega,
+                          const double *e_in, const double *b, double *e_out);
+
 /* Wait for all work issued on the context stream. */
 int pmg_sync(pmg_ctx *ctx);
 /* Text of the last CUDA error seen by this thread ("" if none). */

@@ -68,6 +68,8 @@ _SIGS = {
                          ctypes.POINTER(c_double)],
     "pmg_launch_count": [ctypes.POINTER(ctypes.c_longlong)],
     "pmg_selftest_convert": [c_void_p, c_void_p, c_void_p, c_void_p, c_int],
+    "pmg_selftest_smooth32": [c_void_p, c_int, c_int, c_int, c_int, c_int, c_double, c_void_p, c_void_p,
+                              c_void_p],
     "pmg_sync": [c_void_p],
     "pmg_last_error": [],
     "pmg_status_string": [c_int],

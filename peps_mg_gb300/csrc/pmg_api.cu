@@ -1170,6 +1170,17 @@ int pmg_selftest_convert(const double *in64, float *out32, const float *in32, do
     return pmg::cuda_status(cudaDeviceSynchronize(), "conversion self-test");
 }
 
+int pmg_selftest_smooth32(pmg_ctx *ctx, int level, int impl, int variant, int kchunk, int zero_in, double omega,
+                          const double *e_in, const double *b, double *e_out)
+{
+    PMG_TRY(check_ctx_level(ctx, level));
+    if (!e_in || !b || !e_out || impl < 0 || impl > 1 || variant < 0 || variant > 2 || kchunk < 0) {
+        pmg::set_error("invalid smoother self-test arguments");
+        return PMG_EINVAL;
+    }
+    return ctx->impl.selftest_smooth32(level, impl, variant, kchunk, zero_in != 0, omega, e_in, b, e_out);
+}
+
 int pmg_sync(pmg_ctx *ctx)
 {
     if (!ctx) return PMG_EINVAL;

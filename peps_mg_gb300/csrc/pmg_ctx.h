@@ -100,6 +100,9 @@ struct Ctx {
     int upload_tail32(int maxit, double omega, double tol);
     int vcycle32(int maxit, double omega, bool zero_start);
     int outer_residual(double *sol, double *rsd, const double *rhs, int slot);
+    int check_pipeline();
+    int selftest_smooth32(int level, int impl, int variant, int kchunk, bool zero_in, double omega,
+                          const double *e_in, const double *b, double *e_out);
     void destroy_mixed();
     int solve(double *sol, double *rsd, const double *rhs, int maxit, double tol, double omega, pmg_report_t *rep);
     int level_scratch(int l, double **bufs, int count);

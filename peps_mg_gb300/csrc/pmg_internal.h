@@ -1,6 +1,7 @@
 // pmg_internal.h -- host-side declarations shared by the library's translation units.
 #pragma once
 
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include <string>
@@ -72,13 +73,27 @@ int f64_check(const double *num, const double *den, double tol, int le, int iter
 // One out-of-place red-black iteration e_out = RB(e_in) of a whole level (zero_in: e_in
 // is zero and is not read).  Needs the padded FP32 layout checked by rb32_fused_layout_ok.
 bool rb32_fused_layout_ok(const LevelK<float> &L, const void *e, const void *b);
+// Tensor maps of one padded FP32 level for the TMA-fed variant of the smoother: the two
+// e buffers and b, one map per tile variant (the copy box depends on the tile height).
+struct Rb32Tma {
+    bool ok = false;
+    CUtensorMap e[2][3];
+    CUtensorMap b[3];
+};
+// base[3]: allocation starts of e[0], e[1], b (cell (0,0,0) at base + 5 + sy + sz);
+// rows, planes: allocated rows per plane and planes.  Leaves t->ok false (and returns
+// PMG_OK) when the tensor-map encoder is unavailable or rejects the layout.
+int rb32_tma_setup(Rb32Tma *t, const LevelK<float> &L, float *const base[3], long long rows, long long planes);
 // variant: 0 = 60 x 14 tiles (512 threads), 1 = 60 x 6 (256), 2 = 60 x 10 (384);
-// kchunk: planes per work item (0 = automatic).
+// kchunk: planes per work item (0 = automatic).  With tma (tma->ok), the TMA-fed kernel
+// runs; ein must then be buffer in_buf of the maps, and err receives 1 if one of its
+// bounded pipeline waits gave up.
 int rb32_fused(const LevelK<float> &L, const Launch &ln, const float *ein, float *eout, const float *b, float omega,
-               float omw, bool zero_in, cudaStream_t s, int variant = 0, int kchunk = 0);
+               float omw, bool zero_in, cudaStream_t s, int variant = 0, int kchunk = 0,
+               const Rb32Tma *tma = nullptr, int in_buf = 0, int *err = nullptr);
 // Picks the fastest tile variant and k-chunk for a level (process-wide cache).
 int tune_smoother(const LevelK<float> &L, const Launch &ln, float *e0, float *e1, const float *b, cudaStream_t s,
-                  int *variant, int *kchunk);
+                  int *variant, int *kchunk, const Rb32Tma *tma = nullptr, int *err = nullptr);
 // Integer-pipe precision conversions used by the outer kernels (self-test hook).
 int convert_selftest(const double *in64, float *out32, const float *in32, double *out64, int n, cudaStream_t s);
 

@@ -14,6 +14,8 @@
 // This translation unit is compiled with --fmad=true.
 #include <cuda_runtime.h>
 
+#include <cstdlib>
+
 #include <algorithm>
 #include <cmath>
 #include <cstring>
@@ -23,6 +25,7 @@
 #include "pmg_ctx.h"
 #include "pmg_mixed.h"
 #include "pmg_smooth32.cuh"
+#include "pmg_smooth32_tma.cuh"
 
 namespace pmg {
 
@@ -215,20 +218,30 @@ static int mstatus(cudaError_t e, const char *what) { return cuda_status(e, what
 // ny+1+RB_PAD_ROWS, planes -1 .. nz+1+RB_PAD_PLANES.  The data pointer (cell (0,0,0)) sits
 // an odd number of floats past the 256-byte aligned allocation, so the pair of cells
 // (i, i+1) with i odd is 8-byte aligned.  Padding is never written.
-static int alloc_f32(MixedState *m, int nx, int ny, int nz, int *pitch, long long *plane, float **data)
+// Padded FP32 level array: pitch a multiple of 4 floats with room for every smoother
+// tile's 64 columns, one row and one plane of padding in front, zero rows and planes
+// behind; cell (0,0,0) at base + RBT_DATA_OFF + pitch + plane (an odd float offset, so
+// the smoother's cell pairs (odd i, i+1) are 8-byte aligned and its TMA boxes, which
+// start at cell i0 - 2 = 60 bx - 1, begin on a 16-byte boundary).
+static int alloc_f32(MixedState *m, int nx, int ny, int nz, int *pitch, long long *plane, float **data,
+                     float **base, long long *rows_out, long long *planes_out)
 {
     int p = std::max(64 * ((nx + 63) / 64) + 8, RB_TX * ((nx + RB_TX - 1) / RB_TX) + 8);
-    p += p & 1;
+    p = (p + 3) & ~3;
     const long long rows = (long long)ny + 2 + 1 + RB_PAD_ROWS;
+    const long long planes = (long long)nz + 2 + 1 + RB_PAD_PLANES;
     const long long pl = (long long)p * rows;
-    const size_t n = (size_t)pl * (size_t)(nz + 2 + 1 + RB_PAD_PLANES) + 8;
+    const size_t n = (size_t)pl * (size_t)planes + 8;
     float *a = nullptr;
     PMG_TRY_M(mstatus(cudaMalloc(&a, n * sizeof(float)), "mixed level allocation"));
     PMG_TRY_M(mstatus(cudaMemset(a, 0, n * sizeof(float)), "mixed level init"));
     m->alloc.push_back(a);
     *pitch = p;
     *plane = pl;
-    *data = a + 3 + p + pl;     // skip 3 columns, one row and one plane of padding
+    *data = a + RBT_DATA_OFF + p + pl;
+    *base = a;
+    *rows_out = rows;
+    *planes_out = planes;
     return PMG_OK;
 }
 
@@ -272,19 +285,30 @@ int Ctx::setup_mixed()
     m->fused.assign((size_t)nl + 1, false);
     m->variant.assign((size_t)nl + 1, 0);
     m->kchunk.assign((size_t)nl + 1, 0);
+    m->tma.assign((size_t)nl + 1, Rb32Tma());
+    m->rows.assign((size_t)nl + 1, 0);
+    m->planes.assign((size_t)nl + 1, 0);
+    // PEPS_MG_SMOOTHER=window selects the register-window smoother everywhere
+    const char *sm_env = std::getenv("PEPS_MG_SMOOTHER");
+    const bool use_tma = !(sm_env && std::strcmp(sm_env, "window") == 0);
     for (int l = 0; l <= nl; ++l) {
         const LevelK<double> &k = K[l];
         LevelK<float> &f = m->K[l];
         int pitch = 0;
         long long plane = 0;
-        PMG_TRY_M(alloc_f32(m, k.nx, k.ny, k.nz, &pitch, &plane, &m->e[0][l]));
-        PMG_TRY_M(alloc_f32(m, k.nx, k.ny, k.nz, &pitch, &plane, &m->e[1][l]));
-        PMG_TRY_M(alloc_f32(m, k.nx, k.ny, k.nz, &pitch, &plane, &m->b[l]));
+        float *base[3];
+        long long rows = 0, planes = 0;
+        PMG_TRY_M(alloc_f32(m, k.nx, k.ny, k.nz, &pitch, &plane, &m->e[0][l], &base[0], &rows, &planes));
+        PMG_TRY_M(alloc_f32(m, k.nx, k.ny, k.nz, &pitch, &plane, &m->e[1][l], &base[1], &rows, &planes));
+        PMG_TRY_M(alloc_f32(m, k.nx, k.ny, k.nz, &pitch, &plane, &m->b[l], &base[2], &rows, &planes));
         f.nx = k.nx; f.ny = k.ny; f.nz = k.nz; f.sy = pitch; f.sz = plane;
         f.cxm = F(k.cxm); f.cxp = F(k.cxp); f.sx = F(k.sx);
         f.cym = F(k.cym); f.cyp = F(k.cyp); f.czm = F(k.czm); f.czp = F(k.czp);
         m->fused[l] = l < tail_l0 && rb32_fused_layout_ok(f, m->e[0][l], m->b[l]) &&
                       rb32_fused_layout_ok(f, m->e[1][l], m->b[l]);
+        m->rows[l] = rows;
+        m->planes[l] = planes;
+        if (m->fused[l] && use_tma) PMG_TRY_M(rb32_tma_setup(&m->tma[l], f, base, rows, planes));
     }
     for (int l = 0; l < nl; ++l) {
         const XferK<double> &x = X[l];
@@ -298,9 +322,13 @@ int Ctx::setup_mixed()
         y.pzp = F(x.pzp); y.pzn = F(x.pzn);
     }
     PMG_TRY_M(mstatus(cudaMalloc(&m->d_tail, sizeof(TailDesc<float>)), "mixed tail descriptor"));
+    PMG_TRY_M(mstatus(cudaMalloc(&m->d_err, sizeof(int)), "mixed error flag"));
+    PMG_TRY_M(mstatus(cudaMemset(m->d_err, 0, sizeof(int)), "mixed error flag"));
     for (int l = 0; l < tail_l0; ++l)
-        if (m->fused[l] && autotune) PMG_TRY_M(tune_smoother(m->K[l], launch[l], m->e[0][l], m->e[1][l], m->b[l], stream,
-                                                 &m->variant[l], &m->kchunk[l]));
+        if (m->fused[l] && autotune)
+            PMG_TRY_M(tune_smoother(m->K[l], launch[l], m->e[0][l], m->e[1][l], m->b[l], stream, &m->variant[l],
+                                    &m->kchunk[l], &m->tma[l], m->d_err));
+    PMG_TRY_M(check_pipeline());
     return PMG_OK;
 }
 
@@ -343,7 +371,7 @@ int Ctx::vcycle32(int maxit, double omega, bool zero_start)
         if (m->fused[l]) {
             for (int it = 0; it < maxit; ++it) {
                 PMG_TRY_M(rb32_fused(L, launch[l], m->E(l), m->Eother(l), m->b[l], om, omw, zs && it == 0, stream,
-                                     m->variant[l], m->kchunk[l]));
+                                     m->variant[l], m->kchunk[l], &m->tma[l], m->cur[l], m->d_err));
                 m->cur[l] = 1 - m->cur[l];
             }
             prof.end(pi, PC_SMOOTH32, maxit, 12.0 * N, stream);
@@ -473,6 +501,61 @@ int Ctx::solve_mixed(double *sol, double *rsd, const double *rhs, int maxit, dou
         rep->res0 = std::sqrt(res0tol);
         rep->final_ratio = ratio;
         rep->inner_cycles = inner_total;
+    }
+    return check_pipeline();
+}
+
+int Ctx::selftest_smooth32(int level, int impl, int variant, int kchunk, bool zero_in, double omega,
+                           const double *e_in, const double *b, double *e_out)
+{
+    PMG_TRY_M(setup_mixed());
+    MixedState *m = mixed;
+    if (!m->fused[level] || (impl == 0 && !m->tma[level].ok)) {
+        set_error("the level has no fused smoother of that kind");
+        return PMG_EINVAL;
+    }
+    const LevelK<float> &L = m->K[level];
+    const size_t total = (size_t)L.sz * (size_t)m->planes[level] + 8;
+    const long long front = RBT_DATA_OFF + L.sy + L.sz;
+    const int nx = L.nx, ny = L.ny, nz = L.nz;
+    std::vector<float> he(total, 0.f), hb(total, 0.f);
+    for (int k = 0; k <= nz + 1; ++k)
+        for (int j = 0; j <= ny + 1; ++j)
+            for (int i = 0; i <= nx + 1; ++i) {
+                const size_t src = (size_t)i + (size_t)(nx + 2) * ((size_t)j + (size_t)(ny + 2) * k);
+                const size_t dst = (size_t)(front + i + (long long)L.sy * j + L.sz * k);
+                he[dst] = (float)e_in[src];
+                hb[dst] = (float)b[src];
+            }
+    float *be = m->e[0][level] - front, *bo = m->e[1][level] - front, *bb = m->b[level] - front;
+    PMG_TRY_M(mstatus(cudaMemcpy(be, he.data(), total * sizeof(float), cudaMemcpyHostToDevice), "self-test upload"));
+    PMG_TRY_M(mstatus(cudaMemcpy(bb, hb.data(), total * sizeof(float), cudaMemcpyHostToDevice), "self-test upload"));
+    PMG_TRY_M(mstatus(cudaMemset(bo, 0, total * sizeof(float)), "self-test init"));
+    const float om = (float)omega, omw = (float)(1.0 - omega);
+    PMG_TRY_M(rb32_fused(L, launch[level], m->e[0][level], m->e[1][level], m->b[level], om, omw, zero_in, stream,
+                         variant, kchunk, impl == 0 ? &m->tma[level] : nullptr, 0, m->d_err));
+    PMG_TRY_M(check_pipeline());
+    PMG_TRY_M(mstatus(cudaMemcpy(he.data(), bo, total * sizeof(float), cudaMemcpyDeviceToHost), "self-test read"));
+    for (int k = 0; k <= nz + 1; ++k)
+        for (int j = 0; j <= ny + 1; ++j)
+            for (int i = 0; i <= nx + 1; ++i)
+                e_out[(size_t)i + (size_t)(nx + 2) * ((size_t)j + (size_t)(ny + 2) * k)] =
+                    (double)he[(size_t)(front + i + (long long)L.sy * j + L.sz * k)];
+    m->cur[level] = 0;
+    return PMG_OK;
+}
+
+// The TMA-fed smoother sets the error flag when one of its bounded waits for a copied
+// plane gave up (its results are then incomplete).
+int Ctx::check_pipeline()
+{
+    int e = 0;
+    PMG_TRY_M(mstatus(cudaMemcpyAsync(&e, mixed->d_err, sizeof(int), cudaMemcpyDeviceToHost, stream), "error flag"));
+    PMG_TRY_M(mstatus(cudaStreamSynchronize(stream), "error flag"));
+    if (e) {
+        cudaMemsetAsync(mixed->d_err, 0, sizeof(int), stream);
+        set_error("fused smoother: a wait for a TMA copy timed out");
+        return PMG_ETIMEOUT;
     }
     return PMG_OK;
 }

@@ -19,6 +19,9 @@ struct MixedState {
     std::vector<int> cur;            // current buffer of e at each level
     std::vector<bool> fused;         // level uses the fused out-of-place smoother
     std::vector<int> variant, kchunk;  // autotuned tile variant and k-chunk of the fused smoother
+    std::vector<Rb32Tma> tma;        // tensor maps of the TMA-fed smoother, per level
+    std::vector<long long> rows, planes;   // allocated rows per plane and planes, per level
+    int *d_err = nullptr;            // set by the TMA-fed smoother when a bounded wait gave up
     TailDesc<float> tail_host;
     TailDesc<float> *d_tail = nullptr;
     int inner = 2;
@@ -28,6 +31,7 @@ struct MixedState {
         cudaFree(diag64);
         for (auto p : alloc) cudaFree(p);
         cudaFree(d_tail);
+        cudaFree(d_err);
     }
     float *E(int l) const { return e[cur[l]][l]; }
     float *Eother(int l) const { return e[1 - cur[l]][l]; }

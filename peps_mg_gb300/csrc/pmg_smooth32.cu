@@ -1,20 +1,27 @@
 // pmg_smooth32.cu -- launchers and autotuner of the fused FP32 red-black iteration
-// (device code in pmg_smooth32.cuh).
+// (device code in pmg_smooth32_tma.cuh and pmg_smooth32.cuh).
 //
 // A launch performs one RBGS iteration of a whole level, out of place.  Work items are
 // (60 x TY tile) x (chunk of k planes); a persistent grid of resident CTAs walks them
 // chunk-major.  TY is 6, 10 or 14 (CTAs of 256, 384 or 512 threads); the autotuner
 // times every (TY, k-chunk) candidate on the level's own buffers and keeps the fastest.
+// Two kernels share that mapping: the TMA-fed one (planes copied into a ring of shared
+// stages by the tensor-memory accelerator) wherever the level's tensor maps could be
+// encoded, and the register-window one (per-thread loads three planes ahead) otherwise.
+#include <cuda.h>
+#include <cudaTypedefs.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>
 #include <array>
+#include <cstring>
 #include <map>
 #include <mutex>
 
 #include "../../include/peps_mg.h"
 #include "pmg_internal.h"
 #include "pmg_smooth32.cuh"
+#include "pmg_smooth32_tma.cuh"
 
 namespace pmg {
 
@@ -43,6 +50,48 @@ __global__ void __launch_bounds__(rb_threads<TY>(), rb_min_blocks<TY>()) k_rb32_
         const int k0 = 1 + kchunk * bz;
         const int k1 = min(L.nz, k0 + kchunk - 1);
         rb32_item<TY, ZERO_IN, OMEGA1>(S, L, ein, eout, b, omega, omw, bx, by, k0, k1);
+    }
+}
+
+// blocks per SM the TMA-fed kernel's register budget is sized for
+template <int TY>
+constexpr int rbt_min_blocks() { return TY <= 6 ? 4 : 2; }
+
+template <int TY, bool ZERO_IN, bool OMEGA1>
+__global__ void __launch_bounds__(RbtShape<TY>::THREADS, rbt_min_blocks<TY>())
+    k_rb32_tma(const __grid_constant__ CUtensorMap me, const __grid_constant__ CUtensorMap mb, LevelK<float> L,
+               float *__restrict__ eout, float omega, float omw, RbtItems W, int *err)
+{
+    using S = RbtShape<TY>;
+    extern __shared__ unsigned char smem_raw[];
+    // 128-byte aligned stages (TMA destinations), then the mbarriers
+    unsigned char *smem = smem_raw + ((128u - (rbtdetail::smem_addr(smem_raw) & 127u)) & 127u);
+    unsigned long long *bars = reinterpret_cast<unsigned long long *>(smem + RBT_NS * S::STAGE);
+    if (threadIdx.x == 0) {
+        for (int q = 0; q < RBT_NS; ++q) rbtdetail::mbar_init(&bars[q], 1);
+        rbtdetail::fence_mbar_init();
+    }
+    __syncthreads();
+    RbtProducer<TY, ZERO_IN> prod;
+    if (threadIdx.x == 0) {
+        prod.start(W);
+        prod.issue_upto(RBT_NS - 1, W, smem, bars, &me, &mb);
+    }
+    int cbase = 0;
+    for (int it = blockIdx.x; it < W.nitems; it += gridDim.x) {
+        int bx, by, k0, k1;
+        W.decode(it, bx, by, k0, k1);
+        if (!rbt_item<TY, ZERO_IN, OMEGA1>(smem, bars, L, eout, omega, omw, bx, by, k0, k1, cbase, prod, W, &me,
+                                            &mb)) {
+            if (threadIdx.x == 0) {
+                atomicOr(err, 1);
+                // let the copies still in flight land before the CTA exits (bounded)
+                for (int q = max(0, prod.slot - RBT_NS); q < prod.slot; ++q)
+                    rbtdetail::mbar_wait_bounded(&bars[q % RBT_NS], (unsigned)(q / RBT_NS) & 1u);
+            }
+            return;
+        }
+        cbase += k1 - k0 + 5;
     }
 }
 
@@ -98,11 +147,141 @@ int launch_ty(const LevelK<float> &L, const Launch &ln, const float *ein, float 
     return cuda_status(cudaGetLastError(), "fused fp32 smoother");
 }
 
+template <int TY, bool Z, bool O>
+int tma_attr()
+{
+    static std::once_flag once;
+    static cudaError_t err = cudaSuccess;
+    std::call_once(once, [] {
+        err = cudaFuncSetAttribute(k_rb32_tma<TY, Z, O>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   RbtShape<TY>::SMEM);
+    });
+    return cuda_status(err, "TMA smoother shared memory attribute");
+}
+
+template <int TY>
+int tma_slots(int *slots)
+{
+    static std::once_flag once;
+    static int per = 0, sms = 0;
+    static cudaError_t err = cudaSuccess;
+    std::call_once(once, [] {
+        err = cudaFuncSetAttribute(k_rb32_tma<TY, false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   RbtShape<TY>::SMEM);
+        if (err == cudaSuccess)
+            err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_rb32_tma<TY, false, false>,
+                                                                RbtShape<TY>::THREADS, RbtShape<TY>::SMEM);
+        int dev = 0;
+        if (err == cudaSuccess) err = cudaGetDevice(&dev);
+        if (err == cudaSuccess) err = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    });
+    *slots = std::max(1, per) * std::max(1, sms);
+    return cuda_status(err, "TMA smoother occupancy");
+}
+
+template <int TY>
+int launch_tma(const LevelK<float> &L, const Launch &ln, const Rb32Tma &t, int vi, int in_buf, float *eout,
+               float omega, float omw, bool zero_in, int kchunk_hint, int *err, cudaStream_t s)
+{
+    int slots = 0;
+    PMG_TRY_S(tma_slots<TY>(&slots));
+    RbtItems W;
+    W.ntx = (L.nx + RBT_TX - 1) / RBT_TX;
+    W.nty = (L.ny + TY - 1) / TY;
+    W.nz = L.nz;
+    int kchunk = kchunk_hint;
+    if (kchunk <= 0) {
+        const int want = std::max(1, (4 * slots + W.ntx * W.nty - 1) / (W.ntx * W.nty));
+        kchunk = std::max(16, (L.nz + want - 1) / want);
+    }
+    if (ln.collapse[2]) kchunk = L.nz;
+    W.kchunk = std::max(1, std::min(kchunk, L.nz));
+    W.nitems = W.ntx * W.nty * ((L.nz + W.kchunk - 1) / W.kchunk);
+    const int grid = std::max(1, std::min(W.nitems, slots));
+    const bool one = omega == 1.f;
+    const CUtensorMap &me = t.e[in_buf][vi], &mb = t.b[vi];
+    constexpr int T = RbtShape<TY>::THREADS, SM = RbtShape<TY>::SMEM;
+    if (zero_in && one) {
+        PMG_TRY_S((tma_attr<TY, true, true>()));
+        k_rb32_tma<TY, true, true><<<grid, T, SM, s>>>(me, mb, L, eout, omega, omw, W, err);
+    } else if (zero_in) {
+        PMG_TRY_S((tma_attr<TY, true, false>()));
+        k_rb32_tma<TY, true, false><<<grid, T, SM, s>>>(me, mb, L, eout, omega, omw, W, err);
+    } else if (one) {
+        PMG_TRY_S((tma_attr<TY, false, true>()));
+        k_rb32_tma<TY, false, true><<<grid, T, SM, s>>>(me, mb, L, eout, omega, omw, W, err);
+    } else {
+        PMG_TRY_S((tma_attr<TY, false, false>()));
+        k_rb32_tma<TY, false, false><<<grid, T, SM, s>>>(me, mb, L, eout, omega, omw, W, err);
+    }
+    count_launches(1);
+    return cuda_status(cudaGetLastError(), "TMA fp32 smoother");
+}
+
+PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder()
+{
+    static std::once_flag once;
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+    std::call_once(once, [] {
+        void *p = nullptr;
+        cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+        cudaGetLastError();
+    });
+    return fn;
+}
+
+// 3-D map of a padded FP32 array: x = column (pitch sy), y = row, z = plane; box of 64
+// columns x `box_rows` rows x 1 plane; out-of-range elements read as zero.
+bool encode_map(CUtensorMap *m, float *base, const LevelK<float> &L, long long rows, long long planes, int box_rows)
+{
+    auto enc = tensor_map_encoder();
+    if (!enc) return false;
+    const cuuint64_t dims[3] = {(cuuint64_t)L.sy, (cuuint64_t)rows, (cuuint64_t)planes};
+    const cuuint64_t strides[2] = {(cuuint64_t)L.sy * 4u, (cuuint64_t)L.sz * 4u};
+    const cuuint32_t box[3] = {(cuuint32_t)RBT_W, (cuuint32_t)box_rows, 1u};
+    const cuuint32_t estr[3] = {1u, 1u, 1u};
+    return enc(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, base, dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+               CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+               CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
 }  // namespace
 
-int rb32_fused(const LevelK<float> &L, const Launch &ln, const float *ein, float *eout, const float *b, float omega,
-               float omw, bool zero_in, cudaStream_t s, int variant, int kchunk)
+int rb32_tma_setup(Rb32Tma *t, const LevelK<float> &L, float *const base[3], long long rows, long long planes)
 {
+    t->ok = false;
+    // TMA: 16-byte aligned bases and strides; the first copied column, 5 + 60 bx - 1, is a
+    // multiple of 4 floats for every tile
+    static_assert((RBT_DATA_OFF - 1) % 4 == 0 && RBT_TX % 4 == 0, "TMA column alignment");
+    if (L.sy % 4 != 0 || L.sz % 4 != 0) return PMG_OK;
+    for (int q = 0; q < 3; ++q)
+        if (reinterpret_cast<uintptr_t>(base[q]) % 16 != 0) return PMG_OK;
+    if (L.sy < RBT_TX * ((L.nx + RBT_TX - 1) / RBT_TX) + 8) return PMG_OK;
+    const int tys[3] = {14, 6, 10};
+    for (int v = 0; v < 3; ++v) {
+        for (int q = 0; q < 2; ++q)
+            if (!encode_map(&t->e[q][v], base[q], L, rows, planes, tys[v] + 4)) return PMG_OK;
+        if (!encode_map(&t->b[v], base[2], L, rows, planes, tys[v] + 2)) return PMG_OK;
+    }
+    t->ok = true;
+    return PMG_OK;
+}
+
+int rb32_fused(const LevelK<float> &L, const Launch &ln, const float *ein, float *eout, const float *b, float omega,
+               float omw, bool zero_in, cudaStream_t s, int variant, int kchunk, const Rb32Tma *tma, int in_buf,
+               int *err)
+{
+    if (tma && tma->ok && err) {
+        switch (variant) {
+        case 1: return launch_tma<6>(L, ln, *tma, 1, in_buf, eout, omega, omw, zero_in, kchunk, err, s);
+        case 2: return launch_tma<10>(L, ln, *tma, 2, in_buf, eout, omega, omw, zero_in, kchunk, err, s);
+        default: return launch_tma<14>(L, ln, *tma, 0, in_buf, eout, omega, omw, zero_in, kchunk, err, s);
+        }
+    }
     switch (variant) {
     case 1: return launch_ty<6>(L, ln, ein, eout, b, omega, omw, zero_in, kchunk, s);
     case 2: return launch_ty<10>(L, ln, ein, eout, b, omega, omw, zero_in, kchunk, s);
@@ -122,11 +301,12 @@ bool rb32_fused_layout_ok(const LevelK<float> &L, const void *e, const void *b)
 }
 
 int tune_smoother(const LevelK<float> &L, const Launch &ln, float *e0, float *e1, const float *b, cudaStream_t s,
-                  int *variant, int *kchunk)
+                  int *variant, int *kchunk, const Rb32Tma *tma, int *err)
 {
     static std::mutex mu;
-    static std::map<std::array<int, 4>, std::pair<int, int>> cache;
-    const std::array<int, 4> key = {L.nx, L.ny, L.nz, ln.collapse[2] ? 1 : 0};
+    static std::map<std::array<int, 5>, std::pair<int, int>> cache;
+    const bool use_tma = tma && tma->ok && err;
+    const std::array<int, 5> key = {L.nx, L.ny, L.nz, ln.collapse[2] ? 1 : 0, use_tma ? 1 : 0};
     *variant = 0;
     *kchunk = 0;
     if ((long long)L.nx * L.ny * L.nz < (1LL << 15)) return PMG_OK;
@@ -147,9 +327,9 @@ int tune_smoother(const LevelK<float> &L, const Launch &ln, float *e0, float *e1
     const int chunks[4] = {0, 16, 32, 64};
     for (int v = 0; v < 3; ++v)
         for (int c : chunks) {
-            if (rb32_fused(L, ln, e0, e1, b, 1.f, 0.f, false, s, v, c) != PMG_OK) continue;
+            if (rb32_fused(L, ln, e0, e1, b, 1.f, 0.f, false, s, v, c, tma, 0, err) != PMG_OK) continue;
             cudaEventRecord(a, s);
-            for (int q = 0; q < 3; ++q) rb32_fused(L, ln, e0, e1, b, 1.f, 0.f, false, s, v, c);
+            for (int q = 0; q < 3; ++q) rb32_fused(L, ln, e0, e1, b, 1.f, 0.f, false, s, v, c, tma, 0, err);
             cudaEventRecord(z, s);
             if (cudaEventSynchronize(z) != cudaSuccess) break;
             float ms = 0.f;

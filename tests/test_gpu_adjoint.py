@@ -107,7 +107,9 @@ def test_autograd_against_finite_differences():
     L.backward()
     gb, gg = b.grad.detach().cpu().numpy(), g.grad.detach().numpy()
     with torch.no_grad():
-        for h, rtol in ((1e-2, 1e-7), (1e-6, 1e-5)):
+        # h = 1e-2 is exact for this quadratic loss up to the solves' rounding; at h = 1e-6
+        # the signal 2 h dL/db(cell) is ~1e-10 against ~1e-14 of FP64 rounding in u+ - u-
+        for h, rtol in ((1e-2, 1e-7), (1e-6, 2e-3)):
             for (k, j, i) in [(1, 1, 1), (8, 8, 8), (3, 12, 15), (16, 2, 9), (10, 16, 4)]:
                 bp, bm = b0.clone(), b0.clone()
                 bp[k, j, i] += h
