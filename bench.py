@@ -44,7 +44,7 @@ def parse():
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
     p.add_argument("--n", type=int, default=N_DEFAULT)
-    p.add_argument("--inner", type=int, default=2, help="FP32 V-cycles per FP64 correction")
+    p.add_argument("--inner", type=int, default=4, help="FP32 V-cycles per FP64 correction (4 is fastest at 512^3)")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--quick", action="store_true",
                    help="time the mixed solve only (no FP64 comparison, e2e or CPU baseline); for profiling")

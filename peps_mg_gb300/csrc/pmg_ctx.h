@@ -101,6 +101,7 @@ struct Ctx {
     int vcycle32(int maxit, double omega, bool zero_start);
     int outer_residual(double *sol, double *rsd, const double *rhs, int slot);
     int check_pipeline();
+    int resrestrict32(int l);
     int selftest_smooth32(int level, int impl, int variant, int kchunk, bool zero_in, double omega,
                           const double *e_in, const double *b, double *e_out);
     void destroy_mixed();

@@ -21,7 +21,8 @@ struct MixedState {
     std::vector<int> variant, kchunk;  // autotuned tile variant and k-chunk of the fused smoother
     std::vector<Rb32Tma> tma;        // tensor maps of the TMA-fed smoother, per level
     std::vector<long long> rows, planes;   // allocated rows per plane and planes, per level
-    int *d_err = nullptr;            // set by the TMA-fed smoother when a bounded wait gave up
+    int *d_err = nullptr;
+    bool march = true;               // marching transfer kernels where every axis involved is halved            // set by the TMA-fed smoother when a bounded wait gave up
     TailDesc<float> tail_host;
     TailDesc<float> *d_tail = nullptr;
     int inner = 2;

@@ -72,7 +72,7 @@ struct RbItem {
     const float *pe, *po, *pb;       // e_in row, outer row, b row at plane 0
     float *pw;                       // e_out row at plane 0
     float omega, omw;
-    float dxc[2], cxm[2], cxp[2], cym, cyp, dy;
+    float dxy[2], cxm[2], cxp[2], cym, cyp;   // dxy = x-part + y-part of -c0
     float2 E[6], B[6];               // planes t-2 .. t+3 at window positions (P .. P+5) % 6
     float2 O[3];                     // outer row, planes t+1 .. t+3 at positions (P .. P+2) % 3
 
@@ -124,7 +124,7 @@ struct RbItem {
                 s = fmaf(cyp, yr, s);
                 s = fmaf(czm, cq<Q>(E[im1]), s);
                 s = fmaf(czp, cq<Q>(E[ip1]), s);
-                const float c0 = -(dxc[Q] + (dy + (czm + czp)));
+                const float c0 = -(dxy[Q] + (czm + czp));
                 const float v = upd(cq<Q>(E[i00]), cq<Q>(B[i00]), s, c0);
                 sq<Q>(E[i00], v);
                 St[r][2 * lane + Q] = v;
@@ -153,7 +153,7 @@ struct RbItem {
                     s = fmaf(cyp, yr, s);
                     s = fmaf(czm, cq<Q>(E[im2]), s);
                     s = fmaf(czp, cq<Q>(E[i00]), s);
-                    const float c0 = -(dxc[Q] + (dy + (czm + czp)));
+                    const float c0 = -(dxy[Q] + (czm + czp));
                     const float v = upd(cq<Q>(E[im1]), cq<Q>(B[im1]), s, c0);
                     sq<Q>(E[im1], v);
                 }
@@ -227,17 +227,17 @@ __device__ __forceinline__ void rb32_item(RbSmem<TY> &S, const LevelK<float> &L,
     I.pb = b + rowoff;
     I.pw = eout + rowoff;
     I.po = ein + (long long)a + (long long)L.sy * jo;
+    I.cym = row_in ? L.cym[j] : 0.f;
+    I.cyp = row_in ? L.cyp[j] : 0.f;
+    const float dy = I.cym + I.cyp;
 #pragma unroll
     for (int q = 0; q < 2; ++q) {
         const int i = a + q;
         const bool in = i >= 1 && i <= nx;
-        I.dxc[q] = in ? L.sx[i] : 0.f;
+        I.dxy[q] = (in ? L.sx[i] : 0.f) + dy;
         I.cxm[q] = in ? L.cxm[i] : 0.f;
         I.cxp[q] = in ? L.cxp[i] : 0.f;
     }
-    I.cym = row_in ? L.cym[j] : 0.f;
-    I.cyp = row_in ? L.cyp[j] : 0.f;
-    I.dy = I.cym + I.cyp;
 
     // window at the first step t = k0 - 1: positions 0..5 = planes k0-3 .. k0+2
     I.E[0] = make_float2(0.f, 0.f);

@@ -177,6 +177,7 @@ struct RbtProducer {
 template <int TY, bool ZERO_IN, bool OMEGA1>
 struct RbtItem {
     using S = RbtShape<TY>;
+    static_assert((RBT_NS & (RBT_NS - 1)) == 0, "stage count must be a power of two");
     unsigned char *smem;
     unsigned long long *bars;
     const float *czm_t, *czp_t;
@@ -185,74 +186,72 @@ struct RbtItem {
     float *pw;
     long long sz;
     float omega, omw;
-    float dxc[2], cxm[2], cxp[2], cym, cyp, dy;
+    float dxy[2], cxm[2], cxp[2], cym, cyp;   // dxy = x-part + y-part of -c0
     float2 E[4], B[2];
     float czm_n, czp_n;     // z coefficients of the next plane (prefetched)
     bool fail;
 
-    __device__ __forceinline__ const float *se(int slot) const
+    __device__ __forceinline__ float *stage_e(int slot) const
     {
-        return reinterpret_cast<const float *>(smem + (slot % RBT_NS) * S::STAGE);
-    }
-    __device__ __forceinline__ float *se_w(int slot) const
-    {
-        return reinterpret_cast<float *>(smem + (slot % RBT_NS) * S::STAGE);
-    }
-    __device__ __forceinline__ const float *sb(int slot) const
-    {
-        return reinterpret_cast<const float *>(smem + (slot % RBT_NS) * S::STAGE + S::EBYTES);
+        return reinterpret_cast<float *>(smem + (unsigned)(slot & (RBT_NS - 1)) * (unsigned)S::STAGE);
     }
     __device__ __forceinline__ void wait(int slot)
     {
-        if (!rbtdetail::mbar_wait_bounded(&bars[slot % RBT_NS], (unsigned)(slot / RBT_NS) & 1u)) fail = true;
+        if (!rbtdetail::mbar_wait_bounded(&bars[slot & (RBT_NS - 1)], (unsigned)(slot / RBT_NS) & 1u)) fail = true;
     }
-    __device__ __forceinline__ float2 own_e(int slot) const
+    __device__ __forceinline__ float2 own_e(const float *st) const
     {
         if (ZERO_IN) return make_float2(0.f, 0.f);
-        return *reinterpret_cast<const float2 *>(se(slot) + r * RBT_W + 2 * lane);
+        return *reinterpret_cast<const float2 *>(st + r * RBT_W + 2 * lane);
     }
-    __device__ __forceinline__ float2 own_b(int slot) const
+    __device__ __forceinline__ float2 own_b(const float *st) const
     {
-        return *reinterpret_cast<const float2 *>(sb(slot) + w * RBT_W + 2 * lane);
+        return *reinterpret_cast<const float2 *>(st + S::EBYTES / 4 + w * RBT_W + 2 * lane);
     }
     __device__ __forceinline__ float upd(float old, float bb, float s, float c0) const
     {
         if (OMEGA1) return __fdividef(bb - s, c0);
         return fmaf(omw, old, __fdividef(omega * (bb - s), c0));
     }
+    // z coefficients of plane k; CHECKED clamps k to the table (entries 0 and nz+1 are 0)
+    template <bool CHECKED>
     __device__ __forceinline__ void load_cz(int k)
     {
-        const bool in = k >= 1 && k <= nz;
-        czm_n = in ? __ldg(czm_t + k) : 0.f;
-        czp_n = in ? __ldg(czp_t + k) : 0.f;
+        if (CHECKED) k = min(k, nz + 1);
+        czm_n = __ldg(czm_t + k);
+        czp_n = __ldg(czp_t + k);
     }
 
     // Step t: first colour on plane t, second colour on plane t-1.  P = window position of
-    // plane t-2; Q = index within the pair of the first-colour cell on plane t.  Returns
-    // false when a wait gave up (uniform across the CTA).
-    template <int P, int Q>
-    __device__ __forceinline__ bool step(int t, float &czm_c, float &czp_c, float &czm_p, float &czp_p,
-                                         RbtProducer<TY, ZERO_IN> &prod, const RbtItems &W, const CUtensorMap *me,
-                                         const CUtensorMap *mb)
+    // plane t-2; Q = index within the pair of the first-colour cell on plane t.  CHECKED
+    // steps test at run time whether plane t is a grid plane (first colour) and whether
+    // plane t-1 belongs to the item (second colour); the steps in between, k0 < t <= k1,
+    // need neither test.  Returns false when a wait gave up (uniform across the CTA).
+    template <int P, int Q, bool CHECKED>
+    __device__ __forceinline__ bool step(int t, float (&cz)[6], RbtProducer<TY, ZERO_IN> &prod, const RbtItems &W,
+                                         const CUtensorMap *me, const CUtensorMap *mb)
     {
         using namespace rbtdetail;
         constexpr int im2 = P % 4, im1 = (P + 1) % 4, i00 = (P + 2) % 4, ip1 = (P + 3) % 4;
         constexpr int bm1 = P % 2, b00 = (P + 1) % 2;
         const int cs = cbase + (t - k0 + 2);      // slot of plane t
+        float *St = stage_e(cs);
         wait(cs + 1);
-        E[ip1] = own_e(cs + 1);
-        B[b00] = own_b(cs);
-        // z coefficients: plane t (current) from the prefetch, plane t+1 prefetched now
-        czm_p = czm_c;
-        czp_p = czp_c;
-        czm_c = czm_n;
-        czp_c = czp_n;
-        load_cz(t + 1);
+        E[ip1] = own_e(stage_e(cs + 1));
+        B[b00] = own_b(St);
+        // z coefficients (czm, czp, czm + czp) of plane t-1 in cz[0..2] and of plane t in
+        // cz[3..5]; plane t+1 is prefetched
+        cz[0] = cz[3];
+        cz[1] = cz[4];
+        cz[2] = cz[5];
+        cz[3] = czm_n;
+        cz[4] = czp_n;
+        cz[5] = czm_n + czp_n;
+        load_cz<CHECKED>(t + 1);
         {
             const float up = __shfl_up_sync(0xffffffffu, E[i00].y, 1);
             const float dn = __shfl_down_sync(0xffffffffu, E[i00].x, 1);
-            float *St = se_w(cs);
-            if ((Q ? need1 : need0) && t >= 1 && t <= nz) {
+            if ((Q ? need1 : need0) && (!CHECKED || (t >= 1 && t <= nz))) {
                 const float yl = ZERO_IN ? 0.f : St[(r - 1) * RBT_W + 2 * lane + Q];
                 const float yr = ZERO_IN ? 0.f : St[(r + 1) * RBT_W + 2 * lane + Q];
                 const float left = Q ? E[i00].x : up;
@@ -261,9 +260,9 @@ struct RbtItem {
                 s = fmaf(cxp[Q], right, s);
                 s = fmaf(cym, yl, s);
                 s = fmaf(cyp, yr, s);
-                s = fmaf(czm_c, cq<Q>(E[im1]), s);
-                s = fmaf(czp_c, cq<Q>(E[ip1]), s);
-                const float c0 = -(dxc[Q] + (dy + (czm_c + czp_c)));
+                s = fmaf(cz[3], cq<Q>(E[im1]), s);
+                s = fmaf(cz[4], cq<Q>(E[ip1]), s);
+                const float c0 = -(dxy[Q] + cz[5]);
                 const float v = upd(cq<Q>(E[i00]), cq<Q>(B[b00]), s, c0);
                 sq<Q>(E[i00], v);
             }
@@ -278,9 +277,9 @@ struct RbtItem {
             const int s1 = t - 1;
             const float up = __shfl_up_sync(0xffffffffu, E[im1].y, 1);
             const float dn = __shfl_down_sync(0xffffffffu, E[im1].x, 1);
-            if (store_lane && s1 >= k0 && s1 <= k1) {
+            if (store_lane && (!CHECKED || (s1 >= k0 && s1 <= k1))) {
                 if (Q == 0 || st_full) {
-                    const float *Ss = se(cs - 1);
+                    const float *Ss = stage_e(cs - 1);
                     const float yl = Ss[(r - 1) * RBT_W + 2 * lane + Q];
                     const float yr = Ss[(r + 1) * RBT_W + 2 * lane + Q];
                     const float left = Q ? E[im1].x : up;
@@ -289,9 +288,9 @@ struct RbtItem {
                     s = fmaf(cxp[Q], right, s);
                     s = fmaf(cym, yl, s);
                     s = fmaf(cyp, yr, s);
-                    s = fmaf(czm_p, cq<Q>(E[im2]), s);
-                    s = fmaf(czp_p, cq<Q>(E[i00]), s);
-                    const float c0 = -(dxc[Q] + (dy + (czm_p + czp_p)));
+                    s = fmaf(cz[0], cq<Q>(E[im2]), s);
+                    s = fmaf(cz[1], cq<Q>(E[i00]), s);
+                    const float c0 = -(dxy[Q] + cz[2]);
                     const float v = upd(cq<Q>(E[im1]), cq<Q>(B[bm1]), s, c0);
                     sq<Q>(E[im1], v);
                 }
@@ -305,22 +304,28 @@ struct RbtItem {
         return true;
     }
 
+    // Steps t = k0-1 .. k1+1: two checked steps, unchecked steps k0+1 .. k1 unrolled by
+    // the four-plane register window, then the remaining steps checked.
     template <int Q0>
     __device__ __forceinline__ bool run(RbtProducer<TY, ZERO_IN> &prod, const RbtItems &W, const CUtensorMap *me,
                                         const CUtensorMap *mb)
     {
-        float czm_c = 0.f, czp_c = 0.f, czm_p = 0.f, czp_p = 0.f;
-        load_cz(k0 - 1);
+        float cz[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+        load_cz<true>(k0 - 1);
         int t = k0 - 1;
-        for (; t + 3 <= k1 + 1; t += 4) {
-            if (!step<0, Q0>(t, czm_c, czp_c, czm_p, czp_p, prod, W, me, mb)) return false;
-            if (!step<1, 1 - Q0>(t + 1, czm_c, czp_c, czm_p, czp_p, prod, W, me, mb)) return false;
-            if (!step<2, Q0>(t + 2, czm_c, czp_c, czm_p, czp_p, prod, W, me, mb)) return false;
-            if (!step<3, 1 - Q0>(t + 3, czm_c, czp_c, czm_p, czp_p, prod, W, me, mb)) return false;
+        if (!step<0, Q0, true>(t, cz, prod, W, me, mb)) return false;
+        if (!step<1, 1 - Q0, true>(t + 1, cz, prod, W, me, mb)) return false;
+        t += 2;
+        for (; t + 3 <= k1; t += 4) {
+            if (!step<2, Q0, false>(t, cz, prod, W, me, mb)) return false;
+            if (!step<3, 1 - Q0, false>(t + 1, cz, prod, W, me, mb)) return false;
+            if (!step<0, Q0, false>(t + 2, cz, prod, W, me, mb)) return false;
+            if (!step<1, 1 - Q0, false>(t + 3, cz, prod, W, me, mb)) return false;
         }
-        if (t <= k1 + 1 && !step<0, Q0>(t++, czm_c, czp_c, czm_p, czp_p, prod, W, me, mb)) return false;
-        if (t <= k1 + 1 && !step<1, 1 - Q0>(t++, czm_c, czp_c, czm_p, czp_p, prod, W, me, mb)) return false;
-        if (t <= k1 + 1 && !step<2, Q0>(t++, czm_c, czp_c, czm_p, czp_p, prod, W, me, mb)) return false;
+        if (t <= k1 + 1 && !step<2, Q0, true>(t++, cz, prod, W, me, mb)) return false;
+        if (t <= k1 + 1 && !step<3, 1 - Q0, true>(t++, cz, prod, W, me, mb)) return false;
+        if (t <= k1 + 1 && !step<0, Q0, true>(t++, cz, prod, W, me, mb)) return false;
+        if (t <= k1 + 1 && !step<1, 1 - Q0, true>(t++, cz, prod, W, me, mb)) return false;
         return true;
     }
 };
@@ -361,24 +366,24 @@ __device__ __forceinline__ bool rbt_item(unsigned char *smem, unsigned long long
     I.store_lane = (w >= 1 && w <= TY) && row_in && mid && a <= nx;
     I.st_full = a + 1 <= nx;
     I.pw = eout + (long long)a + (long long)L.sy * j;
+    I.cym = row_in ? L.cym[j] : 0.f;
+    I.cyp = row_in ? L.cyp[j] : 0.f;
+    const float dy = I.cym + I.cyp;
 #pragma unroll
     for (int q = 0; q < 2; ++q) {
         const int i = a + q;
         const bool in = i >= 1 && i <= nx;
-        I.dxc[q] = in ? L.sx[i] : 0.f;
+        I.dxy[q] = (in ? L.sx[i] : 0.f) + dy;
         I.cxm[q] = in ? L.cxm[i] : 0.f;
         I.cxp[q] = in ? L.cxp[i] : 0.f;
     }
-    I.cym = row_in ? L.cym[j] : 0.f;
-    I.cyp = row_in ? L.cyp[j] : 0.f;
-    I.dy = I.cym + I.cyp;
     // window at the first step t = k0 - 1: positions 0..3 = planes k0-3 .. k0; position 0
     // (plane k0-3) is never read, position 3 is loaded by the step itself
     I.E[0] = make_float2(0.f, 0.f);
     I.wait(cbase);
-    I.E[1] = I.own_e(cbase);
+    I.E[1] = I.own_e(I.stage_e(cbase));
     I.wait(cbase + 1);
-    I.E[2] = I.own_e(cbase + 1);
+    I.E[2] = I.own_e(I.stage_e(cbase + 1));
     I.B[0] = make_float2(0.f, 0.f);
     // the pair's first cell a is odd, so it carries the first colour on plane k when j + k
     // is even ((i + j + k) odd, src/rbgs_poisson_matrix.f90:242)

@@ -65,8 +65,9 @@ def test_one_iteration_against_oracle(n):
                         assert np.array_equal(outs[0], outs[1]), (variant, kchunk, zero_in, omega)
 
 
-def test_tma_and_window_solves_agree(tmp_path):
-    """A whole mixed-precision solve with either smoother kernel gives the same bits."""
+def test_kernel_variants_give_identical_solves(tmp_path):
+    """A whole mixed-precision solve gives the same bits with either smoother kernel and
+    with either kind of transfer kernel (marching or one thread per cell)."""
     import os
     import subprocess
     import sys
@@ -86,11 +87,12 @@ print(rep.cycles)
 '''
     root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
     outs = []
-    for mode in ("tma", "window"):
-        env = dict(os.environ, PEPS_MG_SMOOTHER=mode, PYTHONPATH=root)
-        path = str(tmp_path / ("%s.npy" % mode))
+    for sm, tr in (("tma", "march"), ("window", "march"), ("tma", "cell")):
+        env = dict(os.environ, PEPS_MG_SMOOTHER=sm, PEPS_MG_TRANSFER=tr, PYTHONPATH=root)
+        path = str(tmp_path / ("%s_%s.npy" % (sm, tr)))
         r = subprocess.run([sys.executable, "-c", code, path], cwd=root, env=env, capture_output=True, text=True,
                            timeout=300)
         assert r.returncode == 0, r.stderr[-2000:]
         outs.append(np.load(path))
     assert np.array_equal(outs[0], outs[1])
+    assert np.array_equal(outs[0], outs[2])
