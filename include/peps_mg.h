@@ -208,7 +208,8 @@ int pmg_vv_dot_static(const double *x, const double *y, int nx, int ny, int nz, 
 /* Enable (1) or disable (0) CUDA-event timing of the finest-level launches; resets
  * the accumulated figures. */
 int pmg_profile(pmg_ctx *ctx, int enable);
-/* Accumulated device time, launch count and algorithmic bytes per launch of a class. */
+/* Accumulated device time, launch count and algorithmic bytes per launch (averaged over
+ * the launches) of a class. */
 int pmg_profile_read(pmg_ctx *ctx, int kernel_class, double *total_ms, long long *launches, double *bytes);
 /* Kernels launched by this library so far (all contexts of the process). */
 int pmg_launch_count(long long *count);

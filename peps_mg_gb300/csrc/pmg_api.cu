@@ -93,7 +93,7 @@ void Profiler::flush()
         if (cudaEventElapsedTime(&ms, r.a, r.b) == cudaSuccess) {
             total_ms[r.cls] += ms;
             count[r.cls] += r.launches;
-            bytes[r.cls] = r.bytes;
+            bytes[r.cls] += r.bytes * r.launches;
         } else {
             cudaGetLastError();
         }
@@ -1148,7 +1148,7 @@ int pmg_profile_read(pmg_ctx *ctx, int kernel_class, double *total_ms, long long
     c.prof.flush();
     if (total_ms) *total_ms = c.prof.total_ms[kernel_class];
     if (launches) *launches = c.prof.count[kernel_class];
-    if (bytes) *bytes = c.prof.bytes[kernel_class];
+    if (bytes) *bytes = c.prof.count[kernel_class] ? c.prof.bytes[kernel_class] / (double)c.prof.count[kernel_class] : 0.0;
     return PMG_OK;
 }
 

@@ -37,7 +37,7 @@ struct Profiler {
     std::vector<Rec> pending;
     double total_ms[PC_COUNT] = {};
     long long count[PC_COUNT] = {};
-    double bytes[PC_COUNT] = {};
+    double bytes[PC_COUNT] = {};     // algorithmic bytes summed over launches
     ~Profiler();
     void reset();
     cudaEvent_t get();

@@ -549,7 +549,8 @@ int Ctx::vcycle32(int maxit, double omega, bool zero_start)
                                      m->variant[l], m->kchunk[l], &m->tma[l], m->cur[l], m->d_err));
                 m->cur[l] = 1 - m->cur[l];
             }
-            prof.end(pi, PC_SMOOTH32, maxit, 12.0 * N, stream);
+            // 12 B per cell (e_in, b read, e_out written); 8 B for an iteration from e = 0
+            prof.end(pi, PC_SMOOTH32, maxit, (12.0 * maxit - (zs ? 4.0 : 0.0)) / std::max(1, maxit) * N, stream);
         } else {
             const dim3 gc = grid3m((L.nx + 1) / 2, L.ny, L.nz, launch[l]), gf = grid3m(L.nx, L.ny, L.nz, launch[l]);
             for (int it = 0; it < maxit; ++it)

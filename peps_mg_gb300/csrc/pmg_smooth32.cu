@@ -55,7 +55,7 @@ __global__ void __launch_bounds__(rb_threads<TY>(), rb_min_blocks<TY>()) k_rb32_
 
 // blocks per SM the TMA-fed kernel's register budget is sized for
 template <int TY>
-constexpr int rbt_min_blocks() { return TY <= 6 ? 4 : 2; }
+constexpr int rbt_min_blocks() { return TY <= 6 ? 5 : TY <= 10 ? 3 : 2; }
 
 template <int TY, bool ZERO_IN, bool OMEGA1>
 __global__ void __launch_bounds__(RbtShape<TY>::THREADS, rbt_min_blocks<TY>())
@@ -67,8 +67,10 @@ __global__ void __launch_bounds__(RbtShape<TY>::THREADS, rbt_min_blocks<TY>())
     // 128-byte aligned stages (TMA destinations), then the mbarriers
     unsigned char *smem = smem_raw + ((128u - (rbtdetail::smem_addr(smem_raw) & 127u)) & 127u);
     unsigned long long *bars = reinterpret_cast<unsigned long long *>(smem + RBT_NS * S::STAGE);
+    volatile int *abort_flag = reinterpret_cast<volatile int *>(bars + RBT_NS);
     if (threadIdx.x == 0) {
         for (int q = 0; q < RBT_NS; ++q) rbtdetail::mbar_init(&bars[q], 1);
+        *abort_flag = 0;
         rbtdetail::fence_mbar_init();
     }
     __syncthreads();
@@ -81,8 +83,8 @@ __global__ void __launch_bounds__(RbtShape<TY>::THREADS, rbt_min_blocks<TY>())
     for (int it = blockIdx.x; it < W.nitems; it += gridDim.x) {
         int bx, by, k0, k1;
         W.decode(it, bx, by, k0, k1);
-        if (!rbt_item<TY, ZERO_IN, OMEGA1>(smem, bars, L, eout, omega, omw, bx, by, k0, k1, cbase, prod, W, &me,
-                                            &mb)) {
+        if (!rbt_item<TY, ZERO_IN, OMEGA1>(smem, bars, abort_flag, L, eout, omega, omw, bx, by, k0, k1, cbase, prod,
+                                            W, &me, &mb)) {
             if (threadIdx.x == 0) {
                 atomicOr(err, 1);
                 // let the copies still in flight land before the CTA exits (bounded)
@@ -155,6 +157,8 @@ int tma_attr()
     std::call_once(once, [] {
         err = cudaFuncSetAttribute(k_rb32_tma<TY, Z, O>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                    RbtShape<TY>::SMEM);
+        if (err == cudaSuccess)
+            err = cudaFuncSetAttribute(k_rb32_tma<TY, Z, O>, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
     });
     return cuda_status(err, "TMA smoother shared memory attribute");
 }
@@ -168,6 +172,9 @@ int tma_slots(int *slots)
     std::call_once(once, [] {
         err = cudaFuncSetAttribute(k_rb32_tma<TY, false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                    RbtShape<TY>::SMEM);
+        if (err == cudaSuccess)
+            err = cudaFuncSetAttribute(k_rb32_tma<TY, false, false>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                       100);
         if (err == cudaSuccess)
             err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_rb32_tma<TY, false, false>,
                                                                 RbtShape<TY>::THREADS, RbtShape<TY>::SMEM);

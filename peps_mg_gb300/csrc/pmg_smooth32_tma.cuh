@@ -1,10 +1,11 @@
 // pmg_smooth32_tma.cuh -- device code of the TMA-fed fused FP32 red-black iteration.
 //
-// Same arithmetic and thread mapping as pmg_smooth32.cuh (one RBGS iteration of
+// Same arithmetic as pmg_smooth32.cuh (one RBGS iteration of
 // src/rbgs_poisson_matrix.f90:235-273, out of place, on (TX = 60) x TY tiles over chunks
-// of planes; warp w owns row j0 - 1 + w, lane l the cell pair (i0 - 2 + 2l, i0 - 1 + 2l)),
-// but the planes reach shared memory through the tensor-memory accelerator instead of
-// per-thread loads:
+// of planes; lane l owns the cell pair (i0 - 2 + 2l, i0 - 1 + 2l)), but warp w owns TWO
+// rows, j0 - 1 + 2w and j0 + 2w (so the y-neighbour between them stays in registers and
+// the per-plane overhead is shared by two rows), and the planes reach shared memory
+// through the tensor-memory accelerator instead of per-thread loads:
 //
 //  * A ring of NS stages; stage s holds one plane of e_in (rows j0-2 .. j0+TY+1, 64
 //    columns from i0-2) and of b (rows j0-1 .. j0+TY).  One thread issues both copies of
@@ -15,8 +16,12 @@
 //  * Step t: first colour on plane t, written back into its stage (the y-neighbours of
 //    the second colour), barrier, then the stage of plane t-2 is refilled NS slots ahead
 //    and the second colour on plane t-1 is computed and stored to e_out.
-//  * Each thread keeps its pair of planes t-2 .. t+1 and b of planes t-1, t in registers
-//    (z-neighbours), takes x-neighbours by shuffles and y-neighbours from the stage.
+//  * Each thread keeps its two pairs of planes t-2 .. t+1 and b of planes t-1, t in
+//    registers (z-neighbours), takes x-neighbours by shuffles and the outer y-neighbours
+//    from the stage.
+//  * A wait that runs out (about a second) sets a shared abort flag, after which every
+//    wait of the CTA returns at once; the CTA stops at the end of the item and the host
+//    reads the error flag.
 //
 // DRAM traffic per iteration: e_in and b read once, e_out written once (12 B per cell,
 // 8 B when e_in = 0: then no e_in copies are issued at all).
@@ -38,9 +43,14 @@ struct RbtShape {
     static constexpr int EROWS = TY + 4, BROWS = TY + 2;
     static constexpr int EBYTES = EROWS * RBT_W * 4, BBYTES = BROWS * RBT_W * 4;
     static constexpr int STAGE = EBYTES + BBYTES;
-    static constexpr int SMEM = RBT_NS * STAGE + RBT_NS * 8 + 128;   // stages, mbarriers, alignment slack
-    static constexpr int THREADS = (TY + 2) * 32;
+    static constexpr int SMEM = RBT_NS * STAGE + RBT_NS * 8 + 16 + 128;   // stages, mbarriers, abort flag, slack
+    static constexpr int WARPS = (TY + 2) / 2;                               // two rows per warp
+    static constexpr int THREADS = WARPS * 32;
+    static_assert(TY % 2 == 0, "tile height must be even");
 };
+
+template <int TY>
+__host__ __device__ constexpr int S_EB() { return RbtShape<TY>::EBYTES; }
 
 namespace rbtdetail {
 
@@ -85,6 +95,22 @@ __device__ __forceinline__ bool mbar_wait_bounded(unsigned long long *bar, unsig
     const long long t0 = clock64();
     while (!mbar_try_wait(bar, parity))
         if (clock64() - t0 > (1LL << 31)) return false;
+    return true;
+}
+
+// Slow path of a wait: spins until the phase completes, about a second passes (then it
+// raises the CTA's abort flag) or another thread has raised the flag.  Returns false on
+// failure.
+static __device__ __noinline__ bool mbar_wait_slow(unsigned long long *bar, unsigned parity, volatile int *abort_flag)
+{
+    const long long t0 = clock64();
+    while (!mbar_try_wait(bar, parity)) {
+        if (*abort_flag) return false;
+        if (clock64() - t0 > (1LL << 31)) {
+            *abort_flag = 1;
+            return false;
+        }
+    }
     return true;
 }
 
@@ -180,66 +206,82 @@ struct RbtItem {
     static_assert((RBT_NS & (RBT_NS - 1)) == 0, "stage count must be a power of two");
     unsigned char *smem;
     unsigned long long *bars;
+    volatile int *abort_flag;
     const float *czm_t, *czp_t;
-    int nz, k0, k1, lane, w, r, cbase;
-    bool need0, need1, store_lane, st_full;
-    float *pw;
+    int nz, k0, k1, cbase;
+    int oe, ob;                        // byte offsets in a stage of row a's own e pair and b pair
+    bool nA[2], nB[2];                 // rows a / b: cell 0 / 1 of the pair takes a first-colour update
+    bool stA, stB, st_full;            // rows a / b are stored; the pair is stored whole
+    float *pwA;                        // e_out at row a, plane 0 (row b at + sy)
+    int sy;
     long long sz;
     float omega, omw;
-    float dxy[2], cxm[2], cxp[2], cym, cyp;   // dxy = x-part + y-part of -c0
-    float2 E[4], B[2];
-    float czm_n, czp_n;     // z coefficients of the next plane (prefetched)
+    float cxm[2], cxp[2];
+    float dA[2], dB[2];                // x-part + y-part of -c0, rows a and b
+    float cymA, cypA, cymB, cypB;
+    float2 EA[4], EB[4], BA[2], BB[2];
+    float czm_n, czp_n;                // z coefficients of the next plane (prefetched)
     bool fail;
 
-    __device__ __forceinline__ float *stage_e(int slot) const
+    __device__ __forceinline__ unsigned stage_off(int slot) const
     {
-        return reinterpret_cast<float *>(smem + (unsigned)(slot & (RBT_NS - 1)) * (unsigned)S::STAGE);
+        return (unsigned)(slot & (RBT_NS - 1)) * (unsigned)S::STAGE;
     }
     __device__ __forceinline__ void wait(int slot)
     {
-        if (!rbtdetail::mbar_wait_bounded(&bars[slot & (RBT_NS - 1)], (unsigned)(slot / RBT_NS) & 1u)) fail = true;
+        unsigned long long *bar = &bars[slot & (RBT_NS - 1)];
+        const unsigned par = (unsigned)(slot / RBT_NS) & 1u;
+        if (!rbtdetail::mbar_try_wait(bar, par) && !rbtdetail::mbar_wait_slow(bar, par, abort_flag)) fail = true;
     }
-    __device__ __forceinline__ float2 own_e(const float *st) const
+    __device__ __forceinline__ float2 lds2(unsigned off) const
     {
-        if (ZERO_IN) return make_float2(0.f, 0.f);
-        return *reinterpret_cast<const float2 *>(st + r * RBT_W + 2 * lane);
+        return *reinterpret_cast<const float2 *>(smem + off);
     }
-    __device__ __forceinline__ float2 own_b(const float *st) const
+    __device__ __forceinline__ float lds(unsigned off) const { return *reinterpret_cast<const float *>(smem + off); }
+    __device__ __forceinline__ void sts2(unsigned off, float2 v) const
     {
-        return *reinterpret_cast<const float2 *>(st + S::EBYTES / 4 + w * RBT_W + 2 * lane);
+        *reinterpret_cast<float2 *>(smem + off) = v;
     }
-    __device__ __forceinline__ float upd(float old, float bb, float s, float c0) const
+    // first- or second-colour update of one cell: s = off-diagonal sum, d = -c0
+    __device__ __forceinline__ float upd(float old, float bb, float s, float d) const
     {
-        if (OMEGA1) return __fdividef(bb - s, c0);
-        return fmaf(omw, old, __fdividef(omega * (bb - s), c0));
+        if (OMEGA1) return __fdividef(s - bb, d);
+        return fmaf(omw, old, __fdividef(omega * (s - bb), d));
     }
-    // z coefficients of plane k; CHECKED clamps k to the table (entries 0 and nz+1 are 0)
     template <bool CHECKED>
     __device__ __forceinline__ void load_cz(int k)
     {
-        if (CHECKED) k = min(k, nz + 1);
+        if (CHECKED) k = min(k, nz + 1);   // table entries 0 and nz+1 are 0
         czm_n = __ldg(czm_t + k);
         czp_n = __ldg(czp_t + k);
     }
 
-    // Step t: first colour on plane t, second colour on plane t-1.  P = window position of
-    // plane t-2; Q = index within the pair of the first-colour cell on plane t.  CHECKED
-    // steps test at run time whether plane t is a grid plane (first colour) and whether
-    // plane t-1 belongs to the item (second colour); the steps in between, k0 < t <= k1,
-    // need neither test.  Returns false when a wait gave up (uniform across the CTA).
+    // Step t: first colour on plane t, second colour on plane t-1, for both rows.  P =
+    // window position of plane t-2; Q = index within the pair of row a's first-colour
+    // cell on plane t (row b's is 1 - Q; on plane t-1 the second-colour cells are at the
+    // same indices).  CHECKED steps test at run time whether plane t is a grid plane
+    // and whether plane t-1 belongs to the item; the steps k0 < t <= k1 need neither.
     template <int P, int Q, bool CHECKED>
-    __device__ __forceinline__ bool step(int t, float (&cz)[6], RbtProducer<TY, ZERO_IN> &prod, const RbtItems &W,
+    __device__ __forceinline__ void step(int t, float (&cz)[6], RbtProducer<TY, ZERO_IN> &prod, const RbtItems &W,
                                          const CUtensorMap *me, const CUtensorMap *mb)
     {
         using namespace rbtdetail;
         constexpr int im2 = P % 4, im1 = (P + 1) % 4, i00 = (P + 2) % 4, ip1 = (P + 3) % 4;
         constexpr int bm1 = P % 2, b00 = (P + 1) % 2;
+        constexpr int QB = 1 - Q;
         const int cs = cbase + (t - k0 + 2);      // slot of plane t
-        float *St = stage_e(cs);
+        const unsigned s0 = stage_off(cs), sp = stage_off(cs + 1), sm = stage_off(cs - 1);
         wait(cs + 1);
-        E[ip1] = own_e(stage_e(cs + 1));
-        B[b00] = own_b(St);
-        // z coefficients (czm, czp, czm + czp) of plane t-1 in cz[0..2] and of plane t in
+        if (ZERO_IN) {
+            EA[ip1] = make_float2(0.f, 0.f);
+            EB[ip1] = make_float2(0.f, 0.f);
+        } else {
+            EA[ip1] = lds2(sp + oe);
+            EB[ip1] = lds2(sp + oe + RBT_W * 4);
+        }
+        BA[b00] = lds2(s0 + ob);
+        BB[b00] = lds2(s0 + ob + RBT_W * 4);
+        // z coefficients (czm, czp, czm + czp) of plane t-1 in cz[0..2], of plane t in
         // cz[3..5]; plane t+1 is prefetched
         cz[0] = cz[3];
         cz[1] = cz[4];
@@ -248,147 +290,196 @@ struct RbtItem {
         cz[4] = czp_n;
         cz[5] = czm_n + czp_n;
         load_cz<CHECKED>(t + 1);
+        const bool plane_in = !CHECKED || (t >= 1 && t <= nz);
         {
-            const float up = __shfl_up_sync(0xffffffffu, E[i00].y, 1);
-            const float dn = __shfl_down_sync(0xffffffffu, E[i00].x, 1);
-            if ((Q ? need1 : need0) && (!CHECKED || (t >= 1 && t <= nz))) {
-                const float yl = ZERO_IN ? 0.f : St[(r - 1) * RBT_W + 2 * lane + Q];
-                const float yr = ZERO_IN ? 0.f : St[(r + 1) * RBT_W + 2 * lane + Q];
-                const float left = Q ? E[i00].x : up;
-                const float right = Q ? dn : E[i00].y;
-                float s = cxm[Q] * left;
-                s = fmaf(cxp[Q], right, s);
-                s = fmaf(cym, yl, s);
-                s = fmaf(cyp, yr, s);
-                s = fmaf(cz[3], cq<Q>(E[im1]), s);
-                s = fmaf(cz[4], cq<Q>(E[ip1]), s);
-                const float c0 = -(dxy[Q] + cz[5]);
-                const float v = upd(cq<Q>(E[i00]), cq<Q>(B[b00]), s, c0);
-                sq<Q>(E[i00], v);
+            const float upA = __shfl_up_sync(0xffffffffu, EA[i00].y, 1);
+            const float dnA = __shfl_down_sync(0xffffffffu, EA[i00].x, 1);
+            const float upB = __shfl_up_sync(0xffffffffu, EB[i00].y, 1);
+            const float dnB = __shfl_down_sync(0xffffffffu, EB[i00].x, 1);
+            // row a, cell Q: y-neighbours = the stage row below and row b (old values)
+            const float yA = ZERO_IN ? 0.f : lds(s0 + oe - RBT_W * 4 + 4 * Q);
+            const float yB = ZERO_IN ? 0.f : lds(s0 + oe + 2 * RBT_W * 4 + 4 * QB);
+            float vA = 0.f, vB = 0.f;
+            if (nA[Q] && plane_in) {
+                float s = cxm[Q] * (Q ? EA[i00].x : upA);
+                s = fmaf(cxp[Q], Q ? dnA : EA[i00].y, s);
+                s = fmaf(cymA, yA, s);
+                s = fmaf(cypA, cq<Q>(EB[i00]), s);
+                s = fmaf(cz[3], cq<Q>(EA[im1]), s);
+                s = fmaf(cz[4], cq<Q>(EA[ip1]), s);
+                vA = upd(cq<Q>(EA[i00]), cq<Q>(BA[b00]), s, dA[Q] + cz[5]);
             }
-            // the whole pair: with e_in = 0 the stage holds no copied plane, and cells that
-            // are not updated (ghosts, cells beyond the grid) must read as zero there
-            *reinterpret_cast<float2 *>(St + r * RBT_W + 2 * lane) = E[i00];
+            if (nB[QB] && plane_in) {
+                float s = cxm[QB] * (QB ? EB[i00].x : upB);
+                s = fmaf(cxp[QB], QB ? dnB : EB[i00].y, s);
+                s = fmaf(cymB, cq<QB>(EA[i00]), s);
+                s = fmaf(cypB, yB, s);
+                s = fmaf(cz[3], cq<QB>(EB[im1]), s);
+                s = fmaf(cz[4], cq<QB>(EB[ip1]), s);
+                vB = upd(cq<QB>(EB[i00]), cq<QB>(BB[b00]), s, dB[QB] + cz[5]);
+            }
+            if (nA[Q] && plane_in) sq<Q>(EA[i00], vA);
+            if (nB[QB] && plane_in) sq<QB>(EB[i00], vB);
+            // whole pairs: with e_in = 0 the stage holds no copied plane, and cells that are
+            // not updated (ghosts, cells beyond the grid) must read as zero there
+            sts2(s0 + oe, EA[i00]);
+            sts2(s0 + oe + RBT_W * 4, EB[i00]);
         }
         fence_proxy_async();
-        if (__syncthreads_or(fail)) return false;
+        __syncthreads();
         if (threadIdx.x == 0) prod.issue_upto(cs - 2 + RBT_NS, W, smem, bars, me, mb);
-        {
-            const int s1 = t - 1;
-            const float up = __shfl_up_sync(0xffffffffu, E[im1].y, 1);
-            const float dn = __shfl_down_sync(0xffffffffu, E[im1].x, 1);
-            if (store_lane && (!CHECKED || (s1 >= k0 && s1 <= k1))) {
-                if (Q == 0 || st_full) {
-                    const float *Ss = stage_e(cs - 1);
-                    const float yl = Ss[(r - 1) * RBT_W + 2 * lane + Q];
-                    const float yr = Ss[(r + 1) * RBT_W + 2 * lane + Q];
-                    const float left = Q ? E[im1].x : up;
-                    const float right = Q ? dn : E[im1].y;
-                    float s = cxm[Q] * left;
-                    s = fmaf(cxp[Q], right, s);
-                    s = fmaf(cym, yl, s);
-                    s = fmaf(cyp, yr, s);
-                    s = fmaf(cz[0], cq<Q>(E[im2]), s);
-                    s = fmaf(cz[1], cq<Q>(E[i00]), s);
-                    const float c0 = -(dxy[Q] + cz[2]);
-                    const float v = upd(cq<Q>(E[im1]), cq<Q>(B[bm1]), s, c0);
-                    sq<Q>(E[im1], v);
-                }
-                float *g = pw + sz * s1;
+        if (!CHECKED || (t - 1 >= k0 && t - 1 <= k1)) {
+            const float upA = __shfl_up_sync(0xffffffffu, EA[im1].y, 1);
+            const float dnA = __shfl_down_sync(0xffffffffu, EA[im1].x, 1);
+            const float upB = __shfl_up_sync(0xffffffffu, EB[im1].y, 1);
+            const float dnB = __shfl_down_sync(0xffffffffu, EB[im1].x, 1);
+            // row a, cell Q: y-neighbours = the stage row below (first colour, plane t-1)
+            // and row b's updated first-colour cell; row b, cell 1-Q: row a and the row above
+            const float yA = lds(sm + oe - RBT_W * 4 + 4 * Q);
+            const float yB = lds(sm + oe + 2 * RBT_W * 4 + 4 * QB);
+            float *gA = pwA + sz * (t - 1);
+            if (stA && (Q == 0 || st_full)) {
+                float s = cxm[Q] * (Q ? EA[im1].x : upA);
+                s = fmaf(cxp[Q], Q ? dnA : EA[im1].y, s);
+                s = fmaf(cymA, yA, s);
+                s = fmaf(cypA, cq<Q>(EB[im1]), s);
+                s = fmaf(cz[0], cq<Q>(EA[im2]), s);
+                s = fmaf(cz[1], cq<Q>(EA[i00]), s);
+                const float v = upd(cq<Q>(EA[im1]), cq<Q>(BA[bm1]), s, dA[Q] + cz[2]);
+                sq<Q>(EA[im1], v);
+            }
+            if (stB && (QB == 0 || st_full)) {
+                float s = cxm[QB] * (QB ? EB[im1].x : upB);
+                s = fmaf(cxp[QB], QB ? dnB : EB[im1].y, s);
+                s = fmaf(cymB, cq<QB>(EA[im1]), s);
+                s = fmaf(cypB, yB, s);
+                s = fmaf(cz[0], cq<QB>(EB[im2]), s);
+                s = fmaf(cz[1], cq<QB>(EB[i00]), s);
+                const float v = upd(cq<QB>(EB[im1]), cq<QB>(BB[bm1]), s, dB[QB] + cz[2]);
+                sq<QB>(EB[im1], v);
+            }
+            if (stA) {
                 if (st_full)
-                    *reinterpret_cast<float2 *>(g) = E[im1];
+                    *reinterpret_cast<float2 *>(gA) = EA[im1];
                 else
-                    g[0] = E[im1].x;
+                    gA[0] = EA[im1].x;
+            }
+            if (stB) {
+                if (st_full)
+                    *reinterpret_cast<float2 *>(gA + sy) = EB[im1];
+                else
+                    gA[sy] = EB[im1].x;
             }
         }
-        return true;
     }
 
     // Steps t = k0-1 .. k1+1: two checked steps, unchecked steps k0+1 .. k1 unrolled by
     // the four-plane register window, then the remaining steps checked.
     template <int Q0>
-    __device__ __forceinline__ bool run(RbtProducer<TY, ZERO_IN> &prod, const RbtItems &W, const CUtensorMap *me,
+    __device__ __forceinline__ void run(RbtProducer<TY, ZERO_IN> &prod, const RbtItems &W, const CUtensorMap *me,
                                         const CUtensorMap *mb)
     {
         float cz[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
         load_cz<true>(k0 - 1);
         int t = k0 - 1;
-        if (!step<0, Q0, true>(t, cz, prod, W, me, mb)) return false;
-        if (!step<1, 1 - Q0, true>(t + 1, cz, prod, W, me, mb)) return false;
+        step<0, Q0, true>(t, cz, prod, W, me, mb);
+        step<1, 1 - Q0, true>(t + 1, cz, prod, W, me, mb);
         t += 2;
         for (; t + 3 <= k1; t += 4) {
-            if (!step<2, Q0, false>(t, cz, prod, W, me, mb)) return false;
-            if (!step<3, 1 - Q0, false>(t + 1, cz, prod, W, me, mb)) return false;
-            if (!step<0, Q0, false>(t + 2, cz, prod, W, me, mb)) return false;
-            if (!step<1, 1 - Q0, false>(t + 3, cz, prod, W, me, mb)) return false;
+            step<2, Q0, false>(t, cz, prod, W, me, mb);
+            step<3, 1 - Q0, false>(t + 1, cz, prod, W, me, mb);
+            step<0, Q0, false>(t + 2, cz, prod, W, me, mb);
+            step<1, 1 - Q0, false>(t + 3, cz, prod, W, me, mb);
         }
-        if (t <= k1 + 1 && !step<2, Q0, true>(t++, cz, prod, W, me, mb)) return false;
-        if (t <= k1 + 1 && !step<3, 1 - Q0, true>(t++, cz, prod, W, me, mb)) return false;
-        if (t <= k1 + 1 && !step<0, Q0, true>(t++, cz, prod, W, me, mb)) return false;
-        if (t <= k1 + 1 && !step<1, 1 - Q0, true>(t++, cz, prod, W, me, mb)) return false;
-        return true;
+        if (t <= k1 + 1) step<2, Q0, true>(t++, cz, prod, W, me, mb);
+        if (t <= k1 + 1) step<3, 1 - Q0, true>(t++, cz, prod, W, me, mb);
+        if (t <= k1 + 1) step<0, Q0, true>(t++, cz, prod, W, me, mb);
+        if (t <= k1 + 1) step<1, 1 - Q0, true>(t++, cz, prod, W, me, mb);
     }
 };
 
-// One work item.  cbase = slot of plane k0 - 2.  Returns false when a wait gave up.
+// One work item.  cbase = slot of plane k0 - 2.  Returns false (uniformly across the
+// CTA) when a wait gave up.
 template <int TY, bool ZERO_IN, bool OMEGA1>
-__device__ __forceinline__ bool rbt_item(unsigned char *smem, unsigned long long *bars, const LevelK<float> &L,
-                                         float *__restrict__ eout, float omega, float omw, int bx, int by, int k0,
-                                         int k1, int cbase, RbtProducer<TY, ZERO_IN> &prod, const RbtItems &W,
-                                         const CUtensorMap *me, const CUtensorMap *mb)
+__device__ __forceinline__ bool rbt_item(unsigned char *smem, unsigned long long *bars, volatile int *abort_flag,
+                                         const LevelK<float> &L, float *__restrict__ eout, float omega, float omw,
+                                         int bx, int by, int k0, int k1, int cbase, RbtProducer<TY, ZERO_IN> &prod,
+                                         const RbtItems &W, const CUtensorMap *me, const CUtensorMap *mb)
 {
     RbtItem<TY, ZERO_IN, OMEGA1> I;
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const int i0 = 1 + RBT_TX * bx, j0 = 1 + TY * by;
     const int nx = L.nx, ny = L.ny;
     const int a = i0 - 2 + 2 * lane;
-    const int j = j0 - 1 + w;
+    const int ja = j0 - 1 + 2 * w, jb = ja + 1;
     I.smem = smem;
     I.bars = bars;
+    I.abort_flag = abort_flag;
     I.czm_t = L.czm;
     I.czp_t = L.czp;
     I.nz = L.nz;
     I.k0 = k0;
     I.k1 = k1;
-    I.lane = lane;
-    I.w = w;
-    I.r = w + 1;
     I.cbase = cbase;
+    I.oe = ((2 * w + 1) * RBT_W + 2 * lane) * 4;
+    I.ob = S_EB<TY>() + ((2 * w) * RBT_W + 2 * lane) * 4;
+    I.sy = L.sy;
     I.sz = L.sz;
     I.omega = omega;
     I.omw = omw;
     I.fail = false;
-    const bool row_in = j >= 1 && j <= ny;
+    const bool inA = ja >= 1 && ja <= ny, inB = jb >= 1 && jb <= ny;
     const bool in0 = a >= 1 && a <= nx, in1 = a + 1 >= 1 && a + 1 <= nx;
     const bool mid = lane >= 1 && lane <= 30;
-    I.need0 = row_in && in0 && (mid || lane == 31);
-    I.need1 = row_in && in1 && (mid || lane == 0);
-    I.store_lane = (w >= 1 && w <= TY) && row_in && mid && a <= nx;
+    // a lane updates the first-colour cell of its pair when it is interior and in the tile
+    // or the ring cell beside it (lane 0: its second cell, lane 31: its first cell)
+    const bool c0ok = in0 && (mid || lane == 31), c1ok = in1 && (mid || lane == 0);
+    I.nA[0] = inA && c0ok;
+    I.nA[1] = inA && c1ok;
+    I.nB[0] = inB && c0ok;
+    I.nB[1] = inB && c1ok;
+    const bool col_store = mid && a <= nx;
+    I.stA = col_store && inA && w >= 1;                          // row a of warp 0 is the ring row
+    I.stB = col_store && inB && w <= RbtShape<TY>::WARPS - 2;               // row b of the last warp is the ring row
     I.st_full = a + 1 <= nx;
-    I.pw = eout + (long long)a + (long long)L.sy * j;
-    I.cym = row_in ? L.cym[j] : 0.f;
-    I.cyp = row_in ? L.cyp[j] : 0.f;
-    const float dy = I.cym + I.cyp;
+    I.pwA = eout + (long long)a + (long long)L.sy * ja;
+    I.cymA = inA ? L.cym[ja] : 0.f;
+    I.cypA = inA ? L.cyp[ja] : 0.f;
+    I.cymB = inB ? L.cym[jb] : 0.f;
+    I.cypB = inB ? L.cyp[jb] : 0.f;
+    const float dyA = I.cymA + I.cypA, dyB = I.cymB + I.cypB;
 #pragma unroll
     for (int q = 0; q < 2; ++q) {
         const int i = a + q;
         const bool in = i >= 1 && i <= nx;
-        I.dxy[q] = (in ? L.sx[i] : 0.f) + dy;
+        const float sx = in ? L.sx[i] : 0.f;
+        I.dA[q] = sx + dyA;
+        I.dB[q] = sx + dyB;
         I.cxm[q] = in ? L.cxm[i] : 0.f;
         I.cxp[q] = in ? L.cxp[i] : 0.f;
     }
     // window at the first step t = k0 - 1: positions 0..3 = planes k0-3 .. k0; position 0
     // (plane k0-3) is never read, position 3 is loaded by the step itself
-    I.E[0] = make_float2(0.f, 0.f);
+    I.EA[0] = I.EB[0] = make_float2(0.f, 0.f);
     I.wait(cbase);
-    I.E[1] = I.own_e(I.stage_e(cbase));
     I.wait(cbase + 1);
-    I.E[2] = I.own_e(I.stage_e(cbase + 1));
-    I.B[0] = make_float2(0.f, 0.f);
-    // the pair's first cell a is odd, so it carries the first colour on plane k when j + k
-    // is even ((i + j + k) odd, src/rbgs_poisson_matrix.f90:242)
-    if (((j + k0 - 1) & 1) == 0) return I.template run<0>(prod, W, me, mb);
-    return I.template run<1>(prod, W, me, mb);
+    if (ZERO_IN) {
+        I.EA[1] = I.EB[1] = I.EA[2] = I.EB[2] = make_float2(0.f, 0.f);
+    } else {
+        const unsigned s1 = I.stage_off(cbase), s2 = I.stage_off(cbase + 1);
+        I.EA[1] = I.lds2(s1 + I.oe);
+        I.EB[1] = I.lds2(s1 + I.oe + RBT_W * 4);
+        I.EA[2] = I.lds2(s2 + I.oe);
+        I.EB[2] = I.lds2(s2 + I.oe + RBT_W * 4);
+    }
+    I.BA[0] = I.BB[0] = make_float2(0.f, 0.f);
+    // the pair's first cell a is odd, so on row a it carries the first colour on plane k
+    // when ja + k is even ((i + j + k) odd, src/rbgs_poisson_matrix.f90:242)
+    if (((ja + k0 - 1) & 1) == 0)
+        I.template run<0>(prod, W, me, mb);
+    else
+        I.template run<1>(prod, W, me, mb);
+    return !__syncthreads_or(I.fail);
 }
 
 }  // namespace pmg
