@@ -55,7 +55,7 @@ __global__ void __launch_bounds__(rb_threads<TY>(), rb_min_blocks<TY>()) k_rb32_
 
 // blocks per SM the TMA-fed kernel's register budget is sized for
 template <int TY>
-constexpr int rbt_min_blocks() { return TY <= 6 ? 5 : TY <= 10 ? 3 : 2; }
+constexpr int rbt_min_blocks() { return TY <= 6 ? 5 : 3; }
 
 template <int TY, bool ZERO_IN, bool OMEGA1>
 __global__ void __launch_bounds__(RbtShape<TY>::THREADS, rbt_min_blocks<TY>())
@@ -68,16 +68,16 @@ __global__ void __launch_bounds__(RbtShape<TY>::THREADS, rbt_min_blocks<TY>())
     unsigned char *smem = smem_raw + ((128u - (rbtdetail::smem_addr(smem_raw) & 127u)) & 127u);
     unsigned long long *bars = reinterpret_cast<unsigned long long *>(smem + RBT_NS * S::STAGE);
     volatile int *abort_flag = reinterpret_cast<volatile int *>(bars + RBT_NS);
+    RbtProducer<TY, ZERO_IN> *prod = reinterpret_cast<RbtProducer<TY, ZERO_IN> *>(bars + RBT_NS + 2);
     if (threadIdx.x == 0) {
         for (int q = 0; q < RBT_NS; ++q) rbtdetail::mbar_init(&bars[q], 1);
         *abort_flag = 0;
         rbtdetail::fence_mbar_init();
     }
     __syncthreads();
-    RbtProducer<TY, ZERO_IN> prod;
     if (threadIdx.x == 0) {
-        prod.start(W);
-        prod.issue_upto(RBT_NS - 1, W, smem, bars, &me, &mb);
+        prod->start(W);
+        prod->issue_upto(RBT_NS - 1, W, smem, bars, &me, &mb);
     }
     int cbase = 0;
     for (int it = blockIdx.x; it < W.nitems; it += gridDim.x) {
@@ -88,7 +88,7 @@ __global__ void __launch_bounds__(RbtShape<TY>::THREADS, rbt_min_blocks<TY>())
             if (threadIdx.x == 0) {
                 atomicOr(err, 1);
                 // let the copies still in flight land before the CTA exits (bounded)
-                for (int q = max(0, prod.slot - RBT_NS); q < prod.slot; ++q)
+                for (int q = max(0, prod->slot - RBT_NS); q < prod->slot; ++q)
                     rbtdetail::mbar_wait_bounded(&bars[q % RBT_NS], (unsigned)(q / RBT_NS) & 1u);
             }
             return;
@@ -331,9 +331,12 @@ int tune_smoother(const LevelK<float> &L, const Launch &ln, float *e0, float *e1
     PMG_TRY_S(cuda_status(cudaEventCreate(&z), "tuner event"));
     float best = 1e30f;
     int bv = 0, bk = 0;
-    const int chunks[4] = {0, 16, 32, 64};
+    // the register-window kernel stages at most RB_ZC - 3 planes of z coefficients
+    const int chunks_window[4] = {0, 16, 32, 64}, chunks_tma[4] = {0, 32, 64, 128};
+    const int *chunks = use_tma ? chunks_tma : chunks_window;
     for (int v = 0; v < 3; ++v)
-        for (int c : chunks) {
+        for (int ci = 0; ci < 4; ++ci) {
+            const int c = chunks[ci];
             if (rb32_fused(L, ln, e0, e1, b, 1.f, 0.f, false, s, v, c, tma, 0, err) != PMG_OK) continue;
             cudaEventRecord(a, s);
             for (int q = 0; q < 3; ++q) rb32_fused(L, ln, e0, e1, b, 1.f, 0.f, false, s, v, c, tma, 0, err);

@@ -43,7 +43,8 @@ struct RbtShape {
     static constexpr int EROWS = TY + 4, BROWS = TY + 2;
     static constexpr int EBYTES = EROWS * RBT_W * 4, BBYTES = BROWS * RBT_W * 4;
     static constexpr int STAGE = EBYTES + BBYTES;
-    static constexpr int SMEM = RBT_NS * STAGE + RBT_NS * 8 + 16 + 128;   // stages, mbarriers, abort flag, slack
+    // stages, mbarriers, abort flag and producer state, alignment slack
+    static constexpr int SMEM = RBT_NS * STAGE + RBT_NS * 8 + 64 + 128;
     static constexpr int WARPS = (TY + 2) / 2;                               // two rows per warp
     static constexpr int THREADS = WARPS * 32;
     static_assert(TY % 2 == 0, "tile height must be even");
@@ -155,7 +156,9 @@ struct RbtItems {
     }
 };
 
-// The producer: one thread issuing the planes of the CTA's items, slot after slot.
+// The producer: one thread issuing the planes of the CTA's items, slot after slot.  Its
+// state lives in shared memory (only thread 0 touches it), so it costs the other
+// threads no registers.
 template <int TY, bool ZERO_IN>
 struct RbtProducer {
     int it, q, k0, k1, bx, by;   // item being issued and its next plane q
@@ -262,7 +265,7 @@ struct RbtItem {
     // same indices).  CHECKED steps test at run time whether plane t is a grid plane
     // and whether plane t-1 belongs to the item; the steps k0 < t <= k1 need neither.
     template <int P, int Q, bool CHECKED>
-    __device__ __forceinline__ void step(int t, float (&cz)[6], RbtProducer<TY, ZERO_IN> &prod, const RbtItems &W,
+    __device__ __forceinline__ void step(int t, float (&cz)[6], RbtProducer<TY, ZERO_IN> *prod, const RbtItems &W,
                                          const CUtensorMap *me, const CUtensorMap *mb)
     {
         using namespace rbtdetail;
@@ -327,7 +330,7 @@ struct RbtItem {
         }
         fence_proxy_async();
         __syncthreads();
-        if (threadIdx.x == 0) prod.issue_upto(cs - 2 + RBT_NS, W, smem, bars, me, mb);
+        if (threadIdx.x == 0) prod->issue_upto(cs - 2 + RBT_NS, W, smem, bars, me, mb);
         if (!CHECKED || (t - 1 >= k0 && t - 1 <= k1)) {
             const float upA = __shfl_up_sync(0xffffffffu, EA[im1].y, 1);
             const float dnA = __shfl_down_sync(0xffffffffu, EA[im1].x, 1);
@@ -376,7 +379,7 @@ struct RbtItem {
     // Steps t = k0-1 .. k1+1: two checked steps, unchecked steps k0+1 .. k1 unrolled by
     // the four-plane register window, then the remaining steps checked.
     template <int Q0>
-    __device__ __forceinline__ void run(RbtProducer<TY, ZERO_IN> &prod, const RbtItems &W, const CUtensorMap *me,
+    __device__ __forceinline__ void run(RbtProducer<TY, ZERO_IN> *prod, const RbtItems &W, const CUtensorMap *me,
                                         const CUtensorMap *mb)
     {
         float cz[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
@@ -403,7 +406,7 @@ struct RbtItem {
 template <int TY, bool ZERO_IN, bool OMEGA1>
 __device__ __forceinline__ bool rbt_item(unsigned char *smem, unsigned long long *bars, volatile int *abort_flag,
                                          const LevelK<float> &L, float *__restrict__ eout, float omega, float omw,
-                                         int bx, int by, int k0, int k1, int cbase, RbtProducer<TY, ZERO_IN> &prod,
+                                         int bx, int by, int k0, int k1, int cbase, RbtProducer<TY, ZERO_IN> *prod,
                                          const RbtItems &W, const CUtensorMap *me, const CUtensorMap *mb)
 {
     RbtItem<TY, ZERO_IN, OMEGA1> I;
