@@ -48,7 +48,29 @@ def parse():
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--quick", action="store_true",
                    help="time the mixed solve only (no FP64 comparison, e2e or CPU baseline); for profiling")
+    p.add_argument("--precision", default="mixed", choices=["mixed", "fp64"],
+                   help="with --quick: the precision of the timed solve")
+    p.add_argument("--workload", default="solve", choices=["solve", "batch"],
+                   help="batch: the 128-problem batched solve (sizes from {32..192}, PCG64(4)); prints "
+                        "its own JSON line (cells per second)")
+    p.add_argument("--batch", type=int, default=128, help="problems of --workload batch")
     return p.parse_args()
+
+
+def max_over_ranks(value, world, device):
+    """The job's time: the maximum of a per-rank value over all ranks (replicas)."""
+    if world <= 1:
+        return value
+    import torch
+    t = torch.tensor([value], device=device, dtype=torch.float64)
+    torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_throughput(cells_per_rank, ms, world):
+    """Whole-job cells per second of `world` replicas that each solved `cells_per_rank`
+    cells in (the slowest rank's) `ms` milliseconds."""
+    return cells_per_rank * world / (ms * 1e-3)
 
 
 def dist_env():
@@ -219,7 +241,8 @@ def run_ours(args):
             torch.distributed.barrier()
             torch.cuda.synchronize()
 
-    mg = pmg.Multigrid(mesh, nl, 100, "cgs", precision="mixed", mixed_inner_cycles=args.inner,
+    prec = args.precision if args.quick else "mixed"
+    mg = pmg.Multigrid(mesh, nl, 100, "cgs", precision=prec, mixed_inner_cycles=args.inner,
                        stream=stream.cuda_stream)
 
     def step():
@@ -247,16 +270,14 @@ def run_ours(args):
     prof = {pmg.PROF_CLASSES[c]: mg.profile_read(c) for c in pmg.PROF_CLASSES}
     mg.profile(False)
     clk = clocks.stop()
-    if world > 1:
-        t = torch.tensor([ms], device=dev, dtype=torch.float64)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = max_over_ranks(ms, world, dev)
     rep = reps[-1]
-    assert rep.converged and rep.final_ratio < TOL, "mixed solve did not converge"
+    assert rep.converged and rep.final_ratio < TOL, "solve did not converge"
 
     if args.quick:
         if rank == 0:
-            print(json.dumps({"metric": METRIC, "value": round(ms, 3), "unit": "ms", "quick": True,
+            print(json.dumps({"metric": METRIC, "value": round(ms, 3), "unit": "ms", "quick": True, "n": n,
+                              "precision": prec, "cycles": rep.cycles,
                               "kernels": {k: v for k, v in prof.items() if v[1]}, "gpu_launches": launches}))
         mg.destroy()
         return
@@ -333,7 +354,7 @@ def run_ours(args):
                     "d2h_bytes_per_step": 2 * nbytes},
             "gpu_launches": launches,
             "clocks": clk,
-            "cells_per_s": round(cells / (ms * 1e-3), 1),
+            "cells_per_s": round(replica_throughput(cells, ms, world), 1),
         }
         print(json.dumps(line), flush=True)
     mg.destroy()
@@ -341,9 +362,52 @@ def run_ours(args):
         torch.distributed.destroy_process_group()
 
 
+def run_batch(args):
+    """The batched configuration: one solve of every problem to 1e-10 (mixed precision,
+    depth-synchronous persistent launches, graph-captured corrections), timed with CUDA
+    events on the batch's stream; value = interior cells of all problems / solve time."""
+    import torch
+    from peps_mg_gb300 import problems
+    from peps_mg_gb300.batch import BatchSolver
+
+    rank, world, local = dist_env()
+    if world > 1:
+        torch.cuda.set_device(local)
+    dims = problems.batch_dims(args.batch)
+    with BatchSolver(dims, mixed_inner_cycles=args.inner) as bs:
+        rhs = bs.field()
+        for p, vals in enumerate(problems.batch_rhs(dims)):
+            bs.view(rhs, p)[1:-1, 1:-1, 1:-1] = torch.from_numpy(vals).cuda()
+        sol = bs.field()
+        for _ in range(max(args.warmup, 3)):
+            sol.zero_()
+            cycles, ratio, _ = bs.solve(sol, rhs, MAXIT, TOL, OMEGA, max_cycles=100)
+        times = []
+        for _ in range(args.steps):
+            sol.zero_()
+            torch.cuda.synchronize()
+            cycles, ratio, ms = bs.solve(sol, rhs, MAXIT, TOL, OMEGA, max_cycles=100)
+            times.append(ms)
+        assert np.all(ratio < TOL), "batched solve did not converge"
+        cells = int(np.prod(dims, axis=1).sum())
+        ms = statistics.mean(times)
+        if rank == 0:
+            print(json.dumps({"metric": "batched_solve_cells_per_s", "value": round(cells / (ms * 1e-3), 1),
+                              "unit": "cells/s", "ms_per_step": round(ms, 3), "steps": args.steps,
+                              "higher_is_better": True, "dtype": "f32+f64", "data": "synthetic (U[-1,1], PCG64)",
+                              "config": {"workload": "%d independent problems, axis sizes from {32..192} "
+                                                     "(PCG64(4)), mixed precision to 1e-10" % args.batch,
+                                         "problems": args.batch, "cells": cells,
+                                         "inner_cycles_per_correction": args.inner,
+                                         "corrections_max": int(cycles.max()),
+                                         "corrections_mean": round(float(cycles.mean()), 2)}}))
+
+
 def main():
     args = parse()
-    if args.impl == "reference":
+    if args.workload == "batch":
+        run_batch(args)
+    elif args.impl == "reference":
         run_reference(args)
     else:
         run_ours(args)

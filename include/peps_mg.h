@@ -156,9 +156,9 @@ int pmg_adjoint(pmg_ctx *ctx, const double *dLdu, double *dLdb, double dLdg[6], 
  * rules with as many levels as its sizes allow), solved together in mixed precision:
  * every V-cycle operation at a depth is one persistent launch over all problems, one
  * outer correction is captured in a CUDA graph, smoother tiles are autotuned per depth.
- * dims: 3 ints per problem.  meshes: NULL (uniform meshes of the unit cube) or 6 host
- * pointers per problem (dxm, dxg, dym, dyg, dzm, dzg, each n+2 values; NULL entries mean
- * uniform).  sol and rhs are packed device arrays: problem p occupies elements
+ * dims: 3 ints per problem.  meshes: NULL (uniform meshes of cubic cells, width
+ * 1/max(nx,ny,nz), so the longest axis spans [0,1]) or 6 host pointers per problem (dxm,
+ * dxg, dym, dyg, dzm, dzg, each n+2 values; NULL entries mean that uniform axis).  sol and rhs are packed device arrays: problem p occupies elements
  * offsets[p] .. offsets[p+1]-1 in the usual (0:n+1)^3 Fortran layout
  * (pmg_batch_layout). */
 typedef struct pmg_batch pmg_batch;

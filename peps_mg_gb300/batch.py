@@ -1,6 +1,6 @@
 """Batched solver: many independent problems of uneven sizes in one set of launches.
 
-    bs = BatchSolver(dims)                      # dims: (n, 3) sizes, uniform unit-cube meshes
+    bs = BatchSolver(dims)                      # dims: (n, 3) sizes; uniform meshes of cubic cells
     sol, rhs = bs.field(), bs.field()           # packed CUDA arrays
     bs.view(rhs, p)[...] = ...                  # problem p as a (nz+2, ny+2, nx+2) view
     cycles, ratio, ms = bs.solve(sol, rhs, 2, 1e-10, 1.0, max_cycles=50)
@@ -45,6 +45,14 @@ class BatchSolver:
         check(self._lib.pmg_batch_layout(self._h, off, lev), "batch_layout")
         self.offsets = np.array(off[:], dtype=np.int64)
         self.levels = np.array(lev[:], dtype=np.int32)
+
+    def mesh(self, p):
+        """The default mesh of problem p (no meshes given): cubic cells of width
+        1/max(nx, ny, nz), the same values the library builds."""
+        from . import geometry as G
+        d = [int(v) for v in self.dims[p]]
+        h = 1.0 / float(max(d))
+        return [G.mesh_from_widths(np.full(m, h)) for m in d]
 
     @property
     def total(self):

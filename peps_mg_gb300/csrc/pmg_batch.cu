@@ -368,20 +368,22 @@ int batch_create(Batch **out, int n, const int *dims, const double *const *meshe
         std::vector<double> ax[3][3];
         const double *mp[9];
         const int nn[3] = {nx, ny, nz};
+        const double h = 1.0 / (double)std::max(nx, std::max(ny, nz));   // cubic cells
         for (int d = 0; d < 3; ++d) {
             if (meshes && meshes[6 * p + 2 * d] && meshes[6 * p + 2 * d + 1]) {
                 mp[3 * d] = meshes[6 * p + 2 * d];
                 mp[3 * d + 1] = meshes[6 * p + 2 * d + 1];
                 mp[3 * d + 2] = nullptr;
             } else {
-                // uniform mesh of the unit interval (src/geometry.f90:180-189)
+                // uniform mesh of cubic cells of width 1/max(nx,ny,nz), so the longest axis
+                // spans [0,1] (src/geometry.f90:180-189)
                 auto &dm = ax[d][0], &dg = ax[d][1], &xg = ax[d][2];
                 const int m = nn[d];
                 dm.assign((size_t)m + 2, 0.0);
                 dg.assign((size_t)m + 2, 0.0);
                 xg.assign((size_t)m + 2, 0.0);
                 for (int i = 1; i <= m; ++i) {
-                    dm[i] = 1.0 / (double)m;
+                    dm[i] = h;
                     dg[i] = 0.5 * (dm[i] + dm[i - 1]);
                     xg[i] = xg[i - 1] + dg[i];
                 }

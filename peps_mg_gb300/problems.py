@@ -11,6 +11,9 @@ the mesh as three (dm, dg, xg) triples.
 * gaussian_blobs(n)  unit cube, sum of 8 Gaussians (sigma 0.05, centres U[0.1,0.9]^3,
                      amplitudes U[-10,10]) plus 1e-3 U[-1,1] noise, PCG64(3) (the 512^3
                      mixed-precision case)
+* batch_dims(count)  the batched case: `count` problems, each axis size drawn from
+                     {32, 48, 64, 96, 128, 192} by PCG64(4); batch_rhs fills a packed
+                     right-hand side with U[-1,1] (PCG64(seed + 100)) problem by problem
 """
 import numpy as np
 
@@ -55,3 +58,18 @@ def gaussian_blobs(n, seed=3, blobs=8, sigma=0.05, noise=1e-3):
         gz = np.exp(-(xc - c[2]) ** 2 * inv)
         vals += a * (gz[:, None, None] * (gy[None, :, None] * gx[None, None, :]))
     return [ax, ax, ax], _interior((n, n, n), vals)
+
+
+BATCH_SIZES = (32, 48, 64, 96, 128, 192)
+
+
+def batch_dims(count=128, seed=4, sizes=BATCH_SIZES):
+    """(count, 3) int array of (nx, ny, nz)."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    return rng.choice(np.asarray(sizes), size=(count, 3))
+
+
+def batch_rhs(dims, seed=4):
+    """Interior values U[-1,1] per problem, in (k, j, i) order."""
+    rng = np.random.Generator(np.random.PCG64(seed + 100))
+    return [rng.uniform(-1.0, 1.0, size=(int(d[2]), int(d[1]), int(d[0]))) for d in dims]

@@ -42,7 +42,7 @@ def test_batch_matches_single_problem_solves():
         assert np.all(ratio < 1e-10), ratio
         for p in range(bs.n):
             nx, ny, nz = (int(v) for v in dims[p])
-            mesh = [pmg.geometry.uniform_axis(m, 0.0, 1.0) for m in (nx, ny, nz)]
+            mesh = bs.mesh(p)
             with pmg.Multigrid(mesh, int(bs.levels[p]), 60, "cgs", precision="mixed") as mg:
                 s1 = torch.zeros_like(bs.view(rhs, p))
                 r1 = torch.zeros_like(s1)
@@ -60,7 +60,7 @@ def test_batch_against_fp64_oracle_sample():
         assert np.all(ratio < 1e-10)
         for p in (0, 3, 5):
             nx, ny, nz = (int(v) for v in dims[p])
-            mesh = [pmg.geometry.uniform_axis(m, 0.0, 1.0) for m in (nx, ny, nz)]
+            mesh = bs.mesh(p)
             omg = O.OracleMG(mesh, int(bs.levels[p]), 100, 0)
             ref, rr = O.field(nx, ny, nz), O.field(nx, ny, nz)
             omg.solve(ref, rr, from_dev(bs.view(rhs, p)), 2, 1e-10, 1.0)
@@ -70,3 +70,32 @@ def test_batch_against_fp64_oracle_sample():
 def test_batch_rejects_bad_sizes():
     with pytest.raises(pmg.PmgError):
         BatchSolver([[9, 9, 9]])
+
+
+def test_batch_128_problems_full_size():
+    """The batched workload at full size: 128 problems, axis sizes from {32..192}
+    (PCG64(4)), rhs U[-1,1]; every problem converges, and a sample matches single-problem
+    mixed solves and the FP64 oracle."""
+    from peps_mg_gb300 import problems
+    dims = problems.batch_dims(128)
+    with BatchSolver(dims, mixed_inner_cycles=4) as bs:
+        rhs = bs.field()
+        for p, vals in enumerate(problems.batch_rhs(dims)):
+            bs.view(rhs, p)[1:-1, 1:-1, 1:-1] = torch.from_numpy(vals).cuda()
+        sol = bs.field()
+        cycles, ratio, ms = bs.solve(sol, rhs, 2, 1e-10, 1.0, max_cycles=60)
+        assert np.all(ratio < 1e-10), ratio.max()
+        order = np.argsort(np.prod(dims, axis=1))
+        for p in (int(order[0]), int(order[len(order) // 2]), int(order[-1])):
+            nx, ny, nz = (int(v) for v in dims[p])
+            mesh = bs.mesh(p)
+            with pmg.Multigrid(mesh, int(bs.levels[p]), 60, "cgs", precision="mixed", mixed_inner_cycles=4) as mg:
+                s1 = torch.zeros_like(bs.view(rhs, p))
+                r1 = torch.zeros_like(s1)
+                mg.solve_vcycle(s1, r1, bs.view(rhs, p).contiguous(), 2, 1e-10, 1.0)
+            assert rel(from_dev(bs.view(sol, p)), from_dev(s1)) < 1e-8
+            omg = O.OracleMG(mesh, int(bs.levels[p]), 100, 0, omp=True)
+            ref, rr = O.field(nx, ny, nz), O.field(nx, ny, nz)
+            omg.solve(ref, rr, from_dev(bs.view(rhs, p)), 2, 1e-10, 1.0)
+            omg.close()
+            assert rel(from_dev(bs.view(sol, p)), ref) < 1e-8

@@ -218,3 +218,24 @@ def test_nan_rhs_reports_divergence():
         with pytest.raises(pmg.PmgError) as e:
             mg.solve_vcycle(sol, torch.zeros_like(sol), to_dev(rhs), 1, 1e-10, 1.0)
         assert e.value.status == 3
+
+
+def test_tanh_256_aggregation_methods_against_oracle():
+    """The 256^3 tanh-z workload at full size: rhs U[-1,1] (PCG64(2)), 7 levels down to
+    2^3; CGS, CGA from 16^3 (CGA_level 4) and CGPSA give the oracle's bits."""
+    n = 256
+    mesh, rhs = tanh_z_problem(n)
+    omg = O.OracleMG(mesh, 7, 60, 0, omp=True)
+    osol, orsd = O.field(n, n, n), O.field(n, n, n)
+    ncyc, hist, ci = omg.solve(osol, orsd, F(rhs), 2, 1e-10, 1.0)
+    omg.close()
+    for method, cga, cg3 in (("cgs", 0, (0, 0, 0)), ("cga", 4, (0, 0, 0)), ("cgpsa", 0, (4, 5, 6))):
+        with pmg.Multigrid(mesh, 7, 60, method, cga, cg3) as mg:
+            sol = torch.zeros((n + 2,) * 3, dtype=torch.float64, device="cuda")
+            rsd = torch.zeros_like(sol)
+            rep = mg.solve_vcycle(sol, rsd, to_dev(rhs), 2, 1e-10, 1.0)
+        assert rep.converged and rep.cycles == ncyc, method
+        assert rel(rep.history, hist) < TOL, method
+        assert np.array_equal(rep.coarse_iterations, ci), method
+        assert np.array_equal(from_dev(sol), osol), method
+        del sol, rsd
