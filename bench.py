@@ -278,6 +278,7 @@ def run_ours(args):
         if rank == 0:
             print(json.dumps({"metric": METRIC, "value": round(ms, 3), "unit": "ms", "quick": True, "n": n,
                               "precision": prec, "cycles": rep.cycles,
+                              "coarse_iterations": [int(v) for v in rep.coarse_iterations],
                               "kernels": {k: v for k, v in prof.items() if v[1]}, "gpu_launches": launches}))
         mg.destroy()
         return

@@ -409,11 +409,12 @@ int batch_create(Batch **out, int n, const int *dims, const double *const *meshe
         std::unique_ptr<Ctx> c(new (std::nothrow) Ctx());
         if (!c) return PMG_ENOMEM;
         c->autotune = false;
+        c->deep_tail = false;   // the batch runs every depth above the coarsest on its grid launches
         PMG_TRY_B(c->build(&cfg, B->stream));
         PMG_TRY_B(c->setup_mixed());
         B->dmax = std::max(B->dmax, c->nl);
         B->offset[p + 1] = B->offset[p] + (long long)c->lv[0].total;
-        B->tail_threads = std::max(B->tail_threads, c->tail_threads);
+        B->tail_threads = std::max(B->tail_threads, c->tail32_threads);
         B->probs.push_back(std::move(c));
     }
     B->total = B->offset[n];

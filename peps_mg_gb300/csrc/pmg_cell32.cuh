@@ -204,11 +204,11 @@ __device__ __forceinline__ double outer_residual_cell(const LevelK<double> &L, d
 template <typename F>
 __device__ __forceinline__ void for_cells(int nx, int ny, int nz, F f)
 {
-    const long long n = (long long)nx * ny * nz;
-    for (long long q = threadIdx.x; q < n; q += blockDim.x) {
-        const int i = (int)(q % nx) + 1;
-        const long long rr = q / nx;
-        f(i, (int)(rr % ny) + 1, (int)(rr / ny) + 1);
+    // tail levels hold at most 2^18 cells, so 32-bit index arithmetic suffices
+    const int n = nx * ny * nz;
+    for (int q = threadIdx.x; q < n; q += blockDim.x) {
+        const int rr = q / nx;
+        f(q - rr * nx + 1, rr % ny + 1, rr / ny + 1);
     }
 }
 
@@ -216,7 +216,7 @@ __device__ void t32_sweeps(const LevelK<float> &L, float *x, const float *b, int
                            bool zero_start)
 {
     const int hx = (L.nx + 1) / 2;
-    const long long nq = (long long)hx * L.ny * L.nz;
+    const int nq = hx * L.ny * L.nz;
     for (int it = 0; it < iters; ++it)
         for (int colour = 0; colour < 2; ++colour) {
             if (zero_start && it == 0 && colour == 0) {
@@ -225,10 +225,10 @@ __device__ void t32_sweeps(const LevelK<float> &L, float *x, const float *b, int
                     x[p] = ((i + j + k) & 1) ? __fdividef(omega * b[p], diag32(L, i, j, k)) : 0.f;
                 });
             } else {
-                for (long long q = threadIdx.x; q < nq; q += blockDim.x) {
-                    const int t = (int)(q % hx);
-                    const long long rr = q / hx;
-                    const int j = (int)(rr % L.ny) + 1, k = (int)(rr / L.ny) + 1;
+                for (int q = threadIdx.x; q < nq; q += blockDim.x) {
+                    const int rr = q / hx;
+                    const int t = q - rr * hx;
+                    const int j = rr % L.ny + 1, k = rr / L.ny + 1;
                     const int i = 2 * t + 1 + ((j + k + colour) & 1);
                     if (i <= L.nx) x[lin(i, j, k, L.sy, L.sz)] = rbgs32(L, x, b, i, j, k, omega, omw);
                 }
@@ -237,15 +237,17 @@ __device__ void t32_sweeps(const LevelK<float> &L, float *x, const float *b, int
         }
 }
 
-// Body of the single-CTA FP32 coarse tail for one problem (see k_tail32).
-__device__ void tail32_body(const TailDesc<float> &D, double *sw)
+// The single-CTA FP32 coarse tail for one problem on the level descriptors Ls / Xs and
+// arrays xs / bs (the global arrays of D, or shared-memory copies).
+__device__ void tail32_run(const TailDesc<float> &D, const LevelK<float> *Ls, const XferK<float> *Xs,
+                           float *const *xs, float *const *bs, double *sw)
 {
     const float omega = D.omega, omw = D.omw;
     for (int l = D.l0; l < D.nl; ++l) {
-        const LevelK<float> L = D.L[l];
-        const XferK<float> X = D.X[l];
-        float *x = D.x[l], *bc = D.b[l + 1];
-        const float *b = D.b[l];
+        const LevelK<float> L = Ls[l];
+        const XferK<float> X = Xs[l];
+        float *x = xs[l], *bc = bs[l + 1];
+        const float *b = bs[l];
         t32_sweeps(L, x, b, D.maxit, omega, omw, true);
         for_cells(X.ncx, X.ncy, X.ncz, [&](int i, int j, int k) {
             bc[lin(i, j, k, X.csy, X.csz)] = resrestrict_cell32(L, X, x, b, i, j, k);
@@ -255,31 +257,106 @@ __device__ void tail32_body(const TailDesc<float> &D, double *sw)
     // coarsest level: solved in FP64 (b converted up, x converted down), so its
     // convergence test against the FP64 tolerance is attainable
     {
-        const LevelK<float> L = D.L[D.nl];
+        const LevelK<float> L = Ls[D.nl];
         const LevelK<double> &C = D.C64;
-        float *x = D.x[D.nl];
-        const float *b = D.b[D.nl];
-        for_cells(L.nx, L.ny, L.nz, [&](int i, int j, int k) {
-            D.cb64[lin(i, j, k, C.sy, C.sz)] = (double)b[lin(i, j, k, L.sy, L.sz)];
-        });
-        __syncthreads();
-        const int iters = coarse_solve_f64(C, D.cx64, D.cb64, D.cp64, D.cap64, D.crr64, D.coarse_solver,
-                                           D.coarse_maxit, D.tol, D.omega64, D.omw64, sw);
-        for_cells(L.nx, L.ny, L.nz, [&](int i, int j, int k) {
-            x[lin(i, j, k, L.sy, L.sz)] = (float)D.cx64[lin(i, j, k, C.sy, C.sz)];
-        });
-        if (threadIdx.x == 0 && D.iters_out) *D.iters_out = iters;
+        float *x = xs[D.nl];
+        const float *b = bs[D.nl];
+        if (C.sz * (C.nz + 2) <= kWarpCoarseMax) {
+            // small coarsest level: shared memory, one warp, no block barriers per iteration
+            __shared__ double cs[5][kWarpCoarseMax];
+            const int total = (int)(C.sz * (C.nz + 2));
+            for (int q = threadIdx.x; q < total; q += blockDim.x) cs[1][q] = 0.0;
+            __syncthreads();
+            for_cells(L.nx, L.ny, L.nz, [&](int i, int j, int k) {
+                cs[1][lin(i, j, k, C.sy, C.sz)] = (double)b[lin(i, j, k, L.sy, L.sz)];
+            });
+            __syncthreads();
+            int iters = 0;
+            if (threadIdx.x < 32)
+                iters = coarse_solve_warp_f64(C, cs[0], cs[1], cs[2], cs[3], cs[4], D.coarse_solver, D.coarse_maxit,
+                                              D.tol, D.omega64, D.omw64);
+            if (threadIdx.x == 0 && D.iters_out) *D.iters_out = iters;
+            __syncthreads();
+            for_cells(L.nx, L.ny, L.nz, [&](int i, int j, int k) {
+                x[lin(i, j, k, L.sy, L.sz)] = (float)cs[0][lin(i, j, k, C.sy, C.sz)];
+            });
+        } else {
+            for_cells(L.nx, L.ny, L.nz, [&](int i, int j, int k) {
+                D.cb64[lin(i, j, k, C.sy, C.sz)] = (double)b[lin(i, j, k, L.sy, L.sz)];
+            });
+            __syncthreads();
+            const int iters = coarse_solve_f64(C, D.cx64, D.cb64, D.cp64, D.cap64, D.crr64, D.coarse_solver,
+                                               D.coarse_maxit, D.tol, D.omega64, D.omw64, sw);
+            for_cells(L.nx, L.ny, L.nz, [&](int i, int j, int k) {
+                x[lin(i, j, k, L.sy, L.sz)] = (float)D.cx64[lin(i, j, k, C.sy, C.sz)];
+            });
+            if (threadIdx.x == 0 && D.iters_out) *D.iters_out = iters;
+        }
         __syncthreads();
     }
     for (int l = D.nl - 1; l >= D.l0; --l) {
-        const LevelK<float> L = D.L[l];
-        const XferK<float> X = D.X[l];
-        float *x = D.x[l], *xc = D.x[l + 1];
-        const float *b = D.b[l];
+        const LevelK<float> L = Ls[l];
+        const XferK<float> X = Xs[l];
+        float *x = xs[l], *xc = xs[l + 1];
+        const float *b = bs[l];
         for_cells(X.ncx, X.ncy, X.ncz, [&](int i, int j, int k) { prolong_add_cell32(X, xc, x, i, j, k); });
         __syncthreads();
         t32_sweeps(L, x, b, D.maxit, omega, omw, false);
     }
+}
+
+__device__ void tail32_body(const TailDesc<float> &D, double *sw) { tail32_run(D, D.L, D.X, D.x, D.b, sw); }
+
+// The tail with x and b of every tail level copied into shared memory `sm` (D.sm_floats
+// floats, each array in the level's unpadded (nx+2)(ny+2)(nz+2) layout): b of the first
+// tail level comes in from global memory and x of that level goes back, every other
+// access stays on chip.
+__device__ void tail32_body_smem(const TailDesc<float> &D, double *sw, float *sm)
+{
+    __shared__ LevelK<float> sL[kMaxLevels];
+    __shared__ XferK<float> sX[kMaxLevels];
+    __shared__ float *sxp[kMaxLevels], *sbp[kMaxLevels];
+    if (threadIdx.x == 0) {
+        int off = 0;
+        for (int l = D.l0; l <= D.nl; ++l) {
+            LevelK<float> L = D.L[l];
+            L.sy = L.nx + 2;
+            L.sz = (long long)L.sy * (L.ny + 2);
+            const int tot = (int)(L.sz * (L.nz + 2));
+            sL[l] = L;
+            sxp[l] = sm + off;
+            off += (tot + 3) & ~3;
+            sbp[l] = sm + off;
+            off += (tot + 3) & ~3;
+        }
+        for (int l = D.l0; l < D.nl; ++l) {
+            XferK<float> X = D.X[l];
+            X.fsy = sL[l].sy;
+            X.fsz = sL[l].sz;
+            X.csy = sL[l + 1].sy;
+            X.csz = sL[l + 1].sz;
+            sX[l] = X;
+        }
+    }
+    for (int q = threadIdx.x; q < D.sm_floats; q += blockDim.x) sm[q] = 0.f;
+    __syncthreads();
+    const LevelK<float> &G = D.L[D.l0];
+    const LevelK<float> &S = sL[D.l0];
+    {
+        const float *gb = D.b[D.l0];
+        float *sb = sbp[D.l0];
+        for_cells(G.nx, G.ny, G.nz,
+                  [&](int i, int j, int k) { sb[lin(i, j, k, S.sy, S.sz)] = gb[lin(i, j, k, G.sy, G.sz)]; });
+    }
+    __syncthreads();
+    tail32_run(D, sL, sX, sxp, sbp, sw);
+    {
+        float *gx = D.x[D.l0];
+        const float *sx = sxp[D.l0];
+        for_cells(G.nx, G.ny, G.nz,
+                  [&](int i, int j, int k) { gx[lin(i, j, k, G.sy, G.sz)] = sx[lin(i, j, k, S.sy, S.sz)]; });
+    }
+    __syncthreads();
 }
 
 }  // namespace

@@ -12,6 +12,8 @@ namespace pmg {
 // Levels above this many cells (ghosts included) stay on the grid kernels instead of
 // the single-CTA tail.
 constexpr size_t kTailMaxCells = 1u << 18;
+// FP32 levels of at most this many cells run inside the single-CTA tail of the mixed cycle.
+constexpr long long kTail32Cells = 1LL << 12;
 
 struct Level {
     int n[3] = {0, 0, 0};
@@ -63,6 +65,10 @@ struct Ctx {
     std::vector<Launch> launch;
     int tail_l0 = 0;
     int tail_threads = 1024;   // block size of the single-CTA tail kernels
+    int tail32_l0 = 0;         // first level of the mixed cycle's single-CTA tail
+    int tail32_threads = 1024;
+    int tail32_smem = 0;       // dynamic shared memory bytes of the mixed cycle's tail
+    bool deep_tail = true;     // mixed cycle: move small levels into the tail (batch members keep tail_l0)
     TailDesc<double> tail_host;
     TailDesc<double> *d_tail = nullptr;
     double *d_partials = nullptr;

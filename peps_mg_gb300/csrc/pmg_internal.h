@@ -38,6 +38,9 @@ struct TailDesc {
     LevelK<double> C64;
     double *cx64, *cb64, *cp64, *cap64, *crr64;
     double omega64, omw64;
+    // FP32 tail only: floats of dynamic shared memory holding x and b of every tail level
+    // (0 = the tail works on the global arrays)
+    int sm_floats;
 };
 
 // ---- FP64 (bitwise) launchers, pmg_f64.cu -------------------------------------

@@ -32,7 +32,8 @@ namespace pmg {
 namespace {
 
 constexpr int kBX = 32, kBY = 8;
-constexpr int kTail32Threads = 1024;
+constexpr int kTail32Threads = 512;
+constexpr long long kTail32SmemBytes = 128 * 1024;   // dynamic shared memory of an on-chip tail
 constexpr int kMaxGridZ = 65535;
 
 __device__ __forceinline__ int tid2() { return threadIdx.x + blockDim.x * threadIdx.y; }
@@ -335,7 +336,11 @@ __global__ void k_convert_test(const double *in64, float *out32, const float *in
 __global__ void __launch_bounds__(kTail32Threads) k_tail32(const TailDesc<float> *__restrict__ Dp)
 {
     __shared__ double sw[kTail32Threads / 32];
-    tail32_body(*Dp, sw);
+    extern __shared__ float tail_sm[];
+    if (Dp->sm_floats > 0)
+        tail32_body_smem(*Dp, sw, tail_sm);
+    else
+        tail32_body(*Dp, sw);
 }
 
 // One CTA per problem: the coarse tails of a batch (problems marked done are skipped).
@@ -424,6 +429,20 @@ int Ctx::setup_mixed()
         set_error("mixed precision needs a coarsest level small enough for the single-CTA coarse solver");
         return PMG_EINVAL;
     }
+    // The FP32 cycle hands every level of at most kTail32Cells cells (and the levels the
+    // aggregation method already assigns to the tail) to the single-CTA tail kernel: such
+    // levels are latency bound on the grid kernels (a few microseconds of work behind
+    // each launch and each plane step), and one 1024-thread CTA runs them back to back.
+    tail32_l0 = tail_l0;
+    if (deep_tail)
+        while (tail32_l0 > 1 && (long long)lv[tail32_l0 - 1].n[0] * lv[tail32_l0 - 1].n[1] * lv[tail32_l0 - 1].n[2] <=
+                                    kTail32Cells)
+            --tail32_l0;
+    {
+        long long cells = 1;
+        for (int l = tail32_l0; l <= nl; ++l) cells = std::max(cells, (long long)lv[l].n[0] * lv[l].n[1] * lv[l].n[2]);
+        tail32_threads = (int)std::min<long long>(kTail32Threads, std::max<long long>(64, ((cells / 2 + 31) / 32) * 32));
+    }
     MixedState *m = new (std::nothrow) MixedState();
     if (!m) return PMG_ENOMEM;
     mixed = m;
@@ -479,7 +498,7 @@ int Ctx::setup_mixed()
         f.nx = k.nx; f.ny = k.ny; f.nz = k.nz; f.sy = pitch; f.sz = plane;
         f.cxm = F(k.cxm); f.cxp = F(k.cxp); f.sx = F(k.sx);
         f.cym = F(k.cym); f.cyp = F(k.cyp); f.czm = F(k.czm); f.czp = F(k.czp);
-        m->fused[l] = l < tail_l0 && rb32_fused_layout_ok(f, m->e[0][l], m->b[l]) &&
+        m->fused[l] = l < tail32_l0 && rb32_fused_layout_ok(f, m->e[0][l], m->b[l]) &&
                       rb32_fused_layout_ok(f, m->e[1][l], m->b[l]);
         m->rows[l] = rows;
         m->planes[l] = planes;
@@ -499,7 +518,7 @@ int Ctx::setup_mixed()
     PMG_TRY_M(mstatus(cudaMalloc(&m->d_tail, sizeof(TailDesc<float>)), "mixed tail descriptor"));
     PMG_TRY_M(mstatus(cudaMalloc(&m->d_err, sizeof(int)), "mixed error flag"));
     PMG_TRY_M(mstatus(cudaMemset(m->d_err, 0, sizeof(int)), "mixed error flag"));
-    for (int l = 0; l < tail_l0; ++l)
+    for (int l = 0; l < tail32_l0; ++l)
         if (m->fused[l] && autotune)
             PMG_TRY_M(tune_smoother(m->K[l], launch[l], m->e[0][l], m->e[1][l], m->b[l], stream, &m->variant[l],
                                     &m->kchunk[l], &m->tma[l], m->d_err));
@@ -512,7 +531,7 @@ int Ctx::upload_tail32(int maxit, double omega, double tol)
     MixedState *m = mixed;
     TailDesc<float> &D = m->tail_host;
     std::memset(&D, 0, sizeof(D));
-    D.l0 = tail_l0;
+    D.l0 = tail32_l0;
     D.nl = nl;
     D.maxit = maxit;
     D.coarse_solver = coarse_solver;
@@ -529,6 +548,21 @@ int Ctx::upload_tail32(int maxit, double omega, double tol)
         D.r[l] = nullptr;
     }
     fill_coarse64(D.C64, D.cx64, D.cb64, D.cp64, D.cap64, D.crr64, D.omega64, D.omw64, omega);
+    // x and b of the tail levels in shared memory when they fit (not for batch members,
+    // whose tails share one launch)
+    D.sm_floats = 0;
+    if (deep_tail) {
+        long long fl = 0;
+        for (int l = tail32_l0; l <= nl; ++l) {
+            const long long tot = (long long)(lv[l].n[0] + 2) * (lv[l].n[1] + 2) * (lv[l].n[2] + 2);
+            fl += 2 * ((tot + 3) & ~3LL);
+        }
+        if (fl * (long long)sizeof(float) <= kTail32SmemBytes) D.sm_floats = (int)fl;
+    }
+    tail32_smem = D.sm_floats * (int)sizeof(float);
+    if (tail32_smem > 0)
+        PMG_TRY_M(mstatus(cudaFuncSetAttribute(k_tail32, cudaFuncAttributeMaxDynamicSharedMemorySize, tail32_smem),
+                          "tail shared memory"));
     return mstatus(cudaMemcpyAsync(m->d_tail, &D, sizeof(D), cudaMemcpyHostToDevice, stream), "tail upload");
 }
 
@@ -574,18 +608,18 @@ int Ctx::vcycle32(int maxit, double omega, bool zero_start)
         prof.end(pi, PC_RESRESTRICT32, 1, 8.5 * N, stream);
         ++nlaunch;
     }
-    for (int l = 1; l < tail_l0; ++l) {
+    for (int l = 1; l < tail32_l0; ++l) {
         PMG_TRY_M(sweeps(l, true));
         PMG_TRY_M(resrestrict32(l));
         ++nlaunch;
     }
     {
         const int pi = prof.begin(stream);
-        k_tail32<<<1, tail_threads, 0, stream>>>(m->d_tail);
+        k_tail32<<<1, tail32_threads, tail32_smem, stream>>>(m->d_tail);
         prof.end(pi, PC_TAIL32, 1, 0.0, stream);
         ++nlaunch;
     }
-    for (int l = tail_l0 - 1; l >= 0; --l) {
+    for (int l = tail32_l0 - 1; l >= 0; --l) {
         const XferK<float> &Xl = m->X[l];
         const int pi = l == 0 ? prof.begin(stream) : -1;
         {

@@ -14,6 +14,8 @@
 
 #include <algorithm>
 #include <array>
+#include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <map>
 #include <mutex>
@@ -316,7 +318,7 @@ int tune_smoother(const LevelK<float> &L, const Launch &ln, float *e0, float *e1
     const std::array<int, 5> key = {L.nx, L.ny, L.nz, ln.collapse[2] ? 1 : 0, use_tma ? 1 : 0};
     *variant = 0;
     *kchunk = 0;
-    if ((long long)L.nx * L.ny * L.nz < (1LL << 15)) return PMG_OK;
+
     {
         std::lock_guard<std::mutex> g(mu);
         auto it = cache.find(key);
@@ -331,11 +333,14 @@ int tune_smoother(const LevelK<float> &L, const Launch &ln, float *e0, float *e1
     PMG_TRY_S(cuda_status(cudaEventCreate(&z), "tuner event"));
     float best = 1e30f;
     int bv = 0, bk = 0;
+    const char *log_env = std::getenv("PEPS_MG_TUNE_LOG");   // print every candidate's time
+    const bool log = log_env && log_env[0] == '1';
     // the register-window kernel stages at most RB_ZC - 3 planes of z coefficients
-    const int chunks_window[4] = {0, 16, 32, 64}, chunks_tma[4] = {0, 32, 64, 128};
+    const int chunks_window[] = {0, 16, 32, 64}, chunks_tma[] = {0, 4, 8, 16, 32, 64, 128};
     const int *chunks = use_tma ? chunks_tma : chunks_window;
+    const int nchunks = use_tma ? 7 : 4;
     for (int v = 0; v < 3; ++v)
-        for (int ci = 0; ci < 4; ++ci) {
+        for (int ci = 0; ci < nchunks; ++ci) {
             const int c = chunks[ci];
             if (rb32_fused(L, ln, e0, e1, b, 1.f, 0.f, false, s, v, c, tma, 0, err) != PMG_OK) continue;
             cudaEventRecord(a, s);
@@ -344,6 +349,9 @@ int tune_smoother(const LevelK<float> &L, const Launch &ln, float *e0, float *e1
             if (cudaEventSynchronize(z) != cudaSuccess) break;
             float ms = 0.f;
             cudaEventElapsedTime(&ms, a, z);
+            if (log)
+                std::fprintf(stderr, "[peps_mg tune] %dx%dx%d %s TY=%d kchunk=%d: %.1f us\n", L.nx, L.ny, L.nz,
+                             use_tma ? "tma" : "window", v == 1 ? 6 : v == 2 ? 10 : 14, c, ms * 1e3f / 3.f);
             if (ms < best) {
                 best = ms;
                 bv = v;

@@ -182,5 +182,177 @@ __device__ int coarse_solve_f64(const LevelK<double> &L, double *x, const double
     return iters;
 }
 
+// Coarsest-level solve by ONE warp on a level held in shared memory (at most
+// kWarpCoarseMax stored values, ghosts included): the per-cell arithmetic of
+// coarse_solve_f64 (rbgs_cell_f64 / ax_cell_f64, the same exit tests), the sums in a
+// 32-lane butterfly order (every lane obtains the same bits, so the exit decision is
+// uniform), and __syncwarp instead of block barriers.  x, b, p, ap, rr are shared
+// arrays of the level's layout; only the calling warp touches them.
+constexpr int kWarpCoarseMax = 1000;
+
+__device__ __forceinline__ double warp_sum_f64(double v)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = __dadd_rn(v, __shfl_xor_sync(0xffffffffu, v, o));
+    return v;
+}
+
+__device__ int coarse_solve_warp_f64(const LevelK<double> &L, double *x, const double *b, double *p, double *ap,
+                                     double *rr, int solver, int maxit, double tol, double omega, double omw)
+{
+    const int lane = threadIdx.x & 31;
+    const int nx = L.nx, ny = L.ny, n = L.nx * L.ny * L.nz;
+    const int total = (int)(L.sz * (L.nz + 2));
+    for (int q = lane; q < total; q += 32) {
+        x[q] = 0.0;
+        p[q] = 0.0;
+        ap[q] = 0.0;
+        rr[q] = 0.0;
+    }
+    __syncwarp();
+    if (n == 1) {
+        if (lane == 0) {
+            const long long c = lin(1, 1, 1, L.sy, L.sz);
+            x[c] = __ddiv_rn(b[c], diag_f64(L, 1, 1, 1));
+        }
+        __syncwarp();
+        return 0;
+    }
+    auto residual = [&](bool norm) -> double {
+        double acc = 0.0;
+        for (int q = lane; q < n; q += 32) {
+            const int i = q % nx + 1, r2 = q / nx, j = r2 % ny + 1, k = r2 / ny + 1;
+            const long long c = lin(i, j, k, L.sy, L.sz);
+            const double r = __dsub_rn(b[c], ax_cell_f64(L, x, i, j, k));
+            rr[c] = r;
+            acc = __dadd_rn(acc, __dmul_rn(r, r));
+        }
+        __syncwarp();
+        return norm ? warp_sum_f64(acc) : 0.0;
+    };
+    auto dot = [&](const double *u, const double *v) -> double {
+        double acc = 0.0;
+        for (int q = lane; q < n; q += 32) {
+            const int i = q % nx + 1, r2 = q / nx, j = r2 % ny + 1, k = r2 / ny + 1;
+            const long long c = lin(i, j, k, L.sy, L.sz);
+            acc = __dadd_rn(acc, __dmul_rn(u[c], v[c]));
+        }
+        return warp_sum_f64(acc);
+    };
+    // op 0: a = c; op 1: a += s c, bb -= s d; op 2: a = c + s a
+    auto interior = [&](int op, double sc, double *a, double *bb, const double *c, const double *d) {
+        for (int q = lane; q < n; q += 32) {
+            const int i = q % nx + 1, r2 = q / nx, j = r2 % ny + 1, k = r2 / ny + 1;
+            const long long e = lin(i, j, k, L.sy, L.sz);
+            if (op == 0) {
+                a[e] = c[e];
+            } else if (op == 1) {
+                a[e] = __dadd_rn(a[e], __dmul_rn(sc, c[e]));
+                bb[e] = __dsub_rn(bb[e], __dmul_rn(sc, d[e]));
+            } else {
+                a[e] = __dadd_rn(c[e], __dmul_rn(sc, a[e]));
+            }
+        }
+        __syncwarp();
+    };
+    int it = 0;
+    if (solver == 0 && n <= 64) {
+        // at most two cells per lane: their offsets, coefficients, 1/c0 and b stay in
+        // registers, so an iteration is a few shared-memory loads and FP64 FMA chains
+        // (the update multiplies by 1/c0 instead of dividing by c0)
+        long long cidx[2];
+        double cw[2][6], c0v[2], ic0[2], bv[2];
+        bool has[2], odd[2];
+#pragma unroll
+        for (int u = 0; u < 2; ++u) {
+            const int q = lane + 32 * u;
+            has[u] = q < n;
+            const int qq = has[u] ? q : 0;
+            const int i = qq % nx + 1, r2 = qq / nx, j = r2 % ny + 1, k = r2 / ny + 1;
+            cidx[u] = lin(i, j, k, L.sy, L.sz);
+            odd[u] = ((i + j + k) & 1) != 0;
+            cw[u][0] = L.cxm[i];
+            cw[u][1] = L.cxp[i];
+            cw[u][2] = L.cym[j];
+            cw[u][3] = L.cyp[j];
+            cw[u][4] = L.czm[k];
+            cw[u][5] = L.czp[k];
+            c0v[u] = diag_f64(L, i, j, k);
+            ic0[u] = __ddiv_rn(1.0, c0v[u]);
+            bv[u] = b[cidx[u]];
+        }
+        const long long sy = L.sy, sz = L.sz;
+        auto nbsum = [&](int u) {
+            const long long c = cidx[u];
+            double t = __dmul_rn(cw[u][0], x[c - 1]);
+            t = __dadd_rn(t, __dmul_rn(cw[u][1], x[c + 1]));
+            t = __dadd_rn(t, __dmul_rn(cw[u][2], x[c - sy]));
+            t = __dadd_rn(t, __dmul_rn(cw[u][3], x[c + sy]));
+            t = __dadd_rn(t, __dmul_rn(cw[u][4], x[c - sz]));
+            return __dadd_rn(t, __dmul_rn(cw[u][5], x[c + sz]));
+        };
+        auto norm = [&]() {
+            double acc = 0.0;
+#pragma unroll
+            for (int u = 0; u < 2; ++u)
+                if (has[u]) {
+                    const double r = __dsub_rn(bv[u], __dadd_rn(__dmul_rn(c0v[u], x[cidx[u]]), nbsum(u)));
+                    acc = __dadd_rn(acc, __dmul_rn(r, r));
+                }
+            return warp_sum_f64(acc);
+        };
+        const double r0 = norm();
+        for (it = 0; it < maxit; ++it) {
+#pragma unroll
+            for (int colour = 0; colour < 2; ++colour) {
+                // first colour: (i + j + k) odd (src/rbgs_poisson_matrix.f90:242)
+#pragma unroll
+                for (int u = 0; u < 2; ++u)
+                    if (has[u] && odd[u] == (colour == 0)) {
+                        const double t = nbsum(u);
+                        x[cidx[u]] = __dadd_rn(__dmul_rn(__dmul_rn(omega, __dsub_rn(bv[u], t)), ic0[u]),
+                                               __dmul_rn(omw, x[cidx[u]]));
+                    }
+                __syncwarp();
+            }
+            const double rn = norm();
+            if (sqrt(__ddiv_rn(rn, r0)) <= tol) break;
+        }
+    } else if (solver == 0) {
+        const int hx = (nx + 1) / 2, nq = hx * ny * L.nz;
+        const double r0 = residual(true);
+        for (it = 0; it < maxit; ++it) {
+            for (int colour = 0; colour < 2; ++colour) {
+                for (int q = lane; q < nq; q += 32) {
+                    const int t = q % hx, r2 = q / hx, j = r2 % ny + 1, k = r2 / ny + 1;
+                    const int i = 2 * t + 1 + ((j + k + colour) & 1);
+                    if (i <= nx) x[lin(i, j, k, L.sy, L.sz)] = rbgs_cell_f64(L, x, b, i, j, k, omega, omw);
+                }
+                __syncwarp();
+            }
+            const double rn = residual(true);
+            if (sqrt(__ddiv_rn(rn, r0)) <= tol) break;
+        }
+    } else {
+        residual(false);
+        interior(0, 0.0, p, nullptr, rr, nullptr);
+        const double r0 = dot(rr, rr);
+        for (it = 0; it < maxit; ++it) {
+            const double t1 = dot(rr, rr);
+            for (int q = lane; q < n; q += 32) {
+                const int i = q % nx + 1, r2 = q / nx, j = r2 % ny + 1, k = r2 / ny + 1;
+                ap[lin(i, j, k, L.sy, L.sz)] = ax_cell_f64(L, p, i, j, k);
+            }
+            __syncwarp();
+            const double alpha = __ddiv_rn(t1, dot(ap, p));
+            interior(1, alpha, x, rr, p, ap);
+            const double t2 = dot(rr, rr);
+            if (sqrt(__ddiv_rn(t2, r0)) < tol) break;
+            interior(2, __ddiv_rn(t2, t1), p, nullptr, rr, nullptr);
+        }
+    }
+    return it;
+}
+
 }  // namespace
 }  // namespace pmg
