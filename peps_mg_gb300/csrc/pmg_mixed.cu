@@ -276,6 +276,28 @@ __global__ void __launch_bounds__(kBX *kBY) k_resrestrict_march32(LevelK<float> 
 // as the FP32 right-hand side of the inner system, with the per-block sum of r^2.
 // Each thread handles four cells of a row, 32 apart.
 constexpr int kOuterVec = 4;
+// True for the whole warp when x is exactly +0 (all bits clear) at every cell a lane of
+// the warp handles in row (j, k) and at their six neighbours.
+__device__ __noinline__ bool x_zero_around(const LevelK<double> &L, const double *__restrict__ x, int i0, int j,
+                                           int k)
+{
+    unsigned long long bits = 0ull;
+#pragma unroll
+    for (int u = 0; u < kOuterVec; ++u) {
+        const int i = i0 + u * kBX;
+        if (i > L.nx) break;
+        const long long p = lin(i, j, k, L.sy, L.sz);
+        bits |= (unsigned long long)(__double_as_longlong(x[p]) | __double_as_longlong(x[p - 1]) |
+                                     __double_as_longlong(x[p + 1]) | __double_as_longlong(x[p - L.sy]) |
+                                     __double_as_longlong(x[p + L.sy]) | __double_as_longlong(x[p - L.sz]) |
+                                     __double_as_longlong(x[p + L.sz]));
+    }
+    return __all_sync(__activemask(), bits == 0ull);
+}
+
+// ZS: test for an x that is exactly zero around the cell (the initial residual of a
+// solve, which usually starts from x = 0) and skip the FP64 chain there.
+template <bool ZS>
 __global__ void __launch_bounds__(kBX *kBY) k_outer_residual(LevelK<double> L, const double *__restrict__ dyy,
                                                              const double *__restrict__ dzz,
                                                              const double *__restrict__ x,
@@ -290,6 +312,21 @@ __global__ void __launch_bounds__(kBX *kBY) k_outer_residual(LevelK<double> L, c
             const double dyz = dyy[j] + dz;
             for (int i0 = blockIdx.x * (blockDim.x * kOuterVec) + threadIdx.x + 1; i0 <= L.nx;
                  i0 += gridDim.x * blockDim.x * kOuterVec) {
+                if (ZS && x_zero_around(L, x, i0, j, k)) {
+                    // x is exactly +0 at these cells and their neighbours: every product of
+                    // the FMA chain is a signed zero and the chain returns b + 0
+#pragma unroll
+                    for (int u = 0; u < kOuterVec; ++u) {
+                        const int i = i0 + u * kBX;
+                        if (i > L.nx) break;
+                        const long long p = lin(i, j, k, L.sy, L.sz);
+                        const double v = __dadd_rn(b[p], 0.0);
+                        r[p] = v;
+                        r32[lin(i, j, k, sy32, sz32)] = f64_to_f32_rn(v);
+                        acc = fma(v, v, acc);
+                    }
+                    continue;
+                }
 #pragma unroll
                 for (int u = 0; u < kOuterVec; ++u) {
                     const int i = i0 + u * kBX;
@@ -668,8 +705,13 @@ int Ctx::outer_residual(double *sol, double *rsd, const double *rhs, int slot)
     const LevelK<double> &L = K[0];
     const dim3 g = grid3m((L.nx + kOuterVec - 1) / kOuterVec, L.ny, L.nz, launch[0]), bl(kBX, kBY, 1);
     const int pi = prof.begin(stream);
-    k_outer_residual<<<g, bl, 0, stream>>>(L, mixed->dyy[0], mixed->dzz[0], sol, rhs, rsd, mixed->b[0],
-                                           mixed->K[0].sy, mixed->K[0].sz, d_partials);
+    // the first residual of a solve (slot 0) checks for a zero initial guess
+    if (slot == 0)
+        k_outer_residual<true><<<g, bl, 0, stream>>>(L, mixed->dyy[0], mixed->dzz[0], sol, rhs, rsd, mixed->b[0],
+                                                     mixed->K[0].sy, mixed->K[0].sz, d_partials);
+    else
+        k_outer_residual<false><<<g, bl, 0, stream>>>(L, mixed->dyy[0], mixed->dzz[0], sol, rhs, rsd, mixed->b[0],
+                                                      mixed->K[0].sy, mixed->K[0].sz, d_partials);
     prof.end(pi, PC_OUTER_RES, 1, 28.0 * (double)L.nx * L.ny * L.nz, stream);
     count_launches(1);
     PMG_TRY_M(cuda_status(cudaGetLastError(), "outer residual"));
