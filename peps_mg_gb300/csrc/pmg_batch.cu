@@ -26,6 +26,7 @@
 #include "pmg_ctx.h"
 #include "pmg_mixed.h"
 #include "pmg_smooth32.cuh"
+#include "pmg_smooth32_tma.cuh"
 
 #define PMG_TRY_B(expr)                \
     do {                               \
@@ -80,6 +81,52 @@ __global__ void __launch_bounds__(rb_threads<TY>()) k_batch_rb32(const BLevel *_
         const int k1 = min(L.nz, w.k0 + D.kchunk - 1);
         rb32_item<TY, ZERO_IN, OMEGA1>(S, L, D.e[which], D.e[1 - which], D.b, omega, omw, w.bx, w.by, w.k0, k1);
     }
+}
+
+// ---- TMA-fed smoother over a (problem, tile) list ------------------------------------------
+// Item source of the TMA-fed smoother for one depth: the CTA's items of unconverged
+// problems in list order, each item's planes from its problem's k-chunk and the tensor
+// maps of its problem (buffer `which` of e as input, tile variant vi).
+struct BatchTmaSrc {
+    const BLevel *lv;
+    const Rb32Tma *maps;
+    const Item *items;
+    const int *done;
+    int nitems, which, vi;
+    __device__ __forceinline__ int skip(int it) const
+    {
+        while (it < nitems && done[items[it].p]) it += gridDim.x;
+        return it;
+    }
+    __device__ __forceinline__ int first() const { return skip(blockIdx.x); }
+    __device__ __forceinline__ int next(int it) const { return skip(it + gridDim.x); }
+    __device__ __forceinline__ bool valid(int it) const { return it < nitems; }
+    __device__ __forceinline__ void geom(int it, int &bx, int &by, int &k0, int &k1) const
+    {
+        const Item w = items[it];
+        bx = w.bx;
+        by = w.by;
+        k0 = w.k0;
+        k1 = min(lv[w.p].L.nz, w.k0 + lv[w.p].kchunk - 1);
+    }
+    __device__ __forceinline__ const CUtensorMap *map_e(int it) const { return &maps[items[it].p].e[which][vi]; }
+    __device__ __forceinline__ const CUtensorMap *map_b(int it) const { return &maps[items[it].p].b[vi]; }
+};
+
+template <int TY, bool ZERO_IN, bool OMEGA1>
+__global__ void __launch_bounds__(RbtShape<TY>::THREADS, rbt_min_ctas<TY>())
+    k_batch_rb32_tma(const BLevel *__restrict__ lv, const Rb32Tma *__restrict__ maps, const Item *__restrict__ items,
+                     int nitems, int which, int vi, float omega, float omw, const int *__restrict__ done, int *err)
+{
+    const BatchTmaSrc src{lv, maps, items, done, nitems, which, vi};
+    rbt_cta<TY, ZERO_IN, OMEGA1>(
+        src,
+        [&](int it, const LevelK<float> *&L, float *&eo) {
+            const BLevel &D = lv[items[it].p];
+            L = &D.L;
+            eo = D.e[1 - which];
+        },
+        omega, omw, err);
 }
 
 // ---- residual + restriction into depth d+1: one item per coarse plane ---------------------
@@ -233,8 +280,11 @@ struct Batch {
     double *rsd = nullptr;                  // packed FP64 residual
     const TailDesc<float> **d_tails = nullptr;
     int tail_threads = 64;
-    std::vector<int> variant;               // chosen smoother variant per depth
-    int slots[3] = {0, 0, 0};
+    std::vector<int> variant;               // chosen smoother variant per depth (3..5: TMA-fed)
+    int slots[6] = {0, 0, 0, 0, 0, 0};
+    Rb32Tma *d_maps = nullptr;              // [(dmax+1) * n] tensor maps of every depth and problem
+    std::vector<bool> tma_ok;               // per depth: every problem with that depth has maps
+    int *d_err = nullptr;                   // set by a TMA-fed launch whose bounded wait gave up
     cudaGraphExec_t graph = nullptr;
     int graph_maxit = -1;
     double graph_omega = 0.0, graph_tol = 0.0;
@@ -260,6 +310,8 @@ Batch::~Batch()
     cudaFree(d_ndone);
     cudaFree(rsd);
     cudaFree(d_tails);
+    cudaFree(d_maps);
+    cudaFree(d_err);
 }
 
 }  // namespace pmg
@@ -306,6 +358,58 @@ int setup_variant(int *slots)
     return PMG_OK;
 }
 
+template <int TY, bool Z, bool O>
+int tma_batch_attr()
+{
+    int rc = cuda_status(cudaFuncSetAttribute(k_batch_rb32_tma<TY, Z, O>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                              RbtShape<TY>::SMEM),
+                         "batch TMA smoother shared memory");
+    if (rc != PMG_OK) return rc;
+    return cuda_status(cudaFuncSetAttribute(k_batch_rb32_tma<TY, Z, O>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                            100),
+                       "batch TMA smoother carveout");
+}
+
+template <int TY>
+int setup_tma_variant(int *slots)
+{
+    PMG_TRY_B((tma_batch_attr<TY, false, false>()));
+    PMG_TRY_B((tma_batch_attr<TY, false, true>()));
+    PMG_TRY_B((tma_batch_attr<TY, true, false>()));
+    PMG_TRY_B((tma_batch_attr<TY, true, true>()));
+    int per = 0, dev = 0, sms = 0;
+    PMG_TRY_B(cuda_status(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_batch_rb32_tma<TY, false, false>,
+                                                                        RbtShape<TY>::THREADS, RbtShape<TY>::SMEM),
+                          "batch TMA smoother occupancy"));
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    *slots = std::max(1, per) * std::max(1, sms);
+    return PMG_OK;
+}
+
+template <int TY>
+void launch_batch_tma(const Batch &B, int d, const Batch::List &Ls, int slots, int vi, int which, float om, float omw,
+                      bool zs)
+{
+    const int grid = std::max(1, std::min(Ls.n, slots));
+    const BLevel *lv = B.d_lv + (size_t)d * B.n;
+    const Rb32Tma *mp = B.d_maps + (size_t)d * B.n;
+    const bool one = om == 1.f;
+    constexpr int nt = RbtShape<TY>::THREADS, sm = RbtShape<TY>::SMEM;
+    if (zs && one)
+        k_batch_rb32_tma<TY, true, true><<<grid, nt, sm, B.stream>>>(lv, mp, Ls.d, Ls.n, which, vi, om, omw, B.d_done,
+                                                                    B.d_err);
+    else if (zs)
+        k_batch_rb32_tma<TY, true, false><<<grid, nt, sm, B.stream>>>(lv, mp, Ls.d, Ls.n, which, vi, om, omw,
+                                                                     B.d_done, B.d_err);
+    else if (one)
+        k_batch_rb32_tma<TY, false, true><<<grid, nt, sm, B.stream>>>(lv, mp, Ls.d, Ls.n, which, vi, om, omw,
+                                                                     B.d_done, B.d_err);
+    else
+        k_batch_rb32_tma<TY, false, false><<<grid, nt, sm, B.stream>>>(lv, mp, Ls.d, Ls.n, which, vi, om, omw,
+                                                                      B.d_done, B.d_err);
+}
+
 template <int TY>
 void launch_batch_rb(const Batch &B, int d, const Batch::List &Ls, int slots, int which, float om, float omw, bool zs)
 {
@@ -323,10 +427,22 @@ void launch_batch_rb(const Batch &B, int d, const Batch::List &Ls, int slots, in
         k_batch_rb32<TY, false, false><<<grid, nt, 0, B.stream>>>(lv, Ls.d, Ls.n, which, om, omw, B.d_done);
 }
 
+// v = 0, 1, 2: register-window kernel with 60 x 14 / 6 / 10 tiles; 3, 4, 5: TMA-fed kernel
+// with the same tiles (and the same work lists).
 void launch_rb(const Batch &B, int v, int d, int which, float om, float omw, bool zs)
 {
-    const Batch::List &Ls = B.smooth[v][d];
+    const Batch::List &Ls = B.smooth[v % 3][d];
     if (!Ls.n) return;
+    if (v >= 3) {
+        if (v == 3)
+            launch_batch_tma<14>(B, d, Ls, B.slots[3], 0, which, om, omw, zs);
+        else if (v == 4)
+            launch_batch_tma<6>(B, d, Ls, B.slots[4], 1, which, om, omw, zs);
+        else
+            launch_batch_tma<10>(B, d, Ls, B.slots[5], 2, which, om, omw, zs);
+        count_launches(1);
+        return;
+    }
     if (v == 0)
         launch_batch_rb<14>(B, d, Ls, B.slots[0], which, om, omw, zs);
     else if (v == 1)
@@ -441,6 +557,21 @@ int batch_create(Batch **out, int n, const int *dims, const double *const *meshe
         }
     }
     PMG_TRY_B(upload(lv, &B->d_lv));
+    // tensor maps of the TMA-fed smoother (encoded by each problem's setup)
+    {
+        std::vector<Rb32Tma> maps((size_t)(D + 1) * n);
+        B->tma_ok.assign((size_t)D + 1, true);
+        for (int p = 0; p < n; ++p) {
+            MixedState *m = B->probs[p]->mixed;
+            for (int d = 0; d <= B->probs[p]->nl; ++d) {
+                maps[(size_t)d * n + p] = m->tma[d];
+                if (d < B->probs[p]->nl && !m->tma[d].ok) B->tma_ok[d] = false;
+            }
+        }
+        PMG_TRY_B(upload(maps, &B->d_maps));
+        PMG_TRY_B(cuda_status(cudaMalloc(&B->d_err, sizeof(int)), "batch allocation"));
+        PMG_TRY_B(cuda_status(cudaMemset(B->d_err, 0, sizeof(int)), "batch init"));
+    }
     // work lists
     for (int v = 0; v < 3; ++v) {
         B->smooth[v].resize((size_t)D);
@@ -498,6 +629,9 @@ int batch_create(Batch **out, int n, const int *dims, const double *const *meshe
     PMG_TRY_B(setup_variant<14>(&B->slots[0]));
     PMG_TRY_B(setup_variant<6>(&B->slots[1]));
     PMG_TRY_B(setup_variant<10>(&B->slots[2]));
+    PMG_TRY_B(setup_tma_variant<14>(&B->slots[3]));
+    PMG_TRY_B(setup_tma_variant<6>(&B->slots[4]));
+    PMG_TRY_B(setup_tma_variant<10>(&B->slots[5]));
     B->variant.assign((size_t)D, -1);
     B->h_outer.resize((size_t)n);
     *out = B.release();
@@ -513,8 +647,8 @@ static int batch_autotune(Batch &B)
     for (int d = 0; d < B.dmax; ++d) {
         float best = 1e30f;
         int bv = 0;
-        for (int v = 0; v < 3; ++v) {
-            if (!B.smooth[v][d].n) continue;
+        for (int v = 0; v < 6; ++v) {
+            if (!B.smooth[v % 3][d].n || (v >= 3 && !B.tma_ok[d])) continue;
             launch_rb(B, v, d, 0, 1.f, 0.f, false);
             cudaEventRecord(a, B.stream);
             for (int r = 0; r < 3; ++r) launch_rb(B, v, d, 0, 1.f, 0.f, false);
@@ -652,6 +786,13 @@ int batch_solve(Batch &B, double *sol, const double *rhs, int maxit, double tol,
     cudaEventDestroy(e1);
     if (cycles) PMG_TRY_B(cuda_status(cudaMemcpy(cycles, B.d_cycles, n * sizeof(int), cudaMemcpyDeviceToHost), "copy"));
     if (ratio) PMG_TRY_B(cuda_status(cudaMemcpy(ratio, B.d_ratio, n * sizeof(double), cudaMemcpyDeviceToHost), "copy"));
+    int err = 0;
+    PMG_TRY_B(cuda_status(cudaMemcpy(&err, B.d_err, sizeof(int), cudaMemcpyDeviceToHost), "batch error flag"));
+    if (err) {
+        cudaMemset(B.d_err, 0, sizeof(int));
+        set_error("batched smoother: a wait for a TMA copy timed out");
+        return PMG_ETIMEOUT;
+    }
     return PMG_OK;
 }
 

@@ -57,46 +57,21 @@ __global__ void __launch_bounds__(rb_threads<TY>(), rb_min_blocks<TY>()) k_rb32_
 
 // blocks per SM the TMA-fed kernel's register budget is sized for
 template <int TY>
-constexpr int rbt_min_blocks() { return TY <= 6 ? 5 : 3; }
+constexpr int rbt_min_blocks() { return rbt_min_ctas<TY>(); }
 
 template <int TY, bool ZERO_IN, bool OMEGA1>
 __global__ void __launch_bounds__(RbtShape<TY>::THREADS, rbt_min_blocks<TY>())
     k_rb32_tma(const __grid_constant__ CUtensorMap me, const __grid_constant__ CUtensorMap mb, LevelK<float> L,
                float *__restrict__ eout, float omega, float omw, RbtItems W, int *err)
 {
-    using S = RbtShape<TY>;
-    extern __shared__ unsigned char smem_raw[];
-    // 128-byte aligned stages (TMA destinations), then the mbarriers
-    unsigned char *smem = smem_raw + ((128u - (rbtdetail::smem_addr(smem_raw) & 127u)) & 127u);
-    unsigned long long *bars = reinterpret_cast<unsigned long long *>(smem + RBT_NS * S::STAGE);
-    volatile int *abort_flag = reinterpret_cast<volatile int *>(bars + RBT_NS);
-    RbtProducer<TY, ZERO_IN> *prod = reinterpret_cast<RbtProducer<TY, ZERO_IN> *>(bars + RBT_NS + 2);
-    if (threadIdx.x == 0) {
-        for (int q = 0; q < RBT_NS; ++q) rbtdetail::mbar_init(&bars[q], 1);
-        *abort_flag = 0;
-        rbtdetail::fence_mbar_init();
-    }
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        prod->start(W);
-        prod->issue_upto(RBT_NS - 1, W, smem, bars, &me, &mb);
-    }
-    int cbase = 0;
-    for (int it = blockIdx.x; it < W.nitems; it += gridDim.x) {
-        int bx, by, k0, k1;
-        W.decode(it, bx, by, k0, k1);
-        if (!rbt_item<TY, ZERO_IN, OMEGA1>(smem, bars, abort_flag, L, eout, omega, omw, bx, by, k0, k1, cbase, prod,
-                                            W, &me, &mb)) {
-            if (threadIdx.x == 0) {
-                atomicOr(err, 1);
-                // let the copies still in flight land before the CTA exits (bounded)
-                for (int q = max(0, prod->slot - RBT_NS); q < prod->slot; ++q)
-                    rbtdetail::mbar_wait_bounded(&bars[q % RBT_NS], (unsigned)(q / RBT_NS) & 1u);
-            }
-            return;
-        }
-        cbase += k1 - k0 + 5;
-    }
+    const RbtGridSrc src{&W, &me, &mb};
+    rbt_cta<TY, ZERO_IN, OMEGA1>(
+        src,
+        [&](int, const LevelK<float> *&Li, float *&eo) {
+            Li = &L;
+            eo = eout;
+        },
+        omega, omw, err);
 }
 
 template <int TY>

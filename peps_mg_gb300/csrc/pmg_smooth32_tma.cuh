@@ -53,6 +53,10 @@ struct RbtShape {
 template <int TY>
 __host__ __device__ constexpr int S_EB() { return RbtShape<TY>::EBYTES; }
 
+// CTAs per SM the TMA-fed kernels' register budget is sized for
+template <int TY>
+constexpr int rbt_min_ctas() { return TY <= 6 ? 5 : 3; }
+
 namespace rbtdetail {
 
 __device__ __forceinline__ unsigned smem_addr(const void *p)
@@ -142,7 +146,7 @@ __device__ __forceinline__ void sq(float2 &v, float x)
 
 }  // namespace rbtdetail
 
-// Work item geometry: item it -> tile (bx, by) and planes k0..k1.
+// Work item geometry of one level: item it -> tile (bx, by) and planes k0..k1.
 struct RbtItems {
     int ntx, nty, kchunk, nz, nitems;
     __device__ __forceinline__ void decode(int it, int &bx, int &by, int &k0, int &k1) const
@@ -156,29 +160,52 @@ struct RbtItems {
     }
 };
 
+// A source of work items for the TMA-fed smoother: the CTA's items in order (first /
+// next / valid), each item's tile and planes (geom) and the tensor maps of its e_in and b
+// (map_e / map_b).  RbtGridSrc serves one level; the batched solver has its own source
+// over (problem, tile) lists.
+struct RbtGridSrc {
+    const RbtItems *W;            // the kernel parameter (read from the constant bank)
+    const CUtensorMap *me, *mb;
+    __device__ __forceinline__ int first() const { return blockIdx.x; }
+    __device__ __forceinline__ int next(int it) const { return it + gridDim.x; }
+    __device__ __forceinline__ bool valid(int it) const { return it < W->nitems; }
+    __device__ __forceinline__ void geom(int it, int &bx, int &by, int &k0, int &k1) const
+    {
+        W->decode(it, bx, by, k0, k1);
+    }
+    __device__ __forceinline__ const CUtensorMap *map_e(int) const { return me; }
+    __device__ __forceinline__ const CUtensorMap *map_b(int) const { return mb; }
+};
+
 // The producer: one thread issuing the planes of the CTA's items, slot after slot.  Its
 // state lives in shared memory (only thread 0 touches it), so it costs the other
 // threads no registers.
-template <int TY, bool ZERO_IN>
+template <int TY, bool ZERO_IN, class Src>
 struct RbtProducer {
     int it, q, k0, k1, bx, by;   // item being issued and its next plane q
     int slot;                    // next slot to issue
-    __device__ __forceinline__ void start(const RbtItems &W)
+    const CUtensorMap *me, *mb;  // tensor maps of the item being issued
+    __device__ __forceinline__ void load_item(const Src &src)
     {
-        it = blockIdx.x;
-        slot = 0;
-        if (it < W.nitems) {
-            W.decode(it, bx, by, k0, k1);
+        if (src.valid(it)) {
+            src.geom(it, bx, by, k0, k1);
             q = k0 - 2;
+            me = src.map_e(it);
+            mb = src.map_b(it);
         }
     }
+    __device__ __forceinline__ void start(const Src &src)
+    {
+        it = src.first();
+        slot = 0;
+        load_item(src);
+    }
     // issue every slot up to and including `limit`
-    __device__ __forceinline__ void issue_upto(int limit, const RbtItems &W, unsigned char *smem,
-                                               unsigned long long *bars, const CUtensorMap *me,
-                                               const CUtensorMap *mb)
+    __device__ __forceinline__ void issue_upto(int limit, const Src &src, unsigned char *smem, unsigned long long *bars)
     {
         using S = RbtShape<TY>;
-        while (slot <= limit && it < W.nitems) {
+        while (slot <= limit && src.valid(it)) {
             const int s = slot % RBT_NS;
             unsigned char *st = smem + s * S::STAGE;
             const bool with_b = q >= k0 - 1 && q <= k1 + 1;
@@ -193,11 +220,8 @@ struct RbtProducer {
             }
             ++slot;
             if (++q > k1 + 2) {
-                it += gridDim.x;
-                if (it < W.nitems) {
-                    W.decode(it, bx, by, k0, k1);
-                    q = k0 - 2;
-                }
+                it = src.next(it);
+                load_item(src);
             }
         }
     }
@@ -264,9 +288,8 @@ struct RbtItem {
     // cell on plane t (row b's is 1 - Q; on plane t-1 the second-colour cells are at the
     // same indices).  CHECKED steps test at run time whether plane t is a grid plane
     // and whether plane t-1 belongs to the item; the steps k0 < t <= k1 need neither.
-    template <int P, int Q, bool CHECKED>
-    __device__ __forceinline__ void step(int t, float (&cz)[6], RbtProducer<TY, ZERO_IN> *prod, const RbtItems &W,
-                                         const CUtensorMap *me, const CUtensorMap *mb)
+    template <int P, int Q, bool CHECKED, class Src>
+    __device__ __forceinline__ void step(int t, float (&cz)[6], RbtProducer<TY, ZERO_IN, Src> *prod, const Src &src)
     {
         using namespace rbtdetail;
         constexpr int im2 = P % 4, im1 = (P + 1) % 4, i00 = (P + 2) % 4, ip1 = (P + 3) % 4;
@@ -330,7 +353,7 @@ struct RbtItem {
         }
         fence_proxy_async();
         __syncthreads();
-        if (threadIdx.x == 0) prod->issue_upto(cs - 2 + RBT_NS, W, smem, bars, me, mb);
+        if (threadIdx.x == 0) prod->issue_upto(cs - 2 + RBT_NS, src, smem, bars);
         if (!CHECKED || (t - 1 >= k0 && t - 1 <= k1)) {
             const float upA = __shfl_up_sync(0xffffffffu, EA[im1].y, 1);
             const float dnA = __shfl_down_sync(0xffffffffu, EA[im1].x, 1);
@@ -378,36 +401,35 @@ struct RbtItem {
 
     // Steps t = k0-1 .. k1+1: two checked steps, unchecked steps k0+1 .. k1 unrolled by
     // the four-plane register window, then the remaining steps checked.
-    template <int Q0>
-    __device__ __forceinline__ void run(RbtProducer<TY, ZERO_IN> *prod, const RbtItems &W, const CUtensorMap *me,
-                                        const CUtensorMap *mb)
+    template <int Q0, class Src>
+    __device__ __forceinline__ void run(RbtProducer<TY, ZERO_IN, Src> *prod, const Src &src)
     {
         float cz[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
         load_cz<true>(k0 - 1);
         int t = k0 - 1;
-        step<0, Q0, true>(t, cz, prod, W, me, mb);
-        step<1, 1 - Q0, true>(t + 1, cz, prod, W, me, mb);
+        step<0, Q0, true>(t, cz, prod, src);
+        step<1, 1 - Q0, true>(t + 1, cz, prod, src);
         t += 2;
         for (; t + 3 <= k1; t += 4) {
-            step<2, Q0, false>(t, cz, prod, W, me, mb);
-            step<3, 1 - Q0, false>(t + 1, cz, prod, W, me, mb);
-            step<0, Q0, false>(t + 2, cz, prod, W, me, mb);
-            step<1, 1 - Q0, false>(t + 3, cz, prod, W, me, mb);
+            step<2, Q0, false>(t, cz, prod, src);
+            step<3, 1 - Q0, false>(t + 1, cz, prod, src);
+            step<0, Q0, false>(t + 2, cz, prod, src);
+            step<1, 1 - Q0, false>(t + 3, cz, prod, src);
         }
-        if (t <= k1 + 1) step<2, Q0, true>(t++, cz, prod, W, me, mb);
-        if (t <= k1 + 1) step<3, 1 - Q0, true>(t++, cz, prod, W, me, mb);
-        if (t <= k1 + 1) step<0, Q0, true>(t++, cz, prod, W, me, mb);
-        if (t <= k1 + 1) step<1, 1 - Q0, true>(t++, cz, prod, W, me, mb);
+        if (t <= k1 + 1) step<2, Q0, true>(t++, cz, prod, src);
+        if (t <= k1 + 1) step<3, 1 - Q0, true>(t++, cz, prod, src);
+        if (t <= k1 + 1) step<0, Q0, true>(t++, cz, prod, src);
+        if (t <= k1 + 1) step<1, 1 - Q0, true>(t++, cz, prod, src);
     }
 };
 
 // One work item.  cbase = slot of plane k0 - 2.  Returns false (uniformly across the
 // CTA) when a wait gave up.
-template <int TY, bool ZERO_IN, bool OMEGA1>
+template <int TY, bool ZERO_IN, bool OMEGA1, class Src>
 __device__ __forceinline__ bool rbt_item(unsigned char *smem, unsigned long long *bars, volatile int *abort_flag,
                                          const LevelK<float> &L, float *__restrict__ eout, float omega, float omw,
-                                         int bx, int by, int k0, int k1, int cbase, RbtProducer<TY, ZERO_IN> *prod,
-                                         const RbtItems &W, const CUtensorMap *me, const CUtensorMap *mb)
+                                         int bx, int by, int k0, int k1, int cbase, RbtProducer<TY, ZERO_IN, Src> *prod,
+                                         const Src &src)
 {
     RbtItem<TY, ZERO_IN, OMEGA1> I;
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
@@ -479,10 +501,57 @@ __device__ __forceinline__ bool rbt_item(unsigned char *smem, unsigned long long
     // the pair's first cell a is odd, so on row a it carries the first colour on plane k
     // when ja + k is even ((i + j + k) odd, src/rbgs_poisson_matrix.f90:242)
     if (((ja + k0 - 1) & 1) == 0)
-        I.template run<0>(prod, W, me, mb);
+        I.template run<0>(prod, src);
     else
-        I.template run<1>(prod, W, me, mb);
+        I.template run<1>(prod, src);
     return !__syncthreads_or(I.fail);
+}
+
+// One CTA of a TMA-fed launch over the items of `src`: shared-memory ring and mbarriers,
+// the producer's first fills, then every item in order; per(it, L, eout) gives an item's
+// level descriptor (a pointer) and output array.  When a wait gave up, thread 0 sets *err, lets the
+// copies in flight land (bounded) and the CTA returns.
+template <int TY, bool ZERO_IN, bool OMEGA1, class Src, class Per>
+__device__ __forceinline__ void rbt_cta(const Src &src, Per per, float omega, float omw, int *err)
+{
+    using S = RbtShape<TY>;
+    extern __shared__ unsigned char rbt_smem_raw[];
+    // 128-byte aligned stages (TMA destinations), then the mbarriers, the abort flag and
+    // the producer state
+    unsigned char *smem = rbt_smem_raw + ((128u - (rbtdetail::smem_addr(rbt_smem_raw) & 127u)) & 127u);
+    unsigned long long *bars = reinterpret_cast<unsigned long long *>(smem + RBT_NS * S::STAGE);
+    volatile int *abort_flag = reinterpret_cast<volatile int *>(bars + RBT_NS);
+    using Prod = RbtProducer<TY, ZERO_IN, Src>;
+    static_assert(sizeof(Prod) <= 48, "producer state exceeds its shared-memory slot");
+    Prod *prod = reinterpret_cast<Prod *>(bars + RBT_NS + 2);
+    if (threadIdx.x == 0) {
+        for (int q = 0; q < RBT_NS; ++q) rbtdetail::mbar_init(&bars[q], 1);
+        *abort_flag = 0;
+        rbtdetail::fence_mbar_init();
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        prod->start(src);
+        prod->issue_upto(RBT_NS - 1, src, smem, bars);
+    }
+    int cbase = 0;
+    for (int it = src.first(); src.valid(it); it = src.next(it)) {
+        int bx, by, k0, k1;
+        src.geom(it, bx, by, k0, k1);
+        const LevelK<float> *L;
+        float *eout;
+        per(it, L, eout);
+        if (!rbt_item<TY, ZERO_IN, OMEGA1>(smem, bars, abort_flag, *L, eout, omega, omw, bx, by, k0, k1, cbase, prod,
+                                            src)) {
+            if (threadIdx.x == 0) {
+                atomicOr(err, 1);
+                for (int q = max(0, prod->slot - RBT_NS); q < prod->slot; ++q)
+                    rbtdetail::mbar_wait_bounded(&bars[q % RBT_NS], (unsigned)(q / RBT_NS) & 1u);
+            }
+            return;
+        }
+        cbase += k1 - k0 + 5;
+    }
 }
 
 }  // namespace pmg
