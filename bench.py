@@ -384,11 +384,13 @@ def run_batch(args):
             sol.zero_()
             cycles, ratio, _ = bs.solve(sol, rhs, MAXIT, TOL, OMEGA, max_cycles=100)
         times = []
+        torch.cuda.nvtx.range_push("timed")
         for _ in range(args.steps):
             sol.zero_()
             torch.cuda.synchronize()
             cycles, ratio, ms = bs.solve(sol, rhs, MAXIT, TOL, OMEGA, max_cycles=100)
             times.append(ms)
+        torch.cuda.nvtx.range_pop()
         assert np.all(ratio < TOL), "batched solve did not converge"
         cells = int(np.prod(dims, axis=1).sum())
         ms = statistics.mean(times)

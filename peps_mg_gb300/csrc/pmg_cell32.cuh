@@ -151,6 +151,145 @@ __device__ __forceinline__ void side_weights(int st, int f, const float *pp, con
     }
 }
 
+// e_f += P e_c on the fine x-pair (2 ic - 1, 2 ic) of fine row jf for the coarse planes
+// m0 .. m1 of a transfer that halves x and z: the coarse values of planes kc-1, kc, kc+1
+// (x-indices ic-1 .. ic+1, rows jc and jn) stay in registers, so each fine pair is read
+// and written once with 8-byte accesses and each coarse plane is loaded once; the
+// arithmetic per child is that of prolong_add_cell32.
+__device__ __forceinline__ void prolong_column_march32(const XferK<float> &X, int jf, int ic, int m0, int m1,
+                                                       const float *__restrict__ vc, float *__restrict__ vf)
+{
+    int jc, jn;
+    float ay, by;
+    side_weights(X.sty, jf, X.pyp, X.pyn, &jc, &jn, &ay, &by);
+    const int iz = 2 * ic - 1, ip = 2 * ic;
+    const float lo_a = X.pxp[iz], lo_b = X.pxp[ip], hi_a = X.pxn[ip], hi_b = X.pxn[iz];
+    const float *rc = vc + lin(ic, jc, 0, X.csy, X.csz), *rn = vc + lin(ic, jn, 0, X.csy, X.csz);
+    // [row jc: x-1, x, x+1, row jn: x-1, x, x+1] of coarse planes m-1 (A), m (B)
+    float A[6], B[6], C[6];
+    auto load = [&](float (&V)[6], int kc) {
+        const long long o = X.csz * kc;
+        V[0] = __ldg(rc + o - 1);
+        V[1] = __ldg(rc + o);
+        V[2] = __ldg(rc + o + 1);
+        V[3] = __ldg(rn + o - 1);
+        V[4] = __ldg(rn + o);
+        V[5] = __ldg(rn + o + 1);
+    };
+    load(A, m0 - 1);
+    load(B, m0);
+    float *pf = vf + lin(iz, jf, 0, X.fsy, X.fsz);
+    for (int m = m0; m <= m1; ++m) {
+        load(C, m + 1);
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            // h = 0: fine plane 2m-1 (neighbour plane m-1); h = 1: 2m (m+1)
+            const int kf = 2 * m - 1 + h;
+            const float az = h ? X.pzn[kf] : X.pzp[kf];
+            const float bz = h ? X.pzn[kf - 1] : X.pzp[kf + 1];
+            const float *Z = h ? C : A;
+            const float lo = prolong_child32(lo_a, lo_b, ay, by, az, bz, B[1], B[0], B[4], Z[1], B[3],
+                                             Z[0], Z[4], Z[3]);
+            const float hi = prolong_child32(hi_a, hi_b, ay, by, az, bz, B[1], B[2], B[4], Z[1], B[5],
+                                             Z[2], Z[4], Z[5]);
+            float2 *q = reinterpret_cast<float2 *>(pf + X.fsz * kf);
+            float2 v = *q;
+            v.x += lo;
+            v.y += hi;
+            *q = v;
+        }
+#pragma unroll
+        for (int u = 0; u < 6; ++u) {
+            A[u] = B[u];
+            B[u] = C[u];
+        }
+    }
+}
+
+// Fused residual + restriction on coarse column (ic, jc), coarse planes m0 .. m1, of a
+// transfer that halves every axis: each fine plane's 2 x 2 block of e (own pairs, 8-byte
+// loads) is held for planes k-1 .. k+1 in registers; x- and y-neighbours and b are loaded
+// per plane.  Residuals and the restriction sum are those of resrestrict_cell32 (same
+// operations, same order).
+__device__ __forceinline__ void resrestrict_column_march32(const LevelK<float> &F, const XferK<float> &X, int ic,
+                                                           int jc, int m0, int m1, const float *__restrict__ e,
+                                                           const float *__restrict__ b, float *__restrict__ bc)
+{
+    const int jz = 2 * jc - 1, jp = 2 * jc;
+    const int iz = 2 * ic - 1, ip = 2 * ic;
+    const float xz = X.wx[iz], xp = X.wx[ip], yz = X.wy[jz], yp = X.wy[jp];
+    const float cxm0 = F.cxm[iz], cxp0 = F.cxp[iz], sx0 = F.sx[iz];
+    const float cxm1 = F.cxm[ip], cxp1 = F.cxp[ip], sx1 = F.sx[ip];
+    const float cym0 = F.cym[jz], cyp0 = F.cyp[jz], dy0 = cym0 + cyp0;
+    const float cym1 = F.cym[jp], cyp1 = F.cyp[jp], dy1 = cym1 + cyp1;
+    const float *e0 = e + lin(iz, jz, 0, F.sy, F.sz);   // row jz; row jp at + sy
+    const float *b0 = b + lin(iz, jz, 0, F.sy, F.sz);
+    const long long sz = F.sz;
+    const int sy = F.sy;
+    auto own = [&](float2 (&V)[2], int k) {
+        V[0] = __ldg(reinterpret_cast<const float2 *>(e0 + sz * k));
+        V[1] = __ldg(reinterpret_cast<const float2 *>(e0 + sz * k + sy));
+    };
+    // residuals of fine plane k into r[0..3] = (iz,jz), (ip,jz), (iz,jp), (ip,jp)
+    auto resid_plane = [&](const float2 (&Em)[2], const float2 (&E0)[2], const float2 (&Ep)[2], int k,
+                           float (&r)[4]) {
+        const float *pe = e0 + sz * k;
+        const float czm = F.czm[k], czp = F.czp[k], dz = czm + czp;
+        const float xl0 = __ldg(pe - 1), xr0 = __ldg(pe + 2);
+        const float xl1 = __ldg(pe + sy - 1), xr1 = __ldg(pe + sy + 2);
+        const float2 yd = __ldg(reinterpret_cast<const float2 *>(pe - sy));
+        const float2 yu = __ldg(reinterpret_cast<const float2 *>(pe + 2 * sy));
+        const float2 b0v = __ldg(reinterpret_cast<const float2 *>(b0 + sz * k));
+        const float2 b1v = __ldg(reinterpret_cast<const float2 *>(b0 + sz * k + sy));
+        auto cell = [&](float cxm, float cxp, float sx, float cym, float cyp, float dy, float xm, float xp_,
+                        float ym, float yp_, float zm, float zp_, float x0, float bb) {
+            float t = cxm * xm;
+            t = fmaf(cxp, xp_, t);
+            t = fmaf(cym, ym, t);
+            t = fmaf(cyp, yp_, t);
+            t = fmaf(czm, zm, t);
+            t = fmaf(czp, zp_, t);
+            const float d = -((sx + dy) + dz);
+            return bb - fmaf(d, x0, t);
+        };
+        r[0] = cell(cxm0, cxp0, sx0, cym0, cyp0, dy0, xl0, E0[0].y, yd.x, E0[1].x, Em[0].x, Ep[0].x,
+                    E0[0].x, b0v.x);
+        r[1] = cell(cxm1, cxp1, sx1, cym0, cyp0, dy0, E0[0].x, xr0, yd.y, E0[1].y, Em[0].y, Ep[0].y,
+                    E0[0].y, b0v.y);
+        r[2] = cell(cxm0, cxp0, sx0, cym1, cyp1, dy1, xl1, E0[1].y, E0[0].x, yu.x, Em[1].x, Ep[1].x,
+                    E0[1].x, b1v.x);
+        r[3] = cell(cxm1, cxp1, sx1, cym1, cyp1, dy1, E0[1].x, xr1, E0[0].y, yu.y, Em[1].y, Ep[1].y,
+                    E0[1].y, b1v.y);
+    };
+    float2 Wm[2], W0[2], Wp[2], Wq[2];
+    own(Wm, 2 * m0 - 2);
+    own(W0, 2 * m0 - 1);
+    for (int m = m0; m <= m1; ++m) {
+        const int kz = 2 * m - 1, kp = 2 * m;
+        own(Wp, kp);
+        own(Wq, kp + 1);
+        float rz[4], rp[4];
+        resid_plane(Wm, W0, Wp, kz, rz);
+        resid_plane(W0, Wp, Wq, kp, rp);
+        const float zz = X.wz[kz], zp = X.wz[kp];
+        // children in the order of resrestrict_cell32: c = 0..7 with bit 0 ->
+        // x (iz), bit 1 -> y (jz), bit 2 -> z (kz); unset bits take the p child
+        float vol = 0.f, s = 0.f;
+#pragma unroll
+        for (int c = 0; c < 8; ++c) {
+            const float wv = ((c & 1) ? xp : xz) * ((c & 2) ? yp : yz) * ((c & 4) ? zp : zz);
+            const int q = ((c & 1) ? 0 : 1) + ((c & 2) ? 0 : 2);
+            vol += wv;
+            s = fmaf(wv, (c & 4) ? rz[q] : rp[q], s);
+        }
+        bc[lin(ic, jc, m, X.csy, X.csz)] = __fdividef(s, vol);
+        Wm[0] = Wp[0];
+        Wm[1] = Wp[1];
+        W0[0] = Wq[0];
+        W0[1] = Wq[1];
+    }
+}
+
 // Round-to-nearest-even double -> float, from the IEEE-754 encodings, on the integer
 // pipe (the FP64 pipe is the bottleneck of the outer kernels).  Results that are not
 // normal floats (zero, subnormal, overflow, NaN) use the hardware conversion.
