@@ -290,37 +290,58 @@ __device__ __forceinline__ void resrestrict_column_march32(const LevelK<float> &
     }
 }
 
-// Round-to-nearest-even double -> float, from the IEEE-754 encodings, on the integer
-// pipe (the FP64 pipe is the bottleneck of the outer kernels).  Results that are not
-// normal floats (zero, subnormal, overflow, NaN) use the hardware conversion.
+// Round-to-nearest-even double -> float from the IEEE-754 encodings, entirely on the
+// integer pipe (the FP64 pipe is the bottleneck of the outer kernels): normal results by
+// truncating the mantissa to 23 bits and rounding the 29 dropped bits to nearest even (a
+// carry may reach the exponent, up to infinity); results below the normal range by
+// shifting the full 53-bit mantissa into the float's subnormal unit 2^-149 with the same
+// rounding; overflow to infinity; NaN stays NaN (quiet, top payload bits kept).
 __device__ __forceinline__ float f64_to_f32_rn(double v)
 {
     const unsigned long long bits = (unsigned long long)__double_as_longlong(v);
-    const int e = (int)((bits >> 52) & 0x7ff) - 1023;
-    if (e < -126 || e > 127) return __double2float_rn(v);
+    const unsigned sign = (unsigned)(bits >> 32) & 0x80000000u;
+    const int ef = (int)((bits >> 52) & 0x7ff);
+    const int e = ef - 1023;
     const unsigned long long m = bits & 0xFFFFFFFFFFFFFull;
-    const unsigned hi = (unsigned)(m >> 29);
-    const unsigned long long rem = m & 0x1FFFFFFFull;
-    unsigned f = ((unsigned)(e + 127) << 23) | hi;
-    if (rem > 0x10000000ull || (rem == 0x10000000ull && (hi & 1u))) f += 1u;   // carry may reach the exponent
-    f |= (unsigned)(bits >> 32) & 0x80000000u;
-    return __uint_as_float(f);
+    if (e >= -126 && e <= 127) {
+        const unsigned hi = (unsigned)(m >> 29);
+        const unsigned long long rem = m & 0x1FFFFFFFull;
+        unsigned f = ((unsigned)(e + 127) << 23) | hi;
+        if (rem > 0x10000000ull || (rem == 0x10000000ull && (hi & 1u))) f += 1u;
+        return __uint_as_float(f | sign);
+    }
+    if (ef == 0x7ff) return __uint_as_float(sign | 0x7f800000u | (m ? (0x400000u | (unsigned)(m >> 29)) : 0u));
+    if (e > 127) return __uint_as_float(sign | 0x7f800000u);
+    // below the normal range: value = (2^52 + m) 2^(e-52) = q 2^-149 with q = (2^52 + m) 2^(e+97)
+    const int shift = -e - 97;                       // >= 30 here
+    if (ef == 0 || shift > 53) return __uint_as_float(sign);   // below half the smallest subnormal
+    const unsigned long long mf = m | (1ull << 52);
+    unsigned q = (unsigned)(mf >> shift);
+    const unsigned long long rem = mf & ((1ull << shift) - 1ull), half = 1ull << (shift - 1);
+    if (rem > half || (rem == half && (q & 1u))) q += 1u;     // may become the smallest normal
+    return __uint_as_float(sign | q);
 }
 
-// Exact float -> double from the encodings (integer pipe); subnormal, Inf and NaN
-// inputs use the hardware conversion.
+// Exact float -> double from the encodings, on the integer pipe: subnormal floats are
+// normalised (leading-zero count), Inf and NaN keep their payload.
 __device__ __forceinline__ double f32_to_f64(float f)
 {
     const unsigned u = __float_as_uint(f);
     const unsigned e = (u >> 23) & 0xffu;
+    const unsigned mant = u & 0x7fffffu;
     const unsigned long long sign = (unsigned long long)(u & 0x80000000u) << 32;
+    unsigned long long bits;
     if (e == 0u) {
-        if ((u & 0x7fffffu) == 0u) return __longlong_as_double((long long)sign);
-        return (double)f;
+        if (mant == 0u) return __longlong_as_double((long long)sign);
+        // value = mant 2^-149; shift the leading one to bit 23
+        const int s = __clz(mant) - 8;
+        bits = sign | ((unsigned long long)(1023 - 126 - s) << 52) |
+               ((unsigned long long)((mant << s) & 0x7fffffu) << 29);
+    } else if (e == 255u) {
+        bits = sign | (0x7ffull << 52) | ((unsigned long long)mant << 29);
+    } else {
+        bits = sign | ((unsigned long long)(e + 896u) << 52) | ((unsigned long long)mant << 29);
     }
-    if (e == 255u) return (double)f;
-    const unsigned long long bits = sign | ((unsigned long long)(e + 896u) << 52) |
-                                    ((unsigned long long)(u & 0x7fffffu) << 29);
     return __longlong_as_double((long long)bits);
 }
 
