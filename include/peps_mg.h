@@ -205,6 +205,7 @@ int pmg_vv_dot_static(const double *x, const double *y, int nx, int ny, int nz, 
 #define PMG_PROF_RESTRICT64 8     /* FP64 restriction                        */
 #define PMG_PROF_PROLONG64 9      /* FP64 prolongation + correction          */
 #define PMG_PROF_TAIL64 10        /* FP64 single-CTA coarse tail             */
+#define PMG_PROF_UPDATE_RESIDUAL 11 /* PMG_MIXED residual update r -= A e    */
 /* Enable (1) or disable (0) CUDA-event timing of the finest-level launches; resets
  * the accumulated figures. */
 int pmg_profile(pmg_ctx *ctx, int enable);

@@ -347,11 +347,11 @@ __device__ __forceinline__ double f32_to_f64(float f)
 
 // r(i,j,k) = b - A x in FP64, FMA form r = b + d x - sum c x_nb with d = -c0 = sx(i) + dyz
 // (the per-axis diagonal sums), as the outer residual of the mixed solver.
-__device__ __forceinline__ double outer_residual_cell(const LevelK<double> &L, double dyz, const double *x,
-                                                      const double *b, int i, int j, int k, long long p)
+__device__ __forceinline__ double outer_residual_cell_b(const LevelK<double> &L, double dyz, const double *x,
+                                                        double bp, int i, int j, int k, long long p)
 {
     const double d = L.sx[i] + dyz;
-    double v = fma(d, x[p], b[p]);
+    double v = fma(d, x[p], bp);
     v = fma(-L.cxm[i], x[p - 1], v);
     v = fma(-L.cxp[i], x[p + 1], v);
     v = fma(-L.cym[j], x[p - L.sy], v);
@@ -359,6 +359,48 @@ __device__ __forceinline__ double outer_residual_cell(const LevelK<double> &L, d
     v = fma(-L.czm[k], x[p - L.sz], v);
     v = fma(-L.czp[k], x[p + L.sz], v);
     return v;
+}
+
+// ---------------------------------------------------------------------------------------
+// Compensated FP32 arithmetic for the residual update r_new = r - A e of the mixed solver
+// (e is the FP32 correction, r the FP64 residual).  A e is formed in the difference form
+// sum over the six neighbours of c_n (e_n - e_c) (c0 = -(c1 + ... + c6) per the reference's
+// matrix, src/matrix.f90:67-92), so no term carries the large diagonal product:
+//  * e_n - e_c exactly as an unevaluated FP32 pair by Knuth's two-sum;
+//  * c_n = hi + lo (the FP64 coefficient split into two FP32 values, 48 bits);
+//  * c_hi * d exactly as a pair by the FMA two-product; the small cross terms by FMAs;
+//  * the six products summed with two-sum into (S, Sl).
+// Every rounding error is of order 2^-48 of a term, so A e carries a relative error of
+// about 2^-48 times sum |c_n (e_n - e_c)| / |A e| -- far below the FP64 rounding noise of a
+// recomputed b - A x, with 4 instead of 10 FP64 operations per cell.  All operations use
+// the _rn intrinsics, which the compiler never contracts.
+// ---------------------------------------------------------------------------------------
+__device__ __forceinline__ void two_sum32(float a, float b, float &s, float &err)
+{
+    s = __fadd_rn(a, b);
+    const float bb = __fsub_rn(s, a);
+    err = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+}
+
+// (S, Sl) += c * (en - ec), c = (hi, lo)
+__device__ __forceinline__ void comp_term(float2 c, float en, float ec, float &S, float &Sl)
+{
+    float d, dl;
+    two_sum32(en, -ec, d, dl);
+    const float p = __fmul_rn(c.x, d);
+    float pe = __fmaf_rn(c.x, d, -p);
+    pe = __fmaf_rn(c.x, dl, pe);
+    pe = __fmaf_rn(c.y, d, pe);
+    float s, t;
+    two_sum32(S, p, s, t);
+    S = s;
+    Sl = __fadd_rn(Sl, __fadd_rn(t, pe));
+}
+
+__device__ __forceinline__ double outer_residual_cell(const LevelK<double> &L, double dyz, const double *x,
+                                                      const double *b, int i, int j, int k, long long p)
+{
+    return outer_residual_cell_b(L, dyz, x, b[p], i, j, k, p);
 }
 
 template <typename F>

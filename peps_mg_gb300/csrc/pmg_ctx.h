@@ -106,6 +106,8 @@ struct Ctx {
     int upload_tail32(int maxit, double omega, double tol);
     int vcycle32(int maxit, double omega, bool zero_start);
     int outer_residual(double *sol, double *rsd, const double *rhs, int slot);
+    int update_residual(double *sol, double *rsd, int slot);
+    int correct_and_recompute(double *sol, double *rsd, const double *rhs);
     int check_pipeline();
     int resrestrict32(int l);
     int selftest_smooth32(int level, int impl, int variant, int kchunk, bool zero_in, double omega,

@@ -129,7 +129,8 @@ enum ProfClass {
     PC_RESTRICT64 = 8,   // FP64 restriction                         9 B/cell
     PC_PROLONG64 = 9,    // FP64 prolongation + correction          17 B/cell
     PC_TAIL64 = 10,      // FP64 single-CTA coarse tail
-    PC_COUNT = 11
+    PC_UPDATE_RES = 11,  // x += e, r -= A e, FP32 copy, norm       40 B/cell
+    PC_COUNT = 12
 };
 // Number of kernels this library has launched (all contexts).
 void count_launches(long long n);

@@ -152,7 +152,7 @@ __global__ void __launch_bounds__(kBX *kBY) k_resrestrict_march32(LevelK<float> 
 constexpr int kOuterVec = 4;
 // True for the whole warp when x is exactly +0 (all bits clear) at every cell a lane of
 // the warp handles in row (j, k) and at their six neighbours.
-__device__ __noinline__ bool x_zero_around(const LevelK<double> &L, const double *__restrict__ x, int i0, int j,
+__device__ __forceinline__ bool x_zero_around(const LevelK<double> &L, const double *__restrict__ x, int i0, int j,
                                            int k)
 {
     unsigned long long bits = 0ull;
@@ -186,30 +186,51 @@ __global__ void __launch_bounds__(kBX *kBY) k_outer_residual(LevelK<double> L, c
             const double dyz = dyy[j] + dz;
             for (int i0 = blockIdx.x * (blockDim.x * kOuterVec) + threadIdx.x + 1; i0 <= L.nx;
                  i0 += gridDim.x * blockDim.x * kOuterVec) {
-                if (ZS && x_zero_around(L, x, i0, j, k)) {
-                    // x is exactly +0 at these cells and their neighbours: every product of
-                    // the FMA chain is a signed zero and the chain returns b + 0
+                if constexpr (ZS) {
+                    // b is loaded together with x, so the zero test costs no second round
+                    // trip to memory
+                    double bv[kOuterVec];
+#pragma unroll
+                    for (int u = 0; u < kOuterVec; ++u) {
+                        const int i = i0 + u * kBX;
+                        bv[u] = i <= L.nx ? b[lin(i, j, k, L.sy, L.sz)] : 0.0;
+                    }
+                    if (x_zero_around(L, x, i0, j, k)) {
+                        // x is exactly +0 at these cells and their neighbours: every product
+                        // of the FMA chain is a signed zero and the chain returns b + 0
+#pragma unroll
+                        for (int u = 0; u < kOuterVec; ++u) {
+                            const int i = i0 + u * kBX;
+                            if (i > L.nx) break;
+                            const long long p = lin(i, j, k, L.sy, L.sz);
+                            const double v = __dadd_rn(bv[u], 0.0);
+                            r[p] = v;
+                            r32[lin(i, j, k, sy32, sz32)] = f64_to_f32_rn(v);
+                            acc = fma(v, v, acc);
+                        }
+                    } else {
+#pragma unroll
+                        for (int u = 0; u < kOuterVec; ++u) {
+                            const int i = i0 + u * kBX;
+                            if (i > L.nx) break;
+                            const long long p = lin(i, j, k, L.sy, L.sz);
+                            const double v = outer_residual_cell_b(L, dyz, x, bv[u], i, j, k, p);
+                            r[p] = v;
+                            r32[lin(i, j, k, sy32, sz32)] = f64_to_f32_rn(v);
+                            acc = fma(v, v, acc);
+                        }
+                    }
+                } else {
 #pragma unroll
                     for (int u = 0; u < kOuterVec; ++u) {
                         const int i = i0 + u * kBX;
                         if (i > L.nx) break;
                         const long long p = lin(i, j, k, L.sy, L.sz);
-                        const double v = __dadd_rn(b[p], 0.0);
+                        const double v = outer_residual_cell(L, dyz, x, b, i, j, k, p);
                         r[p] = v;
                         r32[lin(i, j, k, sy32, sz32)] = f64_to_f32_rn(v);
                         acc = fma(v, v, acc);
                     }
-                    continue;
-                }
-#pragma unroll
-                for (int u = 0; u < kOuterVec; ++u) {
-                    const int i = i0 + u * kBX;
-                    if (i > L.nx) break;
-                    const long long p = lin(i, j, k, L.sy, L.sz);
-                    const double v = outer_residual_cell(L, dyz, x, b, i, j, k, p);
-                    r[p] = v;
-                    r32[lin(i, j, k, sy32, sz32)] = f64_to_f32_rn(v);
-                    acc = fma(v, v, acc);
                 }
             }
         }
@@ -229,6 +250,49 @@ __global__ void __launch_bounds__(kBX *kBY) k_add_correction(LevelK<double> L, d
                 const long long p = lin(i, j, k, L.sy, L.sz);
                 x[p] = x[p] + f32_to_f64(e[lin(i, j, k, sy32, sz32)]);
             }
+}
+
+// After a correction: x += e and r -= A e (the residual of the corrected x without the
+// FP64 stencil; A e in compensated FP32 arithmetic, see comp_term), the FP32 copy of r
+// and its FP64 norm.  e's ghost cells are zero (the correction has homogeneous boundary
+// values), so the difference form covers the boundary cells too.
+__global__ void __launch_bounds__(kBX *kBY) k_update_residual(LevelK<double> L, SplitCoef C, double *__restrict__ x,
+                                                              const float *__restrict__ e, double *__restrict__ r,
+                                                              float *__restrict__ r32, int sy32, long long sz32,
+                                                              double *partials)
+{
+    double acc = 0.0;
+    for (int k = blockIdx.z + 1; k <= L.nz; k += gridDim.z) {
+        const float2 czm = C.czm[k], czp = C.czp[k];
+        for (int j = blockIdx.y * blockDim.y + threadIdx.y + 1; j <= L.ny; j += gridDim.y * blockDim.y) {
+            const float2 cym = C.cym[j], cyp = C.cyp[j];
+            for (int i0 = blockIdx.x * (blockDim.x * kOuterVec) + threadIdx.x + 1; i0 <= L.nx;
+                 i0 += gridDim.x * blockDim.x * kOuterVec) {
+#pragma unroll
+                for (int u = 0; u < kOuterVec; ++u) {
+                    const int i = i0 + u * kBX;
+                    if (i > L.nx) break;
+                    const long long p = lin(i, j, k, L.sy, L.sz), q = lin(i, j, k, sy32, sz32);
+                    const float ec = e[q];
+                    float S = 0.f, Sl = 0.f;
+                    comp_term(C.cxm[i], e[q - 1], ec, S, Sl);
+                    comp_term(C.cxp[i], e[q + 1], ec, S, Sl);
+                    comp_term(cym, e[q - sy32], ec, S, Sl);
+                    comp_term(cyp, e[q + sy32], ec, S, Sl);
+                    comp_term(czm, e[q - sz32], ec, S, Sl);
+                    comp_term(czp, e[q + sz32], ec, S, Sl);
+                    x[p] = x[p] + f32_to_f64(ec);
+                    const double v = __dsub_rn(__dsub_rn(r[p], f32_to_f64(S)), f32_to_f64(Sl));
+                    r[p] = v;
+                    r32[q] = f64_to_f32_rn(v);
+                    acc = fma(v, v, acc);
+                }
+            }
+        }
+    }
+    __shared__ double sw[kBX * kBY / 32];
+    const double s = block_sum(acc, sw);
+    if (tid2() == 0) partials[blin()] = s;
 }
 
 // Test hook: convert n values with the integer-pipe conversions.
@@ -376,6 +440,32 @@ int Ctx::setup_mixed()
                           "mixed tables"));
         m->dyy.push_back(m->diag64);
         m->dzz.push_back(m->diag64 + S.n[1] + 2);
+    }
+    // finest-level coefficients as FP32 (hi, lo) pairs for the residual update
+    {
+        const LevelK<double> &k0 = K[0];
+        const double *src[6] = {k0.cxm, k0.cxp, k0.cym, k0.cyp, k0.czm, k0.czp};
+        const int len[6] = {k0.nx + 2, k0.nx + 2, k0.ny + 2, k0.ny + 2, k0.nz + 2, k0.nz + 2};
+        std::vector<float2> h;
+        size_t off[6];
+        for (int a = 0; a < 6; ++a) {
+            off[a] = h.size();
+            const double *t = tables_host.data() + (src[a] - d_tables);
+            for (int q = 0; q < len[a]; ++q) {
+                const float hi = (float)t[q];
+                h.push_back(make_float2(hi, (float)(t[q] - (double)hi)));
+            }
+        }
+        PMG_TRY_M(mstatus(cudaMalloc(&m->split, h.size() * sizeof(float2)), "mixed tables"));
+        PMG_TRY_M(mstatus(cudaMemcpy(m->split, h.data(), h.size() * sizeof(float2), cudaMemcpyHostToDevice),
+                          "mixed tables"));
+        m->sc = SplitCoef{m->split + off[0], m->split + off[1], m->split + off[2],
+                          m->split + off[3], m->split + off[4], m->split + off[5]};
+    }
+    // PEPS_MG_OUTER=recompute: the residual after every correction is b - A x in FP64
+    {
+        const char *oe = std::getenv("PEPS_MG_OUTER");
+        m->update_residual = !(oe && std::strcmp(oe, "recompute") == 0);
     }
     auto F = [&](const double *p) { return (const float *)(m->tables + (p - d_tables)); };
     m->K.resize((size_t)nl + 1);
@@ -592,33 +682,72 @@ int Ctx::outer_residual(double *sol, double *rsd, const double *rhs, int slot)
     return f64_reduce(d_partials, (int)(g.x * g.y * g.z), d_scal + slot, stream);
 }
 
+// x += e and r -= A e with its norm into d_scal[slot] (after a correction).
+int Ctx::update_residual(double *sol, double *rsd, int slot)
+{
+    const LevelK<double> &L = K[0];
+    const dim3 g = grid3m((L.nx + kOuterVec - 1) / kOuterVec, L.ny, L.nz, launch[0]), bl(kBX, kBY, 1);
+    const int pi = prof.begin(stream);
+    k_update_residual<<<g, bl, 0, stream>>>(L, mixed->sc, sol, mixed->E(0), rsd, mixed->b[0], mixed->K[0].sy,
+                                            mixed->K[0].sz, d_partials);
+    prof.end(pi, PC_UPDATE_RES, 1, 40.0 * (double)L.nx * L.ny * L.nz, stream);
+    count_launches(1);
+    PMG_TRY_M(cuda_status(cudaGetLastError(), "residual update"));
+    return f64_reduce(d_partials, (int)(g.x * g.y * g.z), d_scal + slot, stream);
+}
+
+// x += e followed by the FP64 residual b - A x (slot 1).
+int Ctx::correct_and_recompute(double *sol, double *rsd, const double *rhs)
+{
+    const LevelK<double> &L = K[0];
+    const dim3 g = grid3m(L.nx, L.ny, L.nz, launch[0]), bl(kBX, kBY, 1);
+    const int pi = prof.begin(stream);
+    k_add_correction<<<g, bl, 0, stream>>>(L, sol, mixed->E(0), mixed->K[0].sy, mixed->K[0].sz);
+    prof.end(pi, PC_ADDCORR, 1, 20.0 * (double)L.nx * L.ny * L.nz, stream);
+    count_launches(1);
+    return outer_residual(sol, rsd, rhs, 1);
+}
+
+// Defect correction.  After a correction the residual is normally updated (r -= A e,
+// x += e in one pass, no FP64 stencil); the FP64 residual b - A x is recomputed where the
+// solve may end: when the updated residual passes the test (the recomputed one decides,
+// and it is the residual returned), when the previous contraction predicts that this
+// correction passes it by a margin of 10, and after the last allowed correction.
 int Ctx::solve_mixed(double *sol, double *rsd, const double *rhs, int maxit, double tol, double omega,
                      pmg_report_t *rep)
 {
     PMG_TRY_M(setup_mixed());
     MixedState *m = mixed;
     const Level &S = lv[0];
-    PMG_TRY_M(mstatus(cudaMemsetAsync(rsd, 0, S.total * sizeof(double), stream), "rsd init"));
+    // the residual's ghost cells are zero (src/multigrid.f90:1795); the outer residual
+    // writes every interior cell
+    PMG_TRY_M(zero_ghosts_f64(rsd, S.n[0], S.n[1], S.n[2], stream));
     PMG_TRY_M(outer_residual(sol, rsd, rhs, 0));
     double h[2];
     PMG_TRY_M(fetch_scalars(h, 1));
     const double res0tol = h[0];
     PMG_TRY_M(upload_tail32(maxit, omega, tol));
     int cycles = 0, converged = 0, inner_total = 0;
-    double ratio = 0.0;
-    const LevelK<double> &L = K[0];
-    const dim3 g = grid3m(L.nx, L.ny, L.nz, launch[0]), bl(kBX, kBY, 1);
+    double ratio = 0.0, prev_ratio = 1.0, contraction = 1.0;
     for (int cyc = 1; cyc <= n_vcycles; ++cyc) {
         for (int q = 0; q < m->inner; ++q) PMG_TRY_M(vcycle32(maxit, omega, q == 0));
         inner_total += m->inner;
-        const int pi = prof.begin(stream);
-        k_add_correction<<<g, bl, 0, stream>>>(L, sol, m->E(0), m->K[0].sy, m->K[0].sz);
-        prof.end(pi, PC_ADDCORR, 1, 20.0 * (double)L.nx * L.ny * L.nz, stream);
-        count_launches(1);
-        PMG_TRY_M(outer_residual(sol, rsd, rhs, 1));
-        PMG_TRY_M(fetch_scalars(h, 2));
+        const bool recompute = !m->update_residual || cyc == n_vcycles || prev_ratio * contraction < 0.1 * tol;
+        if (recompute) {
+            PMG_TRY_M(correct_and_recompute(sol, rsd, rhs));
+            PMG_TRY_M(fetch_scalars(h, 2));
+        } else {
+            PMG_TRY_M(update_residual(sol, rsd, 1));
+            PMG_TRY_M(fetch_scalars(h, 2));
+            if (std::isfinite(h[1]) && std::sqrt(h[1] / res0tol) < tol) {
+                PMG_TRY_M(outer_residual(sol, rsd, rhs, 1));
+                PMG_TRY_M(fetch_scalars(h, 2));
+            }
+        }
         const double rsd_val = h[1];
         ratio = std::sqrt(rsd_val / res0tol);
+        contraction = ratio / prev_ratio;
+        prev_ratio = ratio;
         cycles = cyc;
         if (rep && rep->history) {
             rep->history[3 * (cyc - 1) + 0] = std::sqrt(rsd_val);

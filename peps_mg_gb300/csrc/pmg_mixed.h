@@ -7,10 +7,19 @@
 
 namespace pmg {
 
+// Finest-level coefficients split into FP32 pairs (hi = c rounded to FP32, lo = c - hi
+// rounded to FP32), per axis and side, for the compensated residual update.
+struct SplitCoef {
+    const float2 *cxm, *cxp, *cym, *cyp, *czm, *czp;
+};
+
 struct MixedState {
     std::vector<float> tables_host;
     float *tables = nullptr;
     double *diag64 = nullptr;        // per level: dyy (ny+2) and dzz (nz+2) for the outer residual
+    float2 *split = nullptr;         // storage of sc
+    SplitCoef sc{};
+    bool update_residual = true;     // residual after a correction by r -= A e (else b - A x)
     std::vector<const double *> dyy, dzz;
     std::vector<LevelK<float>> K;
     std::vector<XferK<float>> X;
@@ -30,6 +39,7 @@ struct MixedState {
     {
         cudaFree(tables);
         cudaFree(diag64);
+        cudaFree(split);
         for (auto p : alloc) cudaFree(p);
         cudaFree(d_tail);
         cudaFree(d_err);

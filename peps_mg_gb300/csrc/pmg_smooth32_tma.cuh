@@ -298,10 +298,7 @@ struct RbtItem {
         const int cs = cbase + (t - k0 + 2);      // slot of plane t
         const unsigned s0 = stage_off(cs), sp = stage_off(cs + 1), sm = stage_off(cs - 1);
         wait(cs + 1);
-        if (ZERO_IN) {
-            EA[ip1] = make_float2(0.f, 0.f);
-            EB[ip1] = make_float2(0.f, 0.f);
-        } else {
+        if (!ZERO_IN) {
             EA[ip1] = lds2(sp + oe);
             EB[ip1] = lds2(sp + oe + RBT_W * 4);
         }
@@ -317,7 +314,15 @@ struct RbtItem {
         cz[5] = czm_n + czp_n;
         load_cz<CHECKED>(t + 1);
         const bool plane_in = !CHECKED || (t >= 1 && t <= nz);
-        {
+        if (ZERO_IN) {
+            // every neighbour of a first-colour cell still holds the zero input
+            const float vA = nA[Q] && plane_in ? upd(0.f, cq<Q>(BA[b00]), 0.f, dA[Q] + cz[5]) : 0.f;
+            const float vB = nB[QB] && plane_in ? upd(0.f, cq<QB>(BB[b00]), 0.f, dB[QB] + cz[5]) : 0.f;
+            EA[i00] = Q ? make_float2(0.f, vA) : make_float2(vA, 0.f);
+            EB[i00] = QB ? make_float2(0.f, vB) : make_float2(vB, 0.f);
+            sts2(s0 + oe, EA[i00]);
+            sts2(s0 + oe + RBT_W * 4, EB[i00]);
+        } else {
             const float upA = __shfl_up_sync(0xffffffffu, EA[i00].y, 1);
             const float dnA = __shfl_down_sync(0xffffffffu, EA[i00].x, 1);
             const float upB = __shfl_up_sync(0xffffffffu, EB[i00].y, 1);
