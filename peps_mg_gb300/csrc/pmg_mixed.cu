@@ -268,21 +268,44 @@ __global__ void __launch_bounds__(kBX *kBY) k_update_residual(LevelK<double> L, 
             const float2 cym = C.cym[j], cyp = C.cyp[j];
             for (int i0 = blockIdx.x * (blockDim.x * kOuterVec) + threadIdx.x + 1; i0 <= L.nx;
                  i0 += gridDim.x * blockDim.x * kOuterVec) {
+                // every load of the thread's cells first (the kernel is bound by load latency
+                // when each cell's loads wait for the previous cell's arithmetic)
+                float ev[kOuterVec][7];
+                double xv[kOuterVec], rv[kOuterVec];
+                float2 cm[kOuterVec], cp[kOuterVec];
+#pragma unroll
+                for (int u = 0; u < kOuterVec; ++u) {
+                    const int i = i0 + u * kBX;
+                    if (i <= L.nx) {
+                        const long long p = lin(i, j, k, L.sy, L.sz), q = lin(i, j, k, sy32, sz32);
+                        ev[u][0] = e[q];
+                        ev[u][1] = e[q - 1];
+                        ev[u][2] = e[q + 1];
+                        ev[u][3] = e[q - sy32];
+                        ev[u][4] = e[q + sy32];
+                        ev[u][5] = e[q - sz32];
+                        ev[u][6] = e[q + sz32];
+                        xv[u] = x[p];
+                        rv[u] = r[p];
+                        cm[u] = C.cxm[i];
+                        cp[u] = C.cxp[i];
+                    }
+                }
 #pragma unroll
                 for (int u = 0; u < kOuterVec; ++u) {
                     const int i = i0 + u * kBX;
                     if (i > L.nx) break;
                     const long long p = lin(i, j, k, L.sy, L.sz), q = lin(i, j, k, sy32, sz32);
-                    const float ec = e[q];
+                    const float ec = ev[u][0];
                     float S = 0.f, Sl = 0.f;
-                    comp_term(C.cxm[i], e[q - 1], ec, S, Sl);
-                    comp_term(C.cxp[i], e[q + 1], ec, S, Sl);
-                    comp_term(cym, e[q - sy32], ec, S, Sl);
-                    comp_term(cyp, e[q + sy32], ec, S, Sl);
-                    comp_term(czm, e[q - sz32], ec, S, Sl);
-                    comp_term(czp, e[q + sz32], ec, S, Sl);
-                    x[p] = x[p] + f32_to_f64(ec);
-                    const double v = __dsub_rn(__dsub_rn(r[p], f32_to_f64(S)), f32_to_f64(Sl));
+                    comp_term(cm[u], ev[u][1], ec, S, Sl);
+                    comp_term(cp[u], ev[u][2], ec, S, Sl);
+                    comp_term(cym, ev[u][3], ec, S, Sl);
+                    comp_term(cyp, ev[u][4], ec, S, Sl);
+                    comp_term(czm, ev[u][5], ec, S, Sl);
+                    comp_term(czp, ev[u][6], ec, S, Sl);
+                    x[p] = xv[u] + f32_to_f64(ec);
+                    const double v = __dsub_rn(__dsub_rn(rv[u], f32_to_f64(S)), f32_to_f64(Sl));
                     r[p] = v;
                     r32[q] = f64_to_f32_rn(v);
                     acc = fma(v, v, acc);
@@ -352,6 +375,25 @@ void march_chunks(long long columns, int ncz, const Launch &ln, int *kchunk, int
     want = std::max(1LL, std::min<long long>(want, ncz));
     *kchunk = (int)((ncz + want - 1) / want);
     *nchunks = (ncz + *kchunk - 1) / *kchunk;
+}
+
+// Grid of the finest-level FP64 outer kernels (k_outer_residual, k_update_residual): the
+// z extent is cut to about eight waves of three resident CTAs per SM, so every thread
+// walks many planes before the block's FP64 norm reduction (one reduction per four cells
+// cost more than one FP64 operation per cell on a pipe that bounds these kernels).
+dim3 grid_outer(const LevelK<double> &L, const Launch &ln)
+{
+    dim3 g = grid3m((L.nx + kOuterVec - 1) / kOuterVec, L.ny, L.nz, ln);
+    static int sms = 0;
+    if (!sms) {
+        int dev = 0;
+        if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) !=
+                                                      cudaSuccess)
+            sms = 148;
+    }
+    const long long gxy = (long long)g.x * g.y, want = 8LL * 3 * sms;
+    g.z = (unsigned)std::max(1LL, std::min<long long>(g.z, (want + gxy - 1) / gxy));
+    return g;
 }
 
 }  // namespace
@@ -667,7 +709,7 @@ int Ctx::resrestrict32(int l)
 int Ctx::outer_residual(double *sol, double *rsd, const double *rhs, int slot)
 {
     const LevelK<double> &L = K[0];
-    const dim3 g = grid3m((L.nx + kOuterVec - 1) / kOuterVec, L.ny, L.nz, launch[0]), bl(kBX, kBY, 1);
+    const dim3 g = grid_outer(L, launch[0]), bl(kBX, kBY, 1);
     const int pi = prof.begin(stream);
     // the first residual of a solve (slot 0) checks for a zero initial guess
     if (slot == 0)
@@ -686,7 +728,7 @@ int Ctx::outer_residual(double *sol, double *rsd, const double *rhs, int slot)
 int Ctx::update_residual(double *sol, double *rsd, int slot)
 {
     const LevelK<double> &L = K[0];
-    const dim3 g = grid3m((L.nx + kOuterVec - 1) / kOuterVec, L.ny, L.nz, launch[0]), bl(kBX, kBY, 1);
+    const dim3 g = grid_outer(L, launch[0]), bl(kBX, kBY, 1);
     const int pi = prof.begin(stream);
     k_update_residual<<<g, bl, 0, stream>>>(L, mixed->sc, sol, mixed->E(0), rsd, mixed->b[0], mixed->K[0].sy,
                                             mixed->K[0].sz, d_partials);
