@@ -179,8 +179,17 @@ __device__ __forceinline__ void prolong_column_march32(const XferK<float> &X, in
     load(A, m0 - 1);
     load(B, m0);
     float *pf = vf + lin(iz, jf, 0, X.fsy, X.fsz);
+    auto fine = [&](int kf) { return reinterpret_cast<float2 *>(pf + X.fsz * kf); };
+    // the fine pairs of the next coarse plane are loaded while this one is computed (each
+    // pair is read, updated and written by this thread only)
+    float2 F[2] = {*fine(2 * m0 - 1), *fine(2 * m0)};
     for (int m = m0; m <= m1; ++m) {
         load(C, m + 1);
+        float2 N[2] = {F[0], F[1]};
+        if (m < m1) {
+            N[0] = *fine(2 * m + 1);
+            N[1] = *fine(2 * m + 2);
+        }
 #pragma unroll
         for (int h = 0; h < 2; ++h) {
             // h = 0: fine plane 2m-1 (neighbour plane m-1); h = 1: 2m (m+1)
@@ -192,12 +201,12 @@ __device__ __forceinline__ void prolong_column_march32(const XferK<float> &X, in
                                              Z[0], Z[4], Z[3]);
             const float hi = prolong_child32(hi_a, hi_b, ay, by, az, bz, B[1], B[2], B[4], Z[1], B[5],
                                              Z[2], Z[4], Z[5]);
-            float2 *q = reinterpret_cast<float2 *>(pf + X.fsz * kf);
-            float2 v = *q;
-            v.x += lo;
-            v.y += hi;
-            *q = v;
+            F[h].x += lo;
+            F[h].y += hi;
+            *fine(kf) = F[h];
         }
+        F[0] = N[0];
+        F[1] = N[1];
 #pragma unroll
         for (int u = 0; u < 6; ++u) {
             A[u] = B[u];
@@ -230,17 +239,28 @@ __device__ __forceinline__ void resrestrict_column_march32(const LevelK<float> &
         V[0] = __ldg(reinterpret_cast<const float2 *>(e0 + sz * k));
         V[1] = __ldg(reinterpret_cast<const float2 *>(e0 + sz * k + sy));
     };
-    // residuals of fine plane k into r[0..3] = (iz,jz), (ip,jz), (iz,jp), (ip,jp)
-    auto resid_plane = [&](const float2 (&Em)[2], const float2 (&E0)[2], const float2 (&Ep)[2], int k,
-                           float (&r)[4]) {
+    // the x- and y-neighbours and b of the 2 x 2 block on fine plane k
+    struct Nb {
+        float xl0, xr0, xl1, xr1;
+        float2 yd, yu, b0v, b1v;
+    };
+    auto neighbours = [&](int k, Nb &N) {
         const float *pe = e0 + sz * k;
+        N.xl0 = __ldg(pe - 1);
+        N.xr0 = __ldg(pe + 2);
+        N.xl1 = __ldg(pe + sy - 1);
+        N.xr1 = __ldg(pe + sy + 2);
+        N.yd = __ldg(reinterpret_cast<const float2 *>(pe - sy));
+        N.yu = __ldg(reinterpret_cast<const float2 *>(pe + 2 * sy));
+        N.b0v = __ldg(reinterpret_cast<const float2 *>(b0 + sz * k));
+        N.b1v = __ldg(reinterpret_cast<const float2 *>(b0 + sz * k + sy));
+    };
+    // residuals of fine plane k into r[0..3] = (iz,jz), (ip,jz), (iz,jp), (ip,jp)
+    auto resid_plane = [&](const float2 (&Em)[2], const float2 (&E0)[2], const float2 (&Ep)[2], int k, const Nb &N,
+                           float (&r)[4]) {
         const float czm = F.czm[k], czp = F.czp[k], dz = czm + czp;
-        const float xl0 = __ldg(pe - 1), xr0 = __ldg(pe + 2);
-        const float xl1 = __ldg(pe + sy - 1), xr1 = __ldg(pe + sy + 2);
-        const float2 yd = __ldg(reinterpret_cast<const float2 *>(pe - sy));
-        const float2 yu = __ldg(reinterpret_cast<const float2 *>(pe + 2 * sy));
-        const float2 b0v = __ldg(reinterpret_cast<const float2 *>(b0 + sz * k));
-        const float2 b1v = __ldg(reinterpret_cast<const float2 *>(b0 + sz * k + sy));
+        const float xl0 = N.xl0, xr0 = N.xr0, xl1 = N.xl1, xr1 = N.xr1;
+        const float2 yd = N.yd, yu = N.yu, b0v = N.b0v, b1v = N.b1v;
         auto cell = [&](float cxm, float cxp, float sx, float cym, float cyp, float dy, float xm, float xp_,
                         float ym, float yp_, float zm, float zp_, float x0, float bb) {
             float t = cxm * xm;
@@ -261,16 +281,29 @@ __device__ __forceinline__ void resrestrict_column_march32(const LevelK<float> &
         r[3] = cell(cxm1, cxp1, sx1, cym1, cyp1, dy1, E0[1].x, xr1, E0[0].y, yu.y, Em[1].y, Ep[1].y,
                     E0[1].y, b1v.y);
     };
+    // software pipeline: the loads of coarse plane m + 1 are in flight while plane m is
+    // computed
     float2 Wm[2], W0[2], Wp[2], Wq[2];
+    Nb Nz, Np;
     own(Wm, 2 * m0 - 2);
     own(W0, 2 * m0 - 1);
+    own(Wp, 2 * m0);
+    own(Wq, 2 * m0 + 1);
+    neighbours(2 * m0 - 1, Nz);
+    neighbours(2 * m0, Np);
     for (int m = m0; m <= m1; ++m) {
         const int kz = 2 * m - 1, kp = 2 * m;
-        own(Wp, kp);
-        own(Wq, kp + 1);
+        float2 Wr[2] = {Wp[0], Wp[1]}, Ws[2] = {Wq[0], Wq[1]};
+        Nb Mz = Nz, Mp = Np;
+        if (m < m1) {
+            own(Wr, kp + 2);
+            own(Ws, kp + 3);
+            neighbours(kz + 2, Mz);
+            neighbours(kp + 2, Mp);
+        }
         float rz[4], rp[4];
-        resid_plane(Wm, W0, Wp, kz, rz);
-        resid_plane(W0, Wp, Wq, kp, rp);
+        resid_plane(Wm, W0, Wp, kz, Nz, rz);
+        resid_plane(W0, Wp, Wq, kp, Np, rp);
         const float zz = X.wz[kz], zp = X.wz[kp];
         // children in the order of resrestrict_cell32: c = 0..7 with bit 0 ->
         // x (iz), bit 1 -> y (jz), bit 2 -> z (kz); unset bits take the p child
@@ -287,6 +320,12 @@ __device__ __forceinline__ void resrestrict_column_march32(const LevelK<float> &
         Wm[1] = Wp[1];
         W0[0] = Wq[0];
         W0[1] = Wq[1];
+        Wp[0] = Wr[0];
+        Wp[1] = Wr[1];
+        Wq[0] = Ws[0];
+        Wq[1] = Ws[1];
+        Nz = Mz;
+        Np = Mp;
     }
 }
 
