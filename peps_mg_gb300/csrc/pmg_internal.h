@@ -80,14 +80,15 @@ bool rb32_fused_layout_ok(const LevelK<float> &L, const void *e, const void *b);
 // e buffers and b, one map per tile variant (the copy box depends on the tile height).
 struct Rb32Tma {
     bool ok = false;
-    CUtensorMap e[2][3];
-    CUtensorMap b[3];
+    CUtensorMap e[2][4];
+    CUtensorMap b[4];
 };
 // base[3]: allocation starts of e[0], e[1], b (cell (0,0,0) at base + 5 + sy + sz);
 // rows, planes: allocated rows per plane and planes.  Leaves t->ok false (and returns
 // PMG_OK) when the tensor-map encoder is unavailable or rejects the layout.
 int rb32_tma_setup(Rb32Tma *t, const LevelK<float> &L, float *const base[3], long long rows, long long planes);
-// variant: 0 = 60 x 14 tiles (512 threads), 1 = 60 x 6 (256), 2 = 60 x 10 (384);
+// variant: 0 = 60 x 14 tiles (512 threads), 1 = 60 x 6 (256), 2 = 60 x 10 (384), 3 = 60 x 22
+// (TMA-fed kernel only, 384 threads; the register-window kernel runs variant 0 for it);
 // kchunk: planes per work item (0 = automatic).  With tma (tma->ok), the TMA-fed kernel
 // runs; ein must then be buffer in_buf of the maps, and err receives 1 if one of its
 // bounded pipeline waits gave up.

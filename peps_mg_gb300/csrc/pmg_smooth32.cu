@@ -3,7 +3,8 @@
 //
 // A launch performs one RBGS iteration of a whole level, out of place.  Work items are
 // (60 x TY tile) x (chunk of k planes); a persistent grid of resident CTAs walks them
-// chunk-major.  TY is 6, 10 or 14 (CTAs of 256, 384 or 512 threads); the autotuner
+// chunk-major.  TY is 6, 10 or 14 (register-window CTAs of 256, 384 or 512 threads; the
+// TMA-fed kernel also has TY = 22, two rows per warp: 128 to 384 threads); the autotuner
 // times every (TY, k-chunk) candidate on the level's own buffers and keeps the fastest.
 // Two kernels share that mapping: the TMA-fed one (planes copied into a ring of shared
 // stages by the tensor-memory accelerator) wherever the level's tensor maps could be
@@ -245,8 +246,8 @@ int rb32_tma_setup(Rb32Tma *t, const LevelK<float> &L, float *const base[3], lon
     for (int q = 0; q < 3; ++q)
         if (reinterpret_cast<uintptr_t>(base[q]) % 16 != 0) return PMG_OK;
     if (L.sy < RBT_TX * ((L.nx + RBT_TX - 1) / RBT_TX) + 8) return PMG_OK;
-    const int tys[3] = {14, 6, 10};
-    for (int v = 0; v < 3; ++v) {
+    const int tys[4] = {14, 6, 10, 22};
+    for (int v = 0; v < 4; ++v) {
         for (int q = 0; q < 2; ++q)
             if (!encode_map(&t->e[q][v], base[q], L, rows, planes, tys[v] + 4)) return PMG_OK;
         if (!encode_map(&t->b[v], base[2], L, rows, planes, tys[v] + 2)) return PMG_OK;
@@ -263,6 +264,7 @@ int rb32_fused(const LevelK<float> &L, const Launch &ln, const float *ein, float
         switch (variant) {
         case 1: return launch_tma<6>(L, ln, *tma, 1, in_buf, eout, omega, omw, zero_in, kchunk, err, s);
         case 2: return launch_tma<10>(L, ln, *tma, 2, in_buf, eout, omega, omw, zero_in, kchunk, err, s);
+        case 3: return launch_tma<22>(L, ln, *tma, 3, in_buf, eout, omega, omw, zero_in, kchunk, err, s);
         default: return launch_tma<14>(L, ln, *tma, 0, in_buf, eout, omega, omw, zero_in, kchunk, err, s);
         }
     }
@@ -314,7 +316,8 @@ int tune_smoother(const LevelK<float> &L, const Launch &ln, float *e0, float *e1
     const int chunks_window[] = {0, 16, 32, 64}, chunks_tma[] = {0, 4, 8, 16, 32, 64, 128};
     const int *chunks = use_tma ? chunks_tma : chunks_window;
     const int nchunks = use_tma ? 7 : 4;
-    for (int v = 0; v < 3; ++v)
+    const int tys[4] = {14, 6, 10, 22};
+    for (int v = 0; v < (use_tma ? 4 : 3); ++v)
         for (int ci = 0; ci < nchunks; ++ci) {
             const int c = chunks[ci];
             if (rb32_fused(L, ln, e0, e1, b, 1.f, 0.f, false, s, v, c, tma, 0, err) != PMG_OK) continue;
@@ -326,7 +329,7 @@ int tune_smoother(const LevelK<float> &L, const Launch &ln, float *e0, float *e1
             cudaEventElapsedTime(&ms, a, z);
             if (log)
                 std::fprintf(stderr, "[peps_mg tune] %dx%dx%d %s TY=%d kchunk=%d: %.1f us\n", L.nx, L.ny, L.nz,
-                             use_tma ? "tma" : "window", v == 1 ? 6 : v == 2 ? 10 : 14, c, ms * 1e3f / 3.f);
+                             use_tma ? "tma" : "window", tys[v], c, ms * 1e3f / 3.f);
             if (ms < best) {
                 best = ms;
                 bv = v;
@@ -338,6 +341,9 @@ int tune_smoother(const LevelK<float> &L, const Launch &ln, float *e0, float *e1
     PMG_TRY_S(cuda_status(cudaGetLastError(), "smoother autotuning"));
     *variant = bv;
     *kchunk = bk;
+    if (log)
+        std::fprintf(stderr, "[peps_mg tune] %dx%dx%d chosen TY=%d kchunk=%d (%.1f us)\n", L.nx, L.ny, L.nz,
+                     tys[bv], bk, best * 1e3f / 3.f);
     std::lock_guard<std::mutex> g(mu);
     cache[key] = {bv, bk};
     return PMG_OK;

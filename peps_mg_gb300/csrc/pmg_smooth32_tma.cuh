@@ -55,7 +55,7 @@ __host__ __device__ constexpr int S_EB() { return RbtShape<TY>::EBYTES; }
 
 // CTAs per SM the TMA-fed kernels' register budget is sized for
 template <int TY>
-constexpr int rbt_min_ctas() { return TY <= 6 ? 5 : 3; }
+constexpr int rbt_min_ctas() { return TY <= 6 ? 5 : TY <= 14 ? 3 : 2; }
 
 namespace rbtdetail {
 

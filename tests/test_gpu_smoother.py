@@ -37,7 +37,7 @@ def run_selftest(mg, impl, variant, kchunk, zero_in, omega, e_in, b):
     return out
 
 
-# (nx, ny, nz): 200 x 92 x 40 ends part-way through 60-column tiles and 14/10-row
+# (nx, ny, nz): 200 x 92 x 40 ends part-way through 60-column tiles and 14/10/22-row
 # tiles; 124 x 132 x 68 leaves 4 columns in its last tile and 4 planes in its last chunk
 @pytest.mark.parametrize("n", [(200, 92, 40), (124, 132, 68)])
 def test_one_iteration_against_oracle(n):
@@ -54,15 +54,16 @@ def test_one_iteration_against_oracle(n):
                 ref = e0.copy(order="F") if not zero_in else pmg.geometry.field(*n)
                 O.rbgs_iterator(coeff, ref, b, 1, omega)
                 scale = np.abs(ref).max()
-                for variant in (0, 1, 2):
+                # variant 3 (60 x 22 tiles) exists for the TMA-fed kernel only
+                for variant in (0, 1, 2, 3):
                     for kchunk in (0, 16, 7):
                         outs = []
-                        for impl in (0, 1):
+                        for impl in ((0,) if variant == 3 else (0, 1)):
                             got = run_selftest(mg, impl, variant, kchunk, zero_in, omega, e0, b)
                             err = np.abs(got - ref).max() / scale
                             assert err < FP32_TOL, (impl, variant, kchunk, zero_in, omega, err)
                             outs.append(got)
-                        assert np.array_equal(outs[0], outs[1]), (variant, kchunk, zero_in, omega)
+                        assert all(np.array_equal(outs[0], o) for o in outs[1:]), (variant, kchunk, zero_in, omega)
 
 
 def test_kernel_variants_give_identical_solves(tmp_path):
