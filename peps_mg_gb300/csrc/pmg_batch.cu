@@ -172,13 +172,19 @@ __global__ void __launch_bounds__(NTB) k_batch_prolong(const BLevel *__restrict_
         // the coarsest depth of a problem is solved in place in buffer 0
         const float *ec = (d + 1 == D.nl) ? lvc[w.p].e[0] : lvc[w.p].e[which_c];
         float *e = D.e[which];
-        // one thread per coarse cell (measured faster here than marching columns)
         const int m0 = w.k0, m1 = min(X.ncz, w.k0 + kXferPlanes - 1);
-        for (int k = m0; k <= m1; ++k)
-            for (int q = threadIdx.x; q < X.ncx * X.ncy; q += NTB) {
-                const int i = q % X.ncx + 1, j = q / X.ncx + 1;
-                prolong_add_cell32(X, ec, e, i, j, k);
-            }
+        if (X.stx == 2 && X.stz == 2) {
+            // one thread per fine x-pair column of the item's planes
+            const int nfy = D.L.ny;
+            for (int q = threadIdx.x; q < X.ncx * nfy; q += NTB)
+                prolong_column_march32(X, q / X.ncx + 1, q % X.ncx + 1, m0, m1, ec, e);
+        } else {
+            for (int k = m0; k <= m1; ++k)
+                for (int q = threadIdx.x; q < X.ncx * X.ncy; q += NTB) {
+                    const int i = q % X.ncx + 1, j = q / X.ncx + 1;
+                    prolong_add_cell32(X, ec, e, i, j, k);
+                }
+        }
     }
 }
 
