@@ -494,6 +494,9 @@ int Ctx::build(const pmg_config_t *c, cudaStream_t s)
     PMG_CUDA(cudaMalloc(&d_tail, sizeof(TailDesc<double>)), "tail descriptor");
     PMG_CUDA(cudaEventCreate(&ev0), "event");
     PMG_CUDA(cudaEventCreate(&ev1), "event");
+    PMG_CUDA(cudaEventCreateWithFlags(&ev_x, cudaEventDisableTiming), "event");
+    PMG_CUDA(cudaEventCreateWithFlags(&ev_copied, cudaEventDisableTiming), "event");
+    PMG_CUDA(cudaStreamCreateWithFlags(&copy_stream, cudaStreamNonBlocking), "copy stream");
     return PMG_OK;
 }
 
@@ -523,6 +526,9 @@ Ctx::~Ctx()
     cudaFree(adj_faces);
     if (ev0) cudaEventDestroy(ev0);
     if (ev1) cudaEventDestroy(ev1);
+    if (ev_x) cudaEventDestroy(ev_x);
+    if (ev_copied) cudaEventDestroy(ev_copied);
+    if (copy_stream) cudaStreamDestroy(copy_stream);
     destroy_mixed();
 }
 
@@ -808,6 +814,36 @@ static bool is_device_ptr(const void *p)
     return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
 }
 
+// Page-locked (registered or cudaHostAlloc'ed) host memory: copies to it are asynchronous.
+static bool is_pinned_host_ptr(const void *p)
+{
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return a.type == cudaMemoryTypeHost;
+}
+
+int Ctx::early_copy_sol(const double *sol)
+{
+    if (!early_sol_host) return PMG_OK;
+    PMG_CUDA(cudaEventRecord(ev_x, stream), "event");
+    PMG_CUDA(cudaStreamWaitEvent(copy_stream, ev_x, 0), "event");
+    PMG_CUDA(cudaMemcpyAsync(early_sol_host, sol, lv[0].total * sizeof(double), cudaMemcpyDeviceToHost, copy_stream),
+             "D2H");
+    PMG_CUDA(cudaEventRecord(ev_copied, copy_stream), "event");
+    early_pending = early_valid = true;
+    return PMG_OK;
+}
+
+int Ctx::before_x_change()
+{
+    if (early_pending) PMG_CUDA(cudaStreamWaitEvent(stream, ev_copied, 0), "event");
+    early_pending = early_valid = false;
+    return PMG_OK;
+}
+
 int Ctx::solve(double *sol, double *rsd, const double *rhs, int maxit, double tol, double omega, pmg_report_t *rep)
 {
     if (!sol || !rsd || !rhs) {
@@ -838,14 +874,35 @@ int Ctx::solve(double *sol, double *rsd, const double *rhs, int maxit, double to
         s = stage_sol;
         r = stage_rsd;
         b = stage_rhs;
+        if (is_pinned_host_ptr(sol)) early_sol_host = sol;
     }
+    early_valid = early_pending = false;
     int rc = precision == PMG_MIXED ? solve_mixed(s, r, b, maxit, tol, omega, rep)
                                     : solve_f64(s, r, b, maxit, tol, omega, rep);
-    if (rc != PMG_OK && rc != PMG_EDIVERGED) return rc;
-    if (!dev) {
-        PMG_CUDA(cudaMemcpyAsync(sol, stage_sol, bytes, cudaMemcpyDeviceToHost, stream), "D2H");
-        PMG_CUDA(cudaMemcpyAsync(rsd, stage_rsd, bytes, cudaMemcpyDeviceToHost, stream), "D2H");
+    early_sol_host = nullptr;
+    if (rc != PMG_OK && rc != PMG_EDIVERGED) {
+        if (early_pending) cudaStreamWaitEvent(stream, ev_copied, 0);
+        cudaStreamSynchronize(stream);
+        early_valid = early_pending = false;
+        return rc;
     }
+    if (!dev) {
+        if (early_valid) {
+            // the residual follows the solution's copy on the copy stream (one transfer
+            // at a time over the link)
+            PMG_CUDA(cudaEventRecord(ev_x, stream), "event");
+            PMG_CUDA(cudaStreamWaitEvent(copy_stream, ev_x, 0), "event");
+            PMG_CUDA(cudaMemcpyAsync(rsd, stage_rsd, bytes, cudaMemcpyDeviceToHost, copy_stream), "D2H");
+            PMG_CUDA(cudaEventRecord(ev_copied, copy_stream), "event");
+            PMG_CUDA(cudaStreamWaitEvent(stream, ev_copied, 0), "event");
+        } else {
+            PMG_CUDA(cudaMemcpyAsync(sol, stage_sol, bytes, cudaMemcpyDeviceToHost, stream), "D2H");
+            PMG_CUDA(cudaMemcpyAsync(rsd, stage_rsd, bytes, cudaMemcpyDeviceToHost, stream), "D2H");
+        }
+    } else if (early_pending) {
+        PMG_CUDA(cudaStreamWaitEvent(stream, ev_copied, 0), "event");
+    }
+    early_valid = early_pending = false;
     PMG_CUDA(cudaEventRecord(ev1, stream), "event");
     PMG_CUDA(cudaEventSynchronize(ev1), "event sync");
     prof.flush();

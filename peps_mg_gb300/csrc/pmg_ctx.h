@@ -80,6 +80,15 @@ struct Ctx {
     std::vector<double *> scratch_levels;
     size_t scratch_cap = 0;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    // Early copy-back of a staged solve: the mixed solver starts the device-to-host copy of
+    // the solution when it recomputes the residual that may end the solve, so the copy
+    // overlaps that residual; a later change of x first waits for the copy and voids it.
+    double *early_sol_host = nullptr;   // the caller's pinned host sol during a staged solve
+    cudaStream_t copy_stream = nullptr;
+    cudaEvent_t ev_x = nullptr, ev_copied = nullptr;
+    bool early_valid = false, early_pending = false;
+    int early_copy_sol(const double *sol);
+    int before_x_change();
     MixedState *mixed = nullptr;
     Profiler prof;
     bool autotune = true;       // tune the fused smoother per level in setup_mixed

@@ -743,10 +743,13 @@ int Ctx::correct_and_recompute(double *sol, double *rsd, const double *rhs)
 {
     const LevelK<double> &L = K[0];
     const dim3 g = grid3m(L.nx, L.ny, L.nz, launch[0]), bl(kBX, kBY, 1);
+    PMG_TRY_M(before_x_change());
     const int pi = prof.begin(stream);
     k_add_correction<<<g, bl, 0, stream>>>(L, sol, mixed->E(0), mixed->K[0].sy, mixed->K[0].sz);
     prof.end(pi, PC_ADDCORR, 1, 20.0 * (double)L.nx * L.ny * L.nz, stream);
     count_launches(1);
+    PMG_TRY_M(cuda_status(cudaGetLastError(), "correction"));
+    PMG_TRY_M(early_copy_sol(sol));
     return outer_residual(sol, rsd, rhs, 1);
 }
 
@@ -779,9 +782,11 @@ int Ctx::solve_mixed(double *sol, double *rsd, const double *rhs, int maxit, dou
             PMG_TRY_M(correct_and_recompute(sol, rsd, rhs));
             PMG_TRY_M(fetch_scalars(h, 2));
         } else {
+            PMG_TRY_M(before_x_change());
             PMG_TRY_M(update_residual(sol, rsd, 1));
             PMG_TRY_M(fetch_scalars(h, 2));
             if (std::isfinite(h[1]) && std::sqrt(h[1] / res0tol) < tol) {
+                PMG_TRY_M(early_copy_sol(sol));
                 PMG_TRY_M(outer_residual(sol, rsd, rhs, 1));
                 PMG_TRY_M(fetch_scalars(h, 2));
             }

@@ -199,3 +199,21 @@ np.savez(sys.argv[1], sol=from_dev(sol), rsd=from_dev(rsd), hist=rep.history, co
     # eps |c0| |x| (the Dirichlet face makes |x| large here)
     noise = 8 * np.finfo(np.float64).eps * np.abs(coeff[0]).max() * np.abs(u["sol"]).max()
     assert np.max(np.abs(u["rsd"] - r)) < noise
+
+
+def test_mixed_pinned_host_buffers():
+    """Pinned host buffers: the solution's copy back starts while the final residual is
+    computed; the results equal those of device buffers."""
+    mesh, rhs, _ = problems.sine(48)
+    n = 48
+    with pmg.Multigrid(mesh, 4, 50, precision="mixed") as mg:
+        shape = (n + 2,) * 3
+        h_rhs = torch.from_numpy(np.ascontiguousarray(np.asfortranarray(rhs).T)).pin_memory()
+        h_sol = torch.zeros(shape, dtype=torch.float64).pin_memory()
+        h_rsd = torch.zeros(shape, dtype=torch.float64).pin_memory()
+        rep = mg.solve_vcycle(h_sol.numpy(), h_rsd.numpy(), h_rhs.numpy(), 2, 1e-10, 1.0)
+        ds = torch.zeros(shape, dtype=torch.float64, device="cuda")
+        dr = torch.zeros_like(ds)
+        rep2 = mg.solve_vcycle(ds, dr, to_dev(rhs), 2, 1e-10, 1.0)
+    assert rep.converged and np.array_equal(rep.history, rep2.history)
+    assert torch.equal(h_sol, ds.cpu()) and torch.equal(h_rsd, dr.cpu())
