@@ -254,14 +254,18 @@ __global__ void __launch_bounds__(kBX *kBY) k_add_correction(LevelK<double> L, d
 
 // After a correction: x += e and r -= A e (the residual of the corrected x without the
 // FP64 stencil; A e in compensated FP32 arithmetic, see comp_term), the FP32 copy of r
-// and its FP64 norm.  e's ghost cells are zero (the correction has homogeneous boundary
-// values), so the difference form covers the boundary cells too.
+// and its norm.  e's ghost cells are zero (the correction has homogeneous boundary
+// values), so the difference form covers the boundary cells too.  The norm only decides
+// whether the FP64 residual is recomputed (which then decides convergence), so each
+// thread sums (nscale r32)^2 in FP32 -- nscale a power of two that brings the initial
+// residual's RMS to about 1, keeping the squares in FP32's range for residual ratios
+// down to about 1e-19 -- and the block sums the threads' sums in FP64.
 __global__ void __launch_bounds__(kBX *kBY) k_update_residual(LevelK<double> L, SplitCoef C, double *__restrict__ x,
                                                               const float *__restrict__ e, double *__restrict__ r,
                                                               float *__restrict__ r32, int sy32, long long sz32,
-                                                              double *partials)
+                                                              float nscale, double *partials)
 {
-    double acc = 0.0;
+    float acc32 = 0.f;
     for (int k = blockIdx.z + 1; k <= L.nz; k += gridDim.z) {
         const float2 czm = C.czm[k], czp = C.czp[k];
         for (int j = blockIdx.y * blockDim.y + threadIdx.y + 1; j <= L.ny; j += gridDim.y * blockDim.y) {
@@ -307,14 +311,17 @@ __global__ void __launch_bounds__(kBX *kBY) k_update_residual(LevelK<double> L, 
                     x[p] = xv[u] + f32_to_f64(ec);
                     const double v = __dsub_rn(__dsub_rn(rv[u], f32_to_f64(S)), f32_to_f64(Sl));
                     r[p] = v;
-                    r32[q] = f64_to_f32_rn(v);
-                    acc = fma(v, v, acc);
+                    const float v32 = f64_to_f32_rn(v);
+                    r32[q] = v32;
+                    const float w = v32 * nscale;
+                    acc32 = fmaf(w, w, acc32);
                 }
             }
         }
     }
     __shared__ double sw[kBX * kBY / 32];
-    const double s = block_sum(acc, sw);
+    const double inv = 1.0 / ((double)nscale * (double)nscale);
+    const double s = block_sum((double)acc32 * inv, sw);
     if (tid2() == 0) partials[blin()] = s;
 }
 
@@ -724,14 +731,19 @@ int Ctx::outer_residual(double *sol, double *rsd, const double *rhs, int slot)
     return f64_reduce(d_partials, (int)(g.x * g.y * g.z), d_scal + slot, stream);
 }
 
-// x += e and r -= A e with its norm into d_scal[slot] (after a correction).
-int Ctx::update_residual(double *sol, double *rsd, int slot)
+// x += e and r -= A e with its norm into d_scal[slot] (after a correction); res0 = the
+// initial residual's squared norm (sets the norm's FP32 scale).
+int Ctx::update_residual(double *sol, double *rsd, int slot, double res0)
 {
     const LevelK<double> &L = K[0];
     const dim3 g = grid_outer(L, launch[0]), bl(kBX, kBY, 1);
+    const double rms0 = std::sqrt(res0 / ((double)L.nx * L.ny * L.nz));
+    const int ex = rms0 > 0.0 && std::isfinite(rms0) ? std::max(-100, std::min(100, (int)std::floor(std::log2(rms0))))
+                                                     : 0;
+    const float nscale = std::ldexp(1.0f, -ex);
     const int pi = prof.begin(stream);
     k_update_residual<<<g, bl, 0, stream>>>(L, mixed->sc, sol, mixed->E(0), rsd, mixed->b[0], mixed->K[0].sy,
-                                            mixed->K[0].sz, d_partials);
+                                            mixed->K[0].sz, nscale, d_partials);
     prof.end(pi, PC_UPDATE_RES, 1, 40.0 * (double)L.nx * L.ny * L.nz, stream);
     count_launches(1);
     PMG_TRY_M(cuda_status(cudaGetLastError(), "residual update"));
@@ -783,7 +795,7 @@ int Ctx::solve_mixed(double *sol, double *rsd, const double *rhs, int maxit, dou
             PMG_TRY_M(fetch_scalars(h, 2));
         } else {
             PMG_TRY_M(before_x_change());
-            PMG_TRY_M(update_residual(sol, rsd, 1));
+            PMG_TRY_M(update_residual(sol, rsd, 1, res0tol));
             PMG_TRY_M(fetch_scalars(h, 2));
             if (std::isfinite(h[1]) && std::sqrt(h[1] / res0tol) < tol) {
                 PMG_TRY_M(early_copy_sol(sol));

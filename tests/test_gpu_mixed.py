@@ -182,8 +182,9 @@ np.savez(sys.argv[1], sol=from_dev(sol), rsd=from_dev(rsd), hist=rep.history, co
     hu, hc = u["hist"], c["hist"]
     m = min(len(hu), len(hc))
     assert m >= 2
-    # ratio after each correction (column 2): identical corrections until the last one
-    np.testing.assert_allclose(hu[:m - 1, 2], hc[:m - 1, 2], rtol=1e-6, atol=1e-11)
+    # ratio after each correction (column 2): identical corrections until the last one;
+    # the updated residual's norm is summed in FP32 (it only decides when to recompute)
+    np.testing.assert_allclose(hu[:m - 1, 2], hc[:m - 1, 2], rtol=1e-5, atol=1e-11)
     assert hu[-1, 2] < 1e-10
     scale = np.abs(c["sol"]).max()
     assert np.abs(u["sol"] - c["sol"]).max() / scale < 1e-9
