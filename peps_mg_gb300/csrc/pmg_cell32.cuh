@@ -180,15 +180,20 @@ __device__ __forceinline__ void prolong_column_march32(const XferK<float> &X, in
     load(B, m0);
     float *pf = vf + lin(iz, jf, 0, X.fsy, X.fsz);
     auto fine = [&](int kf) { return reinterpret_cast<float2 *>(pf + X.fsz * kf); };
-    // the fine pairs of the next coarse plane are loaded while this one is computed (each
-    // pair is read, updated and written by this thread only)
+    // the fine pairs of the next two coarse planes are loaded while this one is computed
+    // (each pair is read, updated and written by this thread only)
     float2 F[2] = {*fine(2 * m0 - 1), *fine(2 * m0)};
+    float2 N[2] = {F[0], F[1]};
+    if (m0 < m1) {
+        N[0] = *fine(2 * m0 + 1);
+        N[1] = *fine(2 * m0 + 2);
+    }
     for (int m = m0; m <= m1; ++m) {
         load(C, m + 1);
-        float2 N[2] = {F[0], F[1]};
-        if (m < m1) {
-            N[0] = *fine(2 * m + 1);
-            N[1] = *fine(2 * m + 2);
+        float2 NN[2] = {N[0], N[1]};
+        if (m + 1 < m1) {
+            NN[0] = *fine(2 * m + 3);
+            NN[1] = *fine(2 * m + 4);
         }
 #pragma unroll
         for (int h = 0; h < 2; ++h) {
@@ -207,6 +212,8 @@ __device__ __forceinline__ void prolong_column_march32(const XferK<float> &X, in
         }
         F[0] = N[0];
         F[1] = N[1];
+        N[0] = NN[0];
+        N[1] = NN[1];
 #pragma unroll
         for (int u = 0; u < 6; ++u) {
             A[u] = B[u];
