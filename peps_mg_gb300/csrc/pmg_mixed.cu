@@ -150,75 +150,54 @@ __global__ void __launch_bounds__(kBX *kBY) k_resrestrict_march32(LevelK<float> 
 // as the FP32 right-hand side of the inner system, with the per-block sum of r^2.
 // Each thread handles four cells of a row, 32 apart.
 constexpr int kOuterVec = 4;
-// True for the whole warp when x is exactly +0 (all bits clear) at every cell a lane of
-// the warp handles in row (j, k) and at their six neighbours.
-__device__ __forceinline__ bool x_zero_around(const LevelK<double> &L, const double *__restrict__ x, int i0, int j,
-                                           int k)
+// *flag |= 1 unless every value of x (ghosts included) is +0 (all bits clear).
+__global__ void __launch_bounds__(256) k_nonzero_f64(const double *__restrict__ x, long long n, int *flag)
 {
     unsigned long long bits = 0ull;
-#pragma unroll
-    for (int u = 0; u < kOuterVec; ++u) {
-        const int i = i0 + u * kBX;
-        if (i > L.nx) break;
-        const long long p = lin(i, j, k, L.sy, L.sz);
-        bits |= (unsigned long long)(__double_as_longlong(x[p]) | __double_as_longlong(x[p - 1]) |
-                                     __double_as_longlong(x[p + 1]) | __double_as_longlong(x[p - L.sy]) |
-                                     __double_as_longlong(x[p + L.sy]) | __double_as_longlong(x[p - L.sz]) |
-                                     __double_as_longlong(x[p + L.sz]));
-    }
-    return __all_sync(__activemask(), bits == 0ull);
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    for (; q + 3 * stride < n; q += 4 * stride)
+        bits |= (unsigned long long)__double_as_longlong(x[q]) | (unsigned long long)__double_as_longlong(x[q + stride]) |
+                (unsigned long long)__double_as_longlong(x[q + 2 * stride]) |
+                (unsigned long long)__double_as_longlong(x[q + 3 * stride]);
+    for (; q < n; q += stride) bits |= (unsigned long long)__double_as_longlong(x[q]);
+    if (__syncthreads_or(bits != 0ull) && threadIdx.x == 0) atomicOr(flag, 1);
 }
 
-// ZS: test for an x that is exactly zero around the cell (the initial residual of a
-// solve, which usually starts from x = 0) and skip the FP64 chain there.
+// ZS (the first residual of a solve): *nonzero, set by k_nonzero_f64, tells whether the
+// initial guess has a non-zero value; where it has none, every product of the FMA chain
+// is a signed zero and the chain returns b + 0, so the kernel streams b alone.
 template <bool ZS>
 __global__ void __launch_bounds__(kBX *kBY) k_outer_residual(LevelK<double> L, const double *__restrict__ dyy,
                                                              const double *__restrict__ dzz,
                                                              const double *__restrict__ x,
                                                              const double *__restrict__ b, double *__restrict__ r,
                                                              float *__restrict__ r32, int sy32, long long sz32,
-                                                             double *partials)
+                                                             double *partials, const int *__restrict__ nonzero)
 {
     double acc = 0.0;
+    const bool zero_x = ZS && *nonzero == 0;
     for (int k = blockIdx.z + 1; k <= L.nz; k += gridDim.z) {
         const double dz = dzz[k];
         for (int j = blockIdx.y * blockDim.y + threadIdx.y + 1; j <= L.ny; j += gridDim.y * blockDim.y) {
             const double dyz = dyy[j] + dz;
             for (int i0 = blockIdx.x * (blockDim.x * kOuterVec) + threadIdx.x + 1; i0 <= L.nx;
                  i0 += gridDim.x * blockDim.x * kOuterVec) {
-                if constexpr (ZS) {
-                    // b is loaded together with x, so the zero test costs no second round
-                    // trip to memory
+                if (zero_x) {
                     double bv[kOuterVec];
 #pragma unroll
                     for (int u = 0; u < kOuterVec; ++u) {
                         const int i = i0 + u * kBX;
                         bv[u] = i <= L.nx ? b[lin(i, j, k, L.sy, L.sz)] : 0.0;
                     }
-                    if (x_zero_around(L, x, i0, j, k)) {
-                        // x is exactly +0 at these cells and their neighbours: every product
-                        // of the FMA chain is a signed zero and the chain returns b + 0
 #pragma unroll
-                        for (int u = 0; u < kOuterVec; ++u) {
-                            const int i = i0 + u * kBX;
-                            if (i > L.nx) break;
-                            const long long p = lin(i, j, k, L.sy, L.sz);
-                            const double v = __dadd_rn(bv[u], 0.0);
-                            r[p] = v;
-                            r32[lin(i, j, k, sy32, sz32)] = f64_to_f32_rn(v);
-                            acc = fma(v, v, acc);
-                        }
-                    } else {
-#pragma unroll
-                        for (int u = 0; u < kOuterVec; ++u) {
-                            const int i = i0 + u * kBX;
-                            if (i > L.nx) break;
-                            const long long p = lin(i, j, k, L.sy, L.sz);
-                            const double v = outer_residual_cell_b(L, dyz, x, bv[u], i, j, k, p);
-                            r[p] = v;
-                            r32[lin(i, j, k, sy32, sz32)] = f64_to_f32_rn(v);
-                            acc = fma(v, v, acc);
-                        }
+                    for (int u = 0; u < kOuterVec; ++u) {
+                        const int i = i0 + u * kBX;
+                        if (i > L.nx) break;
+                        const double v = __dadd_rn(bv[u], 0.0);
+                        r[lin(i, j, k, L.sy, L.sz)] = v;
+                        r32[lin(i, j, k, sy32, sz32)] = f64_to_f32_rn(v);
+                        acc = fma(v, v, acc);
                     }
                 } else {
 #pragma unroll
@@ -717,14 +696,22 @@ int Ctx::outer_residual(double *sol, double *rsd, const double *rhs, int slot)
 {
     const LevelK<double> &L = K[0];
     const dim3 g = grid_outer(L, launch[0]), bl(kBX, kBY, 1);
+    int *nonzero = d_iscal + 3;
+    if (slot == 0) {
+        // the first residual of a solve: is the initial guess exactly zero?
+        PMG_TRY_M(mstatus(cudaMemsetAsync(nonzero, 0, sizeof(int), stream), "zero test"));
+        const long long n = (long long)lv[0].total;
+        k_nonzero_f64<<<(unsigned)std::max<long long>(1, std::min<long long>((n + 1023) / 1024, 4096)), 256, 0,
+                        stream>>>(sol, n, nonzero);
+        count_launches(1);
+    }
     const int pi = prof.begin(stream);
-    // the first residual of a solve (slot 0) checks for a zero initial guess
     if (slot == 0)
         k_outer_residual<true><<<g, bl, 0, stream>>>(L, mixed->dyy[0], mixed->dzz[0], sol, rhs, rsd, mixed->b[0],
-                                                     mixed->K[0].sy, mixed->K[0].sz, d_partials);
+                                                     mixed->K[0].sy, mixed->K[0].sz, d_partials, nonzero);
     else
         k_outer_residual<false><<<g, bl, 0, stream>>>(L, mixed->dyy[0], mixed->dzz[0], sol, rhs, rsd, mixed->b[0],
-                                                      mixed->K[0].sy, mixed->K[0].sz, d_partials);
+                                                      mixed->K[0].sy, mixed->K[0].sz, d_partials, nonzero);
     prof.end(pi, PC_OUTER_RES, 1, 28.0 * (double)L.nx * L.ny * L.nz, stream);
     count_launches(1);
     PMG_TRY_M(cuda_status(cudaGetLastError(), "outer residual"));
