@@ -153,15 +153,30 @@ constexpr int kOuterVec = 4;
 // *flag |= 1 unless every value of x (ghosts included) is +0 (all bits clear).
 __global__ void __launch_bounds__(256) k_nonzero_f64(const double *__restrict__ x, long long n, int *flag)
 {
+    const unsigned long long *u = reinterpret_cast<const unsigned long long *>(x);
     unsigned long long bits = 0ull;
     const long long stride = (long long)gridDim.x * blockDim.x;
     long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-    for (; q + 3 * stride < n; q += 4 * stride)
-        bits |= (unsigned long long)__double_as_longlong(x[q]) | (unsigned long long)__double_as_longlong(x[q + stride]) |
-                (unsigned long long)__double_as_longlong(x[q + 2 * stride]) |
-                (unsigned long long)__double_as_longlong(x[q + 3 * stride]);
-    for (; q < n; q += stride) bits |= (unsigned long long)__double_as_longlong(x[q]);
+    for (; q + 7 * stride < n; q += 8 * stride) {
+        unsigned long long v[8];
+#pragma unroll
+        for (int t = 0; t < 8; ++t) v[t] = __ldg(u + q + t * stride);
+#pragma unroll
+        for (int t = 0; t < 8; ++t) bits |= v[t];
+    }
+    for (; q < n; q += stride) bits |= __ldg(u + q);
     if (__syncthreads_or(bits != 0ull) && threadIdx.x == 0) atomicOr(flag, 1);
+}
+
+// b + 0 on the integer pipe for every b that is not a NaN (-0 becomes +0, every other
+// value is unchanged); a NaN stays a (quiet) NaN.
+__device__ __forceinline__ double plus_zero(double b)
+{
+    unsigned long long u = (unsigned long long)__double_as_longlong(b);
+    if (u == 0x8000000000000000ull) u = 0ull;
+    if ((u & 0x7ff0000000000000ull) == 0x7ff0000000000000ull && (u & 0x000fffffffffffffull))
+        u |= 0x0008000000000000ull;
+    return __longlong_as_double((long long)u);
 }
 
 // ZS (the first residual of a solve): *nonzero, set by k_nonzero_f64, tells whether the
@@ -194,7 +209,7 @@ __global__ void __launch_bounds__(kBX *kBY) k_outer_residual(LevelK<double> L, c
                     for (int u = 0; u < kOuterVec; ++u) {
                         const int i = i0 + u * kBX;
                         if (i > L.nx) break;
-                        const double v = __dadd_rn(bv[u], 0.0);
+                        const double v = plus_zero(bv[u]);
                         r[lin(i, j, k, L.sy, L.sz)] = v;
                         r32[lin(i, j, k, sy32, sz32)] = f64_to_f32_rn(v);
                         acc = fma(v, v, acc);
