@@ -254,7 +254,6 @@ def run_ours(args):
     barrier()
     clocks = ClockSampler(local)
     clocks.start()
-    mg.profile(True)
     l0 = pmg.launch_count()
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
@@ -267,9 +266,14 @@ def run_ours(args):
     barrier()
     launches = pmg.launch_count() - l0
     ms = e0.elapsed_time(e1) / args.steps
+    clk = clocks.stop()
+    # per-kernel-class breakdown from separate solves with the library's event profiler on
+    # (its events are not inside the timed region)
+    mg.profile(True)
+    for _ in range(args.steps):
+        step()
     prof = {pmg.PROF_CLASSES[c]: mg.profile_read(c) for c in pmg.PROF_CLASSES}
     mg.profile(False)
-    clk = clocks.stop()
     ms = max_over_ranks(ms, world, dev)
     rep = reps[-1]
     assert rep.converged and rep.final_ratio < TOL, "solve did not converge"
@@ -278,6 +282,7 @@ def run_ours(args):
         if rank == 0:
             print(json.dumps({"metric": METRIC, "value": round(ms, 3), "unit": "ms", "quick": True, "n": n,
                               "precision": prec, "cycles": rep.cycles,
+                              "ratios": [float(v) for v in rep.history[:, 2]],
                               "coarse_iterations": [int(v) for v in rep.coarse_iterations],
                               "kernels": {k: v for k, v in prof.items() if v[1]}, "gpu_launches": launches}))
         mg.destroy()
