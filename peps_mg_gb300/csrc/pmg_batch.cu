@@ -60,6 +60,7 @@ struct BOuter {
     long long sz32;
     float *r32;
     float *e0;             // the depth-0 correction buffer the V-cycle leaves its result in
+    SplitCoef sc;          // coefficients as FP32 pairs (residual update)
 };
 
 struct Item {
@@ -189,15 +190,17 @@ __global__ void __launch_bounds__(NTB) k_batch_prolong(const BLevel *__restrict_
 }
 
 // ---- outer FP64 kernels: one item per fine plane ------------------------------------------
+// check (NULL: every problem): the problems whose residual is recomputed
 __global__ void __launch_bounds__(NTB) k_batch_outer_residual(const BOuter *__restrict__ po,
                                                               const Item *__restrict__ items, int nitems,
                                                               double *__restrict__ partials,
-                                                              const int *__restrict__ done)
+                                                              const int *__restrict__ done,
+                                                              const int *__restrict__ check)
 {
     __shared__ double sw[NTB / 32];
     for (int it = blockIdx.x; it < nitems; it += gridDim.x) {
         const Item w = items[it];
-        if (done[w.p]) continue;       // uniform over the block
+        if (done[w.p] || (check && !check[w.p])) continue;       // uniform over the block
         const BOuter &O = po[w.p];
         const LevelK<double> L = O.L;
         const int k = w.k0;
@@ -216,37 +219,109 @@ __global__ void __launch_bounds__(NTB) k_batch_outer_residual(const BOuter *__re
     }
 }
 
-__global__ void __launch_bounds__(NTB) k_batch_add_correction(const BOuter *__restrict__ po,
-                                                              const Item *__restrict__ items, int nitems,
-                                                              const int *__restrict__ done)
+// After the V-cycles of a correction, per fine plane: x += e, and for problems in update
+// mode (mode 0) also r -= A e with A e in compensated FP32 arithmetic (comp_term), the
+// FP32 copy of r and the plane's partial norm (FP32 sum of the squares scaled by a power
+// of two set by the problem's initial residual; it only decides whether the residual is
+// recomputed).  Problems in mode 1 get the FP64 residual recomputed after this.
+__global__ void __launch_bounds__(NTB) k_batch_correct(const BOuter *__restrict__ po, const Item *__restrict__ items,
+                                                       int nitems, double *__restrict__ partials,
+                                                       const int *__restrict__ done, const int *__restrict__ mode,
+                                                       const double *__restrict__ res0)
 {
+    __shared__ double sw[NTB / 32];
     for (int it = blockIdx.x; it < nitems; it += gridDim.x) {
         const Item w = items[it];
         if (done[w.p]) continue;
         const BOuter &O = po[w.p];
         const LevelK<double> L = O.L;
         const int k = w.k0;
+        if (mode[w.p]) {
+            for (int q = threadIdx.x; q < L.nx * L.ny; q += NTB) {
+                const int i = q % L.nx + 1, j = q / L.nx + 1;
+                const long long p = lin(i, j, k, L.sy, L.sz);
+                O.sol[p] = O.sol[p] + f32_to_f64(O.e0[lin(i, j, k, O.sy32, O.sz32)]);
+            }
+            continue;
+        }
+        const double rms0 = sqrt(res0[w.p] / ((double)L.nx * L.ny * L.nz));
+        const int ex = rms0 > 0.0 && rms0 < 1e300 ? max(-100, min(100, ilogb(rms0))) : 0;
+        const float nscale = ldexpf(1.0f, -ex);
+        const SplitCoef C = O.sc;
+        const float2 czm = C.czm[k], czp = C.czp[k];
+        const float *e = O.e0;
+        float acc32 = 0.f;
         for (int q = threadIdx.x; q < L.nx * L.ny; q += NTB) {
             const int i = q % L.nx + 1, j = q / L.nx + 1;
-            const long long p = lin(i, j, k, L.sy, L.sz);
-            O.sol[p] = O.sol[p] + f32_to_f64(O.e0[lin(i, j, k, O.sy32, O.sz32)]);
+            const long long p = lin(i, j, k, L.sy, L.sz), c = lin(i, j, k, O.sy32, O.sz32);
+            const float ec = e[c];
+            float S = 0.f, Sl = 0.f;
+            comp_term(C.cxm[i], e[c - 1], ec, S, Sl);
+            comp_term(C.cxp[i], e[c + 1], ec, S, Sl);
+            comp_term(C.cym[j], e[c - O.sy32], ec, S, Sl);
+            comp_term(C.cyp[j], e[c + O.sy32], ec, S, Sl);
+            comp_term(czm, e[c - O.sz32], ec, S, Sl);
+            comp_term(czp, e[c + O.sz32], ec, S, Sl);
+            O.sol[p] = O.sol[p] + f32_to_f64(ec);
+            const double v = __dsub_rn(__dsub_rn(O.rsd[p], f32_to_f64(S)), f32_to_f64(Sl));
+            O.rsd[p] = v;
+            const float v32 = f64_to_f32_rn(v);
+            O.r32[c] = v32;
+            const float wv = v32 * nscale;
+            acc32 = fmaf(wv, wv, acc32);
         }
+        const double s = block_sum((double)acc32 / ((double)nscale * (double)nscale), sw);
+        if (threadIdx.x == 0) partials[it] = s;
+    }
+}
+
+// After k_batch_correct: the updated residual's ratio of every problem in update mode;
+// check[p] = 1 where the FP64 residual is recomputed next: mode 1, an updated ratio below
+// the tolerance (or not finite), or the last allowed correction.
+__global__ void __launch_bounds__(NTB) k_batch_norms_update(const double *__restrict__ partials,
+                                                            const int *__restrict__ first_item,
+                                                            const double *__restrict__ res0,
+                                                            const int *__restrict__ done, const int *__restrict__ mode,
+                                                            const int *__restrict__ cycles, int *__restrict__ check,
+                                                            double *__restrict__ cheap, double tol, int max_cycles)
+{
+    __shared__ double sw[NTB / 32];
+    const int p = blockIdx.x;
+    if (done[p]) return;
+    if (mode[p]) {
+        if (threadIdx.x == 0) check[p] = 1;
+        return;
+    }
+    double acc = 0.0;
+    for (int q = first_item[p] + threadIdx.x; q < first_item[p + 1]; q += NTB) acc += partials[q];
+    const double s = block_sum(acc, sw);
+    if (threadIdx.x == 0) {
+        const double r = sqrt(s / res0[p]);
+        cheap[p] = r;
+        check[p] = (r < tol || !(r == r) || cycles[p] + 1 >= max_cycles) ? 1 : 0;
     }
 }
 
 // per problem: norm = sum of its items' partials in item order; first = 1 stores res0,
 // else the ratio test of src/multigrid.f90:1973 updates done/cycles/ratio.
+// Only a recomputed FP64 residual (check[p]) ends a problem; after an update alone the
+// ratio is the updated one.  The contraction of the last correction predicts the next:
+// where it would pass the tolerance by a factor of 10, the next correction recomputes
+// the FP64 residual directly (mode 1) instead of updating it first.
 __global__ void __launch_bounds__(NTB) k_batch_norms(const double *__restrict__ partials,
                                                      const int *__restrict__ first_item, double *__restrict__ res0,
                                                      double *__restrict__ ratio, int *__restrict__ done,
                                                      int *__restrict__ cycles, int *__restrict__ ndone, double tol,
-                                                     int first)
+                                                     int first, const int *__restrict__ check,
+                                                     const double *__restrict__ cheap, int *__restrict__ mode,
+                                                     double *__restrict__ prev, double *__restrict__ contraction)
 {
     __shared__ double sw[NTB / 32];
     const int p = blockIdx.x;
     if (!first && done[p]) return;
     double acc = 0.0;
-    for (int q = first_item[p] + threadIdx.x; q < first_item[p + 1]; q += NTB) acc += partials[q];
+    if (first || check[p])
+        for (int q = first_item[p] + threadIdx.x; q < first_item[p + 1]; q += NTB) acc += partials[q];
     const double s = block_sum(acc, sw);
     if (threadIdx.x == 0) {
         if (first) {
@@ -254,14 +329,21 @@ __global__ void __launch_bounds__(NTB) k_batch_norms(const double *__restrict__ 
             ratio[p] = 1.0;
             cycles[p] = 0;
             done[p] = 0;
+            mode[p] = 0;
+            prev[p] = 1.0;
+            contraction[p] = 1.0;
         } else {
-            const double r = sqrt(s / res0[p]);
+            const double r = check[p] ? sqrt(s / res0[p]) : cheap[p];
             ratio[p] = r;
             cycles[p] += 1;
-            if (r < tol || !(r == r)) {
+            if (check[p] && (r < tol || !(r == r))) {
                 done[p] = 1;
                 atomicAdd(ndone, 1);
             }
+            const double c = r / prev[p];
+            contraction[p] = c;
+            prev[p] = r;
+            mode[p] = r * c < 0.1 * tol ? 1 : 0;
         }
     }
 }
@@ -294,6 +376,11 @@ struct Batch {
     int *d_first = nullptr;
     double *d_partials = nullptr, *d_res0 = nullptr, *d_ratio = nullptr;
     int *d_done = nullptr, *d_cycles = nullptr, *d_ndone = nullptr;
+    // residual update state per problem: mode (1: recompute directly), check (recompute
+    // after this correction's update), updated ratio, previous ratio, last contraction
+    int *d_mode = nullptr, *d_check = nullptr;
+    double *d_cheap = nullptr, *d_prev = nullptr, *d_contr = nullptr;
+    int graph_maxcyc = -1;
     double *rsd = nullptr;                  // packed FP64 residual
     const TailDesc<float> **d_tails = nullptr;
     int tail_threads = 64;
@@ -324,6 +411,11 @@ Batch::~Batch()
     cudaFree(d_ratio);
     cudaFree(d_done);
     cudaFree(d_cycles);
+    cudaFree(d_mode);
+    cudaFree(d_check);
+    cudaFree(d_cheap);
+    cudaFree(d_prev);
+    cudaFree(d_contr);
     cudaFree(d_ndone);
     cudaFree(rsd);
     cudaFree(d_tails);
@@ -635,6 +727,12 @@ int batch_create(Batch **out, int n, const int *dims, const double *const *meshe
     PMG_TRY_B(cuda_status(cudaMalloc(&B->d_done, n * sizeof(int)), "batch allocation"));
     PMG_TRY_B(cuda_status(cudaMemset(B->d_done, 0, n * sizeof(int)), "batch init"));
     PMG_TRY_B(cuda_status(cudaMalloc(&B->d_cycles, n * sizeof(int)), "batch allocation"));
+    PMG_TRY_B(cuda_status(cudaMalloc(&B->d_mode, n * sizeof(int)), "batch allocation"));
+    PMG_TRY_B(cuda_status(cudaMalloc(&B->d_check, n * sizeof(int)), "batch allocation"));
+    PMG_TRY_B(cuda_status(cudaMalloc(&B->d_cheap, n * sizeof(double)), "batch allocation"));
+    PMG_TRY_B(cuda_status(cudaMalloc(&B->d_prev, n * sizeof(double)), "batch allocation"));
+    PMG_TRY_B(cuda_status(cudaMalloc(&B->d_contr, n * sizeof(double)), "batch allocation"));
+    PMG_TRY_B(cuda_status(cudaMemset(B->d_check, 0, n * sizeof(int)), "batch init"));
     PMG_TRY_B(cuda_status(cudaMalloc(&B->d_ndone, sizeof(int)), "batch allocation"));
     PMG_TRY_B(cuda_status(cudaMalloc(&B->rsd, (size_t)B->total * sizeof(double)), "batch allocation"));
     PMG_TRY_B(cuda_status(cudaMemset(B->rsd, 0, (size_t)B->total * sizeof(double)), "batch init"));
@@ -717,18 +815,31 @@ static void batch_vcycle(Batch &B, int maxit, float om, float omw, bool zero_sta
     }
 }
 
-static void batch_outer(Batch &B, bool first, double tol)
+// The outer step of a correction (first: the initial residual only).  After the
+// V-cycles: x += e with the residual updated (or, in mode 1, left for the recompute), the
+// updated ratios, the FP64 residual b - A x recomputed for the problems that may end here,
+// and the ratios, convergence flags and next modes.
+static void batch_outer(Batch &B, bool first, double tol, int max_cycles)
 {
     const int n = B.n;
-    if (!first) {
-        k_batch_add_correction<<<grid_for(B.outer.n), NTB, 0, B.stream>>>(B.d_outer, B.outer.d, B.outer.n, B.d_done);
-        count_launches(1);
+    if (first) {
+        k_batch_outer_residual<<<grid_for(B.outer.n), NTB, 0, B.stream>>>(B.d_outer, B.outer.d, B.outer.n,
+                                                                          B.d_partials, B.d_done, nullptr);
+        k_batch_norms<<<n, NTB, 0, B.stream>>>(B.d_partials, B.d_first, B.d_res0, B.d_ratio, B.d_done, B.d_cycles,
+                                               B.d_ndone, tol, 1, B.d_check, B.d_cheap, B.d_mode, B.d_prev,
+                                               B.d_contr);
+        count_launches(2);
+        return;
     }
+    k_batch_correct<<<grid_for(B.outer.n), NTB, 0, B.stream>>>(B.d_outer, B.outer.d, B.outer.n, B.d_partials,
+                                                               B.d_done, B.d_mode, B.d_res0);
+    k_batch_norms_update<<<n, NTB, 0, B.stream>>>(B.d_partials, B.d_first, B.d_res0, B.d_done, B.d_mode, B.d_cycles,
+                                                  B.d_check, B.d_cheap, tol, max_cycles);
     k_batch_outer_residual<<<grid_for(B.outer.n), NTB, 0, B.stream>>>(B.d_outer, B.outer.d, B.outer.n, B.d_partials,
-                                                                      B.d_done);
+                                                                      B.d_done, B.d_check);
     k_batch_norms<<<n, NTB, 0, B.stream>>>(B.d_partials, B.d_first, B.d_res0, B.d_ratio, B.d_done, B.d_cycles,
-                                           B.d_ndone, tol, first ? 1 : 0);
-    count_launches(2);
+                                           B.d_ndone, tol, 0, B.d_check, B.d_cheap, B.d_mode, B.d_prev, B.d_contr);
+    count_launches(4);
 }
 
 int batch_solve(Batch &B, double *sol, const double *rhs, int maxit, double tol, double omega, int max_cycles,
@@ -762,6 +873,7 @@ int batch_solve(Batch &B, double *sol, const double *rhs, int maxit, double tol,
         o.sol = sol + B.offset[p];
         o.rhs = rhs + B.offset[p];
         o.rsd = B.rsd + B.offset[p];
+        o.sc = c.mixed->sc;
         if (std::memcmp(&o, &B.h_outer[p], sizeof(BOuter)) != 0) changed = true;
         B.h_outer[p] = o;
         PMG_TRY_B(c.upload_tail32(maxit, omega, tol));
@@ -772,20 +884,22 @@ int batch_solve(Batch &B, double *sol, const double *rhs, int maxit, double tol,
     if (B.variant[0] < 0) PMG_TRY_B(batch_autotune(B));
     PMG_TRY_B(cuda_status(cudaMemsetAsync(B.d_ndone, 0, sizeof(int), B.stream), "batch init"));
     PMG_TRY_B(cuda_status(cudaMemsetAsync(B.d_done, 0, n * sizeof(int), B.stream), "batch init"));
-    batch_outer(B, true, tol);
+    batch_outer(B, true, tol, max_cycles);
     const float om = (float)omega, omw = (float)(1.0 - omega);
-    if (!B.graph || B.graph_maxit != maxit || B.graph_omega != omega || B.graph_tol != tol || changed) {
+    if (!B.graph || B.graph_maxit != maxit || B.graph_omega != omega || B.graph_tol != tol ||
+        B.graph_maxcyc != max_cycles || changed) {
         if (B.graph) cudaGraphExecDestroy(B.graph);
         B.graph = nullptr;
         cudaGraph_t g;
         PMG_TRY_B(cuda_status(cudaStreamBeginCapture(B.stream, cudaStreamCaptureModeThreadLocal), "graph capture"));
         for (int q = 0; q < B.inner; ++q) batch_vcycle(B, maxit, om, omw, q == 0);
-        batch_outer(B, false, tol);
+        batch_outer(B, false, tol, max_cycles);
         PMG_TRY_B(cuda_status(cudaStreamEndCapture(B.stream, &g), "graph capture"));
         const cudaError_t ie = cudaGraphInstantiate(&B.graph, g, 0);
         cudaGraphDestroy(g);
         PMG_TRY_B(cuda_status(ie, "graph instantiate"));
         B.graph_maxit = maxit;
+        B.graph_maxcyc = max_cycles;
         B.graph_omega = omega;
         B.graph_tol = tol;
     }
