@@ -190,12 +190,29 @@ __global__ void __launch_bounds__(NTB) k_batch_prolong(const BLevel *__restrict_
 }
 
 // ---- outer FP64 kernels: one item per fine plane ------------------------------------------
-// check (NULL: every problem): the problems whose residual is recomputed
+// nonzero[p] |= 1 unless problem p's initial guess (its whole packed range, ghosts
+// included) is +0 everywhere; grid (blocks per problem, problems).
+__global__ void __launch_bounds__(NTB) k_batch_nonzero(const double *__restrict__ sol,
+                                                       const long long *__restrict__ offset, int *__restrict__ nonzero)
+{
+    const int p = blockIdx.y;
+    const unsigned long long *u = reinterpret_cast<const unsigned long long *>(sol);
+    unsigned long long bits = 0ull;
+    for (long long q = offset[p] + blockIdx.x * (long long)NTB + threadIdx.x; q < offset[p + 1];
+         q += (long long)gridDim.x * NTB)
+        bits |= __ldg(u + q);
+    if (__syncthreads_or(bits != 0ull) && threadIdx.x == 0) atomicOr(nonzero + p, 1);
+}
+
+// check (NULL: every problem): the problems whose residual is recomputed.  nonzero
+// (non-NULL for the first residual of a solve): where a problem's initial guess is zero,
+// every product of the FMA chain is a signed zero and the chain returns b + 0.
 __global__ void __launch_bounds__(NTB) k_batch_outer_residual(const BOuter *__restrict__ po,
                                                               const Item *__restrict__ items, int nitems,
                                                               double *__restrict__ partials,
                                                               const int *__restrict__ done,
-                                                              const int *__restrict__ check)
+                                                              const int *__restrict__ check,
+                                                              const int *__restrict__ nonzero)
 {
     __shared__ double sw[NTB / 32];
     for (int it = blockIdx.x; it < nitems; it += gridDim.x) {
@@ -206,6 +223,19 @@ __global__ void __launch_bounds__(NTB) k_batch_outer_residual(const BOuter *__re
         const int k = w.k0;
         const double dz = O.dzz[k];
         double acc = 0.0;
+        if (nonzero && !nonzero[w.p]) {
+            for (int q = threadIdx.x; q < L.nx * L.ny; q += NTB) {
+                const int i = q % L.nx + 1, j = q / L.nx + 1;
+                const long long p = lin(i, j, k, L.sy, L.sz);
+                const double v = plus_zero(O.rhs[p]);
+                O.rsd[p] = v;
+                O.r32[lin(i, j, k, O.sy32, O.sz32)] = f64_to_f32_rn(v);
+                acc = fma(v, v, acc);
+            }
+            const double s = block_sum(acc, sw);
+            if (threadIdx.x == 0) partials[it] = s;
+            continue;
+        }
         for (int q = threadIdx.x; q < L.nx * L.ny; q += NTB) {
             const int i = q % L.nx + 1, j = q / L.nx + 1;
             const long long p = lin(i, j, k, L.sy, L.sz);
@@ -379,6 +409,9 @@ struct Batch {
     // residual update state per problem: mode (1: recompute directly), check (recompute
     // after this correction's update), updated ratio, previous ratio, last contraction
     int *d_mode = nullptr, *d_check = nullptr;
+    int *d_nonzero = nullptr;               // per problem: the initial guess has a non-zero value
+    long long *d_offset = nullptr;          // device copy of offset
+    const double *cur_sol = nullptr;        // the packed solution of the running solve
     double *d_cheap = nullptr, *d_prev = nullptr, *d_contr = nullptr;
     int graph_maxcyc = -1;
     double *rsd = nullptr;                  // packed FP64 residual
@@ -412,6 +445,8 @@ Batch::~Batch()
     cudaFree(d_done);
     cudaFree(d_cycles);
     cudaFree(d_mode);
+    cudaFree(d_nonzero);
+    cudaFree(d_offset);
     cudaFree(d_check);
     cudaFree(d_cheap);
     cudaFree(d_prev);
@@ -728,6 +763,10 @@ int batch_create(Batch **out, int n, const int *dims, const double *const *meshe
     PMG_TRY_B(cuda_status(cudaMemset(B->d_done, 0, n * sizeof(int)), "batch init"));
     PMG_TRY_B(cuda_status(cudaMalloc(&B->d_cycles, n * sizeof(int)), "batch allocation"));
     PMG_TRY_B(cuda_status(cudaMalloc(&B->d_mode, n * sizeof(int)), "batch allocation"));
+    PMG_TRY_B(cuda_status(cudaMalloc(&B->d_nonzero, n * sizeof(int)), "batch allocation"));
+    PMG_TRY_B(cuda_status(cudaMalloc(&B->d_offset, (n + 1) * sizeof(long long)), "batch allocation"));
+    PMG_TRY_B(cuda_status(cudaMemcpy(B->d_offset, B->offset.data(), (n + 1) * sizeof(long long),
+                                     cudaMemcpyHostToDevice), "batch upload"));
     PMG_TRY_B(cuda_status(cudaMalloc(&B->d_check, n * sizeof(int)), "batch allocation"));
     PMG_TRY_B(cuda_status(cudaMalloc(&B->d_cheap, n * sizeof(double)), "batch allocation"));
     PMG_TRY_B(cuda_status(cudaMalloc(&B->d_prev, n * sizeof(double)), "batch allocation"));
@@ -823,12 +862,15 @@ static void batch_outer(Batch &B, bool first, double tol, int max_cycles)
 {
     const int n = B.n;
     if (first) {
+        cudaMemsetAsync(B.d_nonzero, 0, n * sizeof(int), B.stream);
+        k_batch_nonzero<<<dim3(8, (unsigned)n), NTB, 0, B.stream>>>(B.cur_sol, B.d_offset, B.d_nonzero);
         k_batch_outer_residual<<<grid_for(B.outer.n), NTB, 0, B.stream>>>(B.d_outer, B.outer.d, B.outer.n,
-                                                                          B.d_partials, B.d_done, nullptr);
+                                                                          B.d_partials, B.d_done, nullptr,
+                                                                          B.d_nonzero);
         k_batch_norms<<<n, NTB, 0, B.stream>>>(B.d_partials, B.d_first, B.d_res0, B.d_ratio, B.d_done, B.d_cycles,
                                                B.d_ndone, tol, 1, B.d_check, B.d_cheap, B.d_mode, B.d_prev,
                                                B.d_contr);
-        count_launches(2);
+        count_launches(3);
         return;
     }
     k_batch_correct<<<grid_for(B.outer.n), NTB, 0, B.stream>>>(B.d_outer, B.outer.d, B.outer.n, B.d_partials,
@@ -836,7 +878,7 @@ static void batch_outer(Batch &B, bool first, double tol, int max_cycles)
     k_batch_norms_update<<<n, NTB, 0, B.stream>>>(B.d_partials, B.d_first, B.d_res0, B.d_done, B.d_mode, B.d_cycles,
                                                   B.d_check, B.d_cheap, tol, max_cycles);
     k_batch_outer_residual<<<grid_for(B.outer.n), NTB, 0, B.stream>>>(B.d_outer, B.outer.d, B.outer.n, B.d_partials,
-                                                                      B.d_done, B.d_check);
+                                                                      B.d_done, B.d_check, nullptr);
     k_batch_norms<<<n, NTB, 0, B.stream>>>(B.d_partials, B.d_first, B.d_res0, B.d_ratio, B.d_done, B.d_cycles,
                                            B.d_ndone, tol, 0, B.d_check, B.d_cheap, B.d_mode, B.d_prev, B.d_contr);
     count_launches(4);
@@ -884,6 +926,7 @@ int batch_solve(Batch &B, double *sol, const double *rhs, int maxit, double tol,
     if (B.variant[0] < 0) PMG_TRY_B(batch_autotune(B));
     PMG_TRY_B(cuda_status(cudaMemsetAsync(B.d_ndone, 0, sizeof(int), B.stream), "batch init"));
     PMG_TRY_B(cuda_status(cudaMemsetAsync(B.d_done, 0, n * sizeof(int), B.stream), "batch init"));
+    B.cur_sol = sol;
     batch_outer(B, true, tol, max_cycles);
     const float om = (float)omega, omw = (float)(1.0 - omega);
     if (!B.graph || B.graph_maxit != maxit || B.graph_omega != omega || B.graph_tol != tol ||

@@ -391,6 +391,17 @@ __device__ __forceinline__ double f32_to_f64(float f)
     return __longlong_as_double((long long)bits);
 }
 
+// b + 0 on the integer pipe for every b that is not a NaN (-0 becomes +0, every other
+// value is unchanged); a NaN stays a (quiet) NaN.
+__device__ __forceinline__ double plus_zero(double b)
+{
+    unsigned long long u = (unsigned long long)__double_as_longlong(b);
+    if (u == 0x8000000000000000ull) u = 0ull;
+    if ((u & 0x7ff0000000000000ull) == 0x7ff0000000000000ull && (u & 0x000fffffffffffffull))
+        u |= 0x0008000000000000ull;
+    return __longlong_as_double((long long)u);
+}
+
 // r(i,j,k) = b - A x in FP64, FMA form r = b + d x - sum c x_nb with d = -c0 = sx(i) + dyz
 // (the per-axis diagonal sums), as the outer residual of the mixed solver.
 __device__ __forceinline__ double outer_residual_cell_b(const LevelK<double> &L, double dyz, const double *x,

@@ -168,16 +168,6 @@ __global__ void __launch_bounds__(256) k_nonzero_f64(const double *__restrict__ 
     if (__syncthreads_or(bits != 0ull) && threadIdx.x == 0) atomicOr(flag, 1);
 }
 
-// b + 0 on the integer pipe for every b that is not a NaN (-0 becomes +0, every other
-// value is unchanged); a NaN stays a (quiet) NaN.
-__device__ __forceinline__ double plus_zero(double b)
-{
-    unsigned long long u = (unsigned long long)__double_as_longlong(b);
-    if (u == 0x8000000000000000ull) u = 0ull;
-    if ((u & 0x7ff0000000000000ull) == 0x7ff0000000000000ull && (u & 0x000fffffffffffffull))
-        u |= 0x0008000000000000ull;
-    return __longlong_as_double((long long)u);
-}
 
 // ZS (the first residual of a solve): *nonzero, set by k_nonzero_f64, tells whether the
 // initial guess has a non-zero value; where it has none, every product of the FMA chain

@@ -51,6 +51,33 @@ def test_batch_matches_single_problem_solves():
             assert rel(from_dev(bs.view(sol, p)), from_dev(s1)) < 1e-8
 
 
+def test_batch_nonzero_initial_guess():
+    """Problems whose initial guess is not zero (interior values, or a Dirichlet ghost face)
+    next to problems that start from zero: the first residual takes the full FP64 stencil
+    only for the former, and every problem matches its single-problem solve."""
+    dims = batch_dims(6, [16, 24, 32], seed=7)
+    with BatchSolver(dims) as bs:
+        rhs = fill(bs, seed=7)
+        sol = bs.field()
+        rng = np.random.default_rng(3)
+        starts = []
+        for p in range(bs.n):
+            v = bs.view(sol, p)
+            if p % 3 == 1:
+                v[1:-1, 1:-1, 1:-1] = torch.from_numpy(rng.uniform(-0.1, 0.1, tuple(s - 2 for s in v.shape))).cuda()
+            elif p % 3 == 2:
+                v[:, :, 0] = 0.25
+            starts.append(v.clone())
+        cycles, ratio, _ = bs.solve(sol, rhs, 2, 1e-10, 1.0, max_cycles=60)
+        assert np.all(ratio < 1e-10), ratio
+        for p in range(bs.n):
+            with pmg.Multigrid(bs.mesh(p), int(bs.levels[p]), 60, "cgs", precision="mixed") as mg:
+                s1 = starts[p].clone()
+                r1 = torch.zeros_like(s1)
+                mg.solve_vcycle(s1, r1, bs.view(rhs, p).contiguous(), 2, 1e-10, 1.0)
+            assert rel(from_dev(bs.view(sol, p)), from_dev(s1)) < 1e-8, p
+
+
 def test_batch_against_fp64_oracle_sample():
     dims = batch_dims(6, [16, 24, 32], seed=11)
     with BatchSolver(dims) as bs:
