@@ -183,10 +183,11 @@ __device__ int coarse_solve_f64(const LevelK<double> &L, double *x, const double
 }
 
 // Coarsest-level solve by ONE warp on a level held in shared memory (at most
-// kWarpCoarseMax stored values, ghosts included): the per-cell arithmetic of
-// coarse_solve_f64 (rbgs_cell_f64 / ax_cell_f64, the same exit tests), the sums in a
-// 32-lane butterfly order (every lane obtains the same bits, so the exit decision is
-// uniform), and __syncwarp instead of block barriers.  x, b, p, ap, rr are shared
+// kWarpCoarseMax stored values, ghosts included), for the FP32 cycle of the mixed solver:
+// the iterations of coarse_solve_f64 (RBGS or CG, the same exit tests; levels of at most
+// 64 cells take a register fast path with reordered arithmetic), the sums in a 32-lane
+// butterfly order (every lane obtains the same bits, so the exit decision is uniform),
+// and __syncwarp instead of block barriers.  x, b, p, ap, rr are shared
 // arrays of the level's layout; only the calling warp touches them.
 constexpr int kWarpCoarseMax = 1000;
 
@@ -257,11 +258,15 @@ __device__ int coarse_solve_warp_f64(const LevelK<double> &L, double *x, const d
     };
     int it = 0;
     if (solver == 0 && n <= 64) {
-        // at most two cells per lane: their offsets, coefficients, 1/c0 and b stay in
-        // registers, so an iteration is a few shared-memory loads and FP64 FMA chains
-        // (the update multiplies by 1/c0 instead of dividing by c0)
+        // at most two cells per lane: their offsets, coefficients, omega/c0 and b stay in
+        // registers.  Each dependent FP64 operation costs on the order of a hundred
+        // cycles here, so the arithmetic is arranged for short chains: the neighbour sum
+        // as a tree of FMAs, the update x = (omega/c0)(b - t) + (1-omega) x, and the exit
+        // test sqrt(|r|^2/|r0|^2) <= tol as |r|^2 <= tol^2 |r0|^2 (no division or square
+        // root per iteration).  The same RBGS iteration as the reference's solver; the
+        // FP32 cycle that calls it is not bound to the reference's bits.
         long long cidx[2];
-        double cw[2][6], c0v[2], ic0[2], bv[2];
+        double cw[2][6], c0v[2], wv[2], bv[2];
         bool has[2], odd[2];
 #pragma unroll
         for (int u = 0; u < 2; ++u) {
@@ -278,30 +283,29 @@ __device__ int coarse_solve_warp_f64(const LevelK<double> &L, double *x, const d
             cw[u][4] = L.czm[k];
             cw[u][5] = L.czp[k];
             c0v[u] = diag_f64(L, i, j, k);
-            ic0[u] = __ddiv_rn(1.0, c0v[u]);
+            wv[u] = __ddiv_rn(omega, c0v[u]);
             bv[u] = b[cidx[u]];
         }
         const long long sy = L.sy, sz = L.sz;
         auto nbsum = [&](int u) {
             const long long c = cidx[u];
-            double t = __dmul_rn(cw[u][0], x[c - 1]);
-            t = __dadd_rn(t, __dmul_rn(cw[u][1], x[c + 1]));
-            t = __dadd_rn(t, __dmul_rn(cw[u][2], x[c - sy]));
-            t = __dadd_rn(t, __dmul_rn(cw[u][3], x[c + sy]));
-            t = __dadd_rn(t, __dmul_rn(cw[u][4], x[c - sz]));
-            return __dadd_rn(t, __dmul_rn(cw[u][5], x[c + sz]));
+            const double tx = fma(cw[u][1], x[c + 1], __dmul_rn(cw[u][0], x[c - 1]));
+            const double ty = fma(cw[u][3], x[c + sy], __dmul_rn(cw[u][2], x[c - sy]));
+            const double tz = fma(cw[u][5], x[c + sz], __dmul_rn(cw[u][4], x[c - sz]));
+            return __dadd_rn(__dadd_rn(tx, ty), tz);
         };
         auto norm = [&]() {
             double acc = 0.0;
 #pragma unroll
             for (int u = 0; u < 2; ++u)
                 if (has[u]) {
-                    const double r = __dsub_rn(bv[u], __dadd_rn(__dmul_rn(c0v[u], x[cidx[u]]), nbsum(u)));
-                    acc = __dadd_rn(acc, __dmul_rn(r, r));
+                    const double r = __dsub_rn(bv[u], fma(c0v[u], x[cidx[u]], nbsum(u)));
+                    acc = fma(r, r, acc);
                 }
             return warp_sum_f64(acc);
         };
         const double r0 = norm();
+        const double thr = __dmul_rn(__dmul_rn(tol, tol), r0);
         for (it = 0; it < maxit; ++it) {
 #pragma unroll
             for (int colour = 0; colour < 2; ++colour) {
@@ -309,14 +313,13 @@ __device__ int coarse_solve_warp_f64(const LevelK<double> &L, double *x, const d
 #pragma unroll
                 for (int u = 0; u < 2; ++u)
                     if (has[u] && odd[u] == (colour == 0)) {
+                        const double old = x[cidx[u]];
                         const double t = nbsum(u);
-                        x[cidx[u]] = __dadd_rn(__dmul_rn(__dmul_rn(omega, __dsub_rn(bv[u], t)), ic0[u]),
-                                               __dmul_rn(omw, x[cidx[u]]));
+                        x[cidx[u]] = fma(wv[u], __dsub_rn(bv[u], t), __dmul_rn(omw, old));
                     }
                 __syncwarp();
             }
-            const double rn = norm();
-            if (sqrt(__ddiv_rn(rn, r0)) <= tol) break;
+            if (norm() <= thr) break;
         }
     } else if (solver == 0) {
         const int hx = (nx + 1) / 2, nq = hx * ny * L.nz;
