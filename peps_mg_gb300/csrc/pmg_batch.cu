@@ -198,9 +198,15 @@ __global__ void __launch_bounds__(NTB) k_batch_nonzero(const double *__restrict_
     const int p = blockIdx.y;
     const unsigned long long *u = reinterpret_cast<const unsigned long long *>(sol);
     unsigned long long bits = 0ull;
-    for (long long q = offset[p] + blockIdx.x * (long long)NTB + threadIdx.x; q < offset[p + 1];
-         q += (long long)gridDim.x * NTB)
-        bits |= __ldg(u + q);
+    const long long end = offset[p + 1], stride = (long long)gridDim.x * NTB;
+    long long q = offset[p] + blockIdx.x * (long long)NTB + threadIdx.x;
+    for (; q + 3 * stride < end; q += 4 * stride) {
+        unsigned long long v[4];
+#pragma unroll
+        for (int t = 0; t < 4; ++t) v[t] = __ldg(u + q + t * stride);
+        bits |= v[0] | v[1] | v[2] | v[3];
+    }
+    for (; q < end; q += stride) bits |= __ldg(u + q);
     if (__syncthreads_or(bits != 0ull) && threadIdx.x == 0) atomicOr(nonzero + p, 1);
 }
 
@@ -863,7 +869,7 @@ static void batch_outer(Batch &B, bool first, double tol, int max_cycles)
     const int n = B.n;
     if (first) {
         cudaMemsetAsync(B.d_nonzero, 0, n * sizeof(int), B.stream);
-        k_batch_nonzero<<<dim3(8, (unsigned)n), NTB, 0, B.stream>>>(B.cur_sol, B.d_offset, B.d_nonzero);
+        k_batch_nonzero<<<dim3(64, (unsigned)n), NTB, 0, B.stream>>>(B.cur_sol, B.d_offset, B.d_nonzero);
         k_batch_outer_residual<<<grid_for(B.outer.n), NTB, 0, B.stream>>>(B.d_outer, B.outer.d, B.outer.n,
                                                                           B.d_partials, B.d_done, nullptr,
                                                                           B.d_nonzero);
