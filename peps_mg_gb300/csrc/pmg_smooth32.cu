@@ -20,6 +20,7 @@
 #include <cstring>
 #include <map>
 #include <mutex>
+#include <vector>
 
 #include "../../include/peps_mg.h"
 #include "pmg_internal.h"
@@ -314,12 +315,24 @@ int tune_smoother(const LevelK<float> &L, const Launch &ln, float *e0, float *e1
     const bool log = log_env && log_env[0] == '1';
     // the register-window kernel stages at most RB_ZC - 3 planes of z coefficients
     const int chunks_window[] = {0, 16, 32, 64}, chunks_tma[] = {0, 4, 8, 16, 32, 64, 128};
-    const int *chunks = use_tma ? chunks_tma : chunks_window;
-    const int nchunks = use_tma ? 7 : 4;
     const int tys[4] = {14, 6, 10, 22};
-    for (int v = 0; v < (use_tma ? 4 : 3); ++v)
-        for (int ci = 0; ci < nchunks; ++ci) {
-            const int c = chunks[ci];
+    for (int v = 0; v < (use_tma ? 4 : 3); ++v) {
+        std::vector<int> cands(use_tma ? chunks_tma : chunks_window, use_tma ? chunks_tma + 7 : chunks_window + 4);
+        if (use_tma) {
+            // k-chunks that spread the tiles' items evenly over the resident CTA slots (one
+            // to three rounds), besides the powers of two
+            int slots = 0;
+            const int r = v == 1 ? tma_slots<6>(&slots) : v == 2 ? tma_slots<10>(&slots)
+                                                               : v == 3 ? tma_slots<22>(&slots) : tma_slots<14>(&slots);
+            const int tiles = ((L.nx + RBT_TX - 1) / RBT_TX) * ((L.ny + tys[v] - 1) / tys[v]);
+            if (r == PMG_OK && slots > 0)
+                for (int rounds = 1; rounds <= 3; ++rounds) {
+                    const int nch = std::max(1, (rounds * slots) / std::max(1, tiles));
+                    const int c = (L.nz + nch - 1) / nch;
+                    if (c >= 4 && std::find(cands.begin(), cands.end(), c) == cands.end()) cands.push_back(c);
+                }
+        }
+        for (const int c : cands) {
             if (rb32_fused(L, ln, e0, e1, b, 1.f, 0.f, false, s, v, c, tma, 0, err) != PMG_OK) continue;
             cudaEventRecord(a, s);
             for (int q = 0; q < 3; ++q) rb32_fused(L, ln, e0, e1, b, 1.f, 0.f, false, s, v, c, tma, 0, err);
@@ -336,6 +349,7 @@ int tune_smoother(const LevelK<float> &L, const Launch &ln, float *e0, float *e1
                 bk = c;
             }
         }
+    }
     cudaEventDestroy(a);
     cudaEventDestroy(z);
     PMG_TRY_S(cuda_status(cudaGetLastError(), "smoother autotuning"));

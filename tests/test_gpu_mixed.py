@@ -218,3 +218,15 @@ def test_mixed_pinned_host_buffers():
         rep2 = mg.solve_vcycle(ds, dr, to_dev(rhs), 2, 1e-10, 1.0)
     assert rep.converged and np.array_equal(rep.history, rep2.history)
     assert torch.equal(h_sol, ds.cpu()) and torch.equal(h_rsd, dr.cpu())
+
+
+def test_mixed_nan_rhs_reports_divergence():
+    """A NaN in the right-hand side: the mixed solver (zero-guess first residual, residual
+    update, FP64 recompute) reports divergence instead of looping or returning success."""
+    mesh, rhs, _ = problems.sine(32)
+    rhs[7, 9, 11] = np.nan
+    with pmg.Multigrid(mesh, 3, 5, "cgs", precision="mixed") as mg:
+        sol = torch.zeros((34,) * 3, dtype=torch.float64, device="cuda")
+        with pytest.raises(pmg.PmgError) as e:
+            mg.solve_vcycle(sol, torch.zeros_like(sol), to_dev(rhs), 1, 1e-10, 1.0)
+        assert e.value.status == 3
