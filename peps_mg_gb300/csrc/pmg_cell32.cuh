@@ -402,6 +402,20 @@ __device__ __forceinline__ double plus_zero(double b)
     return __longlong_as_double((long long)u);
 }
 
+// float -> double on the integer pipe with one select: exact for normal values, zeros,
+// infinities and NaNs; subnormal floats (below 2^-126) become zero.  For sums whose
+// subnormal parts are far below the accuracy asked of them (the residual update).
+__device__ __forceinline__ double f32_to_f64_fast(float f)
+{
+    const unsigned u = __float_as_uint(f);
+    const unsigned mag = u & 0x7fffffffu, e = mag >> 23;
+    // normal: the exponent rebased by 1023 - 127 = 896; Inf/NaN: exponent field 0x7ff
+    const unsigned long long body =
+        e == 0u ? 0ull : (e == 255u ? ((0x7ffull << 52) | ((unsigned long long)(mag & 0x7fffffu) << 29))
+                                    : (((unsigned long long)mag + (896ull << 23)) << 29));
+    return __longlong_as_double((long long)(((unsigned long long)(u & 0x80000000u) << 32) | body));
+}
+
 // r(i,j,k) = b - A x in FP64, FMA form r = b + d x - sum c x_nb with d = -c0 = sx(i) + dyz
 // (the per-axis diagonal sums), as the outer residual of the mixed solver.
 __device__ __forceinline__ double outer_residual_cell_b(const LevelK<double> &L, double dyz, const double *x,

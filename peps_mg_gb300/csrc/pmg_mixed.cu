@@ -295,7 +295,9 @@ __global__ void __launch_bounds__(kBX *kBY) k_update_residual(LevelK<double> L, 
                     comp_term(czm, ev[u][5], ec, S, Sl);
                     comp_term(czp, ev[u][6], ec, S, Sl);
                     x[p] = xv[u] + f32_to_f64(ec);
-                    const double v = __dsub_rn(__dsub_rn(rv[u], f32_to_f64(S)), f32_to_f64(Sl));
+                    // S and Sl: subnormal parts (below 2^-126) are far below the 2^-48
+                    // relative accuracy of A e
+                    const double v = __dsub_rn(__dsub_rn(rv[u], f32_to_f64_fast(S)), f32_to_f64_fast(Sl));
                     r[p] = v;
                     const float v32 = f64_to_f32_rn(v);
                     r32[q] = v32;
