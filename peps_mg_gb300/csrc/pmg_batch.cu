@@ -299,7 +299,7 @@ __global__ void __launch_bounds__(NTB) k_batch_correct(const BOuter *__restrict_
             comp_term(czm, e[c - O.sz32], ec, S, Sl);
             comp_term(czp, e[c + O.sz32], ec, S, Sl);
             O.sol[p] = O.sol[p] + f32_to_f64(ec);
-            const double v = __dsub_rn(__dsub_rn(O.rsd[p], f32_to_f64(S)), f32_to_f64(Sl));
+            const double v = __dsub_rn(__dsub_rn(O.rsd[p], f32_to_f64_fast(S)), f32_to_f64_fast(Sl));
             O.rsd[p] = v;
             const float v32 = f64_to_f32_rn(v);
             O.r32[c] = v32;
