@@ -246,6 +246,7 @@ __global__ void __launch_bounds__(kBX *kBY) k_add_correction(LevelK<double> L, d
 // thread sums (nscale r32)^2 in FP32 -- nscale a power of two that brings the initial
 // residual's RMS to about 1, keeping the squares in FP32's range for residual ratios
 // down to about 1e-19 -- and the block sums the threads' sums in FP64.
+template <int UV>
 __global__ void __launch_bounds__(kBX *kBY) k_update_residual(LevelK<double> L, SplitCoef C, double *__restrict__ x,
                                                               const float *__restrict__ e, double *__restrict__ r,
                                                               float *__restrict__ r32, int sy32, long long sz32,
@@ -256,15 +257,15 @@ __global__ void __launch_bounds__(kBX *kBY) k_update_residual(LevelK<double> L, 
         const float2 czm = C.czm[k], czp = C.czp[k];
         for (int j = blockIdx.y * blockDim.y + threadIdx.y + 1; j <= L.ny; j += gridDim.y * blockDim.y) {
             const float2 cym = C.cym[j], cyp = C.cyp[j];
-            for (int i0 = blockIdx.x * (blockDim.x * kOuterVec) + threadIdx.x + 1; i0 <= L.nx;
-                 i0 += gridDim.x * blockDim.x * kOuterVec) {
+            for (int i0 = blockIdx.x * (blockDim.x * UV) + threadIdx.x + 1; i0 <= L.nx;
+                 i0 += gridDim.x * blockDim.x * UV) {
                 // every load of the thread's cells first (the kernel is bound by load latency
                 // when each cell's loads wait for the previous cell's arithmetic)
-                float ev[kOuterVec][7];
-                double xv[kOuterVec], rv[kOuterVec];
-                float2 cm[kOuterVec], cp[kOuterVec];
+                float ev[UV][7];
+                double xv[UV], rv[UV];
+                float2 cm[UV], cp[UV];
 #pragma unroll
-                for (int u = 0; u < kOuterVec; ++u) {
+                for (int u = 0; u < UV; ++u) {
                     const int i = i0 + u * kBX;
                     if (i <= L.nx) {
                         const long long p = lin(i, j, k, L.sy, L.sz), q = lin(i, j, k, sy32, sz32);
@@ -282,7 +283,7 @@ __global__ void __launch_bounds__(kBX *kBY) k_update_residual(LevelK<double> L, 
                     }
                 }
 #pragma unroll
-                for (int u = 0; u < kOuterVec; ++u) {
+                for (int u = 0; u < UV; ++u) {
                     const int i = i0 + u * kBX;
                     if (i > L.nx) break;
                     const long long p = lin(i, j, k, L.sy, L.sz), q = lin(i, j, k, sy32, sz32);
@@ -732,13 +733,16 @@ int Ctx::outer_residual(double *sol, double *rsd, const double *rhs, int slot)
 int Ctx::update_residual(double *sol, double *rsd, int slot, double res0)
 {
     const LevelK<double> &L = K[0];
-    const dim3 g = grid_outer(L, launch[0]), bl(kBX, kBY, 1);
+    constexpr int UV = 2;   // cells per thread (64 registers: more resident warps)
+    dim3 g = grid_outer(L, launch[0]);
+    if (!launch[0].collapse[0]) g.x = (unsigned)std::max(1, (L.nx + UV * kBX - 1) / (UV * kBX));
+    const dim3 bl(kBX, kBY, 1);
     const double rms0 = std::sqrt(res0 / ((double)L.nx * L.ny * L.nz));
     const int ex = rms0 > 0.0 && std::isfinite(rms0) ? std::max(-100, std::min(100, (int)std::floor(std::log2(rms0))))
                                                      : 0;
     const float nscale = std::ldexp(1.0f, -ex);
     const int pi = prof.begin(stream);
-    k_update_residual<<<g, bl, 0, stream>>>(L, mixed->sc, sol, mixed->E(0), rsd, mixed->b[0], mixed->K[0].sy,
+    k_update_residual<UV><<<g, bl, 0, stream>>>(L, mixed->sc, sol, mixed->E(0), rsd, mixed->b[0], mixed->K[0].sy,
                                             mixed->K[0].sz, nscale, d_partials);
     prof.end(pi, PC_UPDATE_RES, 1, 40.0 * (double)L.nx * L.ny * L.nz, stream);
     count_launches(1);
