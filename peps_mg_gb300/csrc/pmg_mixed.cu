@@ -226,15 +226,30 @@ __global__ void __launch_bounds__(kBX *kBY) k_outer_residual(LevelK<double> L, c
     if (tid2() == 0) partials[blin()] = s;
 }
 
-// x = x + e (the FP64 correction)
+// x = x + e (the FP64 correction); each thread handles kOuterVec cells of a row, 32
+// apart, with their loads issued together, on the grid of the outer kernels.
 __global__ void __launch_bounds__(kBX *kBY) k_add_correction(LevelK<double> L, double *__restrict__ x,
                                                              const float *__restrict__ e, int sy32, long long sz32)
 {
     for (int k = blockIdx.z + 1; k <= L.nz; k += gridDim.z)
         for (int j = blockIdx.y * blockDim.y + threadIdx.y + 1; j <= L.ny; j += gridDim.y * blockDim.y)
-            for (int i = blockIdx.x * blockDim.x + threadIdx.x + 1; i <= L.nx; i += gridDim.x * blockDim.x) {
-                const long long p = lin(i, j, k, L.sy, L.sz);
-                x[p] = x[p] + f32_to_f64(e[lin(i, j, k, sy32, sz32)]);
+            for (int i0 = blockIdx.x * (blockDim.x * kOuterVec) + threadIdx.x + 1; i0 <= L.nx;
+                 i0 += gridDim.x * blockDim.x * kOuterVec) {
+                double xv[kOuterVec];
+                float ev[kOuterVec];
+#pragma unroll
+                for (int u = 0; u < kOuterVec; ++u) {
+                    const int i = i0 + u * kBX;
+                    if (i <= L.nx) {
+                        xv[u] = x[lin(i, j, k, L.sy, L.sz)];
+                        ev[u] = e[lin(i, j, k, sy32, sz32)];
+                    }
+                }
+#pragma unroll
+                for (int u = 0; u < kOuterVec; ++u) {
+                    const int i = i0 + u * kBX;
+                    if (i <= L.nx) x[lin(i, j, k, L.sy, L.sz)] = xv[u] + f32_to_f64(ev[u]);
+                }
             }
 }
 
@@ -754,7 +769,7 @@ int Ctx::update_residual(double *sol, double *rsd, int slot, double res0)
 int Ctx::correct_and_recompute(double *sol, double *rsd, const double *rhs)
 {
     const LevelK<double> &L = K[0];
-    const dim3 g = grid3m(L.nx, L.ny, L.nz, launch[0]), bl(kBX, kBY, 1);
+    const dim3 g = grid_outer(L, launch[0]), bl(kBX, kBY, 1);
     PMG_TRY_M(before_x_change());
     const int pi = prof.begin(stream);
     k_add_correction<<<g, bl, 0, stream>>>(L, sol, mixed->E(0), mixed->K[0].sy, mixed->K[0].sz);
