@@ -95,7 +95,11 @@ int rb32_tma_setup(Rb32Tma *t, const LevelK<float> &L, float *const base[3], lon
 int rb32_fused(const LevelK<float> &L, const Launch &ln, const float *ein, float *eout, const float *b, float omega,
                float omw, bool zero_in, cudaStream_t s, int variant = 0, int kchunk = 0,
                const Rb32Tma *tma = nullptr, int in_buf = 0, int *err = nullptr);
-// Picks the fastest tile variant and k-chunk for a level (process-wide cache).
+// Picks the fastest kernel, tile variant and k-chunk for a level (process-wide cache).
+// With tensor maps (tma) the TMA-fed and the register-window kernels compete; when the
+// register-window one wins, *variant carries kTuneWindow on top of the tile variant and the
+// caller must run that level without its maps.
+constexpr int kTuneWindow = 8;
 int tune_smoother(const LevelK<float> &L, const Launch &ln, float *e0, float *e1, const float *b, cudaStream_t s,
                   int *variant, int *kchunk, const Rb32Tma *tma = nullptr, int *err = nullptr);
 // Integer-pipe precision conversions used by the outer kernels (self-test hook).

@@ -528,6 +528,7 @@ int Ctx::setup_mixed()
     m->b.assign((size_t)nl + 1, nullptr);
     m->cur.assign((size_t)nl + 1, 0);
     m->fused.assign((size_t)nl + 1, false);
+    m->window.assign((size_t)nl + 1, false);
     m->variant.assign((size_t)nl + 1, 0);
     m->kchunk.assign((size_t)nl + 1, 0);
     m->tma.assign((size_t)nl + 1, Rb32Tma());
@@ -573,9 +574,14 @@ int Ctx::setup_mixed()
     PMG_TRY_M(mstatus(cudaMalloc(&m->d_err, sizeof(int)), "mixed error flag"));
     PMG_TRY_M(mstatus(cudaMemset(m->d_err, 0, sizeof(int)), "mixed error flag"));
     for (int l = 0; l < tail32_l0; ++l)
-        if (m->fused[l] && autotune)
+        if (m->fused[l] && autotune) {
             PMG_TRY_M(tune_smoother(m->K[l], launch[l], m->e[0][l], m->e[1][l], m->b[l], stream, &m->variant[l],
                                     &m->kchunk[l], &m->tma[l], m->d_err));
+            if (m->variant[l] & kTuneWindow) {
+                m->variant[l] &= ~kTuneWindow;
+                m->window[l] = true;   // the register-window kernel is faster on this level
+            }
+        }
     PMG_TRY_M(check_pipeline());
     return PMG_OK;
 }
@@ -634,7 +640,8 @@ int Ctx::vcycle32(int maxit, double omega, bool zero_start)
         if (m->fused[l]) {
             for (int it = 0; it < maxit; ++it) {
                 PMG_TRY_M(rb32_fused(L, launch[l], m->E(l), m->Eother(l), m->b[l], om, omw, zs && it == 0, stream,
-                                     m->variant[l], m->kchunk[l], &m->tma[l], m->cur[l], m->d_err));
+                                     m->variant[l], m->kchunk[l], m->window[l] ? nullptr : &m->tma[l], m->cur[l],
+                                     m->d_err));
                 m->cur[l] = 1 - m->cur[l];
             }
             // 12 B per cell (e_in, b read, e_out written); 8 B for an iteration from e = 0

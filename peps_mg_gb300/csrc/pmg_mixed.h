@@ -27,6 +27,7 @@ struct MixedState {
     std::vector<float *> e[2], b;    // e[buf][l] (two buffers for out-of-place sweeps), b[l]
     std::vector<int> cur;            // current buffer of e at each level
     std::vector<bool> fused;         // level uses the fused out-of-place smoother
+    std::vector<bool> window;        // the autotuner chose the register-window kernel over the TMA-fed one
     std::vector<int> variant, kchunk;  // autotuned tile variant and k-chunk of the fused smoother
     std::vector<Rb32Tma> tma;        // tensor maps of the TMA-fed smoother, per level
     std::vector<long long> rows, planes;   // allocated rows per plane and planes, per level

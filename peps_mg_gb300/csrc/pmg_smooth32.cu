@@ -316,9 +316,14 @@ int tune_smoother(const LevelK<float> &L, const Launch &ln, float *e0, float *e1
     // the register-window kernel stages at most RB_ZC - 3 planes of z coefficients
     const int chunks_window[] = {0, 16, 32, 64}, chunks_tma[] = {0, 4, 8, 16, 32, 64, 128};
     const int tys[4] = {14, 6, 10, 22};
-    for (int v = 0; v < (use_tma ? 4 : 3); ++v) {
-        std::vector<int> cands(use_tma ? chunks_tma : chunks_window, use_tma ? chunks_tma + 7 : chunks_window + 4);
-        if (use_tma) {
+    bool best_window = !use_tma;
+    // the TMA-fed kernel where its tensor maps exist, and the register-window kernel (no
+    // copy pipeline to fill: it can win on small levels)
+    for (int kind = use_tma ? 0 : 1; kind < 2; ++kind) {
+    const bool tk = kind == 0;
+    for (int v = 0; v < (tk ? 4 : 3); ++v) {
+        std::vector<int> cands(tk ? chunks_tma : chunks_window, tk ? chunks_tma + 7 : chunks_window + 4);
+        if (tk) {
             // k-chunks that spread the tiles' items evenly over the resident CTA slots (one
             // to three rounds), besides the powers of two
             int slots = 0;
@@ -332,34 +337,40 @@ int tune_smoother(const LevelK<float> &L, const Launch &ln, float *e0, float *e1
                     if (c >= 4 && std::find(cands.begin(), cands.end(), c) == cands.end()) cands.push_back(c);
                 }
         }
+        const Rb32Tma *tm = tk ? tma : nullptr;
         for (const int c : cands) {
-            if (rb32_fused(L, ln, e0, e1, b, 1.f, 0.f, false, s, v, c, tma, 0, err) != PMG_OK) continue;
+            if (rb32_fused(L, ln, e0, e1, b, 1.f, 0.f, false, s, v, c, tm, 0, err) != PMG_OK) continue;
             cudaEventRecord(a, s);
-            for (int q = 0; q < 3; ++q) rb32_fused(L, ln, e0, e1, b, 1.f, 0.f, false, s, v, c, tma, 0, err);
+            for (int q = 0; q < 3; ++q) rb32_fused(L, ln, e0, e1, b, 1.f, 0.f, false, s, v, c, tm, 0, err);
             cudaEventRecord(z, s);
             if (cudaEventSynchronize(z) != cudaSuccess) break;
             float ms = 0.f;
             cudaEventElapsedTime(&ms, a, z);
             if (log)
                 std::fprintf(stderr, "[peps_mg tune] %dx%dx%d %s TY=%d kchunk=%d: %.1f us\n", L.nx, L.ny, L.nz,
-                             use_tma ? "tma" : "window", tys[v], c, ms * 1e3f / 3.f);
+                             tk ? "tma" : "window", tys[v], c, ms * 1e3f / 3.f);
             if (ms < best) {
                 best = ms;
                 bv = v;
                 bk = c;
+                best_window = !tk;
             }
         }
+    }
     }
     cudaEventDestroy(a);
     cudaEventDestroy(z);
     PMG_TRY_S(cuda_status(cudaGetLastError(), "smoother autotuning"));
-    *variant = bv;
+    // a level with tensor maps whose fastest kernel is the register-window one is flagged
+    // (kTuneWindow): its caller runs the window kernel there
+    const int code = bv + (use_tma && best_window ? kTuneWindow : 0);
+    *variant = code;
     *kchunk = bk;
     if (log)
-        std::fprintf(stderr, "[peps_mg tune] %dx%dx%d chosen TY=%d kchunk=%d (%.1f us)\n", L.nx, L.ny, L.nz,
-                     tys[bv], bk, best * 1e3f / 3.f);
+        std::fprintf(stderr, "[peps_mg tune] %dx%dx%d chosen %s TY=%d kchunk=%d (%.1f us)\n", L.nx, L.ny, L.nz,
+                     best_window ? "window" : "tma", tys[bv], bk, best * 1e3f / 3.f);
     std::lock_guard<std::mutex> g(mu);
-    cache[key] = {bv, bk};
+    cache[key] = {code, bk};
     return PMG_OK;
 }
 
