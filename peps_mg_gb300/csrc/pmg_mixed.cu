@@ -515,6 +515,11 @@ int Ctx::setup_mixed()
         m->sc = SplitCoef{m->split + off[0], m->split + off[1], m->split + off[2],
                           m->split + off[3], m->split + off[4], m->split + off[5]};
     }
+    // PEPS_MG_GRAPHS=0: the FP32 V-cycles are launched kernel by kernel, not as graphs
+    {
+        const char *ge = std::getenv("PEPS_MG_GRAPHS");
+        m->use_graphs = !(ge && std::strcmp(ge, "0") == 0);
+    }
     // PEPS_MG_OUTER=recompute: the residual after every correction is b - A x in FP64
     {
         const char *oe = std::getenv("PEPS_MG_OUTER");
@@ -750,6 +755,60 @@ int Ctx::outer_residual(double *sol, double *rsd, const double *rhs, int slot)
     return f64_reduce(d_partials, (int)(g.x * g.y * g.z), d_scal + slot, stream);
 }
 
+// The inner FP32 V-cycles of one correction.  A V-cycle toggles every level's buffer an
+// even number of times, so a captured cycle stays valid for every later replay; the two
+// graphs (the first cycle of a correction, from e = 0, and the later ones) are captured at
+// the first solve and again when maxit or omega change.  Back-to-back launches of the small
+// levels' kernels cost about 4 us each on the device, about 1 us inside a graph.  With the
+// event profiler on, the kernels are launched one by one.
+int Ctx::run_vcycles(int maxit, double omega)
+{
+    MixedState *m = mixed;
+    if (prof.on || !m->use_graphs) {
+        for (int q = 0; q < m->inner; ++q) PMG_TRY_M(vcycle32(maxit, omega, q == 0));
+        return PMG_OK;
+    }
+    if (!m->vgraph[0] || m->vgraph_maxit != maxit || m->vgraph_omega != omega) {
+        if (!m->cap_stream)
+            PMG_TRY_M(mstatus(cudaStreamCreateWithFlags(&m->cap_stream, cudaStreamNonBlocking), "capture stream"));
+        for (int f = 0; f < 2; ++f) {
+            if (m->vgraph[f]) {
+                cudaGraphExecDestroy(m->vgraph[f]);
+                m->vgraph[f] = nullptr;
+            }
+            // capture on the private stream (the context's stream may be the legacy one,
+            // which cannot be captured); nothing runs while capturing
+            const long long c0 = launches_total();
+            cudaStream_t own = stream;
+            stream = m->cap_stream;
+            cudaError_t ce = cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal);
+            int rc = ce == cudaSuccess ? vcycle32(maxit, omega, f == 0) : PMG_OK;
+            cudaGraph_t g = nullptr;
+            if (ce == cudaSuccess) ce = cudaStreamEndCapture(stream, &g);
+            stream = own;
+            const long long captured = launches_total() - c0;
+            count_launches(-captured);   // recorded, not launched
+            if (rc == PMG_OK) rc = mstatus(ce, "V-cycle graph capture");
+            if (rc == PMG_OK) rc = mstatus(cudaGraphInstantiate(&m->vgraph[f], g, 0), "V-cycle graph instantiate");
+            if (g) cudaGraphDestroy(g);
+            if (rc != PMG_OK) {
+                cudaGetLastError();
+                m->vgraph[f] = nullptr;
+                return rc;
+            }
+            m->vgraph_launches[f] = captured;
+        }
+        m->vgraph_maxit = maxit;
+        m->vgraph_omega = omega;
+    }
+    for (int q = 0; q < m->inner; ++q) {
+        const int f = q == 0 ? 0 : 1;
+        PMG_TRY_M(mstatus(cudaGraphLaunch(m->vgraph[f], stream), "V-cycle graph launch"));
+        count_launches(m->vgraph_launches[f]);
+    }
+    return PMG_OK;
+}
+
 // x += e and r -= A e with its norm into d_scal[slot] (after a correction); res0 = the
 // initial residual's squared norm (sets the norm's FP32 scale).
 int Ctx::update_residual(double *sol, double *rsd, int slot, double res0)
@@ -809,7 +868,7 @@ int Ctx::solve_mixed(double *sol, double *rsd, const double *rhs, int maxit, dou
     int cycles = 0, converged = 0, inner_total = 0;
     double ratio = 0.0, prev_ratio = 1.0, contraction = 1.0;
     for (int cyc = 1; cyc <= n_vcycles; ++cyc) {
-        for (int q = 0; q < m->inner; ++q) PMG_TRY_M(vcycle32(maxit, omega, q == 0));
+        PMG_TRY_M(run_vcycles(maxit, omega));
         inner_total += m->inner;
         const bool recompute = !m->update_residual || cyc == n_vcycles || prev_ratio * contraction < 0.1 * tol;
         if (recompute) {

@@ -36,6 +36,14 @@ struct MixedState {
     TailDesc<float> tail_host;
     TailDesc<float> *d_tail = nullptr;
     int inner = 2;
+    // The FP32 V-cycle as CUDA graphs (first cycle of a correction, from e = 0, and the
+    // later ones), captured on cap_stream and launched on the context's stream.
+    bool use_graphs = true;
+    cudaStream_t cap_stream = nullptr;
+    cudaGraphExec_t vgraph[2] = {nullptr, nullptr};
+    long long vgraph_launches[2] = {0, 0};
+    int vgraph_maxit = -1;
+    double vgraph_omega = 0.0;
     ~MixedState()
     {
         cudaFree(tables);
@@ -44,6 +52,9 @@ struct MixedState {
         for (auto p : alloc) cudaFree(p);
         cudaFree(d_tail);
         cudaFree(d_err);
+        for (auto &g : vgraph)
+            if (g) cudaGraphExecDestroy(g);
+        if (cap_stream) cudaStreamDestroy(cap_stream);
     }
     float *E(int l) const { return e[cur[l]][l]; }
     float *Eother(int l) const { return e[1 - cur[l]][l]; }

@@ -143,6 +143,15 @@ int tma_attr()
 }
 
 template <int TY>
+int tma_attr_all()
+{
+    PMG_TRY_S((tma_attr<TY, false, false>()));
+    PMG_TRY_S((tma_attr<TY, false, true>()));
+    PMG_TRY_S((tma_attr<TY, true, false>()));
+    return tma_attr<TY, true, true>();
+}
+
+template <int TY>
 int tma_slots(int *slots)
 {
     static std::once_flag once;
@@ -253,6 +262,12 @@ int rb32_tma_setup(Rb32Tma *t, const LevelK<float> &L, float *const base[3], lon
             if (!encode_map(&t->e[q][v], base[q], L, rows, planes, tys[v] + 4)) return PMG_OK;
         if (!encode_map(&t->b[v], base[2], L, rows, planes, tys[v] + 2)) return PMG_OK;
     }
+    // every kernel instance's shared-memory attributes now, so that no launch (one being
+    // captured into a graph included) sets them first
+    PMG_TRY_S(tma_attr_all<14>());
+    PMG_TRY_S(tma_attr_all<6>());
+    PMG_TRY_S(tma_attr_all<10>());
+    PMG_TRY_S(tma_attr_all<22>());
     t->ok = true;
     return PMG_OK;
 }

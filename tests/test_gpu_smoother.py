@@ -67,8 +67,9 @@ def test_one_iteration_against_oracle(n):
 
 
 def test_kernel_variants_give_identical_solves(tmp_path):
-    """A whole mixed-precision solve gives the same bits with either smoother kernel and
-    with either kind of transfer kernel (marching or one thread per cell)."""
+    """A whole mixed-precision solve gives the same bits with either smoother kernel, with
+    either kind of transfer kernel (marching or one thread per cell), and with the FP32
+    V-cycles replayed as CUDA graphs or launched kernel by kernel."""
     import os
     import subprocess
     import sys
@@ -88,12 +89,13 @@ print(rep.cycles)
 '''
     root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
     outs = []
-    for sm, tr in (("tma", "march"), ("window", "march"), ("tma", "cell")):
-        env = dict(os.environ, PEPS_MG_SMOOTHER=sm, PEPS_MG_TRANSFER=tr, PYTHONPATH=root)
-        path = str(tmp_path / ("%s_%s.npy" % (sm, tr)))
+    for sm, tr, gr in (("tma", "march", "1"), ("window", "march", "1"), ("tma", "cell", "1"), ("tma", "march", "0")):
+        env = dict(os.environ, PEPS_MG_SMOOTHER=sm, PEPS_MG_TRANSFER=tr, PEPS_MG_GRAPHS=gr, PYTHONPATH=root)
+        path = str(tmp_path / ("%s_%s_%s.npy" % (sm, tr, gr)))
         r = subprocess.run([sys.executable, "-c", code, path], cwd=root, env=env, capture_output=True, text=True,
                            timeout=300)
         assert r.returncode == 0, r.stderr[-2000:]
         outs.append(np.load(path))
     assert np.array_equal(outs[0], outs[1])
     assert np.array_equal(outs[0], outs[2])
+    assert np.array_equal(outs[0], outs[3])
