@@ -93,12 +93,18 @@ class ClockSampler:
         self.lines = []
 
     def start(self):
+        """Starts sampling every 20 ms and returns once the first sample has arrived (at most
+        5 s), so the samples cover the timed region that follows."""
         try:
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.FIELDS,
-                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                          "--format=csv,noheader,nounits", "-lms", "20"],
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
+            t0 = time.time()
+            while not self.lines and time.time() - t0 < 5.0 and self.proc.poll() is None:
+                time.sleep(0.01)
+            self.first = len(self.lines)
         except (FileNotFoundError, OSError):
             self.proc = None
 
