@@ -7,11 +7,14 @@
 // repeated until sqrt(|r|^2 / |r0|^2) < tolerance, the reference's convergence test
 // (src/multigrid.f90:1970-1973), always decided on a residual recomputed in FP64.  Between
 // corrections that cannot end the solve the residual is updated as r -= A e instead (A e
-// in compensated FP32 arithmetic, k_update_residual).  The FP32 V-cycle follows the operation sequence of
-// the reference cycle (src/multigrid.f90:1931-1967) with the same smoother, transfer
-// operators and coarsest-level solver, but in FP32 arithmetic with FMA contraction and
-// approximate reciprocals; the coarsest-level solver's dot products and convergence
-// test stay in FP64.  The finest FP32 residual is fused with the restriction.
+// in compensated FP32 arithmetic, k_update_residual).
+//
+// The FP32 V-cycle follows the operation sequence of the reference cycle
+// (src/multigrid.f90:1931-1967) with the same smoother, transfer operators and
+// coarsest-level solver, but in FP32 arithmetic with FMA contraction and approximate
+// reciprocals; the coarsest-level solver's dot products and convergence test stay in FP64.
+// The finest FP32 residual is fused with the restriction.  The V-cycles of a correction
+// are replayed as CUDA graphs (run_vcycles).
 //
 // This translation unit is compiled with --fmad=true.
 #include <cuda_runtime.h>
