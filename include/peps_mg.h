@@ -23,7 +23,7 @@ extern "C" {
 #define PMG_EINVAL 1      /* argument or configuration the reference rejects          */
 #define PMG_ENOMEM 2      /* device or host allocation failed                         */
 #define PMG_EDIVERGED 3   /* residual norm became NaN or Inf                          */
-#define PMG_ETIMEOUT 4    /* a bounded device loop gave up, or the abort flag was set */
+#define PMG_ETIMEOUT 4    /* a bounded device wait gave up, or the abort flag was set */
 #define PMG_ECUDA 5       /* CUDA runtime error (see pmg_last_error)                  */
 
 /* aggregation_method (&control aggregation_method, src/multigrid.f90:113-124) */
@@ -185,15 +185,19 @@ int pmg_batch_destroy(pmg_batch *batch);
  * Nothing is allocated: the partial sums live in a static 128 KiB device array that every
  * GPU loading this library holds until the process exits.  Limit: ceil(nx/32) *
  * ceil(ny/8) <= 16384 (e.g. planes up to 2048 x 2048); larger planes return PMG_EINVAL
- * with a message in pmg_last_error.  The first call on each device does a one-time
- * set-up on that device (it looks up the array's address and clears it); make that
- * first call before any stream capture.  All calls on one device share the array, so
+ * with a message in pmg_last_error.  Every call looks up the array's address on the
+ * current device (a host query that allocates nothing), so it stays valid after the
+ * device's context was re-created (cudaDeviceReset); the first call on each device also
+ * clears the array with a cudaMemsetAsync: make that first call before any stream
+ * capture.  All calls on one device share the array, so
  * calls that overlap in time (from several host threads, or on several streams at once)
  * race: serialise them.  Synchronous: returns after *result is written. */
 int pmg_vv_dot_static(const double *x, const double *y, int nx, int ny, int nz, void *stream, double *result);
 
 /* ---- Telemetry (no counterpart in the reference; it only prints MPI_Wtime) ------ */
-/* Kernel classes of pmg_profile_read (finest-level launches only). */
+/* Kernel classes of pmg_profile_read: the finest level's launches by kernel, and the grid
+ * levels below it as one class per precision (the single-CTA tails are classes of their
+ * own).  Algorithmic bytes count every array a launch reads or writes once. */
 #define PMG_PROF_SMOOTH32 0       /* FP32 RBGS half-sweep                    */
 #define PMG_PROF_OUTER_RESIDUAL 1 /* FP64 outer residual of PMG_MIXED        */
 #define PMG_PROF_RESRESTRICT32 2  /* FP32 residual fused with restriction    */
@@ -206,8 +210,11 @@ int pmg_vv_dot_static(const double *x, const double *y, int nx, int ny, int nz, 
 #define PMG_PROF_PROLONG64 9      /* FP64 prolongation + correction          */
 #define PMG_PROF_TAIL64 10        /* FP64 single-CTA coarse tail             */
 #define PMG_PROF_UPDATE_RESIDUAL 11 /* PMG_MIXED residual update r -= A e    */
-/* Enable (1) or disable (0) CUDA-event timing of the finest-level launches; resets
- * the accumulated figures. */
+#define PMG_PROF_COARSE32 12      /* FP32 grid levels below the finest: their smoothing and transfers, together */
+#define PMG_PROF_COARSE64 13      /* FP64 grid levels below the finest: smoothing, residuals, transfers       */
+/* Enable (1) or disable (0) CUDA-event timing of the classes above; resets the
+ * accumulated figures.  While it is on, the FP32 V-cycles are launched kernel by kernel
+ * instead of as CUDA graphs. */
 int pmg_profile(pmg_ctx *ctx, int enable);
 /* Accumulated device time, launch count and algorithmic bytes per launch (averaged over
  * the launches) of a class. */
@@ -231,6 +238,29 @@ int pmg_selftest_convert(const double *in64, float *out32, const float *in32, do
  * FP32 work arrays of that level. */
 int pmg_selftest_smooth32(pmg_ctx *ctx, int level, int impl, int variant, int kchunk, int zero_in, double omega,
                           const double *e_in, const double *b, double *e_out);
+
+/* Self-test of the timeout path of the TMA-fed FP32 smoother (no counterpart in the
+ * reference): one launch on `level` of a mixed-precision context in a mode that issues no
+ * copies and limits each bounded wait to a few microseconds, so the waits run out with no
+ * copy in flight.  Returns PMG_ETIMEOUT (the status a solve returns when a wait gives up)
+ * if the kernel raised its error flag, PMG_EINVAL when the level has no TMA-fed smoother.
+ * Clears the level's FP32 work arrays afterwards; the context stays usable.  Synchronous. */
+int pmg_selftest_wait_timeout(pmg_ctx *ctx, int level);
+
+/* ---- Abort and fault injection (no counterpart in the reference) ------------------ */
+/* Sets (flag != 0) or clears the context's abort flag.  The flag lives in mapped
+ * page-locked host memory, so it may be set from another host thread while a solve runs:
+ * the solve loops (V-cycles, outer corrections, the lower API's RBGS and CG solvers) test
+ * it before each cycle and the coarse solvers of the single-CTA tail kernels poll it on
+ * the device every 16 iterations; a solve that sees it returns PMG_ETIMEOUT with the
+ * solution of the last completed cycle.  The flag stays set until cleared. */
+int pmg_set_abort(pmg_ctx *ctx, int flag);
+/* Host-side fault injection for tests: n >= 0 makes the n-th next device allocation of the
+ * library (0 = the next one; every context, batch and lower-API scratch allocation counts)
+ * fail as cudaMalloc fails on an exhausted device, so the call that made it returns
+ * PMG_ENOMEM and releases what it had allocated; the injection is then disarmed.  n < 0
+ * disarms it.  Process-wide. */
+int pmg_inject_alloc_failure(long long n);
 
 /* Wait for all work issued on the context stream. */
 int pmg_sync(pmg_ctx *ctx);

@@ -70,6 +70,9 @@ _SIGS = {
     "pmg_selftest_convert": [c_void_p, c_void_p, c_void_p, c_void_p, c_int],
     "pmg_selftest_smooth32": [c_void_p, c_int, c_int, c_int, c_int, c_int, c_double, c_void_p, c_void_p,
                               c_void_p],
+    "pmg_selftest_wait_timeout": [c_void_p, c_int],
+    "pmg_set_abort": [c_void_p, c_int],
+    "pmg_inject_alloc_failure": [ctypes.c_longlong],
     "pmg_sync": [c_void_p],
     "pmg_last_error": [],
     "pmg_status_string": [c_int],

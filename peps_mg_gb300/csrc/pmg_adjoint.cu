@@ -99,15 +99,28 @@ int Ctx::adjoint(const double *dLdu, double *dLdb, double *dLdg, int maxit, doub
     const Level &S = lv[0];
     const size_t bytes = S.total * sizeof(double);
     if (!adj_rhs) {
-        PMG_TRY_A(cuda_status(cudaMalloc(&adj_rhs, bytes), "adjoint allocation"));
-        PMG_TRY_A(cuda_status(cudaMalloc(&adj_sol, bytes), "adjoint allocation"));
-        PMG_TRY_A(cuda_status(cudaMalloc(&adj_rsd, bytes), "adjoint allocation"));
-        PMG_TRY_A(cuda_status(cudaMalloc(&adj_vol, (S.n[0] + S.n[1] + S.n[2] + 6) * sizeof(double)), "adjoint"));
-        std::vector<double> h;
-        for (int d = 0; d < 3; ++d) h.insert(h.end(), S.dm[d].begin(), S.dm[d].end());
-        PMG_TRY_A(cuda_status(cudaMemcpy(adj_vol, h.data(), h.size() * sizeof(double), cudaMemcpyHostToDevice),
-                              "adjoint tables"));
-        PMG_TRY_A(cuda_status(cudaMalloc(&adj_faces, 6 * sizeof(double)), "adjoint allocation"));
+        // all buffers or none: a failure part way releases what it had allocated, so a
+        // later call starts again instead of finding a partial set
+        double *a[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
+        const size_t sz[5] = {bytes, bytes, bytes, (S.n[0] + S.n[1] + S.n[2] + 6) * sizeof(double),
+                              6 * sizeof(double)};
+        int st = PMG_OK;
+        for (int q = 0; q < 5 && st == PMG_OK; ++q) st = cuda_status(dev_malloc(&a[q], sz[q]), "adjoint allocation");
+        if (st == PMG_OK) {
+            std::vector<double> h;
+            for (int d = 0; d < 3; ++d) h.insert(h.end(), S.dm[d].begin(), S.dm[d].end());
+            st = cuda_status(cudaMemcpy(a[3], h.data(), h.size() * sizeof(double), cudaMemcpyHostToDevice),
+                             "adjoint tables");
+        }
+        if (st != PMG_OK) {
+            for (auto p : a) cudaFree(p);
+            return st;
+        }
+        adj_rhs = a[0];
+        adj_sol = a[1];
+        adj_rsd = a[2];
+        adj_vol = a[3];
+        adj_faces = a[4];
     }
     const double *dxm = adj_vol, *dym = adj_vol + S.n[0] + 2, *dzm = dym + S.n[1] + 2;
     const dim3 g((S.n[0] + kBX - 1) / kBX, (S.n[1] + kBY - 1) / kBY, std::min(S.n[2], 65535)), bl(kBX, kBY, 1);

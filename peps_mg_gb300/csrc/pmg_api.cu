@@ -33,6 +33,25 @@ int cuda_status(cudaError_t e, const char *what)
     return e == cudaErrorMemoryAllocation ? PMG_ENOMEM : PMG_ECUDA;
 }
 
+// Host-side fault injection of device allocations: -1 = off; n >= 0 = the n-th next
+// dev_malloc call (0 = the next one) fails once.
+static std::atomic<long long> g_alloc_fail_countdown{-1};
+
+cudaError_t dev_malloc_bytes(void **p, size_t bytes)
+{
+    long long c = g_alloc_fail_countdown.load();
+    while (c >= 0) {
+        if (g_alloc_fail_countdown.compare_exchange_weak(c, c - 1)) {
+            if (c == 0) {
+                *p = nullptr;
+                return cudaErrorMemoryAllocation;
+            }
+            break;
+        }
+    }
+    return cudaMalloc(p, bytes);
+}
+
 static std::atomic<long long> g_launches{0};
 void count_launches(long long n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
 long long launches_total() { return g_launches.load(); }
@@ -399,7 +418,7 @@ int Ctx::build(const pmg_config_t *c, cudaStream_t s)
             }
         }
     }
-    PMG_CUDA(cudaMalloc(&d_tables, blob.size() * sizeof(double)), "table allocation");
+    PMG_CUDA(dev_malloc(&d_tables, blob.size() * sizeof(double)), "table allocation");
     PMG_CUDA(cudaMemcpy(d_tables, blob.data(), blob.size() * sizeof(double), cudaMemcpyHostToDevice), "table copy");
     tables_host = blob;
 
@@ -467,9 +486,9 @@ int Ctx::build(const pmg_config_t *c, cudaStream_t s)
     size_t max_part = 1;
     for (int l = 1; l <= nl; ++l) {
         Level &L = lv[l];
-        PMG_CUDA(cudaMalloc(&L.x, L.total * sizeof(double)), "level allocation");
-        PMG_CUDA(cudaMalloc(&L.b, L.total * sizeof(double)), "level allocation");
-        PMG_CUDA(cudaMalloc(&L.r, L.total * sizeof(double)), "level allocation");
+        PMG_CUDA(dev_malloc(&L.x, L.total * sizeof(double)), "level allocation");
+        PMG_CUDA(dev_malloc(&L.b, L.total * sizeof(double)), "level allocation");
+        PMG_CUDA(dev_malloc(&L.r, L.total * sizeof(double)), "level allocation");
         PMG_CUDA(cudaMemset(L.x, 0, L.total * sizeof(double)), "level init");
         PMG_CUDA(cudaMemset(L.b, 0, L.total * sizeof(double)), "level init");
         PMG_CUDA(cudaMemset(L.r, 0, L.total * sizeof(double)), "level init");
@@ -480,18 +499,28 @@ int Ctx::build(const pmg_config_t *c, cudaStream_t s)
         max_part = std::max(max_part, (size_t)g.x * g.y * g.z);
     }
     npart_cap = max_part;
-    PMG_CUDA(cudaMalloc(&d_partials, npart_cap * sizeof(double)), "scratch allocation");
-    PMG_CUDA(cudaMalloc(&d_scal, 16 * sizeof(double)), "scratch allocation");
-    PMG_CUDA(cudaMalloc(&d_iscal, 16 * sizeof(int)), "scratch allocation");
+    PMG_CUDA(dev_malloc(&d_partials, npart_cap * sizeof(double)), "scratch allocation");
+    PMG_CUDA(dev_malloc(&d_scal, 16 * sizeof(double)), "scratch allocation");
+    PMG_CUDA(dev_malloc(&d_iscal, 16 * sizeof(int)), "scratch allocation");
+    PMG_CUDA(dev_malloc(&d_cg, sizeof(CgState)), "scratch allocation");
+    PMG_CUDA(cudaMemset(d_cg, 0, sizeof(CgState)), "scratch init");
+    {
+        void *h = nullptr, *d = nullptr;
+        PMG_CUDA(cudaHostAlloc(&h, sizeof(int), cudaHostAllocMapped), "abort flag allocation");
+        abort_host = static_cast<int *>(h);
+        *abort_host = 0;
+        PMG_CUDA(cudaHostGetDevicePointer(&d, h, 0), "abort flag mapping");
+        abort_dev = static_cast<const int *>(d);
+    }
     PMG_CUDA(cudaMemset(d_iscal, 0, 16 * sizeof(int)), "scratch init");
     {
         const Level &C = lv[nl];
         for (double **p : {&d_cp, &d_cap, &d_crr}) {
-            PMG_CUDA(cudaMalloc(p, C.total * sizeof(double)), "coarse scratch");
+            PMG_CUDA(dev_malloc(p, C.total * sizeof(double)), "coarse scratch");
             PMG_CUDA(cudaMemset(*p, 0, C.total * sizeof(double)), "coarse scratch");
         }
     }
-    PMG_CUDA(cudaMalloc(&d_tail, sizeof(TailDesc<double>)), "tail descriptor");
+    PMG_CUDA(dev_malloc(&d_tail, sizeof(TailDesc<double>)), "tail descriptor");
     PMG_CUDA(cudaEventCreate(&ev0), "event");
     PMG_CUDA(cudaEventCreate(&ev1), "event");
     PMG_CUDA(cudaEventCreateWithFlags(&ev_x, cudaEventDisableTiming), "event");
@@ -511,6 +540,8 @@ Ctx::~Ctx()
     cudaFree(d_partials);
     cudaFree(d_scal);
     cudaFree(d_iscal);
+    cudaFree(d_cg);
+    if (abort_host) cudaFreeHost(abort_host);
     cudaFree(d_cp);
     cudaFree(d_cap);
     cudaFree(d_crr);
@@ -579,6 +610,7 @@ int Ctx::upload_tail(int l0, int maxit, double omega, double tol)
         D.r[l] = lv[l].r;
     }
     fill_coarse64(D.C64, D.cx64, D.cb64, D.cp64, D.cap64, D.crr64, D.omega64, D.omw64, omega);
+    D.abort = abort_dev;
     PMG_CUDA(cudaMemcpyAsync(d_tail, &D, sizeof(D), cudaMemcpyHostToDevice, stream), "tail descriptor upload");
     return PMG_OK;
 }
@@ -620,6 +652,19 @@ int Ctx::vcycle_f64(double *sol, double *rsd, const double *rhs, int maxit, doub
     PMG_TRY(f64_restrict(X[0], launch[1], rsd, lv[1].b, stream));
     prof.end(pi, PC_RESTRICT64, 1, 9.0 * N, stream);
     const int grid_end = std::min(tail_l0, nl);
+    // grid levels below the finest, one profiler record each way: per cell of level l,
+    // 16 B per half-sweep, 24 B residual, 9 B restriction (down); 17 B prolongation + add,
+    // 16 B per half-sweep (up)
+    auto coarse_bytes = [&](bool down) {
+        double b = 0.0;
+        for (int l = 1; l < grid_end; ++l) {
+            const double n = (double)K[l].nx * K[l].ny * K[l].nz;
+            b += down ? (32.0 * maxit + 24.0 + 9.0) * n : (17.0 + 32.0 * maxit) * n;
+        }
+        return b;
+    };
+    const int coarse_launches = std::max(0, grid_end - 1) * (2 * maxit + 2);
+    int pc = grid_end > 1 ? prof.begin(stream) : -1;
     for (int l = 1; l < grid_end; ++l) {
         Level &L = lv[l];
         PMG_CUDA(cudaMemsetAsync(L.x, 0, L.total * sizeof(double), stream), "level reset");
@@ -627,6 +672,7 @@ int Ctx::vcycle_f64(double *sol, double *rsd, const double *rhs, int maxit, doub
         PMG_TRY(f64_residual(K[l], launch[l], L.r, L.x, L.b, nullptr, nullptr, stream));
         PMG_TRY(f64_restrict(X[l], launch[l + 1], L.r, lv[l + 1].b, stream));
     }
+    if (coarse_launches > 0) prof.end(pc, PC_COARSE64, coarse_launches, coarse_bytes(true) / coarse_launches, stream);
     if (tail_l0 <= nl) {
         pi = prof.begin(stream);
         PMG_TRY(f64_tail(d_tail, tail_threads, stream));
@@ -640,11 +686,14 @@ int Ctx::vcycle_f64(double *sol, double *rsd, const double *rhs, int maxit, doub
     } else {
         PMG_TRY(coarse_solve_grid(tol, omega, coarse_iters));
     }
+    pc = grid_end > 1 ? prof.begin(stream) : -1;
     for (int l = grid_end - 1; l >= 1; --l) {
         Level &L = lv[l];
         PMG_TRY(f64_prolong(X[l], launch[l + 1], lv[l + 1].x, L.x, true, stream));
         PMG_TRY(f64_rbgs_sweeps(K[l], launch[l], L.x, L.b, maxit, omega, stream));
     }
+    const int up_launches = std::max(0, grid_end - 1) * (2 * maxit + 1);
+    if (up_launches > 0) prof.end(pc, PC_COARSE64, up_launches, coarse_bytes(false) / up_launches, stream);
     pi = prof.begin(stream);
     PMG_TRY(f64_prolong(X[0], launch[1], lv[1].x, sol, true, stream));
     prof.end(pi, PC_PROLONG64, 1, 17.0 * N, stream);
@@ -652,6 +701,13 @@ int Ctx::vcycle_f64(double *sol, double *rsd, const double *rhs, int maxit, doub
     PMG_TRY(f64_rbgs_sweeps(K[0], launch[0], sol, rhs, maxit, omega, stream));
     prof.end(pi, PC_SMOOTH64, 2 * maxit, 16.0 * N, stream);
     return PMG_OK;
+}
+
+// Status of a solve that stopped because the abort flag was set.
+int Ctx::abort_status()
+{
+    set_error("stopped by the abort flag (pmg_set_abort)");
+    return PMG_ETIMEOUT;
 }
 
 int Ctx::solve_f64(double *sol, double *rsd, const double *rhs, int maxit, double tol, double omega,
@@ -664,10 +720,35 @@ int Ctx::solve_f64(double *sol, double *rsd, const double *rhs, int maxit, doubl
     double h[2];
     PMG_TRY(fetch_scalars(h, 1));
     const double res0tol = h[0];
+    if (res0tol == 0.0) {
+        // An exactly zero initial residual (e.g. rhs = 0 and sol = 0): sol already solves
+        // the system, so the solve returns at once with sol unchanged, rsd = b - A x, no
+        // cycles and ratio 0.  The reference divides by the zero norm instead
+        // (src/multigrid.f90:1973) and runs all its cycles on NaN ratios; for rhs = 0,
+        // sol = 0 those leave sol = 0 as well.
+        if (rep) {
+            rep->cycles = 0;
+            rep->converged = 1;
+            rep->res0 = 0.0;
+            rep->final_ratio = 0.0;
+            rep->inner_cycles = 0;
+        }
+        return PMG_OK;
+    }
     if (tail_l0 <= nl) PMG_TRY(upload_tail(tail_l0, maxit, omega, tol));
     int cycles = 0, converged = 0;
     double ratio = 0.0;
     for (int cyc = 1; cyc <= n_vcycles; ++cyc) {
+        if (aborted()) {
+            if (rep) {
+                rep->cycles = cycles;
+                rep->converged = 0;
+                rep->res0 = std::sqrt(res0tol);
+                rep->final_ratio = ratio;
+                rep->inner_cycles = cycles;
+            }
+            return abort_status();
+        }
         int ci = 0;
         PMG_TRY(vcycle_f64(sol, rsd, rhs, maxit, omega, tol, rep && rep->coarse_iterations ? &ci : nullptr));
         int pr = prof.begin(stream);
@@ -719,14 +800,9 @@ int Ctx::level_scratch(int l, double **bufs, int count)
     const size_t need = lv[l].total * (size_t)count;
     if (scratch_cap < need) {
         for (auto &v : scratch_levels) cudaFree(v);
-    cudaFree(adj_rhs);
-    cudaFree(adj_sol);
-    cudaFree(adj_rsd);
-    cudaFree(adj_vol);
-    cudaFree(adj_faces);
         scratch_levels.clear();
         double *p = nullptr;
-        PMG_CUDA(cudaMalloc(&p, need * sizeof(double)), "scratch allocation");
+        PMG_CUDA(dev_malloc(&p, need * sizeof(double)), "scratch allocation");
         scratch_levels.push_back(p);
         scratch_cap = need;
     }
@@ -748,6 +824,7 @@ int Ctx::rbgs_solver_dev(int l, double *x, const double *b, int maxit, double to
     double rn = r0;
     int it = 0;
     for (it = 0; it < maxit; ++it) {
+        if (aborted()) return abort_status();
         PMG_TRY(f64_rbgs_sweeps(K[l], launch[l], x, b, 1, omega, stream));
         PMG_TRY(residual_norm(l, rs, x, b, 3));
         PMG_TRY(fetch_scalars(h, 4));
@@ -759,47 +836,38 @@ int Ctx::rbgs_solver_dev(int l, double *x, const double *b, int maxit, double to
     return PMG_OK;
 }
 
-// cg_solver_poisson_matrix / cg_iterator_poisson_matrix (src/cg_poisson_matrix.f90)
+// cg_solver_poisson_matrix / cg_iterator_poisson_matrix (src/cg_poisson_matrix.f90) with
+// the fused kernels of pmg_f64.cu: the scalars stay on the device, and the solver reads
+// the exit flag once every kCgCheckEvery iterations (iterations queued after the exit
+// return at once).
 int Ctx::cg_dev(int l, double *x, const double *b, int maxit, double tol, bool check, int *iters,
                 double *ratio_out)
 {
+    constexpr int kCgCheckEvery = 8;
     double *bufs[3];
     PMG_TRY(level_scratch(l, bufs, 3));
     double *p = bufs[0], *ap = bufs[1], *rs = bufs[2];
-    double *s = d_scal;   // 4: rsd0tol, 5: temp1, 6: temp2 (p.Ap), 7: alpha, 8: temp2 (r.r), 9: beta
-    PMG_TRY(f64_residual(K[l], launch[l], rs, x, b, nullptr, nullptr, stream));
-    PMG_TRY(f64_copy_interior(K[l], p, rs, stream));
-    double r0 = 0.0, t2 = 0.0;
-    if (check) {
-        PMG_TRY(dot(l, rs, rs, 4));
-        double h[5];
-        PMG_TRY(fetch_scalars(h, 5));
-        r0 = h[4];
+    if ((size_t)f64_cg_partials(K[l], launch[l]) > npart_cap) {
+        set_error("cg: partial-sum buffer too small for the level");
+        return PMG_EINVAL;
     }
-    int it = 0;
-    for (it = 0; it < maxit; ++it) {
-        PMG_TRY(dot(l, rs, rs, 5));
-        PMG_TRY(f64_mv_mul(K[l], launch[l], ap, p, stream));
-        PMG_TRY(dot(l, ap, p, 6));
-        PMG_TRY(f64_cg_scalar(s + 5, s + 6, s + 7, stream));
-        PMG_TRY(f64_cg_update_xr(K[l], launch[l], s + 7, x, rs, p, ap, stream));
-        PMG_TRY(dot(l, rs, rs, 8));
-        if (check) {
-            double h[9];
-            PMG_TRY(fetch_scalars(h, 9));
-            t2 = h[8];
-            if (std::sqrt(t2 / r0) < tol) break;
+    PMG_TRY(f64_cg_init(K[l], launch[l], rs, p, x, b, d_partials, d_cg, stream));
+    CgState h{};
+    for (int it0 = 0; it0 < maxit; it0 += kCgCheckEvery) {
+        if (aborted()) return abort_status();
+        const int it1 = std::min(maxit, it0 + kCgCheckEvery);
+        for (int it = it0; it < it1; ++it)
+            PMG_TRY(f64_cg_iteration(K[l], launch[l], x, rs, p, ap, d_partials, d_cg, tol, check, it, stream));
+        if (check && it1 < maxit) {
+            PMG_CUDA(cudaMemcpyAsync(&h, d_cg, sizeof(h), cudaMemcpyDeviceToHost, stream), "cg state read");
+            PMG_CUDA(cudaStreamSynchronize(stream), "stream sync");
+            if (h.done) break;
         }
-        PMG_TRY(f64_cg_scalar(s + 8, s + 5, s + 9, stream));
-        PMG_TRY(f64_cg_update_p(K[l], launch[l], s + 9, p, rs, stream));
     }
-    if (!check) {
-        double h[9];
-        PMG_TRY(fetch_scalars(h, 9));
-        t2 = h[8];
-    }
-    if (iters) *iters = it;
-    if (ratio_out) *ratio_out = check ? std::sqrt(t2 / r0) : std::sqrt(t2);
+    PMG_CUDA(cudaMemcpyAsync(&h, d_cg, sizeof(h), cudaMemcpyDeviceToHost, stream), "cg state read");
+    PMG_CUDA(cudaStreamSynchronize(stream), "stream sync");
+    if (iters) *iters = h.done ? h.iter : maxit;
+    if (ratio_out) *ratio_out = check ? std::sqrt(h.t2 / h.r0) : std::sqrt(h.t2);
     return PMG_OK;
 }
 
@@ -865,9 +933,18 @@ int Ctx::solve(double *sol, double *rsd, const double *rhs, int maxit, double to
     const double *b = rhs;
     if (!dev) {
         if (!stage_sol) {
-            PMG_CUDA(cudaMalloc(&stage_sol, bytes), "staging allocation");
-            PMG_CUDA(cudaMalloc(&stage_rsd, bytes), "staging allocation");
-            PMG_CUDA(cudaMalloc(&stage_rhs, bytes), "staging allocation");
+            // all three or none: a failed allocation leaves no partial set behind
+            double *a[3] = {nullptr, nullptr, nullptr};
+            for (int q = 0; q < 3; ++q) {
+                const int st = cuda_status(dev_malloc(&a[q], bytes), "staging allocation");
+                if (st != PMG_OK) {
+                    for (int u = 0; u < q; ++u) cudaFree(a[u]);
+                    return st;
+                }
+            }
+            stage_sol = a[0];
+            stage_rsd = a[1];
+            stage_rhs = a[2];
         }
         PMG_CUDA(cudaMemcpyAsync(stage_sol, sol, bytes, cudaMemcpyHostToDevice, stream), "H2D");
         PMG_CUDA(cudaMemcpyAsync(stage_rhs, rhs, bytes, cudaMemcpyHostToDevice, stream), "H2D");
@@ -1216,6 +1293,22 @@ int pmg_launch_count(long long *count)
     return PMG_OK;
 }
 
+int pmg_inject_alloc_failure(long long n)
+{
+    pmg::g_alloc_fail_countdown.store(n < 0 ? -1 : n);
+    return PMG_OK;
+}
+
+int pmg_set_abort(pmg_ctx *ctx, int flag)
+{
+    if (!ctx) {
+        pmg::set_error("pmg_set_abort: ctx is NULL");
+        return PMG_EINVAL;
+    }
+    __atomic_store_n(ctx->impl.abort_host, flag ? 1 : 0, __ATOMIC_RELEASE);
+    return PMG_OK;
+}
+
 int pmg_selftest_convert(const double *in64, float *out32, const float *in32, double *out64, int n)
 {
     if (n < 0 || (n > 0 && (!in64 || !out32 || !in32 || !out64))) {
@@ -1237,6 +1330,12 @@ int pmg_selftest_smooth32(pmg_ctx *ctx, int level, int impl, int variant, int kc
         return PMG_EINVAL;
     }
     return ctx->impl.selftest_smooth32(level, impl, variant, kchunk, zero_in != 0, omega, e_in, b, e_out);
+}
+
+int pmg_selftest_wait_timeout(pmg_ctx *ctx, int level)
+{
+    PMG_TRY(check_ctx_level(ctx, level));
+    return ctx->impl.selftest_wait_timeout(level);
 }
 
 int pmg_sync(pmg_ctx *ctx)

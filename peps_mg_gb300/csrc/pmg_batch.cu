@@ -112,6 +112,7 @@ struct BatchTmaSrc {
     }
     __device__ __forceinline__ const CUtensorMap *map_e(int it) const { return &maps[items[it].p].e[which][vi]; }
     __device__ __forceinline__ const CUtensorMap *map_b(int it) const { return &maps[items[it].p].b[vi]; }
+    __device__ __forceinline__ bool stall() const { return false; }
 };
 
 template <int TY, bool ZERO_IN, bool OMEGA1>
@@ -487,7 +488,7 @@ template <typename T>
 int upload(const std::vector<T> &h, T **d)
 {
     if (h.empty()) return PMG_OK;
-    int rc = cuda_status(cudaMalloc(d, h.size() * sizeof(T)), "batch allocation");
+    int rc = cuda_status(dev_malloc(d, h.size() * sizeof(T)), "batch allocation");
     if (rc != PMG_OK) return rc;
     return cuda_status(cudaMemcpy(*d, h.data(), h.size() * sizeof(T), cudaMemcpyHostToDevice), "batch upload");
 }
@@ -719,7 +720,7 @@ int batch_create(Batch **out, int n, const int *dims, const double *const *meshe
             }
         }
         PMG_TRY_B(upload(maps, &B->d_maps));
-        PMG_TRY_B(cuda_status(cudaMalloc(&B->d_err, sizeof(int)), "batch allocation"));
+        PMG_TRY_B(cuda_status(dev_malloc(&B->d_err, sizeof(int)), "batch allocation"));
         PMG_TRY_B(cuda_status(cudaMemset(B->d_err, 0, sizeof(int)), "batch init"));
     }
     // work lists
@@ -762,24 +763,24 @@ int batch_create(Batch **out, int n, const int *dims, const double *const *meshe
         PMG_TRY_B(upload(it, &B->outer.d));
         PMG_TRY_B(upload(B->first_item, &B->d_first));
     }
-    PMG_TRY_B(cuda_status(cudaMalloc(&B->d_partials, (size_t)B->outer.n * sizeof(double)), "batch allocation"));
-    PMG_TRY_B(cuda_status(cudaMalloc(&B->d_res0, n * sizeof(double)), "batch allocation"));
-    PMG_TRY_B(cuda_status(cudaMalloc(&B->d_ratio, n * sizeof(double)), "batch allocation"));
-    PMG_TRY_B(cuda_status(cudaMalloc(&B->d_done, n * sizeof(int)), "batch allocation"));
+    PMG_TRY_B(cuda_status(dev_malloc(&B->d_partials, (size_t)B->outer.n * sizeof(double)), "batch allocation"));
+    PMG_TRY_B(cuda_status(dev_malloc(&B->d_res0, n * sizeof(double)), "batch allocation"));
+    PMG_TRY_B(cuda_status(dev_malloc(&B->d_ratio, n * sizeof(double)), "batch allocation"));
+    PMG_TRY_B(cuda_status(dev_malloc(&B->d_done, n * sizeof(int)), "batch allocation"));
     PMG_TRY_B(cuda_status(cudaMemset(B->d_done, 0, n * sizeof(int)), "batch init"));
-    PMG_TRY_B(cuda_status(cudaMalloc(&B->d_cycles, n * sizeof(int)), "batch allocation"));
-    PMG_TRY_B(cuda_status(cudaMalloc(&B->d_mode, n * sizeof(int)), "batch allocation"));
-    PMG_TRY_B(cuda_status(cudaMalloc(&B->d_nonzero, n * sizeof(int)), "batch allocation"));
-    PMG_TRY_B(cuda_status(cudaMalloc(&B->d_offset, (n + 1) * sizeof(long long)), "batch allocation"));
+    PMG_TRY_B(cuda_status(dev_malloc(&B->d_cycles, n * sizeof(int)), "batch allocation"));
+    PMG_TRY_B(cuda_status(dev_malloc(&B->d_mode, n * sizeof(int)), "batch allocation"));
+    PMG_TRY_B(cuda_status(dev_malloc(&B->d_nonzero, n * sizeof(int)), "batch allocation"));
+    PMG_TRY_B(cuda_status(dev_malloc(&B->d_offset, (n + 1) * sizeof(long long)), "batch allocation"));
     PMG_TRY_B(cuda_status(cudaMemcpy(B->d_offset, B->offset.data(), (n + 1) * sizeof(long long),
                                      cudaMemcpyHostToDevice), "batch upload"));
-    PMG_TRY_B(cuda_status(cudaMalloc(&B->d_check, n * sizeof(int)), "batch allocation"));
-    PMG_TRY_B(cuda_status(cudaMalloc(&B->d_cheap, n * sizeof(double)), "batch allocation"));
-    PMG_TRY_B(cuda_status(cudaMalloc(&B->d_prev, n * sizeof(double)), "batch allocation"));
-    PMG_TRY_B(cuda_status(cudaMalloc(&B->d_contr, n * sizeof(double)), "batch allocation"));
+    PMG_TRY_B(cuda_status(dev_malloc(&B->d_check, n * sizeof(int)), "batch allocation"));
+    PMG_TRY_B(cuda_status(dev_malloc(&B->d_cheap, n * sizeof(double)), "batch allocation"));
+    PMG_TRY_B(cuda_status(dev_malloc(&B->d_prev, n * sizeof(double)), "batch allocation"));
+    PMG_TRY_B(cuda_status(dev_malloc(&B->d_contr, n * sizeof(double)), "batch allocation"));
     PMG_TRY_B(cuda_status(cudaMemset(B->d_check, 0, n * sizeof(int)), "batch init"));
-    PMG_TRY_B(cuda_status(cudaMalloc(&B->d_ndone, sizeof(int)), "batch allocation"));
-    PMG_TRY_B(cuda_status(cudaMalloc(&B->rsd, (size_t)B->total * sizeof(double)), "batch allocation"));
+    PMG_TRY_B(cuda_status(dev_malloc(&B->d_ndone, sizeof(int)), "batch allocation"));
+    PMG_TRY_B(cuda_status(dev_malloc(&B->rsd, (size_t)B->total * sizeof(double)), "batch allocation"));
     PMG_TRY_B(cuda_status(cudaMemset(B->rsd, 0, (size_t)B->total * sizeof(double)), "batch init"));
     {
         std::vector<const TailDesc<float> *> t((size_t)n);
@@ -926,7 +927,7 @@ int batch_solve(Batch &B, double *sol, const double *rhs, int maxit, double tol,
         B.h_outer[p] = o;
         PMG_TRY_B(c.upload_tail32(maxit, omega, tol));
     }
-    if (!B.d_outer) PMG_TRY_B(cuda_status(cudaMalloc(&B.d_outer, n * sizeof(BOuter)), "batch allocation"));
+    if (!B.d_outer) PMG_TRY_B(cuda_status(dev_malloc(&B.d_outer, n * sizeof(BOuter)), "batch allocation"));
     PMG_TRY_B(cuda_status(cudaMemcpyAsync(B.d_outer, B.h_outer.data(), n * sizeof(BOuter), cudaMemcpyHostToDevice,
                                           B.stream), "batch upload"));
     if (B.variant[0] < 0) PMG_TRY_B(batch_autotune(B));

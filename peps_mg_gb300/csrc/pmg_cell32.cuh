@@ -547,7 +547,7 @@ __device__ void tail32_run(const TailDesc<float> &D, const LevelK<float> *Ls, co
             int iters = 0;
             if (threadIdx.x < 32)
                 iters = coarse_solve_warp_f64(C, cs[0], cs[1], cs[2], cs[3], cs[4], D.coarse_solver, D.coarse_maxit,
-                                              D.tol, D.omega64, D.omw64);
+                                              D.tol, D.omega64, D.omw64, D.abort);
             if (threadIdx.x == 0 && D.iters_out) *D.iters_out = iters;
             __syncthreads();
             for_cells(L.nx, L.ny, L.nz, [&](int i, int j, int k) {
@@ -559,7 +559,7 @@ __device__ void tail32_run(const TailDesc<float> &D, const LevelK<float> *Ls, co
             });
             __syncthreads();
             const int iters = coarse_solve_f64(C, D.cx64, D.cb64, D.cp64, D.cap64, D.crr64, D.coarse_solver,
-                                               D.coarse_maxit, D.tol, D.omega64, D.omw64, sw);
+                                               D.coarse_maxit, D.tol, D.omega64, D.omw64, sw, D.abort);
             for_cells(L.nx, L.ny, L.nz, [&](int i, int j, int k) {
                 x[lin(i, j, k, L.sy, L.sz)] = (float)D.cx64[lin(i, j, k, C.sy, C.sz)];
             });

@@ -76,6 +76,13 @@ struct Ctx {
     double *d_scal = nullptr;
     int *d_iscal = nullptr;
     double *d_cp = nullptr, *d_cap = nullptr, *d_crr = nullptr;
+    CgState *d_cg = nullptr;   // scalars of the fused CG solver (lower API, large coarsest levels)
+    // Abort flag (pmg_set_abort) in mapped page-locked host memory: the host loops read it
+    // between cycles, the coarse solvers of the single-CTA tails poll it on the device.
+    int *abort_host = nullptr;
+    const int *abort_dev = nullptr;
+    bool aborted() const { return abort_host && __atomic_load_n(abort_host, __ATOMIC_ACQUIRE) != 0; }
+    int abort_status();
     double *stage_sol = nullptr, *stage_rsd = nullptr, *stage_rhs = nullptr;
     std::vector<double *> scratch_levels;
     size_t scratch_cap = 0;
@@ -112,6 +119,7 @@ struct Ctx {
     int solve_mixed(double *sol, double *rsd, const double *rhs, int maxit, double tol, double omega,
                     pmg_report_t *rep);
     int setup_mixed();
+    int build_mixed();
     int upload_tail32(int maxit, double omega, double tol);
     int vcycle32(int maxit, double omega, bool zero_start);
     int outer_residual(double *sol, double *rsd, const double *rhs, int slot);
@@ -122,6 +130,7 @@ struct Ctx {
     int resrestrict32(int l);
     int selftest_smooth32(int level, int impl, int variant, int kchunk, bool zero_in, double omega,
                           const double *e_in, const double *b, double *e_out);
+    int selftest_wait_timeout(int level);
     void destroy_mixed();
     int solve(double *sol, double *rsd, const double *rhs, int maxit, double tol, double omega, pmg_report_t *rep);
     int level_scratch(int l, double **bufs, int count);

@@ -75,8 +75,13 @@ __global__ void __launch_bounds__(1024) k_reduce_static(const double *__restrict
 std::mutex g_setup_mu;
 double *g_scratch_ptr[kMaxDevices] = {};
 
-// Once per device, with that device current: the address of this device's copy of the
-// scratch array, which is then cleared (in the order of stream s).
+// With the device current: the address of this device's copy of the scratch array.  The
+// address is looked up on every call (a host-side query that allocates nothing), so a
+// context that the caller destroyed and re-created, e.g. by cudaDeviceReset, is served
+// with the array of the new context and never with a stale address.  The array is
+// cleared (in the order of stream s) whenever its address differs from the one this
+// device's previous call saw, which includes the first call on each device; no result
+// depends on that clearing, since every slot a call reads is written earlier in the call.
 int scratch_for_current_device(cudaStream_t s, double **out)
 {
     int dev = 0;
@@ -86,17 +91,18 @@ int scratch_for_current_device(cudaStream_t s, double **out)
                   std::to_string(kMaxDevices) + " devices this entry point serves");
         return PMG_EINVAL;
     }
+    double *ptr = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress((void **)&ptr, g_dot_scratch);
+    if (e != cudaSuccess || !ptr)
+        return cuda_status(e != cudaSuccess ? e : cudaErrorInvalidSymbol,
+                           "pmg_vv_dot_static: address of the static scratch");
     std::lock_guard<std::mutex> g(g_setup_mu);
-    if (!g_scratch_ptr[dev]) {
-        double *ptr = nullptr;
-        const cudaError_t e = cudaGetSymbolAddress((void **)&ptr, g_dot_scratch);
-        if (e != cudaSuccess || !ptr) return cuda_status(e != cudaSuccess ? e : cudaErrorInvalidSymbol,
-                                                         "pmg_vv_dot_static: address of the static scratch");
+    if (g_scratch_ptr[dev] != ptr) {
         PMG_TRY_D(cuda_status(cudaMemsetAsync(ptr, 0, sizeof(g_dot_scratch), s),
                               "pmg_vv_dot_static: clearing the static scratch"));
         g_scratch_ptr[dev] = ptr;
     }
-    *out = g_scratch_ptr[dev];
+    *out = ptr;
     return PMG_OK;
 }
 

@@ -154,61 +154,149 @@ __global__ void k_zero_ghosts_f64(double *a, int nx, int ny, int nz)
     }
 }
 
-// Interior copy dst = src (src/cg_poisson_matrix.f90:88: p = rsd).
-__global__ void k_copy_interior_f64(LevelK<double> L, double *__restrict__ d, const double *__restrict__ s)
+// ------------------------------------------------------------------------------------
+// Fused CG (cg_solver_poisson_matrix / cg_iterator_poisson_matrix,
+// src/cg_poisson_matrix.f90:80-138 and :190-238).  Per iteration the reference makes
+// six passes over the level (r.r, A p, Ap.p, the x/r update, r.r, the p update) plus two
+// scalar divisions; here three kernels do the same arithmetic:
+//   k_cg_apdot   Ap = A p and the sum Ap.p; its last CTA forms alpha = temp1 / (Ap.p)
+//   k_cg_update  x += alpha p, r -= alpha Ap and the sum r.r; its last CTA forms temp2,
+//                the exit test sqrt(temp2/rsd0tol) < tol and beta = temp2 / temp1
+//   k_cg_p       p = r + beta p
+// temp1 of an iteration is r.r of the previous one: the reference recomputes it from the
+// same r (:107), which gives the same value.  Each kernel's sum is one partial per CTA
+// (fixed order inside the CTA), added by the last CTA to arrive in a fixed order, so the
+// result depends only on the grid, which is a function of the level.  The scalars stay
+// on the device (CgState); kernels launched after the exit test was met return at once,
+// so the host only reads the state every few iterations.
+// ------------------------------------------------------------------------------------
+__device__ __forceinline__ bool cg_arrive_last(CgState *st, double s, double *partials)
 {
+    __shared__ unsigned int ticket;
+    if (tid_in_block() == 0) {
+        partials[block_lin()] = s;
+        __threadfence();
+        ticket = atomicAdd(&st->arrive, 1u);
+    }
+    __syncthreads();
+    return ticket == gridDim.x * gridDim.y * gridDim.z - 1;
+}
+
+// Sum of the CTAs' partials in a fixed order (called by every thread of the last CTA).
+__device__ __forceinline__ double cg_sum_partials(const double *partials, double *sw)
+{
+    __threadfence();
+    const int n = (int)(gridDim.x * gridDim.y * gridDim.z);
+    double acc = 0.0;
+    for (int q = tid_in_block(); q < n; q += blockDim.x * blockDim.y) acc = __dadd_rn(acc, __ldcg(partials + q));
+    return block_sum(acc, sw);
+}
+
+// r = b - A x, p = r (src/cg_poisson_matrix.f90:80-91), rsd0tol = temp1 = r.r (:94, :107)
+__global__ void __launch_bounds__(kBX *kBY) k_cg_init(LevelK<double> L, double *__restrict__ r,
+                                                      double *__restrict__ p, const double *__restrict__ x,
+                                                      const double *__restrict__ b, double *partials, CgState *st)
+{
+    double acc = 0.0;
     for (int k = blockIdx.z + 1; k <= L.nz; k += gridDim.z)
         for (int j = blockIdx.y * blockDim.y + threadIdx.y + 1; j <= L.ny; j += gridDim.y * blockDim.y)
             for (int i = blockIdx.x * blockDim.x + threadIdx.x + 1; i <= L.nx; i += gridDim.x * blockDim.x) {
-                const long long p = lin(i, j, k, L.sy, L.sz);
-                d[p] = s[p];
+                const long long q = lin(i, j, k, L.sy, L.sz);
+                const double v = __dsub_rn(b[q], ax_cell_f64(L, x, i, j, k));
+                r[q] = v;
+                p[q] = v;
+                acc = __dadd_rn(acc, __dmul_rn(v, v));
             }
+    __shared__ double sw[kBX * kBY / 32];
+    const double s = block_sum(acc, sw);
+    if (cg_arrive_last(st, s, partials)) {
+        const double t = cg_sum_partials(partials, sw);
+        if (tid_in_block() == 0) {
+            st->r0 = t;
+            st->t1 = t;
+            st->t2 = t;
+            st->done = 0;
+            st->iter = 0;
+            st->arrive = 0;
+        }
+    }
 }
 
-__global__ void k_cg_scalar_f64(const double *num, const double *den, double *out)
+// Ap = A p (src/poisson_matrix_operator.f90:146-159), temp2 = Ap.p (:112), alpha (:114)
+__global__ void __launch_bounds__(kBX *kBY) k_cg_apdot(LevelK<double> L, const double *__restrict__ p,
+                                                       double *__restrict__ ap, double *partials, CgState *st)
 {
-    *out = __ddiv_rn(*num, *den);
+    if (st->done) return;
+    double acc = 0.0;
+    for (int k = blockIdx.z + 1; k <= L.nz; k += gridDim.z)
+        for (int j = blockIdx.y * blockDim.y + threadIdx.y + 1; j <= L.ny; j += gridDim.y * blockDim.y)
+            for (int i = blockIdx.x * blockDim.x + threadIdx.x + 1; i <= L.nx; i += gridDim.x * blockDim.x) {
+                const long long q = lin(i, j, k, L.sy, L.sz);
+                const double v = ax_cell_f64(L, p, i, j, k);
+                ap[q] = v;
+                acc = __dadd_rn(acc, __dmul_rn(v, p[q]));
+            }
+    __shared__ double sw[kBX * kBY / 32];
+    const double s = block_sum(acc, sw);
+    if (cg_arrive_last(st, s, partials)) {
+        const double t = cg_sum_partials(partials, sw);
+        if (tid_in_block() == 0) {
+            st->pap = t;
+            st->alpha = __ddiv_rn(st->t1, t);
+            st->arrive = 0;
+        }
+    }
 }
 
-// sol = sol + alpha p ; rsd = rsd - alpha Ap (src/cg_poisson_matrix.f90:117-118)
-__global__ void __launch_bounds__(kBX *kBY) k_cg_xr_f64(LevelK<double> L, const double *alpha_p,
-                                                        double *__restrict__ x, double *__restrict__ r,
-                                                        const double *__restrict__ p,
-                                                        const double *__restrict__ ap)
+// sol += alpha p, rsd -= alpha Ap (:117-118), temp2 = r.r (:123), exit test (:126),
+// beta = temp2 / temp1 (:128)
+__global__ void __launch_bounds__(kBX *kBY) k_cg_update(LevelK<double> L, double *__restrict__ x,
+                                                        double *__restrict__ r, const double *__restrict__ p,
+                                                        const double *__restrict__ ap, double *partials, CgState *st,
+                                                        double tol, int check, int iter)
 {
-    const double alpha = *alpha_p;
+    if (st->done) return;
+    const double alpha = st->alpha;
+    double acc = 0.0;
     for (int k = blockIdx.z + 1; k <= L.nz; k += gridDim.z)
         for (int j = blockIdx.y * blockDim.y + threadIdx.y + 1; j <= L.ny; j += gridDim.y * blockDim.y)
             for (int i = blockIdx.x * blockDim.x + threadIdx.x + 1; i <= L.nx; i += gridDim.x * blockDim.x) {
                 const long long q = lin(i, j, k, L.sy, L.sz);
                 x[q] = __dadd_rn(x[q], __dmul_rn(alpha, p[q]));
-                r[q] = __dsub_rn(r[q], __dmul_rn(alpha, ap[q]));
+                const double v = __dsub_rn(r[q], __dmul_rn(alpha, ap[q]));
+                r[q] = v;
+                acc = __dadd_rn(acc, __dmul_rn(v, v));
             }
+    __shared__ double sw[kBX * kBY / 32];
+    const double s = block_sum(acc, sw);
+    if (cg_arrive_last(st, s, partials)) {
+        const double t = cg_sum_partials(partials, sw);
+        if (tid_in_block() == 0) {
+            st->t2 = t;
+            if (check && sqrt(__ddiv_rn(t, st->r0)) < tol) {
+                st->done = 1;
+                st->iter = iter;
+            } else {
+                st->beta = __ddiv_rn(t, st->t1);
+                st->t1 = t;
+            }
+            st->arrive = 0;
+        }
+    }
 }
 
-// p = rsd + beta p (src/cg_poisson_matrix.f90:134)
-__global__ void __launch_bounds__(kBX *kBY) k_cg_p_f64(LevelK<double> L, const double *beta_p,
-                                                       double *__restrict__ p, const double *__restrict__ r)
+// p = rsd + beta p (:134)
+__global__ void __launch_bounds__(kBX *kBY) k_cg_p(LevelK<double> L, double *__restrict__ p,
+                                                   const double *__restrict__ r, const CgState *st)
 {
-    const double beta = *beta_p;
+    if (st->done) return;
+    const double beta = st->beta;
     for (int k = blockIdx.z + 1; k <= L.nz; k += gridDim.z)
         for (int j = blockIdx.y * blockDim.y + threadIdx.y + 1; j <= L.ny; j += gridDim.y * blockDim.y)
             for (int i = blockIdx.x * blockDim.x + threadIdx.x + 1; i <= L.nx; i += gridDim.x * blockDim.x) {
                 const long long q = lin(i, j, k, L.sy, L.sz);
                 p[q] = __dadd_rn(r[q], __dmul_rn(beta, p[q]));
             }
-}
-
-__global__ void k_check_f64(const double *num, const double *den, double tol, int le, int iter, int *flag,
-                            int *iter_out)
-{
-    if (*flag) return;
-    const double ratio = sqrt(__ddiv_rn(*num, *den));
-    const bool done = le ? (ratio <= tol) : (ratio < tol);
-    if (done) {
-        *flag = 1;
-        *iter_out = iter;
-    }
 }
 
 // ------------------------------------------------------------------------------------
@@ -237,7 +325,7 @@ __global__ void __launch_bounds__(kTailThreads) k_tail_f64(const TailDesc<double
     // coarsest level, src/multigrid.f90:1819-1851
     {
         const int iters = coarse_solve_f64(D.C64, D.cx64, D.cb64, D.cp64, D.cap64, D.crr64, D.coarse_solver,
-                                           D.coarse_maxit, D.tol, D.omega64, D.omw64, sw);
+                                           D.coarse_maxit, D.tol, D.omega64, D.omw64, sw, D.abort);
         if (threadIdx.x == 0 && D.iters_out) *D.iters_out = iters;
         __syncthreads();
     }
@@ -358,46 +446,44 @@ int f64_tail(const TailDesc<double> *dev_desc, int threads, cudaStream_t s)
     return cuda_status(cudaGetLastError(), "coarse tail");
 }
 
-int f64_copy_interior(const LevelK<double> &L, double *dst, const double *src, cudaStream_t s)
+
+// Grid of the fused CG kernels: the level's CTA tiles in x and y, and enough z planes per
+// CTA that the grid is about four waves of 256-thread CTAs (at most 4864 CTAs, so the
+// last CTA's sum over the partials stays short); collapsed axes keep one CTA column.
+static dim3 cg_grid(const LevelK<double> &L, const Launch &ln)
 {
-    const Launch ln{{false, false, false}};
-    const dim3 g = grid3(L.nx, L.ny, L.nz, ln), bl(kBX, kBY, 1);
-    k_copy_interior_f64<<<g, bl, 0, s>>>(L, dst, src);
-    count_launches(1);
-    return cuda_status(cudaGetLastError(), "copy");
+    dim3 g = grid3(L.nx, L.ny, L.nz, ln);
+    const unsigned plane = g.x * g.y;
+    const unsigned target = 4864;
+    unsigned gz = plane >= target ? 1u : (target + plane - 1) / plane;
+    if (gz > g.z) gz = g.z;
+    g.z = gz;
+    return g;
 }
 
-int f64_cg_scalar(const double *num, const double *den, double *out, cudaStream_t s)
+int f64_cg_partials(const LevelK<double> &L, const Launch &ln)
 {
-    k_cg_scalar_f64<<<1, 1, 0, s>>>(num, den, out);
-    count_launches(1);
-    return cuda_status(cudaGetLastError(), "cg scalar");
+    const dim3 g = cg_grid(L, ln);
+    return (int)(g.x * g.y * g.z);
 }
 
-int f64_cg_update_xr(const LevelK<double> &L, const Launch &ln, const double *alpha, double *x, double *r,
-                     const double *p, const double *ap, cudaStream_t s)
+int f64_cg_init(const LevelK<double> &L, const Launch &ln, double *r, double *p, const double *x, const double *b,
+                double *partials, CgState *st, cudaStream_t s)
 {
-    const dim3 g = grid3(L.nx, L.ny, L.nz, ln), bl(kBX, kBY, 1);
-    k_cg_xr_f64<<<g, bl, 0, s>>>(L, alpha, x, r, p, ap);
+    k_cg_init<<<cg_grid(L, ln), dim3(kBX, kBY, 1), 0, s>>>(L, r, p, x, b, partials, st);
     count_launches(1);
-    return cuda_status(cudaGetLastError(), "cg update");
+    return cuda_status(cudaGetLastError(), "cg init");
 }
 
-int f64_cg_update_p(const LevelK<double> &L, const Launch &ln, const double *beta, double *p, const double *r,
-                    cudaStream_t s)
+int f64_cg_iteration(const LevelK<double> &L, const Launch &ln, double *x, double *r, double *p, double *ap,
+                     double *partials, CgState *st, double tol, bool check, int iter, cudaStream_t s)
 {
-    const dim3 g = grid3(L.nx, L.ny, L.nz, ln), bl(kBX, kBY, 1);
-    k_cg_p_f64<<<g, bl, 0, s>>>(L, beta, p, r);
-    count_launches(1);
-    return cuda_status(cudaGetLastError(), "cg update p");
-}
-
-int f64_check(const double *num, const double *den, double tol, int le, int iter, int *flag, int *iter_out,
-              cudaStream_t s)
-{
-    k_check_f64<<<1, 1, 0, s>>>(num, den, tol, le, iter, flag, iter_out);
-    count_launches(1);
-    return cuda_status(cudaGetLastError(), "check");
+    const dim3 g = cg_grid(L, ln), bl(kBX, kBY, 1);
+    k_cg_apdot<<<g, bl, 0, s>>>(L, p, ap, partials, st);
+    k_cg_update<<<g, bl, 0, s>>>(L, x, r, p, ap, partials, st, tol, check ? 1 : 0, iter);
+    k_cg_p<<<g, bl, 0, s>>>(L, p, r, st);
+    count_launches(3);
+    return cuda_status(cudaGetLastError(), "cg iteration");
 }
 
 }  // namespace pmg

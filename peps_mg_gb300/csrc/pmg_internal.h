@@ -41,6 +41,8 @@ struct TailDesc {
     // FP32 tail only: floats of dynamic shared memory holding x and b of every tail level
     // (0 = the tail works on the global arrays)
     int sm_floats;
+    // host abort flag of the context (pmg_set_abort; mapped host memory), or nullptr
+    const volatile int *abort;
 };
 
 // ---- FP64 (bitwise) launchers, pmg_f64.cu -------------------------------------
@@ -60,17 +62,30 @@ int f64_prolong(const XferK<double> &X, const Launch &ln, const double *vc, doub
                 cudaStream_t s);
 int zero_ghosts_f64(double *a, int nx, int ny, int nz, cudaStream_t s);
 int f64_tail(const TailDesc<double> *dev_desc, int threads, cudaStream_t s);
-// CG building blocks on device scalars (src/cg_poisson_matrix.f90:99-138)
-int f64_copy_interior(const LevelK<double> &L, double *dst, const double *src, cudaStream_t s);
-int f64_cg_scalar(const double *num, const double *den, double *out, cudaStream_t s);
-int f64_cg_update_xr(const LevelK<double> &L, const Launch &ln, const double *alpha, double *x, double *r,
-                     const double *p, const double *ap, cudaStream_t s);
-int f64_cg_update_p(const LevelK<double> &L, const Launch &ln, const double *beta, double *p, const double *r,
-                    cudaStream_t s);
-// Convergence flag for device-looped solvers: flag = (sqrt(num/den) <= tol) (le=1) or
-// < tol (le=0); also records the iteration.
-int f64_check(const double *num, const double *den, double tol, int le, int iter, int *flag, int *iter_out,
-              cudaStream_t s);
+// Device state of a fused CG solve (src/cg_poisson_matrix.f90:80-138): the reference's
+// scalars, the exit flag, and the arrival counter of the kernels' last-CTA reductions
+// (zero between launches).
+struct CgState {
+    double r0;              // rsd0tol
+    double t1;              // temp1 = r.r at the start of the iteration
+    double pap;             // temp2 = Ap.p
+    double alpha;           // temp1 / (Ap.p)
+    double t2;              // temp2 = r.r after the update
+    double beta;            // temp2 / temp1
+    int done;               // exit test met (solver only)
+    int iter;               // iteration at which it was met
+    unsigned int arrive;    // CTAs that have added their partial sum
+    int pad;
+};
+// Number of partial sums of the fused CG kernels on a level (the partials buffer must hold them).
+int f64_cg_partials(const LevelK<double> &L, const Launch &ln);
+// r = b - A x, p = r, st->r0 = st->t1 = r.r, st->done = 0.
+int f64_cg_init(const LevelK<double> &L, const Launch &ln, double *r, double *p, const double *x, const double *b,
+                double *partials, CgState *st, cudaStream_t s);
+// One CG iteration (three fused kernels); with check, the exit test sqrt(t2/r0) < tol sets
+// st->done and st->iter = iter, after which further iterations do nothing.
+int f64_cg_iteration(const LevelK<double> &L, const Launch &ln, double *x, double *r, double *p, double *ap,
+                     double *partials, CgState *st, double tol, bool check, int iter, cudaStream_t s);
 
 // ---- FP32 fused smoother, pmg_smooth32.cu ----------------------------------------
 // One out-of-place red-black iteration e_out = RB(e_in) of a whole level (zero_in: e_in
@@ -91,10 +106,11 @@ int rb32_tma_setup(Rb32Tma *t, const LevelK<float> &L, float *const base[3], lon
 // (TMA-fed kernel only, 384 threads; the register-window kernel runs variant 0 for it);
 // kchunk: planes per work item (0 = automatic).  With tma (tma->ok), the TMA-fed kernel
 // runs; ein must then be buffer in_buf of the maps, and err receives 1 if one of its
-// bounded pipeline waits gave up.
+// bounded pipeline waits gave up.  stall (self-test of that path, TMA-fed kernel only):
+// the kernel issues no copies and its waits give up after a few microseconds.
 int rb32_fused(const LevelK<float> &L, const Launch &ln, const float *ein, float *eout, const float *b, float omega,
                float omw, bool zero_in, cudaStream_t s, int variant = 0, int kchunk = 0,
-               const Rb32Tma *tma = nullptr, int in_buf = 0, int *err = nullptr);
+               const Rb32Tma *tma = nullptr, int in_buf = 0, int *err = nullptr, bool stall = false);
 // Picks the fastest kernel, tile variant and k-chunk for a level (process-wide cache).
 // With tensor maps (tma) the TMA-fed and the register-window kernels compete; when the
 // register-window one wins, *variant carries kTuneWindow on top of the tile variant and the
@@ -121,7 +137,8 @@ int batch_size(const Batch &B);
 void grid_for_cells(const LevelK<double> &L, const Launch &ln, dim3 *grid, dim3 *block);
 
 // ---- telemetry --------------------------------------------------------------------
-// Kernel classes timed by the optional profiler (finest level only).
+// Kernel classes timed by the optional profiler: the finest level's kernels one class each,
+// the grid levels below it as one class per precision.
 enum ProfClass {
     PC_SMOOTH32 = 0,     // FP32 RBGS half-sweep                     8 B/cell algorithmic
     PC_OUTER_RES = 1,    // FP64 outer residual (+FP32 copy, norm)  28 B/cell
@@ -135,11 +152,25 @@ enum ProfClass {
     PC_PROLONG64 = 9,    // FP64 prolongation + correction          17 B/cell
     PC_TAIL64 = 10,      // FP64 single-CTA coarse tail
     PC_UPDATE_RES = 11,  // x += e, r -= A e, FP32 copy, norm       40 B/cell
-    PC_COUNT = 12
+    PC_COARSE32 = 12,    // FP32 grid levels below the finest (smoothing and transfers)
+    PC_COARSE64 = 13,    // FP64 grid levels below the finest (smoothing, residual, transfers)
+    PC_COUNT = 14
 };
 // Number of kernels this library has launched (all contexts).
 void count_launches(long long n);
 long long launches_total();
+
+// ---- device allocation ------------------------------------------------------------
+// Every device allocation of the library goes through dev_malloc: cudaMalloc, unless the
+// host-side fault injector (pmg_inject_alloc_failure) has armed a failure, in which case
+// the chosen call allocates nothing and fails with cudaErrorMemoryAllocation, as cudaMalloc
+// does when the device memory is exhausted.
+cudaError_t dev_malloc_bytes(void **p, size_t bytes);
+template <typename T>
+inline cudaError_t dev_malloc(T **p, size_t bytes)
+{
+    return dev_malloc_bytes(reinterpret_cast<void **>(p), bytes);
+}
 
 // ---- errors ---------------------------------------------------------------------
 void set_error(const std::string &msg);

@@ -443,7 +443,7 @@ static int alloc_f32(MixedState *m, int nx, int ny, int nz, int *pitch, long lon
     const long long pl = (long long)p * rows;
     const size_t n = (size_t)pl * (size_t)planes + 8;
     float *a = nullptr;
-    PMG_TRY_M(mstatus(cudaMalloc(&a, n * sizeof(float)), "mixed level allocation"));
+    PMG_TRY_M(mstatus(dev_malloc(&a, n * sizeof(float)), "mixed level allocation"));
     PMG_TRY_M(mstatus(cudaMemset(a, 0, n * sizeof(float)), "mixed level init"));
     m->alloc.push_back(a);
     *pitch = p;
@@ -455,9 +455,19 @@ static int alloc_f32(MixedState *m, int nx, int ny, int nz, int *pitch, long lon
     return PMG_OK;
 }
 
+// The FP32 state is built on the first mixed solve.  A failure part way (an allocation, a
+// copy, the autotuner) releases what was built, so the next solve starts the set-up
+// again instead of finding a half-built state.
 int Ctx::setup_mixed()
 {
     if (mixed) return PMG_OK;
+    const int rc = build_mixed();
+    if (rc != PMG_OK) destroy_mixed();
+    return rc;
+}
+
+int Ctx::build_mixed()
+{
     if (tail_l0 > nl) {
         set_error("mixed precision needs a coarsest level small enough for the single-CTA coarse solver");
         return PMG_EINVAL;
@@ -482,7 +492,7 @@ int Ctx::setup_mixed()
     m->inner = mixed_inner > 0 ? mixed_inner : 2;
     m->tables_host.resize(tables_host.size());
     for (size_t q = 0; q < tables_host.size(); ++q) m->tables_host[q] = (float)tables_host[q];
-    PMG_TRY_M(mstatus(cudaMalloc(&m->tables, m->tables_host.size() * sizeof(float)), "mixed tables"));
+    PMG_TRY_M(mstatus(dev_malloc(&m->tables, m->tables_host.size() * sizeof(float)), "mixed tables"));
     PMG_TRY_M(mstatus(cudaMemcpy(m->tables, m->tables_host.data(), m->tables_host.size() * sizeof(float),
                                  cudaMemcpyHostToDevice),
                       "mixed tables"));
@@ -493,7 +503,7 @@ int Ctx::setup_mixed()
         for (int j = 1; j <= S.n[1]; ++j) h[j] = 1.0 / (S.dm[1][j] * S.dg[1][j]) + 1.0 / (S.dm[1][j] * S.dg[1][j + 1]);
         for (int k = 1; k <= S.n[2]; ++k)
             h[S.n[1] + 2 + k] = 1.0 / (S.dm[2][k] * S.dg[2][k]) + 1.0 / (S.dm[2][k] * S.dg[2][k + 1]);
-        PMG_TRY_M(mstatus(cudaMalloc(&m->diag64, h.size() * sizeof(double)), "mixed tables"));
+        PMG_TRY_M(mstatus(dev_malloc(&m->diag64, h.size() * sizeof(double)), "mixed tables"));
         PMG_TRY_M(mstatus(cudaMemcpy(m->diag64, h.data(), h.size() * sizeof(double), cudaMemcpyHostToDevice),
                           "mixed tables"));
         m->dyy.push_back(m->diag64);
@@ -514,7 +524,7 @@ int Ctx::setup_mixed()
                 h.push_back(make_float2(hi, (float)(t[q] - (double)hi)));
             }
         }
-        PMG_TRY_M(mstatus(cudaMalloc(&m->split, h.size() * sizeof(float2)), "mixed tables"));
+        PMG_TRY_M(mstatus(dev_malloc(&m->split, h.size() * sizeof(float2)), "mixed tables"));
         PMG_TRY_M(mstatus(cudaMemcpy(m->split, h.data(), h.size() * sizeof(float2), cudaMemcpyHostToDevice),
                           "mixed tables"));
         m->sc = SplitCoef{m->split + off[0], m->split + off[1], m->split + off[2],
@@ -580,8 +590,8 @@ int Ctx::setup_mixed()
         y.pxp = F(x.pxp); y.pxn = F(x.pxn); y.pyp = F(x.pyp); y.pyn = F(x.pyn);
         y.pzp = F(x.pzp); y.pzn = F(x.pzn);
     }
-    PMG_TRY_M(mstatus(cudaMalloc(&m->d_tail, sizeof(TailDesc<float>)), "mixed tail descriptor"));
-    PMG_TRY_M(mstatus(cudaMalloc(&m->d_err, sizeof(int)), "mixed error flag"));
+    PMG_TRY_M(mstatus(dev_malloc(&m->d_tail, sizeof(TailDesc<float>)), "mixed tail descriptor"));
+    PMG_TRY_M(mstatus(dev_malloc(&m->d_err, sizeof(int)), "mixed error flag"));
     PMG_TRY_M(mstatus(cudaMemset(m->d_err, 0, sizeof(int)), "mixed error flag"));
     for (int l = 0; l < tail32_l0; ++l)
         if (m->fused[l] && autotune) {
@@ -618,6 +628,7 @@ int Ctx::upload_tail32(int maxit, double omega, double tol)
         D.r[l] = nullptr;
     }
     fill_coarse64(D.C64, D.cx64, D.cb64, D.cp64, D.cap64, D.crr64, D.omega64, D.omw64, omega);
+    D.abort = abort_dev;
     // x and b of the tail levels in shared memory when they fit (not for batch members,
     // whose tails share one launch)
     D.sm_floats = 0;
@@ -679,18 +690,35 @@ int Ctx::vcycle32(int maxit, double omega, bool zero_start)
         prof.end(pi, PC_RESRESTRICT32, 1, 8.5 * N, stream);
         ++nlaunch;
     }
+    // the grid levels below the finest: one profiler record for the way down and one for
+    // the way up (smoothing 8 + 12 B per cell from e = 0, 12 B per later iteration;
+    // residual-restriction and prolongation 8.5 B per fine cell each)
+    auto coarse_bytes = [&](bool down) {
+        double b = 0.0;
+        for (int l = 1; l < tail32_l0; ++l) {
+            const double n = (double)m->K[l].nx * m->K[l].ny * m->K[l].nz;
+            b += down ? (12.0 * maxit - 4.0 + 8.5) * n : (12.0 * maxit + 8.5) * n;
+        }
+        return b;
+    };
+    const int coarse_launches = std::max(0, tail32_l0 - 1) * (maxit + 1);
+    int pc = tail32_l0 > 1 ? prof.begin(stream) : -1;
     for (int l = 1; l < tail32_l0; ++l) {
         PMG_TRY_M(sweeps(l, true));
         PMG_TRY_M(resrestrict32(l));
         ++nlaunch;
     }
+    if (coarse_launches > 0) prof.end(pc, PC_COARSE32, coarse_launches, coarse_bytes(true) / coarse_launches, stream);
     {
         const int pi = prof.begin(stream);
         k_tail32<<<1, tail32_threads, tail32_smem, stream>>>(m->d_tail);
         prof.end(pi, PC_TAIL32, 1, 0.0, stream);
         ++nlaunch;
     }
+    pc = tail32_l0 > 1 ? prof.begin(stream) : -1;
     for (int l = tail32_l0 - 1; l >= 0; --l) {
+        if (l == 0 && coarse_launches > 0)
+            prof.end(pc, PC_COARSE32, coarse_launches, coarse_bytes(false) / coarse_launches, stream);
         const XferK<float> &Xl = m->X[l];
         const int pi = l == 0 ? prof.begin(stream) : -1;
         {
@@ -869,10 +897,32 @@ int Ctx::solve_mixed(double *sol, double *rsd, const double *rhs, int maxit, dou
     double h[2];
     PMG_TRY_M(fetch_scalars(h, 1));
     const double res0tol = h[0];
+    if (res0tol == 0.0) {
+        // an exactly zero initial residual: sol is returned unchanged with rsd = b - A x
+        // and no cycles (the FP64 path does the same; see Ctx::solve_f64)
+        if (rep) {
+            rep->cycles = 0;
+            rep->converged = 1;
+            rep->res0 = 0.0;
+            rep->final_ratio = 0.0;
+            rep->inner_cycles = 0;
+        }
+        return check_pipeline();
+    }
     PMG_TRY_M(upload_tail32(maxit, omega, tol));
     int cycles = 0, converged = 0, inner_total = 0;
     double ratio = 0.0, prev_ratio = 1.0, contraction = 1.0;
     for (int cyc = 1; cyc <= n_vcycles; ++cyc) {
+        if (aborted()) {
+            if (rep) {
+                rep->cycles = cycles;
+                rep->converged = 0;
+                rep->res0 = std::sqrt(res0tol);
+                rep->final_ratio = ratio;
+                rep->inner_cycles = inner_total;
+            }
+            return abort_status();
+        }
         PMG_TRY_M(run_vcycles(maxit, omega));
         inner_total += m->inner;
         const bool recompute = !m->update_residual || cyc == n_vcycles || prev_ratio * contraction < 0.1 * tol;
@@ -968,6 +1018,36 @@ int Ctx::selftest_smooth32(int level, int impl, int variant, int kchunk, bool ze
                     (double)he[(size_t)(front + i + (long long)L.sy * j + L.sz * k)];
     m->cur[level] = 0;
     return PMG_OK;
+}
+
+// Self-test of the timeout path of the TMA-fed smoother: one launch on `level` in its stall
+// mode (no copies issued, waits limited to a few microseconds), so every CTA's first wait
+// runs out with nothing in flight; the error flag then turns into PMG_ETIMEOUT exactly as
+// in a solve.  The level's FP32 work arrays are cleared afterwards (the stalled launch
+// wrote values computed from unfilled stages into the interior of one of them), so the
+// context stays usable.
+int Ctx::selftest_wait_timeout(int level)
+{
+    PMG_TRY_M(setup_mixed());
+    MixedState *m = mixed;
+    if (level < 0 || level > nl || !m->fused[level] || !m->tma[level].ok) {
+        set_error("the level has no TMA-fed smoother");
+        return PMG_EINVAL;
+    }
+    const LevelK<float> &L = m->K[level];
+    const int rc = rb32_fused(L, launch[level], m->e[0][level], m->e[1][level], m->b[level], 1.f, 0.f, false, stream,
+                              0, 0, &m->tma[level], 0, m->d_err, true);
+    const int timeout = rc == PMG_OK ? check_pipeline() : rc;
+    const std::string msg = timeout == PMG_ETIMEOUT ? std::string("fused smoother: a wait for a TMA copy timed out")
+                                                    : std::string();
+    const size_t total = (size_t)L.sz * (size_t)m->planes[level] + 8;
+    const long long front = RBT_DATA_OFF + L.sy + L.sz;
+    for (int q = 0; q < 2; ++q)
+        PMG_TRY_M(mstatus(cudaMemsetAsync(m->e[q][level] - front, 0, total * sizeof(float), stream), "self-test reset"));
+    PMG_TRY_M(mstatus(cudaStreamSynchronize(stream), "self-test reset"));
+    m->cur[level] = 0;
+    if (!msg.empty()) set_error(msg);
+    return timeout;
 }
 
 // The TMA-fed smoother sets the error flag when one of its bounded waits for a copied

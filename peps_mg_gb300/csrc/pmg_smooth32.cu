@@ -176,11 +176,12 @@ int tma_slots(int *slots)
 
 template <int TY>
 int launch_tma(const LevelK<float> &L, const Launch &ln, const Rb32Tma &t, int vi, int in_buf, float *eout,
-               float omega, float omw, bool zero_in, int kchunk_hint, int *err, cudaStream_t s)
+               float omega, float omw, bool zero_in, int kchunk_hint, int *err, cudaStream_t s, bool stall)
 {
     int slots = 0;
     PMG_TRY_S(tma_slots<TY>(&slots));
     RbtItems W;
+    W.stall = stall ? 1 : 0;
     W.ntx = (L.nx + RBT_TX - 1) / RBT_TX;
     W.nty = (L.ny + TY - 1) / TY;
     W.nz = L.nz;
@@ -274,15 +275,19 @@ int rb32_tma_setup(Rb32Tma *t, const LevelK<float> &L, float *const base[3], lon
 
 int rb32_fused(const LevelK<float> &L, const Launch &ln, const float *ein, float *eout, const float *b, float omega,
                float omw, bool zero_in, cudaStream_t s, int variant, int kchunk, const Rb32Tma *tma, int in_buf,
-               int *err)
+               int *err, bool stall)
 {
     if (tma && tma->ok && err) {
         switch (variant) {
-        case 1: return launch_tma<6>(L, ln, *tma, 1, in_buf, eout, omega, omw, zero_in, kchunk, err, s);
-        case 2: return launch_tma<10>(L, ln, *tma, 2, in_buf, eout, omega, omw, zero_in, kchunk, err, s);
-        case 3: return launch_tma<22>(L, ln, *tma, 3, in_buf, eout, omega, omw, zero_in, kchunk, err, s);
-        default: return launch_tma<14>(L, ln, *tma, 0, in_buf, eout, omega, omw, zero_in, kchunk, err, s);
+        case 1: return launch_tma<6>(L, ln, *tma, 1, in_buf, eout, omega, omw, zero_in, kchunk, err, s, stall);
+        case 2: return launch_tma<10>(L, ln, *tma, 2, in_buf, eout, omega, omw, zero_in, kchunk, err, s, stall);
+        case 3: return launch_tma<22>(L, ln, *tma, 3, in_buf, eout, omega, omw, zero_in, kchunk, err, s, stall);
+        default: return launch_tma<14>(L, ln, *tma, 0, in_buf, eout, omega, omw, zero_in, kchunk, err, s, stall);
         }
+    }
+    if (stall) {
+        set_error("the stall self-test needs the TMA-fed smoother");
+        return PMG_EINVAL;
     }
     switch (variant) {
     case 1: return launch_ty<6>(L, ln, ein, eout, b, omega, omw, zero_in, kchunk, s);

@@ -20,8 +20,11 @@
 //    registers (z-neighbours), takes x-neighbours by shuffles and the outer y-neighbours
 //    from the stage.
 //  * A wait that runs out (about a second) sets a shared abort flag, after which every
-//    wait of the CTA returns at once; the CTA stops at the end of the item and the host
-//    reads the error flag.
+//    wait of the CTA returns at once; the CTA stops at the end of the item, thread 0
+//    waits (bounded, about a second each) for the copies it issued to land, and the host
+//    reads the error flag.  A self-test mode ("stall": the item source says so) issues
+//    no copies at all and gives each wait a limit of a few microseconds, so the waits
+//    run out with nothing in flight and that path can be tested on the GPU.
 //
 // DRAM traffic per iteration: e_in and b read once, e_out written once (12 B per cell,
 // 8 B when e_in = 0: then no e_in copies are issued at all).
@@ -103,15 +106,21 @@ __device__ __forceinline__ bool mbar_wait_bounded(unsigned long long *bar, unsig
     return true;
 }
 
-// Slow path of a wait: spins until the phase completes, about a second passes (then it
-// raises the CTA's abort flag) or another thread has raised the flag.  Returns false on
-// failure.
+// Wait limits in clock cycles: about a second in production, a few microseconds in the
+// stall self-test (no copies are in flight there).
+constexpr long long kWaitCycles = 1LL << 31;
+constexpr long long kStallWaitCycles = 1LL << 13;
+
+// Slow path of a wait: spins until the phase completes, the CTA's wait limit passes (then
+// it raises the CTA's abort flag) or another thread has raised the flag.  The limit sits
+// in shared memory in the 8 bytes after the abort flag.  Returns false on failure.
 static __device__ __noinline__ bool mbar_wait_slow(unsigned long long *bar, unsigned parity, volatile int *abort_flag)
 {
+    const long long limit = *(reinterpret_cast<volatile long long *>(abort_flag) + 1);
     const long long t0 = clock64();
     while (!mbar_try_wait(bar, parity)) {
         if (*abort_flag) return false;
-        if (clock64() - t0 > (1LL << 31)) {
+        if (clock64() - t0 > limit) {
             *abort_flag = 1;
             return false;
         }
@@ -149,6 +158,7 @@ __device__ __forceinline__ void sq(float2 &v, float x)
 // Work item geometry of one level: item it -> tile (bx, by) and planes k0..k1.
 struct RbtItems {
     int ntx, nty, kchunk, nz, nitems;
+    int stall;   // self-test only: issue no copies, short wait limit
     __device__ __forceinline__ void decode(int it, int &bx, int &by, int &k0, int &k1) const
     {
         const int per = ntx * nty;
@@ -176,6 +186,7 @@ struct RbtGridSrc {
     }
     __device__ __forceinline__ const CUtensorMap *map_e(int) const { return me; }
     __device__ __forceinline__ const CUtensorMap *map_b(int) const { return mb; }
+    __device__ __forceinline__ bool stall() const { return W->stall != 0; }
 };
 
 // The producer: one thread issuing the planes of the CTA's items, slot after slot.  Its
@@ -205,6 +216,7 @@ struct RbtProducer {
     __device__ __forceinline__ void issue_upto(int limit, const Src &src, unsigned char *smem, unsigned long long *bars)
     {
         using S = RbtShape<TY>;
+        if (src.stall()) return;   // self-test: nothing is issued, every wait runs out
         while (slot <= limit && src.valid(it)) {
             const int s = slot % RBT_NS;
             unsigned char *st = smem + s * S::STAGE;
@@ -521,8 +533,8 @@ __device__ __forceinline__ void rbt_cta(const Src &src, Per per, float omega, fl
 {
     using S = RbtShape<TY>;
     extern __shared__ unsigned char rbt_smem_raw[];
-    // 128-byte aligned stages (TMA destinations), then the mbarriers, the abort flag and
-    // the producer state
+    // 128-byte aligned stages (TMA destinations), then the mbarriers, the abort flag, the
+    // wait limit and the producer state
     unsigned char *smem = rbt_smem_raw + ((128u - (rbtdetail::smem_addr(rbt_smem_raw) & 127u)) & 127u);
     unsigned long long *bars = reinterpret_cast<unsigned long long *>(smem + RBT_NS * S::STAGE);
     volatile int *abort_flag = reinterpret_cast<volatile int *>(bars + RBT_NS);
@@ -532,6 +544,8 @@ __device__ __forceinline__ void rbt_cta(const Src &src, Per per, float omega, fl
     if (threadIdx.x == 0) {
         for (int q = 0; q < RBT_NS; ++q) rbtdetail::mbar_init(&bars[q], 1);
         *abort_flag = 0;
+        *reinterpret_cast<volatile long long *>(bars + RBT_NS + 1) =
+            src.stall() ? rbtdetail::kStallWaitCycles : rbtdetail::kWaitCycles;
         rbtdetail::fence_mbar_init();
     }
     __syncthreads();

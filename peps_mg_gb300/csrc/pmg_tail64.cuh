@@ -135,13 +135,35 @@ __device__ void tail_interior_op(const LevelK<double> &L, int op, double s, doub
 }
 
 
+// The context's host abort flag (pmg_set_abort), read by thread 0 and shared, so that the
+// whole block takes the same decision; every thread of the block must call it.
+__device__ __forceinline__ bool block_abort(const volatile int *abort)
+{
+    if (!abort) return false;
+    __shared__ int s_abort;
+    __syncthreads();
+    if (threadIdx.x == 0) s_abort = *abort;
+    __syncthreads();
+    return s_abort != 0;
+}
+
+// The same for one warp (lane 0 reads, the value is broadcast).
+__device__ __forceinline__ bool warp_abort(const volatile int *abort)
+{
+    int v = 0;
+    if ((threadIdx.x & 31) == 0 && abort) v = *abort;
+    return __shfl_sync(0xffffffffu, v, 0) != 0;
+}
+
 // Coarsest-level solve on one CTA (src/multigrid.f90:1819-1851): x = 0, then x = b/c0 for
 // a single cell, else rbgs_solver_poisson_matrix (src/rbgs_poisson_matrix.f90:69-171,
 // solver 0) or cg_solver_poisson_matrix (src/cg_poisson_matrix.f90:80-138, solver 1)
 // with `maxit` iterations and `tol`.  p, ap, rr: full-size scratch arrays with zero
-// ghosts.  Returns the solver's iteration counter.
+// ghosts.  Every 16 iterations the host abort flag (if any) is polled; when it is set the
+// solve stops there.  Returns the solver's iteration counter.
 __device__ int coarse_solve_f64(const LevelK<double> &L, double *x, const double *b, double *p, double *ap,
-                                double *rr, int solver, int maxit, double tol, double omega, double omw, double *sw)
+                                double *rr, int solver, int maxit, double tol, double omega, double omw, double *sw,
+                                const volatile int *abort = nullptr)
 {
     tail_zero(x, (long long)L.sz * (L.nz + 2));
     __syncthreads();
@@ -159,15 +181,18 @@ __device__ int coarse_solve_f64(const LevelK<double> &L, double *x, const double
             tail_rbgs(L, x, b, 1, omega, omw);
             const double rn = tail_residual<true>(L, rr, x, b, sw);
             if (sqrt(__ddiv_rn(rn, r0)) <= tol) break;
+            if ((it & 15) == 15 && block_abort(abort)) break;
         }
         iters = it;
     } else {
         tail_residual<false>(L, rr, x, b, sw);
         tail_interior_op(L, 0, 0.0, p, nullptr, rr, nullptr);
         const double r0 = tail_dot(L, rr, rr, sw);
+        // temp1 = r.r of the unchanged r (:107) equals the previous iteration's temp2 (and
+        // rsd0tol at the first), so it is carried instead of summed again
+        double t1 = r0;
         int it = 0;
         for (it = 0; it < maxit; ++it) {
-            const double t1 = tail_dot(L, rr, rr, sw);
             tail_mvmul(L, ap, p);
             const double t2a = tail_dot(L, ap, p, sw);
             const double alpha = __ddiv_rn(t1, t2a);
@@ -176,6 +201,8 @@ __device__ int coarse_solve_f64(const LevelK<double> &L, double *x, const double
             if (sqrt(__ddiv_rn(t2, r0)) < tol) break;
             const double beta = __ddiv_rn(t2, t1);
             tail_interior_op(L, 2, beta, p, nullptr, rr, nullptr);
+            t1 = t2;
+            if ((it & 15) == 15 && block_abort(abort)) break;
         }
         iters = it;
     }
@@ -199,7 +226,8 @@ __device__ __forceinline__ double warp_sum_f64(double v)
 }
 
 __device__ int coarse_solve_warp_f64(const LevelK<double> &L, double *x, const double *b, double *p, double *ap,
-                                     double *rr, int solver, int maxit, double tol, double omega, double omw)
+                                     double *rr, int solver, int maxit, double tol, double omega, double omw,
+                                     const volatile int *abort = nullptr)
 {
     const int lane = threadIdx.x & 31;
     const int nx = L.nx, ny = L.ny, n = L.nx * L.ny * L.nz;
@@ -320,6 +348,7 @@ __device__ int coarse_solve_warp_f64(const LevelK<double> &L, double *x, const d
                 __syncwarp();
             }
             if (norm() <= thr) break;
+            if ((it & 15) == 15 && warp_abort(abort)) break;
         }
     } else if (solver == 0) {
         const int hx = (nx + 1) / 2, nq = hx * ny * L.nz;
@@ -335,23 +364,41 @@ __device__ int coarse_solve_warp_f64(const LevelK<double> &L, double *x, const d
             }
             const double rn = residual(true);
             if (sqrt(__ddiv_rn(rn, r0)) <= tol) break;
+            if ((it & 15) == 15 && warp_abort(abort)) break;
         }
     } else {
         residual(false);
         interior(0, 0.0, p, nullptr, rr, nullptr);
         const double r0 = dot(rr, rr);
+        // Fused passes: A p with the sum Ap.p, and the x/r update with the sum r.r.  Each
+        // lane visits its cells in the order dot() does, so the sums are dot()'s; temp1
+        // (r.r of the unchanged r) is the previous iteration's temp2.
+        double t1 = r0;
         for (it = 0; it < maxit; ++it) {
-            const double t1 = dot(rr, rr);
+            double pap = 0.0;
             for (int q = lane; q < n; q += 32) {
                 const int i = q % nx + 1, r2 = q / nx, j = r2 % ny + 1, k = r2 / ny + 1;
-                ap[lin(i, j, k, L.sy, L.sz)] = ax_cell_f64(L, p, i, j, k);
+                const long long c = lin(i, j, k, L.sy, L.sz);
+                const double v = ax_cell_f64(L, p, i, j, k);
+                ap[c] = v;
+                pap = __dadd_rn(pap, __dmul_rn(v, p[c]));
             }
+            const double alpha = __ddiv_rn(t1, warp_sum_f64(pap));
+            double rr2 = 0.0;
+            for (int q = lane; q < n; q += 32) {
+                const int i = q % nx + 1, r2 = q / nx, j = r2 % ny + 1, k = r2 / ny + 1;
+                const long long c = lin(i, j, k, L.sy, L.sz);
+                x[c] = __dadd_rn(x[c], __dmul_rn(alpha, p[c]));
+                const double v = __dsub_rn(rr[c], __dmul_rn(alpha, ap[c]));
+                rr[c] = v;
+                rr2 = __dadd_rn(rr2, __dmul_rn(v, v));
+            }
+            const double t2 = warp_sum_f64(rr2);
             __syncwarp();
-            const double alpha = __ddiv_rn(t1, dot(ap, p));
-            interior(1, alpha, x, rr, p, ap);
-            const double t2 = dot(rr, rr);
             if (sqrt(__ddiv_rn(t2, r0)) < tol) break;
             interior(2, __ddiv_rn(t2, t1), p, nullptr, rr, nullptr);
+            t1 = t2;
+            if ((it & 15) == 15 && warp_abort(abort)) break;
         }
     }
     return it;

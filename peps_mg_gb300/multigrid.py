@@ -268,7 +268,7 @@ class Multigrid:
 
 PROF_CLASSES = {0: "smooth32", 1: "outer_residual64", 2: "resrestrict32", 3: "prolong32", 4: "add_correction64",
                 5: "tail32", 6: "smooth64", 7: "residual64", 8: "restrict64", 9: "prolong64", 10: "tail64",
-                11: "update_residual"}
+                11: "update_residual", 12: "coarse_levels32", 13: "coarse_levels64"}
 
 
 def launch_count():

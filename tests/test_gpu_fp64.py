@@ -239,3 +239,63 @@ def test_tanh_256_aggregation_methods_against_oracle():
         assert np.array_equal(rep.coarse_iterations, ci), method
         assert np.array_equal(from_dev(sol), osol), method
         del sol, rsd
+
+
+@pytest.mark.parametrize("case", ["sine64", "stretched_odd", "cgpsa_collapsed"])
+def test_fused_cg_against_oracle(case):
+    """The fused CG kernels (A p with Ap.p, the x/r update with r.r, the p update; scalars
+    on the device) against the oracle's cg_solver / cg_iterator
+    (src/cg_poisson_matrix.f90:47-241): the same iteration count, iterates within
+    1e-12 (iterator) and 1e-11 (solver to 1e-10) relative.  The last case runs on a
+    coarse level whose axes the CGPSA mapping collapses to one CTA column."""
+    if case == "sine64":
+        mesh, rhs, _ = sine_problem(64)
+        level, lev_mesh = 0, mesh
+        mg = pmg.Multigrid(mesh, 3, 1, "cgs")
+    elif case == "stretched_odd":
+        mesh = [pmg.geometry.uniform_axis(44, 0.0, 1.0), pmg.geometry.tanh_axis(38, 0.0, 2.0, 1.2),
+                pmg.geometry.uniform_axis(30, -1.0, 1.5)]
+        rng = np.random.Generator(np.random.PCG64(11))
+        rhs = pmg.geometry.field(44, 38, 30)
+        rhs[1:-1, 1:-1, 1:-1] = rng.uniform(-1.0, 1.0, size=(44, 38, 30))
+        level, lev_mesh = 0, mesh
+        mg = pmg.Multigrid(mesh, 2, 1, "cgs")
+    else:
+        mesh, _, _ = sine_problem(64)
+        mg = pmg.Multigrid(mesh, 4, 1, "cgpsa", 0, (1, 1, 1))
+        level = 2
+        lev_mesh = [mg.level_mesh(level, a) for a in range(3)]
+        m = mg.level_dims(level)
+        rng = np.random.Generator(np.random.PCG64(12))
+        rhs = pmg.geometry.field(*m)
+        rhs[1:-1, 1:-1, 1:-1] = rng.uniform(-1.0, 1.0, size=m)
+    try:
+        coeff = O.matrix_create(lev_mesh)
+        nx, ny, nz = rhs.shape[0] - 2, rhs.shape[1] - 2, rhs.shape[2] - 2
+        b = to_dev(rhs)
+        # solver to 1e-10 from x0 = 0
+        x = torch.zeros_like(b)
+        it, ratio = mg.cg_solver(level, x, b, 1000, 1e-10)
+        ox = O.field(nx, ny, nz)
+        oit, on2, on02 = O.cg(coeff, ox, F(rhs), 1000, 1e-10, True)
+        assert it == oit, (it, oit)
+        # the final |r| is at most 1e-10 of |r0|, a difference of recursively updated terms of
+        # size |r0|: sums in another order move it by about 1e-16 / 1e-10 relative, and where
+        # CG lands far below the tolerance (the sine right-hand side is an eigenvector) the
+        # ratio is rounding noise of order 1e-13
+        oratio = np.sqrt(on2 / on02)
+        assert ratio < 1e-10 and abs(ratio - oratio) <= max(1e-4 * oratio, 1e-13), (ratio, oratio)
+        assert rel(from_dev(x), ox) < 1e-11, rel(from_dev(x), ox)
+        # iterator: 30 iterations from a non-zero initial guess
+        rng = np.random.Generator(np.random.PCG64(13))
+        x0 = O.field(nx, ny, nz)
+        x0[1:-1, 1:-1, 1:-1] = rng.uniform(-0.1, 0.1, size=(nx, ny, nz))
+        x = to_dev(x0)
+        mg.cg_iterator(level, x, b, 30)
+        ox = x0.copy(order="F")
+        O.cg(coeff, ox, F(rhs), 30, 0.0, False)
+        assert rel(from_dev(x), ox) < 1e-12, rel(from_dev(x), ox)
+        # ghosts untouched
+        assert np.array_equal(from_dev(x)[0], x0[0])
+    finally:
+        mg.destroy()
