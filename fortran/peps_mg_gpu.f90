@@ -39,7 +39,7 @@ module peps_mg_gpu
     integer(c_int), parameter, public :: PMG_ETIMEOUT = 4, PMG_ECUDA = 5
     integer(c_int), parameter, public :: PMG_CGS = 0, PMG_CGA = 1, PMG_CGPSA = 2
     integer(c_int), parameter, public :: PMG_COARSE_RBGS = 0, PMG_COARSE_CG = 1
-    integer(c_int), parameter, public :: PMG_FP64 = 0, PMG_MIXED = 1
+    integer(c_int), parameter, public :: PMG_FP64 = 0, PMG_MIXED = 1, PMG_FP64_FAST = 2
 
     !> pmg_config_t: 3 ints, 9 pointers, 10 ints (C layout: the pointers start at byte
     !> 16 on an LP64 target, 4 bytes of padding after nz; 112 bytes in all)
@@ -424,7 +424,7 @@ contains
 
     !> multigrid_create(sdm, nlevel, ncycle, aggr_method, single_aggr_level,
     !> adaptive_aggr_level) -- src/multigrid.f90:75.  Optional: precision (PMG_FP64, the
-    !> default, or PMG_MIXED), coarse_solver (PMG_COARSE_RBGS, the default, or
+    !> default, PMG_MIXED or PMG_FP64_FAST), coarse_solver (PMG_COARSE_RBGS, the default, or
     !> PMG_COARSE_CG), mixed_inner_cycles, stream (a cudaStream_t), status.
     subroutine multigrid_gpu_create(sdm, nlevel, ncycle, aggr_method, single_aggr_level, adaptive_aggr_level, &
                                     precision, coarse_solver, mixed_inner_cycles, stream, status)

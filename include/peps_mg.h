@@ -40,6 +40,9 @@ extern "C" {
 /* precision of the V-cycle */
 #define PMG_FP64 0        /* plain FP64, bitwise the reference's arithmetic             */
 #define PMG_MIXED 1       /* FP32 V-cycles inside FP64 defect correction                */
+#define PMG_FP64_FAST 2   /* FP64 V-cycles with FMA, a stored omega/c0 per cell and
+                           * per-axis normalised transfer weights: the same level sequence
+                           * and exit test as PMG_FP64, not its bits (rounding differs)  */
 
 typedef struct pmg_ctx pmg_ctx;
 
@@ -57,7 +60,7 @@ typedef struct {
     int cga_level;             /* CGA_level                                              */
     int cgpsa_level[3];        /* CGPSA_level(3)                                         */
     int coarse_solver;         /* PMG_COARSE_RBGS or PMG_COARSE_CG                       */
-    int precision;             /* PMG_FP64 or PMG_MIXED                                  */
+    int precision;             /* PMG_FP64, PMG_MIXED or PMG_FP64_FAST                   */
     int mixed_inner_cycles;    /* PMG_MIXED: FP32 V-cycles per FP64 correction (0 = 2)   */
 } pmg_config_t;
 

@@ -12,7 +12,7 @@ LIB_PATH = os.path.join(HERE, "lib", "libpeps_mg.so")
 PMG_OK, PMG_EINVAL, PMG_ENOMEM, PMG_EDIVERGED, PMG_ETIMEOUT, PMG_ECUDA = range(6)
 PMG_CGS, PMG_CGA, PMG_CGPSA = 0, 1, 2
 PMG_COARSE_RBGS, PMG_COARSE_CG = 0, 1
-PMG_FP64, PMG_MIXED = 0, 1
+PMG_FP64, PMG_MIXED, PMG_FP64_FAST = 0, 1, 2
 
 c_int, c_double, c_float, c_void_p = ctypes.c_int, ctypes.c_double, ctypes.c_float, ctypes.c_void_p
 

@@ -24,6 +24,7 @@ COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-ffp-contract=o
 UNITS = {
     "pmg_api.cu": ["--fmad=false"],
     "pmg_f64.cu": ["--fmad=false"],
+    "pmg_f64fast.cu": ["--fmad=true"],
     "pmg_mixed.cu": ["--fmad=true"],
     "pmg_smooth32.cu": ["--fmad=true"],
     "pmg_batch.cu": ["--fmad=true"],

@@ -326,8 +326,8 @@ int Ctx::build(const pmg_config_t *c, cudaStream_t s)
         set_error("coarse_solver must be PMG_COARSE_RBGS or PMG_COARSE_CG");
         return PMG_EINVAL;
     }
-    if (c->precision != PMG_FP64 && c->precision != PMG_MIXED) {
-        set_error("precision must be PMG_FP64 or PMG_MIXED");
+    if (c->precision != PMG_FP64 && c->precision != PMG_MIXED && c->precision != PMG_FP64_FAST) {
+        set_error("precision must be PMG_FP64, PMG_MIXED or PMG_FP64_FAST");
         return PMG_EINVAL;
     }
     stream = s;
@@ -526,6 +526,61 @@ int Ctx::build(const pmg_config_t *c, cudaStream_t s)
     PMG_CUDA(cudaEventCreateWithFlags(&ev_x, cudaEventDisableTiming), "event");
     PMG_CUDA(cudaEventCreateWithFlags(&ev_copied, cudaEventDisableTiming), "event");
     PMG_CUDA(cudaStreamCreateWithFlags(&copy_stream, cudaStreamNonBlocking), "copy stream");
+    if (precision == PMG_FP64_FAST) PMG_TRY(setup_fast64());
+    return PMG_OK;
+}
+
+// Tables of the FP64 performance mode for the grid levels 0 .. min(tail_l0, nl) - 1 (the
+// levels the V-cycle runs on the grid kernels): one blob of per-axis tables, derived on
+// the device from the plain path's tables, and one omega/c0 array per level.
+int Ctx::setup_fast64()
+{
+    fast64 = true;
+    const int grid_end = std::min(tail_l0, nl);
+    fastK.assign((size_t)std::max(grid_end, 1), FastLevelK{});
+    fastX.assign((size_t)std::max(grid_end, 1), FastXferK{});
+    size_t total = 0;
+    std::vector<size_t> lvl_off((size_t)grid_end + 1, 0);
+    for (int l = 0; l < grid_end; ++l) {
+        lvl_off[l] = total;
+        const Level &L = lv[l];
+        total += (size_t)(L.n[1] + 2) + (size_t)(L.n[2] + 2) + 3 * (size_t)(L.n[0] + 2 + L.n[1] + 2 + L.n[2] + 2);
+    }
+    PMG_CUDA(dev_malloc(&d_fast, std::max<size_t>(total, 1) * sizeof(double)), "fast tables");
+    for (int l = 0; l < grid_end; ++l) {
+        const Level &L = lv[l];
+        double *p = d_fast + lvl_off[l];
+        FastLevelK &F = fastK[l];
+        FastXferK &W = fastX[l];
+        F.dy = p;
+        p += L.n[1] + 2;
+        F.dz = p;
+        p += L.n[2] + 2;
+        double **ax[3][3] = {{&W.rx, &W.pax, &W.pbx}, {&W.ry, &W.pay, &W.pby}, {&W.rz, &W.paz, &W.pbz}};
+        for (int d = 0; d < 3; ++d)
+            for (int t = 0; t < 3; ++t) {
+                *ax[d][t] = p;
+                p += L.n[d] + 2;
+            }
+        double *w = nullptr;
+        PMG_CUDA(dev_malloc(&w, L.total * sizeof(double)), "fast diagonal");
+        fast_wdiag_alloc.push_back(w);
+        F.wdiag = w;
+        PMG_TRY(fast_tables(K[l], &X[l], L.n[0], L.n[1], L.n[2], &F, &W, stream));
+    }
+    PMG_CUDA(cudaStreamSynchronize(stream), "fast tables");
+    fast_omega_set = false;
+    return PMG_OK;
+}
+
+// omega / c0 of the fast mode's grid levels for this solve's omega.
+int Ctx::fast_prepare(double omega)
+{
+    if (fast_omega_set && fast_omega == omega) return PMG_OK;
+    const int grid_end = std::min(tail_l0, nl);
+    for (int l = 0; l < grid_end; ++l) PMG_TRY(fast_wdiag(K[l], omega, fastK[l].wdiag, stream));
+    fast_omega = omega;
+    fast_omega_set = true;
     return PMG_OK;
 }
 
@@ -542,6 +597,8 @@ Ctx::~Ctx()
     cudaFree(d_iscal);
     cudaFree(d_cg);
     if (abort_host) cudaFreeHost(abort_host);
+    cudaFree(d_fast);
+    for (auto p : fast_wdiag_alloc) cudaFree(p);
     cudaFree(d_cp);
     cudaFree(d_cap);
     cudaFree(d_crr);
@@ -575,6 +632,16 @@ int Ctx::residual_norm(int l, double *r, const double *x, const double *b, int s
 {
     int np = 0;
     PMG_TRY(f64_residual(K[l], launch[l], r, x, b, d_partials, &np, stream));
+    return f64_reduce(d_partials, np, d_scal + slot, stream);
+}
+
+// The finest-level residual and its norm of an FP64 solve: bitwise, or in the FP64
+// performance mode its FMA form.
+int Ctx::solve_residual_norm(double *r, const double *x, const double *b, int slot)
+{
+    if (!fast64) return residual_norm(0, r, x, b, slot);
+    int np = 0;
+    PMG_TRY(fast_residual(K[0], fastK[0], launch[0], r, x, b, d_partials, &np, stream));
     return f64_reduce(d_partials, np, d_scal + slot, stream);
 }
 
@@ -642,16 +709,36 @@ int Ctx::vcycle_f64(double *sol, double *rsd, const double *rhs, int maxit, doub
                     int *coarse_iters)
 {
     const double N = (double)K[0].nx * K[0].ny * K[0].nz;
+    const int grid_end = std::min(tail_l0, nl);
+    // the grid levels' operations: bitwise kernels, or those of the FP64 performance mode
+    // (which stores omega/c0: 4 more bytes per updated cell and half-sweep)
+    const bool fast = fast64;
+    auto sweeps = [&](int l, double *x, const double *b) {
+        return fast ? fast_rbgs_sweeps(K[l], fastK[l], launch[l], x, b, maxit, omega, stream)
+                    : f64_rbgs_sweeps(K[l], launch[l], x, b, maxit, omega, stream);
+    };
+    auto resid = [&](int l, double *r, const double *x, const double *b) {
+        return fast ? fast_residual(K[l], fastK[l], launch[l], r, x, b, nullptr, nullptr, stream)
+                    : f64_residual(K[l], launch[l], r, x, b, nullptr, nullptr, stream);
+    };
+    auto restr = [&](int l, const double *vf, double *vc) {
+        return fast ? fast_restrict(X[l], fastX[l], launch[l + 1], vf, vc, stream)
+                    : f64_restrict(X[l], launch[l + 1], vf, vc, stream);
+    };
+    auto prolong = [&](int l, const double *vc, double *vf) {
+        return fast ? fast_prolong(X[l], fastX[l], launch[l + 1], vc, vf, stream)
+                    : f64_prolong(X[l], launch[l + 1], vc, vf, true, stream);
+    };
+    const double sweep_bytes = fast ? 20.0 : 16.0;
     int pi = prof.begin(stream);
-    PMG_TRY(f64_rbgs_sweeps(K[0], launch[0], sol, rhs, maxit, omega, stream));
-    prof.end(pi, PC_SMOOTH64, 2 * maxit, 16.0 * N, stream);
+    PMG_TRY(sweeps(0, sol, rhs));
+    prof.end(pi, PC_SMOOTH64, 2 * maxit, sweep_bytes * N, stream);
     pi = prof.begin(stream);
-    PMG_TRY(f64_residual(K[0], launch[0], rsd, sol, rhs, nullptr, nullptr, stream));
+    PMG_TRY(resid(0, rsd, sol, rhs));
     prof.end(pi, PC_RES64, 1, 24.0 * N, stream);
     pi = prof.begin(stream);
-    PMG_TRY(f64_restrict(X[0], launch[1], rsd, lv[1].b, stream));
+    PMG_TRY(restr(0, rsd, lv[1].b));
     prof.end(pi, PC_RESTRICT64, 1, 9.0 * N, stream);
-    const int grid_end = std::min(tail_l0, nl);
     // grid levels below the finest, one profiler record each way: per cell of level l,
     // 16 B per half-sweep, 24 B residual, 9 B restriction (down); 17 B prolongation + add,
     // 16 B per half-sweep (up)
@@ -659,7 +746,7 @@ int Ctx::vcycle_f64(double *sol, double *rsd, const double *rhs, int maxit, doub
         double b = 0.0;
         for (int l = 1; l < grid_end; ++l) {
             const double n = (double)K[l].nx * K[l].ny * K[l].nz;
-            b += down ? (32.0 * maxit + 24.0 + 9.0) * n : (17.0 + 32.0 * maxit) * n;
+            b += down ? (2.0 * sweep_bytes * maxit + 24.0 + 9.0) * n : (17.0 + 2.0 * sweep_bytes * maxit) * n;
         }
         return b;
     };
@@ -668,9 +755,9 @@ int Ctx::vcycle_f64(double *sol, double *rsd, const double *rhs, int maxit, doub
     for (int l = 1; l < grid_end; ++l) {
         Level &L = lv[l];
         PMG_CUDA(cudaMemsetAsync(L.x, 0, L.total * sizeof(double), stream), "level reset");
-        PMG_TRY(f64_rbgs_sweeps(K[l], launch[l], L.x, L.b, maxit, omega, stream));
-        PMG_TRY(f64_residual(K[l], launch[l], L.r, L.x, L.b, nullptr, nullptr, stream));
-        PMG_TRY(f64_restrict(X[l], launch[l + 1], L.r, lv[l + 1].b, stream));
+        PMG_TRY(sweeps(l, L.x, L.b));
+        PMG_TRY(resid(l, L.r, L.x, L.b));
+        PMG_TRY(restr(l, L.r, lv[l + 1].b));
     }
     if (coarse_launches > 0) prof.end(pc, PC_COARSE64, coarse_launches, coarse_bytes(true) / coarse_launches, stream);
     if (tail_l0 <= nl) {
@@ -689,17 +776,17 @@ int Ctx::vcycle_f64(double *sol, double *rsd, const double *rhs, int maxit, doub
     pc = grid_end > 1 ? prof.begin(stream) : -1;
     for (int l = grid_end - 1; l >= 1; --l) {
         Level &L = lv[l];
-        PMG_TRY(f64_prolong(X[l], launch[l + 1], lv[l + 1].x, L.x, true, stream));
-        PMG_TRY(f64_rbgs_sweeps(K[l], launch[l], L.x, L.b, maxit, omega, stream));
+        PMG_TRY(prolong(l, lv[l + 1].x, L.x));
+        PMG_TRY(sweeps(l, L.x, L.b));
     }
     const int up_launches = std::max(0, grid_end - 1) * (2 * maxit + 1);
     if (up_launches > 0) prof.end(pc, PC_COARSE64, up_launches, coarse_bytes(false) / up_launches, stream);
     pi = prof.begin(stream);
-    PMG_TRY(f64_prolong(X[0], launch[1], lv[1].x, sol, true, stream));
+    PMG_TRY(prolong(0, lv[1].x, sol));
     prof.end(pi, PC_PROLONG64, 1, 17.0 * N, stream);
     pi = prof.begin(stream);
-    PMG_TRY(f64_rbgs_sweeps(K[0], launch[0], sol, rhs, maxit, omega, stream));
-    prof.end(pi, PC_SMOOTH64, 2 * maxit, 16.0 * N, stream);
+    PMG_TRY(sweeps(0, sol, rhs));
+    prof.end(pi, PC_SMOOTH64, 2 * maxit, sweep_bytes * N, stream);
     return PMG_OK;
 }
 
@@ -716,7 +803,8 @@ int Ctx::solve_f64(double *sol, double *rsd, const double *rhs, int maxit, doubl
     const Level &S = lv[0];
     // rsd(:,:,:) = 0 then r = b - A x (src/multigrid.f90:1794-1805, :1924-1925)
     PMG_CUDA(cudaMemsetAsync(rsd, 0, S.total * sizeof(double), stream), "rsd init");
-    PMG_TRY(residual_norm(0, rsd, sol, rhs, 0));
+    if (fast64) PMG_TRY(fast_prepare(omega));
+    PMG_TRY(solve_residual_norm(rsd, sol, rhs, 0));
     double h[2];
     PMG_TRY(fetch_scalars(h, 1));
     const double res0tol = h[0];
@@ -752,7 +840,7 @@ int Ctx::solve_f64(double *sol, double *rsd, const double *rhs, int maxit, doubl
         int ci = 0;
         PMG_TRY(vcycle_f64(sol, rsd, rhs, maxit, omega, tol, rep && rep->coarse_iterations ? &ci : nullptr));
         int pr = prof.begin(stream);
-        PMG_TRY(residual_norm(0, rsd, sol, rhs, 1));     // :1970-1971
+        PMG_TRY(solve_residual_norm(rsd, sol, rhs, 1));  // :1970-1971
         prof.end(pr, PC_RES64, 1, 24.0 * (double)K[0].nx * K[0].ny * K[0].nz, stream);
         PMG_TRY(fetch_scalars(h, 2));
         const double rsd_val = h[1];

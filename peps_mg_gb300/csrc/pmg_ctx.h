@@ -96,6 +96,17 @@ struct Ctx {
     bool early_valid = false, early_pending = false;
     int early_copy_sol(const double *sol);
     int before_x_change();
+    // FP64 performance mode (PMG_FP64_FAST): per grid level the diagonal sums and omega/c0,
+    // per transfer the normalised weights (pmg_f64fast.cu); tables in one device blob
+    bool fast64 = false;
+    std::vector<FastLevelK> fastK;
+    std::vector<FastXferK> fastX;
+    double *d_fast = nullptr;
+    std::vector<double *> fast_wdiag_alloc;
+    double fast_omega = 0.0;
+    bool fast_omega_set = false;
+    int setup_fast64();
+    int fast_prepare(double omega);
     MixedState *mixed = nullptr;
     Profiler prof;
     bool autotune = true;       // tune the fused smoother per level in setup_mixed
@@ -107,6 +118,7 @@ struct Ctx {
 
     int dot(int l, const double *x, const double *y, int slot);
     int residual_norm(int l, double *r, const double *x, const double *b, int slot);
+    int solve_residual_norm(double *r, const double *x, const double *b, int slot);
     int fetch_scalars(double *h, int n);
     int upload_tail(int l0, int maxit, double omega, double tol);
     void fill_coarse64(LevelK<double> &C, double *&x, double *&b, double *&p, double *&ap, double *&rr, double &om,

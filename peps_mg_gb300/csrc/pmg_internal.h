@@ -87,6 +87,33 @@ int f64_cg_init(const LevelK<double> &L, const Launch &ln, double *r, double *p,
 int f64_cg_iteration(const LevelK<double> &L, const Launch &ln, double *x, double *r, double *p, double *ap,
                      double *partials, CgState *st, double tol, bool check, int iter, cudaStream_t s);
 
+// ---- FP64 performance mode, pmg_f64fast.cu -----------------------------------------
+// Tables of one grid level: per-axis diagonal sums (x: LevelK::sx) and omega / c0 per cell.
+struct FastLevelK {
+    double *dy, *dz;
+    double *wdiag;
+};
+// Normalised per-axis transfer weights of the fine indices between level l and l + 1:
+// restriction weight of a child's value, prolongation weights of the own and the
+// neighbouring coarse cell.
+struct FastXferK {
+    double *rx, *ry, *rz;
+    double *pax, *pbx, *pay, *pby, *paz, *pbz;
+};
+// Fills fl->dy, fl->dz and (X != nullptr) the transfer weights *fx from the plain tables.
+int fast_tables(const LevelK<double> &L, const XferK<double> *X, int nfx, int nfy, int nfz, FastLevelK *fl,
+                FastXferK *fx, cudaStream_t s);
+int fast_wdiag(const LevelK<double> &L, double omega, double *wdiag, cudaStream_t s);
+int fast_rbgs_sweeps(const LevelK<double> &L, const FastLevelK &F, const Launch &ln, double *x, const double *b,
+                     int iters, double omega, cudaStream_t s);
+int fast_residual(const LevelK<double> &L, const FastLevelK &F, const Launch &ln, double *r, const double *x,
+                  const double *b, double *partials, int *npart, cudaStream_t s);
+int fast_restrict(const XferK<double> &X, const FastXferK &W, const Launch &ln, const double *vf, double *vc,
+                  cudaStream_t s);
+// x_f += P x_c
+int fast_prolong(const XferK<double> &X, const FastXferK &W, const Launch &ln, const double *vc, double *vf,
+                 cudaStream_t s);
+
 // ---- FP32 fused smoother, pmg_smooth32.cu ----------------------------------------
 // One out-of-place red-black iteration e_out = RB(e_in) of a whole level (zero_in: e_in
 // is zero and is not read).  Needs the padded FP32 layout checked by rb32_fused_layout_ok.

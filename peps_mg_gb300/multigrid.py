@@ -25,7 +25,7 @@ from ._lib import PmgConfig, PmgReport, check
 
 _METHODS = {"cgs": 0, "cga": 1, "cgpsa": 2}
 _COARSE = {"rbgs": 0, "cg": 1}
-_PREC = {"fp64": 0, "mixed": 1}
+_PREC = {"fp64": 0, "mixed": 1, "fp64_fast": 2}
 
 
 def _code(table, v):
