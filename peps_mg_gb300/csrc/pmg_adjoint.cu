@@ -96,6 +96,7 @@ __global__ void __launch_bounds__(1024) k_face_gradients(LevelK<double> L, const
 int Ctx::adjoint(const double *dLdu, double *dLdb, double *dLdg, int maxit, double tol, double omega,
                  pmg_report_t *rep)
 {
+    NvtxRange nvtx_range("pmg_adjoint");
     const Level &S = lv[0];
     const size_t bytes = S.total * sizeof(double);
     if (!adj_rhs) {

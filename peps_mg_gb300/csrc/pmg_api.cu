@@ -708,6 +708,7 @@ int Ctx::coarse_solve_grid(double tol, double omega, int *iters)
 int Ctx::vcycle_f64(double *sol, double *rsd, const double *rhs, int maxit, double omega, double tol,
                     int *coarse_iters)
 {
+    NvtxRange cycle_range(fast64 ? "fp64-fast V-cycle" : "fp64 V-cycle");
     const double N = (double)K[0].nx * K[0].ny * K[0].nz;
     const int grid_end = std::min(tail_l0, nl);
     // the grid levels' operations: bitwise kernels, or those of the FP64 performance mode
@@ -731,8 +732,12 @@ int Ctx::vcycle_f64(double *sol, double *rsd, const double *rhs, int maxit, doub
     };
     const double sweep_bytes = fast ? 20.0 : 16.0;
     int pi = prof.begin(stream);
-    PMG_TRY(sweeps(0, sol, rhs));
+    {
+        NvtxRange r("pre-smoothing");
+        PMG_TRY(sweeps(0, sol, rhs));
+    }
     prof.end(pi, PC_SMOOTH64, 2 * maxit, sweep_bytes * N, stream);
+    NvtxRange down_range("residual, restriction, coarse levels, tail, prolongation");
     pi = prof.begin(stream);
     PMG_TRY(resid(0, rsd, sol, rhs));
     prof.end(pi, PC_RES64, 1, 24.0 * N, stream);
@@ -785,7 +790,10 @@ int Ctx::vcycle_f64(double *sol, double *rsd, const double *rhs, int maxit, doub
     PMG_TRY(prolong(0, lv[1].x, sol));
     prof.end(pi, PC_PROLONG64, 1, 17.0 * N, stream);
     pi = prof.begin(stream);
-    PMG_TRY(sweeps(0, sol, rhs));
+    {
+        NvtxRange r("post-smoothing");
+        PMG_TRY(sweeps(0, sol, rhs));
+    }
     prof.end(pi, PC_SMOOTH64, 2 * maxit, sweep_bytes * N, stream);
     return PMG_OK;
 }
@@ -1002,6 +1010,7 @@ int Ctx::before_x_change()
 
 int Ctx::solve(double *sol, double *rsd, const double *rhs, int maxit, double tol, double omega, pmg_report_t *rep)
 {
+    NvtxRange solve_range("pmg_solve_vcycle");
     if (!sol || !rsd || !rhs) {
         set_error("sol, rsd and rhs are required");
         return PMG_EINVAL;
@@ -1113,6 +1122,7 @@ int pmg_create(pmg_ctx **ctx, const pmg_config_t *cfg, void *stream)
         return PMG_EINVAL;
     }
     *ctx = nullptr;
+    pmg::NvtxRange r("pmg_create");
     pmg_ctx *c = new (std::nothrow) pmg_ctx();
     if (!c) return PMG_ENOMEM;
     const int rc = c->impl.build(cfg, (cudaStream_t)stream);

@@ -894,6 +894,7 @@ static void batch_outer(Batch &B, bool first, double tol, int max_cycles)
 int batch_solve(Batch &B, double *sol, const double *rhs, int maxit, double tol, double omega, int max_cycles,
                 int *cycles, double *ratio, float *elapsed_ms)
 {
+    NvtxRange nvtx_range("pmg_batch_solve");
     const int n = B.n;
     if (!sol || !rhs || maxit < 0 || max_cycles < 0) {
         set_error("invalid batch solve arguments");

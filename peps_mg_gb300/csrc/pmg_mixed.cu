@@ -650,6 +650,7 @@ int Ctx::upload_tail32(int maxit, double omega, double tol)
 // One FP32 V-cycle on A e = b[0] (e = e[0]); zero_start: e[0] enters as 0.
 int Ctx::vcycle32(int maxit, double omega, bool zero_start)
 {
+    NvtxRange cycle_range("fp32 V-cycle");
     MixedState *m = mixed;
     const float om = (float)omega, omw = (float)(1.0 - omega);
     const dim3 bl(kBX, kBY, 1);
@@ -764,6 +765,7 @@ int Ctx::resrestrict32(int l)
 
 int Ctx::outer_residual(double *sol, double *rsd, const double *rhs, int slot)
 {
+    NvtxRange nvtx_range("FP64 outer residual");
     const LevelK<double> &L = K[0];
     const dim3 g = grid_outer(L, launch[0]), bl(kBX, kBY, 1);
     int *nonzero = d_iscal + 3;
@@ -796,6 +798,7 @@ int Ctx::outer_residual(double *sol, double *rsd, const double *rhs, int slot)
 // event profiler on, the kernels are launched one by one.
 int Ctx::run_vcycles(int maxit, double omega)
 {
+    NvtxRange nvtx_range("FP32 V-cycles of a correction");
     MixedState *m = mixed;
     if (prof.on || !m->use_graphs) {
         for (int q = 0; q < m->inner; ++q) PMG_TRY_M(vcycle32(maxit, omega, q == 0));
@@ -846,6 +849,7 @@ int Ctx::run_vcycles(int maxit, double omega)
 // initial residual's squared norm (sets the norm's FP32 scale).
 int Ctx::update_residual(double *sol, double *rsd, int slot, double res0)
 {
+    NvtxRange nvtx_range("correction and residual update");
     const LevelK<double> &L = K[0];
     constexpr int UV = 2;   // cells per thread (64 registers: more resident warps)
     dim3 g = grid_outer(L, launch[0]);
@@ -867,6 +871,7 @@ int Ctx::update_residual(double *sol, double *rsd, int slot, double res0)
 // x += e followed by the FP64 residual b - A x (slot 1).
 int Ctx::correct_and_recompute(double *sol, double *rsd, const double *rhs)
 {
+    NvtxRange nvtx_range("correction and FP64 residual");
     const LevelK<double> &L = K[0];
     const dim3 g = grid_outer(L, launch[0]), bl(kBX, kBY, 1);
     PMG_TRY_M(before_x_change());
