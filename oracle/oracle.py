@@ -35,8 +35,10 @@ def _lib(omp=False):
         lib.orc_mg_create.restype = ctypes.c_void_p
         lib.orc_mg_level_coeff.restype = _dp
         lib.orc_mg_destroy.argtypes = [ctypes.c_void_p]
+        lib.orc_dd_create.restype = ctypes.c_void_p
+        lib.orc_dd_destroy.argtypes = [ctypes.c_void_p]
         for fn in ("orc_mg_solve", "orc_mg_level_dims", "orc_mg_coarsest", "orc_mg_level_mesh",
-                   "orc_mg_level_coeff"):
+                   "orc_mg_level_coeff", "orc_dd_solve", "orc_dd_offset", "orc_dd_level_dims"):
             getattr(lib, fn).argtypes = None
         _LIBS[name] = lib
     return _LIBS[name]
@@ -188,6 +190,58 @@ class OracleMG:
         hist = np.zeros(3 * self.n_vcycles)
         ci = np.zeros(self.n_vcycles, dtype=np.int32)
         ncyc = self._lib.orc_mg_solve(self._h, P(sol), P(rsd), P(rhs), ctypes.c_int(maxiteration),
+                                      ctypes.c_double(tolerance), ctypes.c_double(omega), P(hist),
+                                      ci.ctypes.data_as(_ip))
+        return ncyc, hist[:3 * ncyc].reshape(ncyc, 3), ci[:ncyc]
+
+
+class OracleDD:
+    """The CGS V-cycle on a px x py x pz decomposition of the global problem, every rank
+    simulated in this process (halo exchanges, rank-parity colour offsets and rank-ordered
+    all-reduces as the reference's MPI code has them).  solve() takes and returns global
+    arrays."""
+
+    def __init__(self, mesh, procs, n_levels, n_vcycles, coarse_solver=0, omp=False):
+        self._lib = _lib(omp)
+        (dxm, dxg, xg), (dym, dyg, yg), (dzm, dzg, zg) = mesh
+        self.n = (len(dxm) - 2, len(dym) - 2, len(dzm) - 2)
+        self.procs = tuple(int(p) for p in procs)
+        self.n_levels = n_levels
+        self.n_vcycles = n_vcycles
+        err = ctypes.c_int()
+        h = self._lib.orc_dd_create(ctypes.c_int(self.n[0]), ctypes.c_int(self.n[1]), ctypes.c_int(self.n[2]),
+                                    P(dxm), P(dxg), P(xg), P(dym), P(dyg), P(yg), P(dzm), P(dzg), P(zg),
+                                    ctypes.c_int(self.procs[0]), ctypes.c_int(self.procs[1]),
+                                    ctypes.c_int(self.procs[2]), ctypes.c_int(n_levels), ctypes.c_int(n_vcycles),
+                                    ctypes.c_int(coarse_solver), ctypes.byref(err))
+        if not h:
+            raise ValueError("oracle multigrid_create on %s ranks rejected the configuration" % (self.procs,))
+        self._h = ctypes.c_void_p(h)
+
+    def close(self):
+        if self._h:
+            self._lib.orc_dd_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def offset(self, coords, level):
+        return self._lib.orc_dd_offset(self._h, *(ctypes.c_int(c) for c in coords), ctypes.c_int(level))
+
+    def level_dims(self, level):
+        d = np.zeros(3, dtype=np.int32)
+        self._lib.orc_dd_level_dims(self._h, ctypes.c_int(level), d.ctypes.data_as(_ip))
+        return tuple(int(v) for v in d)
+
+    def solve(self, sol, rsd, rhs, maxiteration, tolerance, omega):
+        """In place on the global sol and rsd; returns (cycles, hist[cycles,3], coarse_iters)."""
+        hist = np.zeros(3 * self.n_vcycles)
+        ci = np.zeros(self.n_vcycles, dtype=np.int32)
+        ncyc = self._lib.orc_dd_solve(self._h, P(sol), P(rsd), P(rhs), ctypes.c_int(maxiteration),
                                       ctypes.c_double(tolerance), ctypes.c_double(omega), P(hist),
                                       ci.ctypes.data_as(_ip))
         return ncyc, hist[:3 * ncyc].reshape(ncyc, 3), ci[:ncyc]

@@ -881,3 +881,427 @@ int orc_mg_solve(orc_mg *mg, double *sol, double *rsd, const double *rhs, int ma
     }
     return ncyc;
 }
+
+/* ------------------------------------------------------------------------------ */
+/* Several ranks: the CGS V-cycle of src/multigrid.f90:1907-1976 on a px x py x pz  */
+/* Cartesian decomposition (src/mpi_topology.f90:53-99, src/geometry.f90), every     */
+/* rank simulated in this process.  Each rank holds its subdomain's hierarchy; the   */
+/* ghost layers facing a neighbour are filled by the halo exchange of               */
+/* geometry_halocell_update_selectively (src/geometry.f90:621-660: x, then y, then  */
+/* z, full planes) at the points where the reference calls it: before each RBGS     */
+/* colour (src/rbgs_poisson_matrix.f90:237,255 and :116,134), before every          */
+/* mv_mul (src/poisson_matrix_operator.f90:131-133, so in every residual), and after */
+/* the post-smoothing of each coarse level (src/multigrid.f90:1961).  Dot products   */
+/* are local sums added over the ranks in rank order (the MPI_Allreduce of          */
+/* src/poisson_matrix_operator.f90:68-97).  The RBGS colour of a rank starts at the  */
+/* parity offset of src/rbgs_poisson_matrix.f90:230-232.                             */
+/*                                                                                  */
+/* Level sizes follow the multi-rank CGS rule (src/multigrid.f90:221-299): an axis   */
+/* split over several ranks must halve at every level (an odd local size stops the  */
+/* reference).  A rank's coarse meshes are the global coarse meshes restricted to    */
+/* its cells, ghost widths from the neighbours (src/multigrid.f90:452-477), so they  */
+/* are built here by slicing the one-rank hierarchy of the global mesh.              */
+/* Ranks are numbered x fastest.  The finest post-smoothing uses the finest level's  */
+/* partition flags: the reference reads mg_sdm(0) there, one element before that     */
+/* array (src/multigrid.f90:1967), which with bounds checks off is not defined.      */
+/* ------------------------------------------------------------------------------ */
+typedef struct {
+    int p[3], nr;
+    int n_levels, n_vcycles, coarse_solver;
+    orc_mg *glob;          /* one-rank hierarchy of the global mesh (meshes only) */
+    orc_mg **rk;           /* per rank */
+    int (*c)[3];           /* rank coordinates */
+    double **sol, **rsd, **rhs;
+} orc_dd;
+
+static int dd_rank(const orc_dd *dd, int cx, int cy, int cz) { return cx + dd->p[0] * (cy + dd->p[1] * cz); }
+
+void orc_dd_destroy(orc_dd *dd)
+{
+    int r;
+    if (!dd) return;
+    for (r = 0; r < dd->nr; ++r) {
+        if (dd->rk) orc_mg_destroy(dd->rk[r]);
+        if (dd->sol) free(dd->sol[r]);
+        if (dd->rsd) free(dd->rsd[r]);
+        if (dd->rhs) free(dd->rhs[r]);
+    }
+    free(dd->rk); free(dd->sol); free(dd->rsd); free(dd->rhs); free(dd->c);
+    orc_mg_destroy(dd->glob);
+    free(dd);
+}
+
+/* Level sizes of one rank under the multi-rank CGS rule; returns ORC_EINVAL where the
+ * reference stops (a split axis with an odd local size, or more levels than any axis
+ * allows, :302-309).  nloc: the rank's finest sizes. */
+static int dd_level_sizes(const int nloc[3], const int p[3], int n_levels, int *sizes, int coarsest[3])
+{
+    int n[3] = {nloc[0], nloc[1], nloc[2]}, l, d;
+    coarsest[0] = coarsest[1] = coarsest[2] = 0;
+    for (d = 0; d < 3; ++d) sizes[d] = n[d];
+    for (l = 1; l <= n_levels; ++l)
+        for (d = 0; d < 3; ++d) {
+            if (n[d] % 2 == 0) { n[d] /= 2; coarsest[d] = l; }
+            else if (p[d] > 1) return ORC_EINVAL;
+            sizes[3 * l + d] = n[d];
+        }
+    if (n_levels > imax3(coarsest)) return ORC_EINVAL;
+    return ORC_OK;
+}
+
+/* The rank's hierarchy: its level sizes, meshes sliced from the global hierarchy and its
+ * coefficient matrices (built from those meshes as src/matrix.f90:39-94 does). */
+static orc_mg *dd_rank_mg(const orc_dd *dd, const int *sizes, const int coarsest[3], const int c[3])
+{
+    orc_mg *mg = (orc_mg *)calloc(1, sizeof(orc_mg));
+    size_t maxtot = 0;
+    int l, d;
+    mg->n_levels = dd->n_levels; mg->n_vcycles = dd->n_vcycles; mg->method = 0;
+    mg->coarse_solver = dd->coarse_solver;
+    for (d = 0; d < 3; ++d) mg->coarsest[d] = coarsest[d];
+    mg->lv = (orc_level *)calloc((size_t)dd->n_levels + 1, sizeof(orc_level));
+    for (l = 0; l <= dd->n_levels; ++l) {
+        orc_level *L = &mg->lv[l];
+        const orc_level *G = &dd->glob->lv[l];
+        int n[3];
+        L->nx = sizes[3 * l]; L->ny = sizes[3 * l + 1]; L->nz = sizes[3 * l + 2];
+        n[0] = L->nx; n[1] = L->ny; n[2] = L->nz;
+        for (d = 0; d < 3; ++d) {
+            const int off = c[d] * n[d];       /* global index of the rank's ghost cell 0 */
+            L->dm[d] = (double *)malloc(sizeof(double) * ((size_t)n[d] + 2));
+            L->dg[d] = (double *)malloc(sizeof(double) * ((size_t)n[d] + 2));
+            L->xg[d] = (double *)malloc(sizeof(double) * ((size_t)n[d] + 2));
+            memcpy(L->dm[d], G->dm[d] + off, sizeof(double) * ((size_t)n[d] + 2));
+            memcpy(L->dg[d], G->dg[d] + off, sizeof(double) * ((size_t)n[d] + 2));
+            memcpy(L->xg[d], G->xg[d] + off, sizeof(double) * ((size_t)n[d] + 2));
+        }
+        L->coeff = (double *)calloc((size_t)7 * n[0] * n[1] * n[2], sizeof(double));
+        orc_matrix_create(L->nx, L->ny, L->nz, L->dm[0], L->dg[0], L->dm[1], L->dg[1], L->dm[2], L->dg[2],
+                          L->coeff);
+        if (l > 0) {
+            L->x = (double *)calloc(lv_total(L), sizeof(double));
+            L->b = (double *)calloc(lv_total(L), sizeof(double));
+            L->r = (double *)calloc(lv_total(L), sizeof(double));
+        }
+        if (lv_total(L) > maxtot) maxtot = lv_total(L);
+    }
+    mg->work = (double *)calloc(4 * maxtot, sizeof(double));
+    return mg;
+}
+
+/* multigrid_create on every rank of a px x py x pz decomposition of the global mesh
+ * (global sizes divisible by the rank counts).  *err: ORC_EINVAL where the reference
+ * stops. */
+orc_dd *orc_dd_create(int nx, int ny, int nz,
+                      const double *dxm, const double *dxg, const double *xg,
+                      const double *dym, const double *dyg, const double *yg,
+                      const double *dzm, const double *dzg, const double *zg,
+                      int px, int py, int pz, int n_levels, int n_vcycles, int coarse_solver, int *err)
+{
+    orc_dd *dd;
+    int *sizes, coarsest[3], nloc[3], r, cx, cy, cz, gerr = 0;
+    *err = ORC_EINVAL;
+    if (px < 1 || py < 1 || pz < 1 || nx % px || ny % py || nz % pz) return NULL;
+    nloc[0] = nx / px; nloc[1] = ny / py; nloc[2] = nz / pz;
+    dd = (orc_dd *)calloc(1, sizeof(orc_dd));
+    dd->p[0] = px; dd->p[1] = py; dd->p[2] = pz;
+    dd->nr = px * py * pz;
+    dd->n_levels = n_levels; dd->n_vcycles = n_vcycles; dd->coarse_solver = coarse_solver;
+    sizes = (int *)calloc((size_t)(n_levels + 1) * 3, sizeof(int));
+    if (n_levels <= 1 || dd_level_sizes(nloc, dd->p, n_levels, sizes, coarsest) != ORC_OK) {
+        free(sizes); free(dd); return NULL;
+    }
+    dd->glob = orc_mg_create(nx, ny, nz, dxm, dxg, xg, dym, dyg, yg, dzm, dzg, zg, n_levels, n_vcycles, 0, 0,
+                             coarse_solver, &gerr);
+    if (!dd->glob) { free(sizes); free(dd); return NULL; }
+    dd->rk = (orc_mg **)calloc((size_t)dd->nr, sizeof(orc_mg *));
+    dd->c = (int (*)[3])calloc((size_t)dd->nr, sizeof(int[3]));
+    dd->sol = (double **)calloc((size_t)dd->nr, sizeof(double *));
+    dd->rsd = (double **)calloc((size_t)dd->nr, sizeof(double *));
+    dd->rhs = (double **)calloc((size_t)dd->nr, sizeof(double *));
+    for (cz = 0; cz < pz; ++cz)
+        for (cy = 0; cy < py; ++cy)
+            for (cx = 0; cx < px; ++cx) {
+                r = dd_rank(dd, cx, cy, cz);
+                dd->c[r][0] = cx; dd->c[r][1] = cy; dd->c[r][2] = cz;
+                dd->rk[r] = dd_rank_mg(dd, sizes, coarsest, dd->c[r]);
+                dd->sol[r] = (double *)calloc(lv_total(&dd->rk[r]->lv[0]), sizeof(double));
+                dd->rsd[r] = (double *)calloc(lv_total(&dd->rk[r]->lv[0]), sizeof(double));
+                dd->rhs[r] = (double *)calloc(lv_total(&dd->rk[r]->lv[0]), sizeof(double));
+            }
+    free(sizes);
+    *err = ORC_OK;
+    return dd;
+}
+
+/* level arrays of every rank: which = 0 x, 1 b, 2 r (levels >= 1) */
+static double *dd_arr(orc_dd *dd, int r, int l, int which)
+{
+    orc_level *L = &dd->rk[r]->lv[l];
+    return which == 0 ? L->x : which == 1 ? L->b : L->r;
+}
+
+/* plane `idx` along axis d of a (0:n+1)^3 array, every index of the other two axes */
+static void dd_copy_plane(int d, const int n[3], double *dst, int dst_idx, const double *src, int src_idx)
+{
+    int a, b;
+    if (d == 0) {
+        for (b = 0; b <= n[2] + 1; ++b)
+            for (a = 0; a <= n[1] + 1; ++a) dst[IDX(dst_idx, a, b, n[0], n[1])] = src[IDX(src_idx, a, b, n[0], n[1])];
+    } else if (d == 1) {
+        for (b = 0; b <= n[2] + 1; ++b)
+            for (a = 0; a <= n[0] + 1; ++a) dst[IDX(a, dst_idx, b, n[0], n[1])] = src[IDX(a, src_idx, b, n[0], n[1])];
+    } else {
+        for (b = 0; b <= n[1] + 1; ++b)
+            for (a = 0; a <= n[0] + 1; ++a) dst[IDX(a, b, dst_idx, n[0], n[1])] = src[IDX(a, b, src_idx, n[0], n[1])];
+    }
+}
+
+/* geometry_halocell_update_selectively (src/geometry.f90:621-660) of one array of level l
+ * on every rank: along each split axis in turn (x, y, z), a rank's last interior plane
+ * becomes its east neighbour's ghost plane 0 and the neighbour's first interior plane
+ * its ghost plane n+1.  arr[r] is rank r's array. */
+static void dd_halo(orc_dd *dd, int l, double **arr)
+{
+    const orc_level *L0 = &dd->rk[0]->lv[l];
+    const int n[3] = {L0->nx, L0->ny, L0->nz};
+    int d, r;
+    for (d = 0; d < 3; ++d) {
+        if (dd->p[d] == 1) continue;
+        for (r = 0; r < dd->nr; ++r) {
+            int ce[3] = {dd->c[r][0], dd->c[r][1], dd->c[r][2]}, e;
+            if (ce[d] + 1 >= dd->p[d]) continue;
+            ce[d] += 1;
+            e = dd_rank(dd, ce[0], ce[1], ce[2]);
+            dd_copy_plane(d, n, arr[e], 0, arr[r], n[d]);
+            dd_copy_plane(d, n, arr[r], n[d] + 1, arr[e], 1);
+        }
+    }
+}
+
+/* the RBGS start offset of rank r on level l (src/rbgs_poisson_matrix.f90:230-232) */
+static int dd_offset(const orc_dd *dd, int r, int l)
+{
+    const orc_level *L = &dd->rk[r]->lv[l];
+    const int n[3] = {L->nx, L->ny, L->nz};
+    int s = 0, d;
+    for (d = 0; d < 3; ++d) s += (n[d] % 2) * ((dd->c[r][d] * (dd->p[d] > 1 ? 1 : 0)) % 2);
+    return s % 2;
+}
+
+/* vv_dot_3d_matrix with its all-reduce: the local sums added in rank order */
+static double dd_dot(orc_dd *dd, int l, double **x, double **y)
+{
+    double s = 0.0;
+    int r;
+    for (r = 0; r < dd->nr; ++r) {
+        const orc_level *L = &dd->rk[r]->lv[l];
+        s += orc_vv_dot(L->nx, L->ny, L->nz, x[r], y[r]);
+    }
+    return s;
+}
+
+static void dd_rbgs_iterator(orc_dd *dd, int l, double **x, double **b, int maxiteration, double omega)
+{
+    int it, c, r;
+    for (it = 0; it < maxiteration; ++it)
+        for (c = 0; c < 2; ++c) {
+            dd_halo(dd, l, x);
+            for (r = 0; r < dd->nr; ++r) {
+                const orc_level *L = &dd->rk[r]->lv[l];
+                rbgs_colour(L->nx, L->ny, L->nz, L->coeff, x[r], b[r], omega, c, dd_offset(dd, r, l));
+            }
+        }
+}
+
+/* multigrid_residual (mv_mul updates the halo of x first) */
+static void dd_residual(orc_dd *dd, int l, double **rr, double **x, double **b)
+{
+    int r;
+    dd_halo(dd, l, x);
+    for (r = 0; r < dd->nr; ++r) {
+        const orc_level *L = &dd->rk[r]->lv[l];
+        orc_residual(L->nx, L->ny, L->nz, L->coeff, x[r], b[r], rr[r]);
+    }
+}
+
+/* rbgs_solver_poisson_matrix on every rank (src/rbgs_poisson_matrix.f90:47-179) */
+static int dd_rbgs_solver(orc_dd *dd, int l, double **x, double **b, double **rr, int maxiteration,
+                          double tolerance, double omega)
+{
+    double r0, rn;
+    int it;
+    dd_residual(dd, l, rr, x, b);
+    r0 = dd_dot(dd, l, rr, rr);
+    for (it = 0; it < maxiteration; ++it) {
+        dd_rbgs_iterator(dd, l, x, b, 1, omega);
+        dd_residual(dd, l, rr, x, b);
+        rn = dd_dot(dd, l, rr, rr);
+        if (sqrt(rn / r0) <= tolerance) break;
+    }
+    return it;
+}
+
+/* cg_solver_poisson_matrix on every rank (src/cg_poisson_matrix.f90:47-146); p, ap, rs are
+ * per-rank scratch of the level's size */
+static int dd_cg_solver(orc_dd *dd, int l, double **x, double **b, double **p, double **ap, double **rs,
+                        int maxiteration, double tolerance)
+{
+    double r0, t1, t2, alpha, beta;
+    int it, r;
+    dd_residual(dd, l, rs, x, b);
+    for (r = 0; r < dd->nr; ++r) {
+        const orc_level *L = &dd->rk[r]->lv[l];
+        int i, j, k;
+        for (k = 1; k <= L->nz; ++k)
+            for (j = 1; j <= L->ny; ++j)
+                for (i = 1; i <= L->nx; ++i) p[r][IDX(i, j, k, L->nx, L->ny)] = rs[r][IDX(i, j, k, L->nx, L->ny)];
+    }
+    r0 = dd_dot(dd, l, rs, rs);
+    t2 = 0.0;
+    for (it = 0; it < maxiteration; ++it) {
+        t1 = dd_dot(dd, l, rs, rs);
+        dd_halo(dd, l, p);                                     /* mv_mul's halo update */
+        for (r = 0; r < dd->nr; ++r) {
+            const orc_level *L = &dd->rk[r]->lv[l];
+            orc_mv_mul(L->nx, L->ny, L->nz, L->coeff, p[r], ap[r]);
+        }
+        t2 = dd_dot(dd, l, ap, p);
+        alpha = t1 / t2;
+        for (r = 0; r < dd->nr; ++r) {
+            const orc_level *L = &dd->rk[r]->lv[l];
+            cg_update_xr(L->nx, L->ny, L->nz, alpha, x[r], rs[r], p[r], ap[r]);
+        }
+        t2 = dd_dot(dd, l, rs, rs);
+        if (sqrt(t2 / r0) < tolerance) break;
+        beta = t2 / t1;
+        for (r = 0; r < dd->nr; ++r) {
+            const orc_level *L = &dd->rk[r]->lv[l];
+            cg_update_p(L->nx, L->ny, L->nz, beta, p[r], rs[r]);
+        }
+    }
+    return it;
+}
+
+/* Scatter of a global (0:N+1)^3 array to the ranks' (0:n+1)^3 arrays (ghost layers from the
+ * neighbours' cells or the global ghost layers), and gather of the interiors back. */
+static void dd_scatter(const orc_dd *dd, const double *g, double **loc)
+{
+    const orc_level *L = &dd->rk[0]->lv[0];
+    const int n[3] = {L->nx, L->ny, L->nz}, gn[3] = {dd->glob->lv[0].nx, dd->glob->lv[0].ny, dd->glob->lv[0].nz};
+    int r, i, j, k;
+    for (r = 0; r < dd->nr; ++r) {
+        const int o[3] = {dd->c[r][0] * n[0], dd->c[r][1] * n[1], dd->c[r][2] * n[2]};
+        for (k = 0; k <= n[2] + 1; ++k)
+            for (j = 0; j <= n[1] + 1; ++j)
+                for (i = 0; i <= n[0] + 1; ++i)
+                    loc[r][IDX(i, j, k, n[0], n[1])] = g[IDX(o[0] + i, o[1] + j, o[2] + k, gn[0], gn[1])];
+    }
+}
+
+static void dd_gather(const orc_dd *dd, double **loc, double *g)
+{
+    const orc_level *L = &dd->rk[0]->lv[0];
+    const int n[3] = {L->nx, L->ny, L->nz}, gn[3] = {dd->glob->lv[0].nx, dd->glob->lv[0].ny, dd->glob->lv[0].nz};
+    int r, i, j, k;
+    for (r = 0; r < dd->nr; ++r) {
+        const int o[3] = {dd->c[r][0] * n[0], dd->c[r][1] * n[1], dd->c[r][2] * n[2]};
+        for (k = 1; k <= n[2]; ++k)
+            for (j = 1; j <= n[1]; ++j)
+                for (i = 1; i <= n[0]; ++i)
+                    g[IDX(o[0] + i, o[1] + j, o[2] + k, gn[0], gn[1])] = loc[r][IDX(i, j, k, n[0], n[1])];
+    }
+}
+
+/* multigrid_CGS_vcycle_solver (src/multigrid.f90:1907-1976) on every rank.  gsol / grsd /
+ * grhs are the global (0:N+1)^3 arrays: they are scattered to the ranks (ghost layers from
+ * the neighbours) and the interiors gathered back (grsd's ghost layers are zero, as the
+ * residual leaves them).  hist and coarse_iters as orc_mg_solve.  Returns the cycles run. */
+int orc_dd_solve(orc_dd *dd, double *gsol, double *grsd, const double *grhs, int maxiteration,
+                 double tolerance, double omega, double *hist, int *coarse_iters)
+{
+    const int nl = dd->n_levels, nr = dd->nr;
+    double ***X = (double ***)calloc((size_t)nl + 1, sizeof(double **));
+    double ***B = (double ***)calloc((size_t)nl + 1, sizeof(double **));
+    double ***R = (double ***)calloc((size_t)nl + 1, sizeof(double **));
+    double **P = (double **)calloc((size_t)nr, sizeof(double *));
+    double **AP = (double **)calloc((size_t)nr, sizeof(double *));
+    double **RS = (double **)calloc((size_t)nr, sizeof(double *));
+    double res0tol, rsd_val;
+    int l, r, cyc, ncyc = 0;
+    for (l = 1; l <= nl; ++l) {
+        X[l] = (double **)calloc((size_t)nr, sizeof(double *));
+        B[l] = (double **)calloc((size_t)nr, sizeof(double *));
+        R[l] = (double **)calloc((size_t)nr, sizeof(double *));
+        for (r = 0; r < nr; ++r) {
+            X[l][r] = dd_arr(dd, r, l, 0);
+            B[l][r] = dd_arr(dd, r, l, 1);
+            R[l][r] = dd_arr(dd, r, l, 2);
+        }
+    }
+    for (r = 0; r < nr; ++r) {
+        const size_t t = lv_total(&dd->rk[r]->lv[nl]);
+        memset(dd->rk[r]->work, 0, sizeof(double) * 3 * t);
+        P[r] = dd->rk[r]->work;
+        AP[r] = dd->rk[r]->work + t;
+        RS[r] = dd->rk[r]->work + 2 * t;
+        memset(dd->rsd[r], 0, sizeof(double) * lv_total(&dd->rk[r]->lv[0]));
+    }
+    dd_scatter(dd, gsol, dd->sol);
+    dd_scatter(dd, grhs, dd->rhs);
+    dd_residual(dd, 0, dd->rsd, dd->sol, dd->rhs);                          /* :1924 */
+    res0tol = dd_dot(dd, 0, dd->rsd, dd->rsd);
+    for (cyc = 1; cyc <= dd->n_vcycles; ++cyc) {
+        double ratio;
+        int ci;
+        dd_rbgs_iterator(dd, 0, dd->sol, dd->rhs, maxiteration, omega);      /* :1931-1933 */
+        dd_residual(dd, 0, dd->rsd, dd->sol, dd->rhs);
+        for (r = 0; r < nr; ++r) restrict_lv(dd->rk[r], 0, dd->rsd[r], B[1][r]);
+        for (l = 1; l <= nl - 1; ++l) {                                      /* :1936-1941 */
+            for (r = 0; r < nr; ++r) memset(X[l][r], 0, sizeof(double) * lv_total(&dd->rk[r]->lv[l]));
+            dd_rbgs_iterator(dd, l, X[l], B[l], maxiteration, omega);
+            dd_residual(dd, l, R[l], X[l], B[l]);
+            for (r = 0; r < nr; ++r) restrict_lv(dd->rk[r], l, R[l][r], B[l + 1][r]);
+        }
+        for (r = 0; r < nr; ++r) memset(X[nl][r], 0, sizeof(double) * lv_total(&dd->rk[r]->lv[nl]));
+        if (dd->coarse_solver == 1)                                          /* :1944-1949 */
+            ci = dd_cg_solver(dd, nl, X[nl], B[nl], P, AP, RS, 1000, tolerance);
+        else
+            ci = dd_rbgs_solver(dd, nl, X[nl], B[nl], R[nl], 1000, tolerance, omega);
+        if (coarse_iters) coarse_iters[cyc - 1] = ci;
+        dd_residual(dd, nl, R[nl], X[nl], B[nl]);                            /* :1951, halo of x */
+        for (l = nl - 1; l >= 1; --l) {                                      /* :1957-1962 */
+            for (r = 0; r < nr; ++r) {
+                prolong_lv(dd->rk[r], l, X[l + 1][r], R[l][r]);
+                add_inplace(lv_total(&dd->rk[r]->lv[l]), X[l][r], R[l][r]);
+            }
+            dd_rbgs_iterator(dd, l, X[l], B[l], maxiteration, omega);
+            dd_halo(dd, l, X[l]);
+        }
+        for (r = 0; r < nr; ++r) {                                           /* :1965-1967 */
+            prolong_lv(dd->rk[r], 0, X[1][r], dd->rsd[r]);
+            add_inplace(lv_total(&dd->rk[r]->lv[0]), dd->sol[r], dd->rsd[r]);
+        }
+        dd_rbgs_iterator(dd, 0, dd->sol, dd->rhs, maxiteration, omega);
+        dd_residual(dd, 0, dd->rsd, dd->sol, dd->rhs);                      /* :1970-1971 */
+        rsd_val = dd_dot(dd, 0, dd->rsd, dd->rsd);
+        ratio = sqrt(rsd_val / res0tol);
+        if (hist) {
+            hist[3 * (cyc - 1) + 0] = sqrt(rsd_val);
+            hist[3 * (cyc - 1) + 1] = sqrt(res0tol);
+            hist[3 * (cyc - 1) + 2] = ratio;
+        }
+        ncyc = cyc;
+        if (ratio < tolerance) break;                                       /* :1973 */
+    }
+    dd_gather(dd, dd->sol, gsol);
+    memset(grsd, 0, sizeof(double) * lv_total(&dd->glob->lv[0]));
+    dd_gather(dd, dd->rsd, grsd);
+    for (l = 1; l <= nl; ++l) { free(X[l]); free(B[l]); free(R[l]); }
+    free(X); free(B); free(R); free(P); free(AP); free(RS);
+    return ncyc;
+}
+
+/* the rank (cx, cy, cz)'s colour offset on level l and its level sizes (test hooks) */
+int orc_dd_offset(const orc_dd *dd, int cx, int cy, int cz, int l) { return dd_offset(dd, dd_rank(dd, cx, cy, cz), l); }
+void orc_dd_level_dims(const orc_dd *dd, int l, int *dims) { orc_mg_level_dims(dd->rk[0], l, dims); }
