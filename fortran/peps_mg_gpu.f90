@@ -75,6 +75,7 @@ module peps_mg_gpu
     public :: pmg_cg_iterator, pmg_cg_solver, pmg_restriction, pmg_prolongation, pmg_prolong_add
     public :: pmg_adjoint, pmg_batch_create, pmg_batch_layout, pmg_batch_solve, pmg_batch_destroy
     public :: pmg_vv_dot_static, pmg_profile, pmg_profile_read, pmg_launch_count, pmg_sync
+    public :: pmg_dd_create, pmg_dd_solve, pmg_dd_destroy, pmg_dd_partition
     public :: pmg_set_abort, pmg_inject_alloc_failure, pmg_selftest_convert, pmg_selftest_smooth32
     public :: pmg_selftest_wait_timeout
     public :: pmg_last_error_c, pmg_status_string_c, pmg_error_message
@@ -269,6 +270,42 @@ module peps_mg_gpu
             import :: c_int, c_ptr
             type(c_ptr), value  :: batch
         end function pmg_batch_destroy
+
+        ! the CGS V-cycle on a procs(1) x procs(2) x procs(3) decomposition of one grid, every
+        ! subdomain on this process's GPU (the reference's multi-rank execution)
+        integer(c_int) function pmg_dd_create(dd, cfg, procs, stream) bind(C, name="pmg_dd_create")
+            import :: c_int, c_ptr, pmg_config_t
+            type(c_ptr), intent(out)        :: dd
+            type(pmg_config_t), intent(in)  :: cfg      !< the global problem
+            integer(c_int), intent(in)      :: procs(3)
+            type(c_ptr), value              :: stream
+        end function pmg_dd_create
+
+        integer(c_int) function pmg_dd_solve(dd, sol, rsd, rhs, maxiteration, tolerance, omega_sor, report) &
+                bind(C, name="pmg_dd_solve")
+            import :: c_int, c_ptr, c_double, pmg_report_t
+            type(c_ptr), value                  :: dd, sol, rsd, rhs   !< global device arrays
+            integer(c_int), value               :: maxiteration
+            real(c_double), value               :: tolerance, omega_sor
+            type(pmg_report_t), intent(inout)   :: report
+        end function pmg_dd_solve
+
+        integer(c_int) function pmg_dd_destroy(dd) bind(C, name="pmg_dd_destroy")
+            import :: c_int, c_ptr
+            type(c_ptr), value  :: dd
+        end function pmg_dd_destroy
+
+        ! one rank's subdomain (host only): sizes, mesh and RBGS colour offset on a level
+        integer(c_int) function pmg_dd_partition(cfg, procs, coords, level, dims, mesh, offset) &
+                bind(C, name="pmg_dd_partition")
+            import :: c_int, c_ptr, pmg_config_t
+            type(pmg_config_t), intent(in)  :: cfg
+            integer(c_int), intent(in)      :: procs(3), coords(3)
+            integer(c_int), value           :: level
+            integer(c_int), intent(out)     :: dims(3)
+            type(c_ptr), intent(in)         :: mesh(9)     !< dxm, dxg, xg, dym, ..., zg (c_null_ptr allowed)
+            integer(c_int), intent(out)     :: offset
+        end function pmg_dd_partition
 
         ! interior dot product with no device allocation (no counterpart in the reference)
         integer(c_int) function pmg_vv_dot_static(x, y, nx, ny, nz, stream, result) &

@@ -175,6 +175,35 @@ int pmg_batch_solve(pmg_batch *batch, double *sol, const double *rhs, int maxite
                     double omega_sor, int max_cycles, int *cycles, double *ratio, float *elapsed_ms);
 int pmg_batch_destroy(pmg_batch *batch);
 
+/* ---- Domain decomposition: the reference's multi-rank execution --------------------- */
+/* The CGS V-cycle on a procs[0] x procs[1] x procs[2] Cartesian decomposition of one grid,
+ * as the reference runs it on that many MPI ranks (src/mpi_topology.f90:53-99): each
+ * subdomain has its own hierarchy, built from the global hierarchy's meshes restricted to
+ * its cells (coarse ghost widths from the neighbours, src/multigrid.f90:452-477); ghost
+ * layers are exchanged where the reference calls geometry_halocell_update_selectively
+ * (src/geometry.f90:621-660: before each RBGS colour, before every residual, after each
+ * coarse level's post-smoothing), by device-side packing, a cudaMemcpyAsync to the
+ * neighbour's buffer and unpacking; dot products are summed over the subdomains in rank order
+ * (src/poisson_matrix_operator.f90:68-97); each subdomain's RBGS colours start at the
+ * rank-parity offset of src/rbgs_poisson_matrix.f90:230-232.  Every subdomain lives on this
+ * process's current GPU.  The solution equals the one-grid solution bit for bit.
+ * cfg: the global problem (plain FP64, CGS, RBGS coarsest solver); the global sizes must be
+ * divisible by procs, and an axis split over several ranks must halve at every level (the
+ * reference stops otherwise, src/multigrid.f90:226-246): PMG_EINVAL. */
+typedef struct pmg_dd pmg_dd;
+int pmg_dd_create(pmg_dd **dd, const pmg_config_t *cfg, const int procs[3], void *stream);
+/* multigrid_solve_vcycle (src/multigrid.f90:1864) on every subdomain; sol, rsd, rhs are
+ * the global (0:nx+1,0:ny+1,0:nz+1) device arrays (scattered to the subdomains, ghost layers
+ * included, and gathered back).  Synchronous. */
+int pmg_dd_solve(pmg_dd *dd, double *sol, double *rsd, const double *rhs, int maxiteration, double tolerance,
+                 double omega_sor, pmg_report_t *report);
+int pmg_dd_destroy(pmg_dd *dd);
+/* The subdomain of the rank at coords (host only, no GPU needed): its sizes on `level`, its
+ * mesh there (mesh: 9 host pointers dxm, dxg, xg, dym, dyg, yg, dzm, dzg, zg of n+2 values,
+ * any may be NULL) and its RBGS colour offset there. */
+int pmg_dd_partition(const pmg_config_t *cfg, const int procs[3], const int coords[3], int level, int dims[3],
+                     double *const mesh[9], int *offset);
+
 /* ---- Dot product without device allocation (no counterpart in the reference) ------ */
 /* For host codes that must not have a library call cudaMalloc: one whose device memory
  * is handed to its own allocator at start-up, or one calling from inside its iteration

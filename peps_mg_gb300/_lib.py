@@ -62,6 +62,11 @@ _SIGS = {
     "pmg_batch_solve": [c_void_p, c_void_p, c_void_p, c_int, c_double, c_double, c_int, ctypes.POINTER(c_int),
                         ctypes.POINTER(c_double), ctypes.POINTER(c_float)],
     "pmg_batch_destroy": [c_void_p],
+    "pmg_dd_create": [ctypes.POINTER(c_void_p), ctypes.POINTER(PmgConfig), ctypes.POINTER(c_int), c_void_p],
+    "pmg_dd_solve": [c_void_p, c_void_p, c_void_p, c_void_p, c_int, c_double, c_double, ctypes.POINTER(PmgReport)],
+    "pmg_dd_destroy": [c_void_p],
+    "pmg_dd_partition": [ctypes.POINTER(PmgConfig), ctypes.POINTER(c_int), ctypes.POINTER(c_int), c_int,
+                         ctypes.POINTER(c_int), ctypes.POINTER(c_void_p), ctypes.POINTER(c_int)],
     "pmg_vv_dot_static": [c_void_p, c_void_p, c_int, c_int, c_int, c_void_p, ctypes.POINTER(c_double)],
     "pmg_profile": [c_void_p, c_int],
     "pmg_profile_read": [c_void_p, c_int, ctypes.POINTER(c_double), ctypes.POINTER(ctypes.c_longlong),

@@ -30,6 +30,7 @@ UNITS = {
     "pmg_batch.cu": ["--fmad=true"],
     "pmg_adjoint.cu": ["--fmad=false"],
     "pmg_dot_static.cu": ["--fmad=false"],
+    "pmg_dd.cu": ["--fmad=false"],
 }
 
 

@@ -315,6 +315,47 @@ static int validate_mesh(const pmg_config_t *c)
     return PMG_OK;
 }
 
+// The level hierarchy's sizes and meshes at one rank (multigrid_subdomain_create_CGS /
+// _CGA / _CGPSA, src/multigrid.f90:167-495, 503-990, 998-1288): level 0 is the caller's
+// mesh, every coarser one from coarsen_axis.  Host only.
+int host_level_meshes(const pmg_config_t *c, std::vector<Level> &lv, int lvc[3])
+{
+    const int nl = c->number_of_levels, method = c->aggregation_method, cga_level = c->cga_level;
+    const int n0[3] = {c->nx, c->ny, c->nz};
+    std::vector<std::array<int, 3>> sizes;
+    PMG_TRY(level_sizes(n0, nl, method, cga_level, sizes, lvc));
+    lv.assign((size_t)nl + 1, Level());
+    const double *fm[3] = {c->dxm, c->dym, c->dzm}, *fg[3] = {c->dxg, c->dyg, c->dzg}, *fx[3] = {c->xg, c->yg, c->zg};
+    double o[3];
+    for (int l = 0; l <= nl; ++l) {
+        Level &L = lv[l];
+        for (int d = 0; d < 3; ++d) L.n[d] = sizes[l][d];
+        L.sy = L.n[0] + 2;
+        L.sz = (long long)(L.n[0] + 2) * (L.n[1] + 2);
+        L.total = (size_t)L.sz * (size_t)(L.n[2] + 2);
+        for (int d = 0; d < 3; ++d) {
+            const int n = L.n[d];
+            if (l == 0) {
+                L.dm[d].assign(fm[d], fm[d] + n + 2);
+                L.dg[d].assign(fg[d], fg[d] + n + 2);
+                if (fx[d])
+                    L.xg[d].assign(fx[d], fx[d] + n + 2);
+                else {
+                    // cell centres from the widths when the caller gives none
+                    L.xg[d].assign((size_t)n + 2, 0.0);
+                    for (int i = 1; i <= n + 1; ++i) L.xg[d][i] = L.xg[d][i - 1] + L.dg[d][i];
+                }
+                o[d] = L.xg[d][1] - 0.5 * L.dm[d][1];   // sdm%ox, src/geometry.f90:378-380
+            } else {
+                const Level &F = lv[l - 1];
+                coarsen_axis(method, cga_level, n, F.dm[d], F.dg[d], F.xg[d], o[d], l, lvc[d], L.dm[d], L.dg[d],
+                             L.xg[d]);
+            }
+        }
+    }
+    return PMG_OK;
+}
+
 int Ctx::build(const pmg_config_t *c, cudaStream_t s)
 {
     PMG_TRY(validate_mesh(c));
@@ -343,44 +384,35 @@ int Ctx::build(const pmg_config_t *c, cudaStream_t s)
         set_error("mixed_inner_cycles must be non-negative");
         return PMG_EINVAL;
     }
-    const int n0[3] = {c->nx, c->ny, c->nz};
-    std::vector<std::array<int, 3>> sizes;
-    PMG_TRY(level_sizes(n0, nl, method, cga_level, sizes, lvc));
-
-    lv.resize((size_t)nl + 1);
-    const double *fm[3] = {c->dxm, c->dym, c->dzm}, *fg[3] = {c->dxg, c->dyg, c->dzg}, *fx[3] = {c->xg, c->yg, c->zg};
-    double o[3];
-    for (int l = 0; l <= nl; ++l) {
-        Level &L = lv[l];
-        for (int d = 0; d < 3; ++d) L.n[d] = sizes[l][d];
-        L.sy = L.n[0] + 2;
-        L.sz = (long long)(L.n[0] + 2) * (L.n[1] + 2);
-        L.total = (size_t)L.sz * (size_t)(L.n[2] + 2);
-        for (int d = 0; d < 3; ++d) {
-            const int n = L.n[d];
-            if (l == 0) {
-                L.dm[d].assign(fm[d], fm[d] + n + 2);
-                L.dg[d].assign(fg[d], fg[d] + n + 2);
-                if (fx[d])
-                    L.xg[d].assign(fx[d], fx[d] + n + 2);
-                else {
-                    // cell centres from the widths when the caller gives none
-                    L.xg[d].assign((size_t)n + 2, 0.0);
-                    for (int i = 1; i <= n + 1; ++i) L.xg[d][i] = L.xg[d][i - 1] + L.dg[d][i];
-                }
-                o[d] = L.xg[d][1] - 0.5 * L.dm[d][1];   // sdm%ox, src/geometry.f90:378-380
-            } else {
-                const Level &F = lv[l - 1];
-                coarsen_axis(method, cga_level, n, F.dm[d], F.dg[d], F.xg[d], o[d], l, lvc[d], L.dm[d], L.dg[d],
-                             L.xg[d]);
-            }
-            for (int i = 1; i <= n; ++i)
-                if (!(L.dm[d][i] > 0.0) || !(L.dg[d][i] > 0.0) || !(L.dg[d][i + 1] > 0.0)) {
+    if (preset_levels) {
+        // the levels of a subdomain of a decomposed solve: sizes and meshes given (the
+        // global hierarchy's meshes restricted to the subdomain, ghost widths from the
+        // neighbours); an axis was coarsened up to the last level that halved it
+        if ((int)preset_levels->size() != nl + 1) {
+            set_error("preset levels do not match number_of_levels");
+            return PMG_EINVAL;
+        }
+        lv = *preset_levels;
+        lvc[0] = lvc[1] = lvc[2] = 0;
+        for (int l = 1; l <= nl; ++l)
+            for (int d = 0; d < 3; ++d)
+                if (2 * lv[l].n[d] == lv[l - 1].n[d]) lvc[d] = l;
+        for (auto &L : lv) {
+            L.sy = L.n[0] + 2;
+            L.sz = (long long)(L.n[0] + 2) * (L.n[1] + 2);
+            L.total = (size_t)L.sz * (size_t)(L.n[2] + 2);
+            L.x = L.b = L.r = nullptr;
+        }
+    } else {
+        PMG_TRY(host_level_meshes(c, lv, lvc));
+    }
+    for (int l = 0; l <= nl; ++l)
+        for (int d = 0; d < 3; ++d)
+            for (int i = 1; i <= lv[l].n[d]; ++i)
+                if (!(lv[l].dm[d][i] > 0.0) || !(lv[l].dg[d][i] > 0.0) || !(lv[l].dg[d][i + 1] > 0.0)) {
                     set_error("mesh widths and spacings of interior cells must be positive");
                     return PMG_EINVAL;
                 }
-        }
-    }
 
     // ---- host tables ------------------------------------------------------------
     std::vector<double> blob;

@@ -51,6 +51,7 @@ struct Profiler {
 
 int level_sizes(const int n0[3], int n_levels, int method, int cga_level, std::vector<std::array<int, 3>> &sizes,
                 int lvc[3]);
+int host_level_meshes(const pmg_config_t *c, std::vector<Level> &lv, int lvc[3]);
 
 struct Ctx {
     cudaStream_t stream = nullptr;
@@ -113,6 +114,8 @@ struct Ctx {
     // adjoint scratch (finest level)
     double *adj_rhs = nullptr, *adj_sol = nullptr, *adj_rsd = nullptr, *adj_vol = nullptr, *adj_faces = nullptr;
 
+    // subdomain of a decomposed solve: the level sizes and meshes to use (set before build)
+    const std::vector<Level> *preset_levels = nullptr;
     int build(const pmg_config_t *c, cudaStream_t s);
     ~Ctx();
 

@@ -369,6 +369,15 @@ int f64_rbgs_sweeps(const LevelK<double> &L, const Launch &ln, double *x, const 
     return cuda_status(cudaGetLastError(), "rbgs sweep");
 }
 
+int f64_rbgs_colour(const LevelK<double> &L, const Launch &ln, double *x, const double *b, double omega, int colour,
+                    cudaStream_t s)
+{
+    const dim3 g = grid3((L.nx + 1) / 2, L.ny, L.nz, ln), bl(kBX, kBY, 1);
+    k_rbgs_f64<<<g, bl, 0, s>>>(L, x, b, omega, 1.0 - omega, colour & 1);
+    count_launches(1);
+    return cuda_status(cudaGetLastError(), "rbgs half-sweep");
+}
+
 int f64_residual(const LevelK<double> &L, const Launch &ln, double *r, const double *x, const double *b,
                  double *partials, int *npart, cudaStream_t s)
 {

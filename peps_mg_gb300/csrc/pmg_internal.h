@@ -49,6 +49,10 @@ struct TailDesc {
 // ---- FP64 (bitwise) launchers, pmg_f64.cu -------------------------------------
 int f64_rbgs_sweeps(const LevelK<double> &L, const Launch &ln, double *x, const double *b, int iters,
                     double omega, cudaStream_t s);
+// One half-sweep: the cells with (i + j + k + colour) odd, i.e. ista = 1 + mod(j+k+colour, 2)
+// (src/rbgs_poisson_matrix.f90:242, :260; colour carries a rank's parity offset).
+int f64_rbgs_colour(const LevelK<double> &L, const Launch &ln, double *x, const double *b, double omega, int colour,
+                    cudaStream_t s);
 // r = b - A x (interior); if partials != nullptr also writes per-block sums of r^2
 // and returns the number of partials in *npart.
 int f64_residual(const LevelK<double> &L, const Launch &ln, double *r, const double *x, const double *b,

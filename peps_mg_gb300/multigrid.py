@@ -304,3 +304,96 @@ def multigrid_solve_vcycle(mg, sol, rsd, rhs, maxiteration, tolerance, omega_sor
 def multigrid_destroy(mg):
     """multigrid_destroy -- src/multigrid.f90:1320."""
     mg.destroy()
+
+
+def _config(mesh, number_of_levels, number_of_vcycles, keep):
+    """A PmgConfig of the plain FP64 CGS path for a global mesh (keep holds the arrays)."""
+    arrs = [tuple(np.ascontiguousarray(a, dtype=np.float64) for a in m) for m in mesh]
+    keep.extend(arrs)
+    cfg = PmgConfig()
+    cfg.nx, cfg.ny, cfg.nz = (arrs[d][0].size - 2 for d in range(3))
+    for d, a in enumerate("xyz"):
+        setattr(cfg, "d%sm" % a, arrs[d][0].ctypes.data)
+        setattr(cfg, "d%sg" % a, arrs[d][1].ctypes.data)
+        setattr(cfg, "%sg" % a, arrs[d][2].ctypes.data)
+    cfg.number_of_levels = int(number_of_levels)
+    cfg.number_of_vcycles = int(number_of_vcycles)
+    cfg.aggregation_method = 0
+    cfg.coarse_solver = 0
+    cfg.precision = 0
+    return cfg
+
+
+class DecomposedMultigrid:
+    """The reference's multi-rank CGS V-cycle on a procs[0] x procs[1] x procs[2]
+    decomposition of one grid, every subdomain on this process's GPU (pmg_dd_*): the
+    subdomains exchange ghost layers where the reference's MPI code does, and the solution
+    equals the one-grid solution bit for bit.  mesh is the GLOBAL mesh; solve_vcycle takes
+    the global (nx+2)(ny+2)(nz+2) CUDA tensors."""
+
+    def __init__(self, mesh, procs, number_of_levels, number_of_vcycles, stream=None):
+        self._lib = _lib.load()
+        self._keep = []
+        cfg = _config(mesh, number_of_levels, number_of_vcycles, self._keep)
+        self.n = (cfg.nx, cfg.ny, cfg.nz)
+        self.number_of_vcycles = cfg.number_of_vcycles
+        p = (ctypes.c_int * 3)(*[int(v) for v in procs])
+        self.stream = _default_stream() if stream is None else stream
+        h = ctypes.c_void_p()
+        check(self._lib.pmg_dd_create(ctypes.byref(h), ctypes.byref(cfg), p, self.stream), "pmg_dd_create")
+        self._h = h
+
+    def destroy(self):
+        if getattr(self, "_h", None):
+            self._lib.pmg_dd_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.destroy()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.destroy()
+
+    def solve_vcycle(self, sol, rsd, rhs, maxiteration, tolerance, omega_sor):
+        need = (self.n[0] + 2) * (self.n[1] + 2) * (self.n[2] + 2)
+        ptrs = []
+        for a, what in ((sol, "sol"), (rsd, "rsd"), (rhs, "rhs")):
+            p, n, dev = _ptr(a)
+            if n != need or not dev:
+                raise ValueError("%s must be a CUDA tensor of %d elements" % (what, need))
+            ptrs.append(p)
+        hist = np.zeros(3 * max(self.number_of_vcycles, 1))
+        citers = np.zeros(max(self.number_of_vcycles, 1), dtype=np.int32)
+        rep = PmgReport()
+        rep.history = hist.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+        rep.coarse_iterations = citers.ctypes.data_as(ctypes.POINTER(ctypes.c_int))
+        check(self._lib.pmg_dd_solve(self._h, ptrs[0], ptrs[1], ptrs[2], int(maxiteration), float(tolerance),
+                                     float(omega_sor), ctypes.byref(rep)), "pmg_dd_solve")
+        return SolveReport(rep.cycles, bool(rep.converged), rep.res0, rep.final_ratio,
+                           hist[:3 * rep.cycles].reshape(rep.cycles, 3).copy(), citers[:rep.cycles].copy(),
+                           rep.elapsed_ms, rep.inner_cycles)
+
+
+def dd_partition(mesh, procs, coords, level, number_of_levels):
+    """The subdomain of the rank at `coords` in a procs decomposition of the global mesh
+    (host only): (dims, [(dm, dg, xg) per axis], colour offset) on `level`."""
+    lib = _lib.load()
+    keep = []
+    cfg = _config(mesh, number_of_levels, 1, keep)
+    p = (ctypes.c_int * 3)(*[int(v) for v in procs])
+    c = (ctypes.c_int * 3)(*[int(v) for v in coords])
+    dims = (ctypes.c_int * 3)()
+    off = ctypes.c_int()
+    check(lib.pmg_dd_partition(ctypes.byref(cfg), p, c, int(level), dims, None, ctypes.byref(off)), "pmg_dd_partition")
+    d = tuple(dims)
+    bufs = [np.zeros(d[a] + 2) for a in range(3) for _ in range(3)]
+    ptrs = (ctypes.c_void_p * 9)(*[b.ctypes.data for b in bufs])
+    check(lib.pmg_dd_partition(ctypes.byref(cfg), p, c, int(level), dims, ptrs, ctypes.byref(off)),
+          "pmg_dd_partition")
+    return d, [tuple(bufs[3 * a:3 * a + 3]) for a in range(3)], off.value

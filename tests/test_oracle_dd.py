@@ -85,3 +85,30 @@ def test_split_axis_that_cannot_halve_is_rejected():
     # sizes not divisible by the rank count
     with pytest.raises(ValueError):
         O.OracleDD([ax, ax, ax], (5, 1, 1), 2, 10)
+
+
+@pytest.mark.parametrize("procs", [(2, 1, 1), (2, 2, 2), (1, 3, 1)])
+def test_library_partition_matches_the_oracle(procs):
+    """pmg_dd_partition (host only): each rank's level sizes and colour offsets are the
+    oracle's, and its meshes are the global hierarchy's meshes restricted to its cells and
+    ghost cells."""
+    import peps_mg_gb300 as pmg
+    mesh = [G.stretched_axis(24, 0.0, 1.0, 1.1), G.uniform_axis(24, 0.0, 2.0), G.tanh_axis(24, 0.0, 1.0, 1.3)]
+    nl = 2
+    dd = O.OracleDD(mesh, procs, nl, 1)
+    glob = O.OracleMG(mesh, nl, 1, 0)
+    for cz in range(procs[2]):
+        for cy in range(procs[1]):
+            for cx in range(procs[0]):
+                co = (cx, cy, cz)
+                for lev in range(nl + 1):
+                    dims, m, off = pmg.dd_partition(mesh, procs, co, lev, nl)
+                    assert dims == dd.level_dims(lev)
+                    assert off == dd.offset(co, lev)
+                    for a in range(3):
+                        o = co[a] * dims[a]
+                        gdm, gdg, _ = glob.level_mesh(lev, a)
+                        assert np.array_equal(m[a][0], gdm[o:o + dims[a] + 2])
+                        assert np.array_equal(m[a][1], gdg[o:o + dims[a] + 2])
+    with pytest.raises(pmg.PmgError):
+        pmg.dd_partition(mesh, (2, 1, 1), (0, 0, 0), 0, 4)     # 24/2 = 12, 6, 3: cannot halve again
