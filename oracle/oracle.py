@@ -134,6 +134,28 @@ def cg(coeff, x, b, maxiteration, tolerance, check_tol=True, omp=False):
     return it, n2.value, n02.value
 
 
+def rbgs_colour(coeff, x, b, omega, colour, offset):
+    """One RBGS colour (0 first, 1 second) with a rank's start offset, in place on x."""
+    _lib().orc_rbgs_colour(*dims_of(x), P(coeff), P(x), P(b), ctypes.c_double(omega), ctypes.c_int(colour),
+                           ctypes.c_int(offset))
+
+
+def restriction(mesh_c, mesh_f, level, coarsest, val_f, val_c):
+    """multigrid_restriction of val_f into val_c (meshes: (dm, dg, xg) per axis)."""
+    ci = (ctypes.c_int * 3)(*coarsest)
+    _lib().orc_restriction(*dims_of(val_c), P(mesh_c[0][0]), P(mesh_c[1][0]), P(mesh_c[2][0]), *dims_of(val_f),
+                           P(mesh_f[0][0]), P(mesh_f[1][0]), P(mesh_f[2][0]), ctypes.c_int(level), ci, P(val_f),
+                           P(val_c))
+
+
+def prolongation(mesh_c, mesh_f, level, coarsest, val_c, val_f):
+    """multigrid_prolongation_linear_on_nonuniform_grid of val_c into val_f."""
+    ci = (ctypes.c_int * 3)(*coarsest)
+    _lib().orc_prolongation(*dims_of(val_c), P(mesh_c[0][0]), P(mesh_c[1][0]), P(mesh_c[2][0]), *dims_of(val_f),
+                            P(mesh_f[0][0]), P(mesh_f[1][0]), P(mesh_f[2][0]), ctypes.c_int(level), ci, P(val_c),
+                            P(val_f))
+
+
 class OracleMG:
     """multigrid_create / multigrid_solve_vcycle / multigrid_destroy on the CPU."""
 

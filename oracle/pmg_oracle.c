@@ -1305,3 +1305,11 @@ int orc_dd_solve(orc_dd *dd, double *gsol, double *grsd, const double *grhs, int
 /* the rank (cx, cy, cz)'s colour offset on level l and its level sizes (test hooks) */
 int orc_dd_offset(const orc_dd *dd, int cx, int cy, int cz, int l) { return dd_offset(dd, dd_rank(dd, cx, cy, cz), l); }
 void orc_dd_level_dims(const orc_dd *dd, int l, int *dims) { orc_mg_level_dims(dd->rk[0], l, dims); }
+
+/* One RBGS colour with a rank's start offset (src/rbgs_poisson_matrix.f90:239-271), for
+ * drivers that run one rank per process. */
+void orc_rbgs_colour(int nx, int ny, int nz, const double *coeff, double *sol, const double *rhs, double omega,
+                     int colour, int offset)
+{
+    rbgs_colour(nx, ny, nz, coeff, sol, rhs, omega, colour, offset);
+}
