@@ -114,7 +114,7 @@ int Ctx::adjoint(const double *dLdu, double *dLdb, double *dLdg, int maxit, doub
                              "adjoint tables");
         }
         if (st != PMG_OK) {
-            for (auto p : a) cudaFree(p);
+            for (auto p : a) dev_free(p);
             return st;
         }
         adj_rhs = a[0];

@@ -12,7 +12,9 @@
 #include <atomic>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
+#include <mutex>
 #include <new>
 #include <string>
 #include <vector>
@@ -37,6 +39,38 @@ int cuda_status(cudaError_t e, const char *what)
 // dev_malloc call (0 = the next one) fails once.
 static std::atomic<long long> g_alloc_fail_countdown{-1};
 
+struct DevArena {
+    std::vector<std::pair<char *, size_t>> chunks;
+    char *cur = nullptr;
+    size_t left = 0;
+};
+static std::mutex g_arena_mu;
+static std::vector<DevArena *> g_arenas;           // live arenas (dev_free's ownership test)
+static thread_local DevArena *t_arena = nullptr;   // the arena of the thread's ArenaScope
+
+DevArena *arena_create()
+{
+    DevArena *a = new (std::nothrow) DevArena();
+    if (!a) return nullptr;
+    std::lock_guard<std::mutex> g(g_arena_mu);
+    g_arenas.push_back(a);
+    return a;
+}
+
+void arena_destroy(DevArena *a)
+{
+    if (!a) return;
+    {
+        std::lock_guard<std::mutex> g(g_arena_mu);
+        g_arenas.erase(std::remove(g_arenas.begin(), g_arenas.end(), a), g_arenas.end());
+    }
+    for (auto &c : a->chunks) cudaFree(c.first);
+    delete a;
+}
+
+ArenaScope::ArenaScope(DevArena *a) : prev(t_arena) { t_arena = a; }
+ArenaScope::~ArenaScope() { t_arena = prev; }
+
 cudaError_t dev_malloc_bytes(void **p, size_t bytes)
 {
     long long c = g_alloc_fail_countdown.load();
@@ -49,7 +83,39 @@ cudaError_t dev_malloc_bytes(void **p, size_t bytes)
             break;
         }
     }
-    return cudaMalloc(p, bytes);
+    DevArena *a = t_arena;
+    if (!a) return cudaMalloc(p, bytes);
+    const size_t need = (bytes + 255) & ~(size_t)255;
+    if (need > a->left) {
+        const size_t chunk = std::max(need, (size_t)256 << 20);
+        void *m = nullptr;
+        const cudaError_t e = cudaMalloc(&m, chunk);
+        if (e != cudaSuccess) {
+            *p = nullptr;
+            return e;
+        }
+        std::lock_guard<std::mutex> g(g_arena_mu);
+        a->chunks.push_back({static_cast<char *>(m), chunk});
+        a->cur = static_cast<char *>(m);
+        a->left = chunk;
+    }
+    *p = a->cur;
+    a->cur += need;
+    a->left -= need;
+    return cudaSuccess;
+}
+
+cudaError_t dev_free(void *p)
+{
+    if (!p) return cudaSuccess;
+    {
+        std::lock_guard<std::mutex> g(g_arena_mu);
+        const char *q = static_cast<const char *>(p);
+        for (const DevArena *a : g_arenas)
+            for (const auto &c : a->chunks)
+                if (q >= c.first && q < c.first + c.second) return cudaSuccess;
+    }
+    return cudaFree(p);
 }
 
 static std::atomic<long long> g_launches{0};
@@ -356,6 +422,158 @@ int host_level_meshes(const pmg_config_t *c, std::vector<Level> &lv, int lvc[3])
     return PMG_OK;
 }
 
+// PEPS_MG_HOST_SETUP=1: coarse meshes and tables computed on the host as well (the same
+// expressions), for checking the device set-up against it
+bool host_setup()
+{
+    const char *e = std::getenv("PEPS_MG_HOST_SETUP");
+    return e && std::strcmp(e, "1") == 0;
+}
+
+// The coarse meshes (unless lv holds every level's mesh already) and the per-axis
+// coefficient tables and transfer weights of every level, built on the device by one
+// launch (hierarchy_setup) into d_tables; the meshes and tables are copied back for the
+// host-side uses (level queries, the FP32 tables of the mixed path).  The layout: per level
+// and axis cm, cp (and sx for x), then per transfer and axis w, pp, pn, each table padded to
+// an even length (16-byte alignment).
+int Ctx::setup_tables()
+{
+    const bool meshes_given = preset_levels || host_setup();
+    HierDesc H;
+    std::memset(&H, 0, sizeof(H));
+    H.nl = nl;
+    H.method = method;
+    H.agg_level = cga_level;
+    H.meshes_given = meshes_given ? 1 : 0;
+    long long mo = 0, to = 0;
+    auto tab = [&](int n) {
+        const long long o = to;
+        to += n + 2 + ((n + 2) & 1);
+        return o;
+    };
+    for (int d = 0; d < 3; ++d) {
+        H.lvc[d] = lvc[d];
+        H.ox[d] = lv[0].xg[d][1] - 0.5 * lv[0].dm[d][1];   // sdm%ox, src/geometry.f90:378-380
+    }
+    for (int l = 0; l <= nl; ++l) {
+        for (int d = 0; d < 3; ++d) {
+            H.n[l][d] = lv[l].n[d];
+            H.mesh_off[l][d] = mo;
+            mo += 3LL * (lv[l].n[d] + 2);
+        }
+        for (int d = 0; d < 3; ++d) {
+            H.cm[l][d] = tab(lv[l].n[d]);
+            H.cp[l][d] = tab(lv[l].n[d]);
+            if (d == 0) H.sx[l] = tab(lv[l].n[d]);
+        }
+        if (l < nl)
+            for (int d = 0; d < 3; ++d) {
+                H.w[l][d] = tab(lv[l].n[d]);
+                H.pp[l][d] = tab(lv[l].n[d]);
+                H.pn[l][d] = tab(lv[l].n[d]);
+            }
+    }
+    std::vector<double> hm((size_t)mo, 0.0);
+    for (int l = 0; l <= (meshes_given ? nl : 0); ++l)
+        for (int d = 0; d < 3; ++d) {
+            double *p = hm.data() + H.mesh_off[l][d];
+            const size_t m = (size_t)lv[l].n[d] + 2;
+            std::memcpy(p, lv[l].dm[d].data(), m * sizeof(double));
+            std::memcpy(p + m, lv[l].dg[d].data(), m * sizeof(double));
+            std::memcpy(p + 2 * m, lv[l].xg[d].data(), m * sizeof(double));
+        }
+    double *d_meshes = nullptr;
+    HierDesc *d_hier = nullptr;
+    PMG_CUDA(dev_malloc(&d_tables, (size_t)to * sizeof(double)), "table allocation");
+    int rc = cuda_status(dev_malloc(&d_meshes, (size_t)mo * sizeof(double)), "set-up allocation");
+    if (rc == PMG_OK) rc = cuda_status(dev_malloc(&d_hier, sizeof(HierDesc)), "set-up allocation");
+    if (rc == PMG_OK)
+        rc = cuda_status(cudaMemcpyAsync(d_meshes, hm.data(), hm.size() * sizeof(double), cudaMemcpyHostToDevice,
+                                         stream),
+                         "mesh upload");
+    if (rc == PMG_OK)
+        rc = cuda_status(cudaMemcpyAsync(d_hier, &H, sizeof(H), cudaMemcpyHostToDevice, stream), "set-up upload");
+    if (rc == PMG_OK)
+        rc = cuda_status(cudaMemsetAsync(d_tables, 0, (size_t)to * sizeof(double), stream), "table init");
+    if (rc == PMG_OK) rc = hierarchy_setup(d_hier, d_meshes, d_tables, stream);
+    tables_host.assign((size_t)to, 0.0);
+    if (rc == PMG_OK)
+        rc = cuda_status(cudaMemcpyAsync(hm.data(), d_meshes, hm.size() * sizeof(double), cudaMemcpyDeviceToHost,
+                                         stream),
+                         "mesh download");
+    if (rc == PMG_OK)
+        rc = cuda_status(cudaMemcpyAsync(tables_host.data(), d_tables, (size_t)to * sizeof(double),
+                                         cudaMemcpyDeviceToHost, stream),
+                         "table download");
+    if (rc == PMG_OK) rc = cuda_status(cudaStreamSynchronize(stream), "hierarchy set-up");
+    dev_free(d_meshes);
+    dev_free(d_hier);
+    if (rc != PMG_OK) return rc;
+    if (!meshes_given)
+        for (int l = 1; l <= nl; ++l)
+            for (int d = 0; d < 3; ++d) {
+                const double *p = hm.data() + H.mesh_off[l][d];
+                const size_t m = (size_t)lv[l].n[d] + 2;
+                lv[l].dm[d].assign(p, p + m);
+                lv[l].dg[d].assign(p + m, p + 2 * m);
+                lv[l].xg[d].assign(p + 2 * m, p + 3 * m);
+            }
+
+    K.resize((size_t)nl + 1);
+    X.resize((size_t)nl);
+    for (int l = 0; l <= nl; ++l) {
+        const Level &L = lv[l];
+        LevelK<double> &k = K[l];
+        k.nx = L.n[0]; k.ny = L.n[1]; k.nz = L.n[2];
+        k.sy = L.sy; k.sz = L.sz;
+        k.cxm = d_tables + H.cm[l][0]; k.cxp = d_tables + H.cp[l][0]; k.sx = d_tables + H.sx[l];
+        k.cym = d_tables + H.cm[l][1]; k.cyp = d_tables + H.cp[l][1];
+        k.czm = d_tables + H.cm[l][2]; k.czp = d_tables + H.cp[l][2];
+        if (l < nl) {
+            const Level &C = lv[l + 1];
+            XferK<double> &x = X[l];
+            x.ncx = C.n[0]; x.ncy = C.n[1]; x.ncz = C.n[2];
+            x.csy = C.sy; x.csz = C.sz;
+            x.fsy = L.sy; x.fsz = L.sz;
+            x.stx = l >= lvc[0] ? 1 : 2;
+            x.sty = l >= lvc[1] ? 1 : 2;
+            x.stz = l >= lvc[2] ? 1 : 2;
+            x.wx = d_tables + H.w[l][0]; x.wy = d_tables + H.w[l][1]; x.wz = d_tables + H.w[l][2];
+            x.pxp = d_tables + H.pp[l][0]; x.pxn = d_tables + H.pn[l][0];
+            x.pyp = d_tables + H.pp[l][1]; x.pyn = d_tables + H.pn[l][1];
+            x.pzp = d_tables + H.pp[l][2]; x.pzn = d_tables + H.pn[l][2];
+        }
+    }
+    if (host_setup()) {
+        // the host computation of the same tables, for checking the device set-up
+        std::vector<double> hb((size_t)to, 0.0);
+        for (int l = 0; l <= nl; ++l) {
+            for (int d = 0; d < 3; ++d) {
+                std::vector<double> cm, cp, sxv;
+                axis_coeff_tables(lv[l].dm[d], lv[l].dg[d], lv[l].n[d], cm, cp, sxv);
+                std::copy(cm.begin(), cm.end(), hb.begin() + H.cm[l][d]);
+                std::copy(cp.begin(), cp.end(), hb.begin() + H.cp[l][d]);
+                if (d == 0) std::copy(sxv.begin(), sxv.end(), hb.begin() + H.sx[l]);
+            }
+            if (l < nl)
+                for (int d = 0; d < 3; ++d) {
+                    const bool s1 = l >= lvc[d];
+                    std::vector<double> w, dp, dn;
+                    restrict_weights(lv[l + 1].dm[d], lv[l].dm[d], lv[l].n[d], s1, w);
+                    prolong_weights(lv[l + 1].dm[d], lv[l].dm[d], lv[l + 1].n[d], lv[l].n[d], s1, dp, dn);
+                    std::copy(w.begin(), w.end(), hb.begin() + H.w[l][d]);
+                    std::copy(dp.begin(), dp.end(), hb.begin() + H.pp[l][d]);
+                    std::copy(dn.begin(), dn.end(), hb.begin() + H.pn[l][d]);
+                }
+        }
+        if (std::memcmp(hb.data(), tables_host.data(), hb.size() * sizeof(double)) != 0) {
+            set_error("device-built tables differ from the host-built ones");
+            return PMG_ECUDA;
+        }
+    }
+    return PMG_OK;
+}
+
 int Ctx::build(const pmg_config_t *c, cudaStream_t s)
 {
     PMG_TRY(validate_mesh(c));
@@ -403,82 +621,50 @@ int Ctx::build(const pmg_config_t *c, cudaStream_t s)
             L.total = (size_t)L.sz * (size_t)(L.n[2] + 2);
             L.x = L.b = L.r = nullptr;
         }
-    } else {
+    } else if (host_setup()) {
         PMG_TRY(host_level_meshes(c, lv, lvc));
+    } else {
+        // level sizes here, the coarse meshes on the device (setup_tables)
+        const int n0[3] = {c->nx, c->ny, c->nz};
+        std::vector<std::array<int, 3>> sizes;
+        PMG_TRY(level_sizes(n0, nl, method, cga_level, sizes, lvc));
+        lv.assign((size_t)nl + 1, Level());
+        const double *fm[3] = {c->dxm, c->dym, c->dzm}, *fg[3] = {c->dxg, c->dyg, c->dzg};
+        const double *fx[3] = {c->xg, c->yg, c->zg};
+        for (int l = 0; l <= nl; ++l) {
+            Level &L = lv[l];
+            for (int d = 0; d < 3; ++d) L.n[d] = sizes[l][d];
+            L.sy = L.n[0] + 2;
+            L.sz = (long long)(L.n[0] + 2) * (L.n[1] + 2);
+            L.total = (size_t)L.sz * (size_t)(L.n[2] + 2);
+        }
+        for (int d = 0; d < 3; ++d) {
+            const int n = lv[0].n[d];
+            lv[0].dm[d].assign(fm[d], fm[d] + n + 2);
+            lv[0].dg[d].assign(fg[d], fg[d] + n + 2);
+            if (fx[d]) {
+                lv[0].xg[d].assign(fx[d], fx[d] + n + 2);
+            } else {
+                lv[0].xg[d].assign((size_t)n + 2, 0.0);
+                for (int i = 1; i <= n + 1; ++i) lv[0].xg[d][i] = lv[0].xg[d][i - 1] + lv[0].dg[d][i];
+            }
+        }
     }
-    for (int l = 0; l <= nl; ++l)
+    // finest widths are checked before any device work; coarse ones after the set-up
+    for (int d = 0; d < 3; ++d)
+        for (int i = 1; i <= lv[0].n[d]; ++i)
+            if (!(lv[0].dm[d][i] > 0.0) || !(lv[0].dg[d][i] > 0.0) || !(lv[0].dg[d][i + 1] > 0.0)) {
+                set_error("mesh widths and spacings of interior cells must be positive");
+                return PMG_EINVAL;
+            }
+    PMG_TRY(setup_tables());
+    for (int l = 1; l <= nl; ++l)
         for (int d = 0; d < 3; ++d)
             for (int i = 1; i <= lv[l].n[d]; ++i)
                 if (!(lv[l].dm[d][i] > 0.0) || !(lv[l].dg[d][i] > 0.0) || !(lv[l].dg[d][i + 1] > 0.0)) {
                     set_error("mesh widths and spacings of interior cells must be positive");
                     return PMG_EINVAL;
                 }
-
-    // ---- host tables ------------------------------------------------------------
-    std::vector<double> blob;
-    auto push = [&](const std::vector<double> &v) {
-        size_t off = blob.size();
-        blob.insert(blob.end(), v.begin(), v.end());
-        // keep every table 16-byte aligned
-        if (blob.size() % 2) blob.push_back(0.0);
-        return off;
-    };
-    struct Off {
-        size_t cm[3], cp[3], s;
-        size_t w[3], pp[3], pn[3];
-    };
-    std::vector<Off> off((size_t)nl + 1);
-    for (int l = 0; l <= nl; ++l) {
-        const Level &L = lv[l];
-        for (int d = 0; d < 3; ++d) {
-            std::vector<double> cm, cp, s;
-            axis_coeff_tables(L.dm[d], L.dg[d], L.n[d], cm, cp, s);
-            off[l].cm[d] = push(cm);
-            off[l].cp[d] = push(cp);
-            if (d == 0) off[l].s = push(s);
-        }
-        if (l < nl) {
-            const Level &C = lv[l + 1];
-            for (int d = 0; d < 3; ++d) {
-                const bool s1 = l >= lvc[d];
-                std::vector<double> w, dp, dn;
-                restrict_weights(C.dm[d], L.dm[d], L.n[d], s1, w);
-                prolong_weights(C.dm[d], L.dm[d], C.n[d], L.n[d], s1, dp, dn);
-                off[l].w[d] = push(w);
-                off[l].pp[d] = push(dp);
-                off[l].pn[d] = push(dn);
-            }
-        }
-    }
-    PMG_CUDA(dev_malloc(&d_tables, blob.size() * sizeof(double)), "table allocation");
-    PMG_CUDA(cudaMemcpy(d_tables, blob.data(), blob.size() * sizeof(double), cudaMemcpyHostToDevice), "table copy");
-    tables_host = blob;
-
-    K.resize((size_t)nl + 1);
-    X.resize((size_t)nl);
-    for (int l = 0; l <= nl; ++l) {
-        const Level &L = lv[l];
-        LevelK<double> &k = K[l];
-        k.nx = L.n[0]; k.ny = L.n[1]; k.nz = L.n[2];
-        k.sy = L.sy; k.sz = L.sz;
-        k.cxm = d_tables + off[l].cm[0]; k.cxp = d_tables + off[l].cp[0]; k.sx = d_tables + off[l].s;
-        k.cym = d_tables + off[l].cm[1]; k.cyp = d_tables + off[l].cp[1];
-        k.czm = d_tables + off[l].cm[2]; k.czp = d_tables + off[l].cp[2];
-        if (l < nl) {
-            const Level &C = lv[l + 1];
-            XferK<double> &x = X[l];
-            x.ncx = C.n[0]; x.ncy = C.n[1]; x.ncz = C.n[2];
-            x.csy = C.sy; x.csz = C.sz;
-            x.fsy = L.sy; x.fsz = L.sz;
-            x.stx = l >= lvc[0] ? 1 : 2;
-            x.sty = l >= lvc[1] ? 1 : 2;
-            x.stz = l >= lvc[2] ? 1 : 2;
-            x.wx = d_tables + off[l].w[0]; x.wy = d_tables + off[l].w[1]; x.wz = d_tables + off[l].w[2];
-            x.pxp = d_tables + off[l].pp[0]; x.pxn = d_tables + off[l].pn[0];
-            x.pyp = d_tables + off[l].pp[1]; x.pyn = d_tables + off[l].pn[1];
-            x.pzp = d_tables + off[l].pp[2]; x.pzn = d_tables + off[l].pn[2];
-        }
-    }
 
     // ---- execution mapping --------------------------------------------------------
     // CGS: every level on the full grid; the coarsest solve in the single-CTA kernel.
@@ -536,7 +722,7 @@ int Ctx::build(const pmg_config_t *c, cudaStream_t s)
     PMG_CUDA(dev_malloc(&d_iscal, 16 * sizeof(int)), "scratch allocation");
     PMG_CUDA(dev_malloc(&d_cg, sizeof(CgState)), "scratch allocation");
     PMG_CUDA(cudaMemset(d_cg, 0, sizeof(CgState)), "scratch init");
-    {
+    if (!light) {
         void *h = nullptr, *d = nullptr;
         PMG_CUDA(cudaHostAlloc(&h, sizeof(int), cudaHostAllocMapped), "abort flag allocation");
         abort_host = static_cast<int *>(h);
@@ -553,11 +739,13 @@ int Ctx::build(const pmg_config_t *c, cudaStream_t s)
         }
     }
     PMG_CUDA(dev_malloc(&d_tail, sizeof(TailDesc<double>)), "tail descriptor");
-    PMG_CUDA(cudaEventCreate(&ev0), "event");
-    PMG_CUDA(cudaEventCreate(&ev1), "event");
-    PMG_CUDA(cudaEventCreateWithFlags(&ev_x, cudaEventDisableTiming), "event");
-    PMG_CUDA(cudaEventCreateWithFlags(&ev_copied, cudaEventDisableTiming), "event");
-    PMG_CUDA(cudaStreamCreateWithFlags(&copy_stream, cudaStreamNonBlocking), "copy stream");
+    if (!light) {
+        PMG_CUDA(cudaEventCreate(&ev0), "event");
+        PMG_CUDA(cudaEventCreate(&ev1), "event");
+        PMG_CUDA(cudaEventCreateWithFlags(&ev_x, cudaEventDisableTiming), "event");
+        PMG_CUDA(cudaEventCreateWithFlags(&ev_copied, cudaEventDisableTiming), "event");
+        PMG_CUDA(cudaStreamCreateWithFlags(&copy_stream, cudaStreamNonBlocking), "copy stream");
+    }
     if (precision == PMG_FP64_FAST) PMG_TRY(setup_fast64());
     return PMG_OK;
 }
@@ -619,31 +807,31 @@ int Ctx::fast_prepare(double omega)
 Ctx::~Ctx()
 {
     for (auto &L : lv) {
-        cudaFree(L.x);
-        cudaFree(L.b);
-        cudaFree(L.r);
+        dev_free(L.x);
+        dev_free(L.b);
+        dev_free(L.r);
     }
-    cudaFree(d_tables);
-    cudaFree(d_partials);
-    cudaFree(d_scal);
-    cudaFree(d_iscal);
-    cudaFree(d_cg);
+    dev_free(d_tables);
+    dev_free(d_partials);
+    dev_free(d_scal);
+    dev_free(d_iscal);
+    dev_free(d_cg);
     if (abort_host) cudaFreeHost(abort_host);
-    cudaFree(d_fast);
-    for (auto p : fast_wdiag_alloc) cudaFree(p);
-    cudaFree(d_cp);
-    cudaFree(d_cap);
-    cudaFree(d_crr);
-    cudaFree(d_tail);
-    cudaFree(stage_sol);
-    cudaFree(stage_rsd);
-    cudaFree(stage_rhs);
-    for (auto &v : scratch_levels) cudaFree(v);
-    cudaFree(adj_rhs);
-    cudaFree(adj_sol);
-    cudaFree(adj_rsd);
-    cudaFree(adj_vol);
-    cudaFree(adj_faces);
+    dev_free(d_fast);
+    for (auto p : fast_wdiag_alloc) dev_free(p);
+    dev_free(d_cp);
+    dev_free(d_cap);
+    dev_free(d_crr);
+    dev_free(d_tail);
+    dev_free(stage_sol);
+    dev_free(stage_rsd);
+    dev_free(stage_rhs);
+    for (auto &v : scratch_levels) dev_free(v);
+    dev_free(adj_rhs);
+    dev_free(adj_sol);
+    dev_free(adj_rsd);
+    dev_free(adj_vol);
+    dev_free(adj_faces);
     if (ev0) cudaEventDestroy(ev0);
     if (ev1) cudaEventDestroy(ev1);
     if (ev_x) cudaEventDestroy(ev_x);
@@ -927,7 +1115,7 @@ int Ctx::level_scratch(int l, double **bufs, int count)
     // count full-size arrays of level l, zero-initialised (ghosts stay zero)
     const size_t need = lv[l].total * (size_t)count;
     if (scratch_cap < need) {
-        for (auto &v : scratch_levels) cudaFree(v);
+        for (auto &v : scratch_levels) dev_free(v);
         scratch_levels.clear();
         double *p = nullptr;
         PMG_CUDA(dev_malloc(&p, need * sizeof(double)), "scratch allocation");
@@ -1067,7 +1255,7 @@ int Ctx::solve(double *sol, double *rsd, const double *rhs, int maxit, double to
             for (int q = 0; q < 3; ++q) {
                 const int st = cuda_status(dev_malloc(&a[q], bytes), "staging allocation");
                 if (st != PMG_OK) {
-                    for (int u = 0; u < q; ++u) cudaFree(a[u]);
+                    for (int u = 0; u < q; ++u) dev_free(a[u]);
                     return st;
                 }
             }

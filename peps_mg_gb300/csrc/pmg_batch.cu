@@ -433,36 +433,42 @@ struct Batch {
     int graph_maxit = -1;
     double graph_omega = 0.0, graph_tol = 0.0;
     int inner = 2;
+    // every device allocation of the batch and of its problems' hierarchies comes from this
+    // arena (a few large cudaMalloc calls instead of thousands); released last
+    DevArena *arena = nullptr;
     ~Batch();
 };
 
 Batch::~Batch()
 {
     if (graph) cudaGraphExecDestroy(graph);
-    cudaFree(d_lv);
-    cudaFree(d_outer);
+    dev_free(d_lv);
+    dev_free(d_outer);
     for (auto &v : smooth)
-        for (auto &l : v) cudaFree(l.d);
-    for (auto &l : xfer) cudaFree(l.d);
-    cudaFree(outer.d);
-    cudaFree(d_first);
-    cudaFree(d_partials);
-    cudaFree(d_res0);
-    cudaFree(d_ratio);
-    cudaFree(d_done);
-    cudaFree(d_cycles);
-    cudaFree(d_mode);
-    cudaFree(d_nonzero);
-    cudaFree(d_offset);
-    cudaFree(d_check);
-    cudaFree(d_cheap);
-    cudaFree(d_prev);
-    cudaFree(d_contr);
-    cudaFree(d_ndone);
-    cudaFree(rsd);
-    cudaFree(d_tails);
-    cudaFree(d_maps);
-    cudaFree(d_err);
+        for (auto &l : v) dev_free(l.d);
+    for (auto &l : xfer) dev_free(l.d);
+    dev_free(outer.d);
+    dev_free(d_first);
+    dev_free(d_partials);
+    dev_free(d_res0);
+    dev_free(d_ratio);
+    dev_free(d_done);
+    dev_free(d_cycles);
+    dev_free(d_mode);
+    dev_free(d_nonzero);
+    dev_free(d_offset);
+    dev_free(d_check);
+    dev_free(d_cheap);
+    dev_free(d_prev);
+    dev_free(d_contr);
+    dev_free(d_ndone);
+    dev_free(rsd);
+    dev_free(d_tails);
+    dev_free(d_maps);
+    dev_free(d_err);
+    if (stream) cudaStreamSynchronize(stream);
+    probs.clear();
+    arena_destroy(arena);
 }
 
 }  // namespace pmg
@@ -617,6 +623,9 @@ int batch_create(Batch **out, int n, const int *dims, const double *const *meshe
     }
     std::unique_ptr<Batch> B(new (std::nothrow) Batch());
     if (!B) return PMG_ENOMEM;
+    B->arena = arena_create();
+    if (!B->arena) return PMG_ENOMEM;
+    ArenaScope scope(B->arena);
     B->n = n;
     B->inner = inner > 0 ? inner : 2;
     PMG_TRY_B(cuda_status(cudaStreamCreateWithFlags(&B->stream, cudaStreamNonBlocking), "batch stream"));
@@ -677,6 +686,7 @@ int batch_create(Batch **out, int n, const int *dims, const double *const *meshe
         if (!c) return PMG_ENOMEM;
         c->autotune = false;
         c->deep_tail = false;   // the batch runs every depth above the coarsest on its grid launches
+        c->light = true;
         PMG_TRY_B(c->build(&cfg, B->stream));
         PMG_TRY_B(c->setup_mixed());
         B->dmax = std::max(B->dmax, c->nl);

@@ -114,9 +114,12 @@ struct Ctx {
     // adjoint scratch (finest level)
     double *adj_rhs = nullptr, *adj_sol = nullptr, *adj_rsd = nullptr, *adj_vol = nullptr, *adj_faces = nullptr;
 
+    // a member of a batch: no events, copy stream or abort flag of its own (set before build)
+    bool light = false;
     // subdomain of a decomposed solve: the level sizes and meshes to use (set before build)
     const std::vector<Level> *preset_levels = nullptr;
     int build(const pmg_config_t *c, cudaStream_t s);
+    int setup_tables();
     ~Ctx();
 
     int dot(int l, const double *x, const double *y, int slot);

@@ -131,10 +131,10 @@ struct Dd {
     ~Dd()
     {
         if (stream) cudaStreamSynchronize(stream);
-        for (auto v : sol) cudaFree(v);
-        for (auto v : rsd) cudaFree(v);
-        for (auto v : rhs) cudaFree(v);
-        for (auto v : halo) cudaFree(v);
+        for (auto v : sol) dev_free(v);
+        for (auto v : rsd) dev_free(v);
+        for (auto v : rhs) dev_free(v);
+        for (auto v : halo) dev_free(v);
     }
     int rank(int cx, int cy, int cz) const { return cx + p[0] * (cy + p[1] * cz); }
 };

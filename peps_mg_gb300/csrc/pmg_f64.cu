@@ -7,6 +7,7 @@
 // column (the CGPSA per-axis step-down), without changing any cell's arithmetic.
 #include <cuda_runtime.h>
 
+#include "../../include/peps_mg.h"
 #include "pmg_internal.h"
 #include "pmg_tail64.cuh"
 
@@ -338,6 +339,86 @@ __global__ void __launch_bounds__(kTailThreads) k_tail_f64(const TailDesc<double
     }
 }
 
+// ------------------------------------------------------------------------------------
+// Device-side hierarchy set-up (multigrid_subdomain_create_*, src/multigrid.f90:167-495,
+// and matrix_heptadiagonal_create, src/matrix.f90:39-94): one CTA per axis builds the
+// meshes of every coarse level from the finer one (unless the meshes are given), then the
+// per-axis coefficient tables of every level and the transfer weights between levels, in
+// the host layout described by HierDesc.  Same expressions, same rounding as the host code
+// (this translation unit is compiled without FMA contraction).
+// ------------------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) k_hierarchy(const HierDesc *__restrict__ Hp, double *__restrict__ meshes,
+                                                   double *__restrict__ tables)
+{
+    const HierDesc &H = *Hp;
+    const int d = blockIdx.x;
+    const int nl = H.nl;
+    // coarse meshes
+    if (!H.meshes_given)
+        for (int l = 1; l <= nl; ++l) {
+            const int n = H.n[l][d], nf = H.n[l - 1][d];
+            double *dm = meshes + H.mesh_off[l][d], *dg = dm + (n + 2), *xg = dg + (n + 2);
+            const double *dmf = meshes + H.mesh_off[l - 1][d], *dgf = dmf + (nf + 2), *xgf = dgf + (nf + 2);
+            if (l <= H.lvc[d]) {
+                for (int i = threadIdx.x + 1; i <= n; i += blockDim.x) dm[i] = dmf[2 * i - 1] + dmf[2 * i];
+                if (threadIdx.x == 0) {
+                    dm[0] = dmf[0];
+                    dm[n + 1] = dmf[2 * n + 1];
+                }
+                __syncthreads();
+                for (int i = threadIdx.x + 1; i <= n + 1; i += blockDim.x) dg[i] = 0.5 * (dm[i] + dm[i - 1]);
+                __syncthreads();
+                if (threadIdx.x == 0) {
+                    const bool from_origin = H.method == PMG_CGS || (H.method == PMG_CGA && l <= H.agg_level);
+                    xg[0] = from_origin ? H.ox[d] - 0.5 * dm[0] : (xgf[0] + 0.5 * dmf[0]) - 0.5 * dm[0];
+                    dg[0] = 0.0;
+                    for (int i = 1; i <= n + 1; ++i) xg[i] = xg[i - 1] + dg[i];
+                }
+            } else {
+                for (int i = threadIdx.x; i <= n + 1; i += blockDim.x) {
+                    dm[i] = dmf[i];
+                    dg[i] = dgf[i];
+                    xg[i] = xgf[i];
+                }
+            }
+            __syncthreads();
+        }
+    // coefficient tables (src/matrix.f90:75-82) and transfer weights
+    for (int l = 0; l <= nl; ++l) {
+        const int n = H.n[l][d];
+        const double *dm = meshes + H.mesh_off[l][d], *dg = dm + (n + 2);
+        double *cm = tables + H.cm[l][d], *cp = tables + H.cp[l][d];
+        double *sx = d == 0 ? tables + H.sx[l] : nullptr;
+        for (int i = threadIdx.x + 1; i <= n; i += blockDim.x) {
+            const double a = __ddiv_rn(1.0, __dmul_rn(dm[i], dg[i]));
+            const double b = __ddiv_rn(1.0, __dmul_rn(dm[i], dg[i + 1]));
+            cm[i] = a;
+            cp[i] = b;
+            if (sx) sx[i] = __dadd_rn(a, b);
+        }
+        if (l == nl) break;
+        const int nc = H.n[l + 1][d];
+        const double *dmc = meshes + H.mesh_off[l + 1][d];
+        double *w = tables + H.w[l][d], *pp = tables + H.pp[l][d], *pn = tables + H.pn[l][d];
+        if (l >= H.lvc[d]) {   // the axis is no longer coarsened: stride 1 (src/multigrid.f90:1415-1458)
+            for (int i = threadIdx.x; i <= n + 1; i += blockDim.x) {
+                w[i] = dm[i];
+                pp[i] = dmc[i];
+                pn[i] = dmc[i];
+            }
+        } else {
+            for (int i = threadIdx.x + 1; i <= n; i += blockDim.x) w[i] = __dsub_rn(dmc[(i - 1) / 2 + 1], dm[i]);
+            for (int i = threadIdx.x + 1; i <= nc; i += blockDim.x) {   // src/multigrid.f90:1604-1610
+                const int f = 2 * i;
+                pp[f - 1] = __dadd_rn(__dmul_rn(1.0, dm[f - 2]), __dmul_rn(0.5, dm[f - 1]));
+                pp[f] = __dmul_rn(0.5, dm[f - 1]);
+                pn[f - 1] = __dmul_rn(0.5, dm[f]);
+                pn[f] = __dadd_rn(__dmul_rn(1.0, dm[f + 1]), __dmul_rn(0.5, dm[f]));
+            }
+        }
+    }
+}
+
 dim3 grid3(int nx_threads, int ny, int nz, const Launch &ln)
 {
     dim3 g;
@@ -446,6 +527,13 @@ int zero_ghosts_f64(double *a, int nx, int ny, int nz, cudaStream_t s)
     k_zero_ghosts_f64<<<(unsigned)blocks, 256, 0, s>>>(a, nx, ny, nz);
     count_launches(1);
     return cuda_status(cudaGetLastError(), "zero ghosts");
+}
+
+int hierarchy_setup(const HierDesc *dev_desc, double *meshes, double *tables, cudaStream_t s)
+{
+    k_hierarchy<<<3, 256, 0, s>>>(dev_desc, meshes, tables);
+    count_launches(1);
+    return cuda_status(cudaGetLastError(), "hierarchy set-up");
 }
 
 int f64_tail(const TailDesc<double> *dev_desc, int threads, cudaStream_t s)

@@ -46,7 +46,24 @@ struct TailDesc {
     const volatile int *abort;
 };
 
+// Layout of a hierarchy built on the device (pmg_f64.cu): level sizes and, per level and
+// axis, the offsets (in doubles) of the mesh (dm, dg, xg, n+2 values each, consecutive) in
+// the mesh blob and of the coefficient tables / transfer weights in the table blob.
+struct HierDesc {
+    int nl;
+    int method, agg_level;
+    int meshes_given;           // 1: every level's mesh is in the blob already
+    int lvc[3];
+    double ox[3];
+    int n[kMaxLevels][3];
+    long long mesh_off[kMaxLevels][3];
+    long long cm[kMaxLevels][3], cp[kMaxLevels][3], sx[kMaxLevels];
+    long long w[kMaxLevels][3], pp[kMaxLevels][3], pn[kMaxLevels][3];
+};
+
 // ---- FP64 (bitwise) launchers, pmg_f64.cu -------------------------------------
+// Builds the coarse meshes (unless given) and every level's tables on the device.
+int hierarchy_setup(const HierDesc *dev_desc, double *meshes, double *tables, cudaStream_t s);
 int f64_rbgs_sweeps(const LevelK<double> &L, const Launch &ln, double *x, const double *b, int iters,
                     double omega, cudaStream_t s);
 // One half-sweep: the cells with (i + j + k + colour) odd, i.e. ista = 1 + mod(j+k+colour, 2)
@@ -203,6 +220,24 @@ inline cudaError_t dev_malloc(T **p, size_t bytes)
 {
     return dev_malloc_bytes(reinterpret_cast<void **>(p), bytes);
 }
+// Releases what dev_malloc returned: cudaFree, except for memory of a device arena (which
+// frees its chunks when it is destroyed).  nullptr is accepted.
+cudaError_t dev_free(void *p);
+
+// A device arena: a bump allocator over large device chunks (256 MiB, or the request when
+// larger; 256-byte aligned pieces).  While an ArenaScope is alive on a thread, every
+// dev_malloc of that thread takes its memory from the scope's arena, so building many
+// small hierarchies (a batch's problems) costs a few cudaMalloc calls instead of thousands.
+struct DevArena;
+DevArena *arena_create();
+void arena_destroy(DevArena *a);
+struct ArenaScope {
+    explicit ArenaScope(DevArena *a);
+    ~ArenaScope();
+    ArenaScope(const ArenaScope &) = delete;
+    ArenaScope &operator=(const ArenaScope &) = delete;
+    DevArena *prev;
+};
 
 // ---- tracing ----------------------------------------------------------------------
 // An NVTX range over a scope: the solve, its cycles and their phases appear by name in

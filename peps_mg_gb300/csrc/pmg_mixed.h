@@ -46,12 +46,12 @@ struct MixedState {
     double vgraph_omega = 0.0;
     ~MixedState()
     {
-        cudaFree(tables);
-        cudaFree(diag64);
-        cudaFree(split);
-        for (auto p : alloc) cudaFree(p);
-        cudaFree(d_tail);
-        cudaFree(d_err);
+        dev_free(tables);
+        dev_free(diag64);
+        dev_free(split);
+        for (auto p : alloc) dev_free(p);
+        dev_free(d_tail);
+        dev_free(d_err);
         for (auto &g : vgraph)
             if (g) cudaGraphExecDestroy(g);
         if (cap_stream) cudaStreamDestroy(cap_stream);
