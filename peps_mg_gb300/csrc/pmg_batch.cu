@@ -64,7 +64,9 @@ struct BOuter {
 };
 
 struct Item {
-    int p, bx, by, k0;     // problem, tile, first plane (smoother) or plane (others)
+    // problem and: smoother -- tile (bx, by), first plane k0; transfers -- column block bx,
+    // first coarse plane k0; outer kernels -- rows bx .. by of plane k0
+    int p, bx, by, k0;
 };
 
 // ---- smoother ----------------------------------------------------------------------------
@@ -131,11 +133,16 @@ __global__ void __launch_bounds__(RbtShape<TY>::THREADS, rbt_min_ctas<TY>())
         omega, omw, err);
 }
 
-// ---- residual + restriction into depth d+1: one item per kXferPlanes coarse planes -------
-// (marching columns where every axis is halved, one thread per coarse cell otherwise)
-constexpr int kXferPlanes = 4;
+// ---- residual + restriction into depth d+1, prolongation + correction back ----------------
+// An item is (problem, block of NTB consecutive columns, chunk of kXferPlanes coarse
+// planes): a column is one thread's marching column (a coarse column of the
+// residual-restriction, a fine x-pair column of the prolongation) or, where an axis is no
+// longer halved, one coarse cell per plane.  Items of equal size keep the CTAs of a launch
+// equally busy whatever the problems' sizes (items of whole planes left the CTAs holding the
+// largest problems' planes running long after the others).
+constexpr int kXferPlanes = 8;
 
-__global__ void __launch_bounds__(NTB) k_batch_resrestrict(const BLevel *__restrict__ lvd,
+__global__ void __launch_bounds__(NTB, 3) k_batch_resrestrict(const BLevel *__restrict__ lvd,
                                                            const BLevel *__restrict__ lvc, const Item *__restrict__ items,
                                                            int nitems, int which, const int *__restrict__ done)
 {
@@ -148,21 +155,18 @@ __global__ void __launch_bounds__(NTB) k_batch_resrestrict(const BLevel *__restr
         const float *e = D.e[which];
         float *bc = lvc[w.p].b;
         const int m0 = w.k0, m1 = min(X.ncz, w.k0 + kXferPlanes - 1);
+        const int q = w.bx * NTB + threadIdx.x;
+        if (q >= X.ncx * X.ncy) continue;
+        const int i = q % X.ncx + 1, j = q / X.ncx + 1;
         if (X.stx == 2 && X.sty == 2 && X.stz == 2) {
-            for (int q = threadIdx.x; q < X.ncx * X.ncy; q += NTB)
-                resrestrict_column_march32(L, X, q % X.ncx + 1, q / X.ncx + 1, m0, m1, e, D.b, bc);
+            resrestrict_column_march32(L, X, i, j, m0, m1, e, D.b, bc);
         } else {
-            for (int k = m0; k <= m1; ++k)
-                for (int q = threadIdx.x; q < X.ncx * X.ncy; q += NTB) {
-                    const int i = q % X.ncx + 1, j = q / X.ncx + 1;
-                    bc[lin(i, j, k, X.csy, X.csz)] = resrestrict_cell32(L, X, e, D.b, i, j, k);
-                }
+            for (int k = m0; k <= m1; ++k) bc[lin(i, j, k, X.csy, X.csz)] = resrestrict_cell32(L, X, e, D.b, i, j, k);
         }
     }
 }
 
-// ---- prolongation + correction from depth d+1 into depth d ---------------------------------
-__global__ void __launch_bounds__(NTB) k_batch_prolong(const BLevel *__restrict__ lvd, const BLevel *__restrict__ lvc,
+__global__ void __launch_bounds__(NTB, 3) k_batch_prolong(const BLevel *__restrict__ lvd, const BLevel *__restrict__ lvc,
                                                        const Item *__restrict__ items, int nitems, int which,
                                                        int which_c, int d, const int *__restrict__ done)
 {
@@ -175,17 +179,15 @@ __global__ void __launch_bounds__(NTB) k_batch_prolong(const BLevel *__restrict_
         const float *ec = (d + 1 == D.nl) ? lvc[w.p].e[0] : lvc[w.p].e[which_c];
         float *e = D.e[which];
         const int m0 = w.k0, m1 = min(X.ncz, w.k0 + kXferPlanes - 1);
+        const int q = w.bx * NTB + threadIdx.x;
         if (X.stx == 2 && X.stz == 2) {
             // one thread per fine x-pair column of the item's planes
-            const int nfy = D.L.ny;
-            for (int q = threadIdx.x; q < X.ncx * nfy; q += NTB)
-                prolong_column_march32(X, q / X.ncx + 1, q % X.ncx + 1, m0, m1, ec, e);
+            if (q >= X.ncx * D.L.ny) continue;
+            prolong_column_march32(X, q / X.ncx + 1, q % X.ncx + 1, m0, m1, ec, e);
         } else {
-            for (int k = m0; k <= m1; ++k)
-                for (int q = threadIdx.x; q < X.ncx * X.ncy; q += NTB) {
-                    const int i = q % X.ncx + 1, j = q / X.ncx + 1;
-                    prolong_add_cell32(X, ec, e, i, j, k);
-                }
+            if (q >= X.ncx * X.ncy) continue;
+            const int i = q % X.ncx + 1, j = q / X.ncx + 1;
+            for (int k = m0; k <= m1; ++k) prolong_add_cell32(X, ec, e, i, j, k);
         }
     }
 }
@@ -211,104 +213,137 @@ __global__ void __launch_bounds__(NTB) k_batch_nonzero(const double *__restrict_
     if (__syncthreads_or(bits != 0ull) && threadIdx.x == 0) atomicOr(nonzero + p, 1);
 }
 
+// An outer item is a set of fine rows of one problem: rows j0 .. j1 of planes k0 .. k1
+// (whole planes of small problems, row blocks of large ones), about kOuterCells cells, so
+// the per-item set-up (descriptor loads) is spread over enough cells and the items of a
+// launch are of about equal size.  Warp w takes the item's rows w, w + 8, ... (in plane-
+// major order); lane l the cells i = 1 + l + 32 u of a row.  Each warp leaves its partial
+// norm in partials[item * kOuterWarps + w] (no block barrier); the norm kernels sum a
+// problem's partials in that order.
+constexpr int kOuterWarps = NTB / 32;
+constexpr int kOuterCells = 8192;
+
+struct OItem {
+    int p, j0, j1, k0, k1;
+};
+
+__device__ __forceinline__ double warp_sum_outer(double v)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = v + __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
 // check (NULL: every problem): the problems whose residual is recomputed.  nonzero
 // (non-NULL for the first residual of a solve): where a problem's initial guess is zero,
 // every product of the FMA chain is a signed zero and the chain returns b + 0.
-__global__ void __launch_bounds__(NTB) k_batch_outer_residual(const BOuter *__restrict__ po,
-                                                              const Item *__restrict__ items, int nitems,
-                                                              double *__restrict__ partials,
-                                                              const int *__restrict__ done,
-                                                              const int *__restrict__ check,
-                                                              const int *__restrict__ nonzero)
+__global__ void __launch_bounds__(NTB, 4) k_batch_outer_residual(const BOuter *__restrict__ po,
+                                                                 const OItem *__restrict__ items, int nitems,
+                                                                 double *__restrict__ partials,
+                                                                 const int *__restrict__ done,
+                                                                 const int *__restrict__ check,
+                                                                 const int *__restrict__ nonzero)
 {
-    __shared__ double sw[NTB / 32];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     for (int it = blockIdx.x; it < nitems; it += gridDim.x) {
-        const Item w = items[it];
+        const OItem w = items[it];
         if (done[w.p] || (check && !check[w.p])) continue;       // uniform over the block
         const BOuter &O = po[w.p];
         const LevelK<double> L = O.L;
-        const int k = w.k0;
-        const double dz = O.dzz[k];
+        const double *__restrict__ x = O.sol;
+        const double *__restrict__ b = O.rhs;
+        double *__restrict__ r = O.rsd;
+        float *__restrict__ r32 = O.r32;
+        const bool zero_x = nonzero && !nonzero[w.p];
+        const int nrow = w.j1 - w.j0 + 1, rows = nrow * (w.k1 - w.k0 + 1);
         double acc = 0.0;
-        if (nonzero && !nonzero[w.p]) {
-            for (int q = threadIdx.x; q < L.nx * L.ny; q += NTB) {
-                const int i = q % L.nx + 1, j = q / L.nx + 1;
-                const long long p = lin(i, j, k, L.sy, L.sz);
-                const double v = plus_zero(O.rhs[p]);
-                O.rsd[p] = v;
-                O.r32[lin(i, j, k, O.sy32, O.sz32)] = f64_to_f32_rn(v);
+        for (int t = wid; t < rows; t += kOuterWarps) {
+            const int j = w.j0 + t % nrow, k = w.k0 + t / nrow;
+            const long long row = lin(0, j, k, L.sy, L.sz), row32 = lin(0, j, k, O.sy32, O.sz32);
+            if (zero_x) {
+                for (int i = 1 + lane; i <= L.nx; i += 32) {
+                    const double v = plus_zero(b[row + i]);
+                    r[row + i] = v;
+                    r32[row32 + i] = f64_to_f32_rn(v);
+                    acc = fma(v, v, acc);
+                }
+                continue;
+            }
+            const double dyz = O.dyy[j] + O.dzz[k];
+            for (int i = 1 + lane; i <= L.nx; i += 32) {
+                const double v = outer_residual_cell(L, dyz, x, b, i, j, k, row + i);
+                r[row + i] = v;
+                r32[row32 + i] = f64_to_f32_rn(v);
                 acc = fma(v, v, acc);
             }
-            const double s = block_sum(acc, sw);
-            if (threadIdx.x == 0) partials[it] = s;
-            continue;
         }
-        for (int q = threadIdx.x; q < L.nx * L.ny; q += NTB) {
-            const int i = q % L.nx + 1, j = q / L.nx + 1;
-            const long long p = lin(i, j, k, L.sy, L.sz);
-            const double v = outer_residual_cell(L, O.dyy[j] + dz, O.sol, O.rhs, i, j, k, p);
-            O.rsd[p] = v;
-            O.r32[lin(i, j, k, O.sy32, O.sz32)] = f64_to_f32_rn(v);
-            acc = fma(v, v, acc);
-        }
-        const double s = block_sum(acc, sw);
-        if (threadIdx.x == 0) partials[it] = s;
+        acc = warp_sum_outer(acc);
+        if (lane == 0) partials[(long long)it * kOuterWarps + wid] = acc;
     }
 }
 
-// After the V-cycles of a correction, per fine plane: x += e, and for problems in update
+// After the V-cycles of a correction, per outer item: x += e, and for problems in update
 // mode (mode 0) also r -= A e with A e in compensated FP32 arithmetic (comp_term), the
-// FP32 copy of r and the plane's partial norm (FP32 sum of the squares scaled by a power
-// of two set by the problem's initial residual; it only decides whether the residual is
+// FP32 copy of r and the warps' partial norms (FP32 sums of the squares scaled by a power
+// of two set by the problem's initial residual; they only decide whether the residual is
 // recomputed).  Problems in mode 1 get the FP64 residual recomputed after this.
-__global__ void __launch_bounds__(NTB) k_batch_correct(const BOuter *__restrict__ po, const Item *__restrict__ items,
-                                                       int nitems, double *__restrict__ partials,
-                                                       const int *__restrict__ done, const int *__restrict__ mode,
-                                                       const double *__restrict__ res0)
+__global__ void __launch_bounds__(NTB, 4) k_batch_correct(const BOuter *__restrict__ po,
+                                                          const OItem *__restrict__ items, int nitems,
+                                                          double *__restrict__ partials,
+                                                          const int *__restrict__ done, const int *__restrict__ mode,
+                                                          const double *__restrict__ res0)
 {
-    __shared__ double sw[NTB / 32];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     for (int it = blockIdx.x; it < nitems; it += gridDim.x) {
-        const Item w = items[it];
+        const OItem w = items[it];
         if (done[w.p]) continue;
         const BOuter &O = po[w.p];
         const LevelK<double> L = O.L;
-        const int k = w.k0;
+        double *__restrict__ x = O.sol;
+        const float *__restrict__ e = O.e0;
+        const int sy32 = O.sy32;
+        const long long sz32 = O.sz32;
+        const int nrow = w.j1 - w.j0 + 1, rows = nrow * (w.k1 - w.k0 + 1);
         if (mode[w.p]) {
-            for (int q = threadIdx.x; q < L.nx * L.ny; q += NTB) {
-                const int i = q % L.nx + 1, j = q / L.nx + 1;
-                const long long p = lin(i, j, k, L.sy, L.sz);
-                O.sol[p] = O.sol[p] + f32_to_f64(O.e0[lin(i, j, k, O.sy32, O.sz32)]);
+            for (int t = wid; t < rows; t += kOuterWarps) {
+                const int j = w.j0 + t % nrow, k = w.k0 + t / nrow;
+                const long long row = lin(0, j, k, L.sy, L.sz), row32 = lin(0, j, k, sy32, sz32);
+                for (int i = 1 + lane; i <= L.nx; i += 32) x[row + i] = x[row + i] + f32_to_f64(e[row32 + i]);
             }
             continue;
         }
+        double *__restrict__ r = O.rsd;
+        float *__restrict__ r32 = O.r32;
         const double rms0 = sqrt(res0[w.p] / ((double)L.nx * L.ny * L.nz));
         const int ex = rms0 > 0.0 && rms0 < 1e300 ? max(-100, min(100, ilogb(rms0))) : 0;
         const float nscale = ldexpf(1.0f, -ex);
         const SplitCoef C = O.sc;
-        const float2 czm = C.czm[k], czp = C.czp[k];
-        const float *e = O.e0;
         float acc32 = 0.f;
-        for (int q = threadIdx.x; q < L.nx * L.ny; q += NTB) {
-            const int i = q % L.nx + 1, j = q / L.nx + 1;
-            const long long p = lin(i, j, k, L.sy, L.sz), c = lin(i, j, k, O.sy32, O.sz32);
-            const float ec = e[c];
-            float S = 0.f, Sl = 0.f;
-            comp_term(C.cxm[i], e[c - 1], ec, S, Sl);
-            comp_term(C.cxp[i], e[c + 1], ec, S, Sl);
-            comp_term(C.cym[j], e[c - O.sy32], ec, S, Sl);
-            comp_term(C.cyp[j], e[c + O.sy32], ec, S, Sl);
-            comp_term(czm, e[c - O.sz32], ec, S, Sl);
-            comp_term(czp, e[c + O.sz32], ec, S, Sl);
-            O.sol[p] = O.sol[p] + f32_to_f64(ec);
-            const double v = __dsub_rn(__dsub_rn(O.rsd[p], f32_to_f64_fast(S)), f32_to_f64_fast(Sl));
-            O.rsd[p] = v;
-            const float v32 = f64_to_f32_rn(v);
-            O.r32[c] = v32;
-            const float wv = v32 * nscale;
-            acc32 = fmaf(wv, wv, acc32);
+        for (int t = wid; t < rows; t += kOuterWarps) {
+            const int j = w.j0 + t % nrow, k = w.k0 + t / nrow;
+            const long long row = lin(0, j, k, L.sy, L.sz), row32 = lin(0, j, k, sy32, sz32);
+            const float2 cym = C.cym[j], cyp = C.cyp[j], czm = C.czm[k], czp = C.czp[k];
+            for (int i = 1 + lane; i <= L.nx; i += 32) {
+                const long long c = row32 + i;
+                const float ec = e[c];
+                float S = 0.f, Sl = 0.f;
+                comp_term(C.cxm[i], e[c - 1], ec, S, Sl);
+                comp_term(C.cxp[i], e[c + 1], ec, S, Sl);
+                comp_term(cym, e[c - sy32], ec, S, Sl);
+                comp_term(cyp, e[c + sy32], ec, S, Sl);
+                comp_term(czm, e[c - sz32], ec, S, Sl);
+                comp_term(czp, e[c + sz32], ec, S, Sl);
+                x[row + i] = x[row + i] + f32_to_f64(ec);
+                const double v = __dsub_rn(__dsub_rn(r[row + i], f32_to_f64_fast(S)), f32_to_f64_fast(Sl));
+                r[row + i] = v;
+                const float v32 = f64_to_f32_rn(v);
+                r32[c] = v32;
+                const float wv = v32 * nscale;
+                acc32 = fmaf(wv, wv, acc32);
+            }
         }
-        const double s = block_sum((double)acc32 / ((double)nscale * (double)nscale), sw);
-        if (threadIdx.x == 0) partials[it] = s;
+        const double s = warp_sum_outer((double)acc32 / ((double)nscale * (double)nscale));
+        if (lane == 0) partials[(long long)it * kOuterWarps + wid] = s;
     }
 }
 
@@ -407,9 +442,13 @@ struct Batch {
         int n = 0;
     };
     std::vector<List> smooth[3];            // [variant][depth]
-    std::vector<List> xfer;                 // [depth]: coarse planes of depth+1 for problems with nl > depth
-    List outer;                             // fine planes
-    std::vector<int> first_item;            // per problem range in `outer`
+    std::vector<List> xfer_rr, xfer_pr;     // [depth]: items of the residual-restriction into depth+1 and
+                                            // of the prolongation back (problems with nl > depth)
+    struct OList {
+        OItem *d = nullptr;
+        int n = 0;
+    } outer;                                // row sets of the finest level
+    std::vector<int> first_item;            // per problem range of the outer partials (kOuterWarps per item)
     int *d_first = nullptr;
     double *d_partials = nullptr, *d_res0 = nullptr, *d_ratio = nullptr;
     int *d_done = nullptr, *d_cycles = nullptr, *d_ndone = nullptr;
@@ -446,7 +485,8 @@ Batch::~Batch()
     dev_free(d_outer);
     for (auto &v : smooth)
         for (auto &l : v) dev_free(l.d);
-    for (auto &l : xfer) dev_free(l.d);
+    for (auto &l : xfer_rr) dev_free(l.d);
+    for (auto &l : xfer_pr) dev_free(l.d);
     dev_free(outer.d);
     dev_free(d_first);
     dev_free(d_partials);
@@ -750,30 +790,52 @@ int batch_create(Batch **out, int n, const int *dims, const double *const *meshe
             PMG_TRY_B(upload(it, &B->smooth[v][d].d));
         }
     }
-    B->xfer.resize((size_t)D);
+    B->xfer_rr.resize((size_t)D);
+    B->xfer_pr.resize((size_t)D);
     for (int d = 0; d < D; ++d) {
-        std::vector<Item> it;
+        std::vector<Item> rr, pr;
         for (int p = 0; p < n; ++p) {
             if (B->probs[p]->nl <= d) continue;
-            const int ncz = lv[(size_t)(d + 1) * n + p].L.nz;
-            for (int k = 1; k <= ncz; k += kXferPlanes) it.push_back({p, 0, 0, k});
+            const XferK<float> &X = lv[(size_t)d * n + p].X;
+            const int nfy = lv[(size_t)d * n + p].L.ny;
+            const int crr = X.ncx * X.ncy;
+            const int cpr = (X.stx == 2 && X.stz == 2) ? X.ncx * nfy : X.ncx * X.ncy;
+            for (int k = 1; k <= X.ncz; k += kXferPlanes) {
+                for (int c = 0; c * NTB < crr; ++c) rr.push_back({p, c, 0, k});
+                for (int c = 0; c * NTB < cpr; ++c) pr.push_back({p, c, 0, k});
+            }
         }
-        B->xfer[d].n = (int)it.size();
-        PMG_TRY_B(upload(it, &B->xfer[d].d));
+        B->xfer_rr[d].n = (int)rr.size();
+        B->xfer_pr[d].n = (int)pr.size();
+        PMG_TRY_B(upload(rr, &B->xfer_rr[d].d));
+        PMG_TRY_B(upload(pr, &B->xfer_pr[d].d));
     }
     {
-        std::vector<Item> it;
+        // outer items: whole planes (up to kOuterCells cells together) or row blocks of a
+        // plane (multiples of kOuterWarps rows), in plane order per problem
+        std::vector<OItem> it;
         B->first_item.assign((size_t)n + 1, 0);
         for (int p = 0; p < n; ++p) {
-            B->first_item[p] = (int)it.size();
-            for (int k = 1; k <= B->probs[p]->lv[0].n[2]; ++k) it.push_back({p, 0, 0, k});
+            B->first_item[p] = (int)it.size() * kOuterWarps;
+            const int *nn = B->probs[p]->lv[0].n;
+            const long long plane = (long long)nn[0] * nn[1];
+            if (plane >= kOuterCells) {
+                int rows = (kOuterCells + nn[0] - 1) / nn[0];
+                rows = (rows + kOuterWarps - 1) / kOuterWarps * kOuterWarps;
+                for (int k = 1; k <= nn[2]; ++k)
+                    for (int j0 = 1; j0 <= nn[1]; j0 += rows) it.push_back({p, j0, std::min(nn[1], j0 + rows - 1), k, k});
+            } else {
+                const int planes = (int)(kOuterCells / plane);
+                for (int k0 = 1; k0 <= nn[2]; k0 += planes) it.push_back({p, 1, nn[1], k0, std::min(nn[2], k0 + planes - 1)});
+            }
         }
-        B->first_item[n] = (int)it.size();
+        B->first_item[n] = (int)it.size() * kOuterWarps;
         B->outer.n = (int)it.size();
         PMG_TRY_B(upload(it, &B->outer.d));
         PMG_TRY_B(upload(B->first_item, &B->d_first));
     }
-    PMG_TRY_B(cuda_status(dev_malloc(&B->d_partials, (size_t)B->outer.n * sizeof(double)), "batch allocation"));
+    PMG_TRY_B(cuda_status(dev_malloc(&B->d_partials, (size_t)B->outer.n * kOuterWarps * sizeof(double)),
+                          "batch allocation"));
     PMG_TRY_B(cuda_status(dev_malloc(&B->d_res0, n * sizeof(double)), "batch allocation"));
     PMG_TRY_B(cuda_status(dev_malloc(&B->d_ratio, n * sizeof(double)), "batch allocation"));
     PMG_TRY_B(cuda_status(dev_malloc(&B->d_done, n * sizeof(int)), "batch allocation"));
@@ -852,7 +914,7 @@ static void batch_vcycle(Batch &B, int maxit, float om, float omw, bool zero_sta
     };
     for (int d = 0; d < D; ++d) {
         smooth(d, d > 0 || zero_start);
-        const Batch::List &X = B.xfer[d];
+        const Batch::List &X = B.xfer_rr[d];
         if (X.n) {
             k_batch_resrestrict<<<grid_for(X.n), NTB, 0, B.stream>>>(B.d_lv + (size_t)d * n, B.d_lv + (size_t)(d + 1) * n,
                                                                      X.d, X.n, par[d], B.d_done);
@@ -861,7 +923,7 @@ static void batch_vcycle(Batch &B, int maxit, float om, float omw, bool zero_sta
     }
     batch_tail32(B.d_tails, n, B.d_done, B.tail_threads, B.stream);
     for (int d = D - 1; d >= 0; --d) {
-        const Batch::List &X = B.xfer[d];
+        const Batch::List &X = B.xfer_pr[d];
         if (X.n) {
             k_batch_prolong<<<grid_for(X.n), NTB, 0, B.stream>>>(B.d_lv + (size_t)d * n, B.d_lv + (size_t)(d + 1) * n,
                                                                  X.d, X.n, par[d], par[d + 1], d, B.d_done);
