@@ -17,6 +17,8 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <memory>
 #include <new>
@@ -39,6 +41,7 @@ namespace pmg {
 namespace {
 
 constexpr int NTB = 256;
+constexpr int kVariants = 7;   // smoother variants: register-window TY 14/6/10, TMA-fed TY 14/6/10/22
 
 // per (depth, problem) descriptor
 struct BLevel {
@@ -65,7 +68,7 @@ struct BOuter {
 
 struct Item {
     // problem and: smoother -- tile (bx, by), first plane k0; transfers -- column block bx,
-    // first coarse plane k0; outer kernels -- rows bx .. by of plane k0
+    // chunk of by coarse planes from k0
     int p, bx, by, k0;
 };
 
@@ -90,57 +93,64 @@ __global__ void __launch_bounds__(rb_threads<TY>()) k_batch_rb32(const BLevel *_
 // Item source of the TMA-fed smoother for one depth: the CTA's items of unconverged
 // problems in list order, each item's planes from its problem's k-chunk and the tensor
 // maps of its problem (buffer `which` of e as input, tile variant vi).
-struct BatchTmaSrc {
+struct BatchTmaArgs {
     const BLevel *lv;
     const Rb32Tma *maps;
     const Item *items;
     const int *done;
     int nitems, which, vi;
+};
+
+// Reads its fields through a pointer to the kernel parameter (the constant bank), so the
+// persistent CTA holds no registers for them across its items.
+struct BatchTmaSrc {
+    const BatchTmaArgs *A;
     __device__ __forceinline__ int skip(int it) const
     {
-        while (it < nitems && done[items[it].p]) it += gridDim.x;
+        while (it < A->nitems && A->done[A->items[it].p]) it += gridDim.x;
         return it;
     }
     __device__ __forceinline__ int first() const { return skip(blockIdx.x); }
     __device__ __forceinline__ int next(int it) const { return skip(it + gridDim.x); }
-    __device__ __forceinline__ bool valid(int it) const { return it < nitems; }
+    __device__ __forceinline__ bool valid(int it) const { return it < A->nitems; }
     __device__ __forceinline__ void geom(int it, int &bx, int &by, int &k0, int &k1) const
     {
-        const Item w = items[it];
+        const Item w = A->items[it];
         bx = w.bx;
         by = w.by;
         k0 = w.k0;
-        k1 = min(lv[w.p].L.nz, w.k0 + lv[w.p].kchunk - 1);
+        k1 = min(A->lv[w.p].L.nz, w.k0 + A->lv[w.p].kchunk - 1);
     }
-    __device__ __forceinline__ const CUtensorMap *map_e(int it) const { return &maps[items[it].p].e[which][vi]; }
-    __device__ __forceinline__ const CUtensorMap *map_b(int it) const { return &maps[items[it].p].b[vi]; }
+    __device__ __forceinline__ const CUtensorMap *map_e(int it) const
+    {
+        return &A->maps[A->items[it].p].e[A->which][A->vi];
+    }
+    __device__ __forceinline__ const CUtensorMap *map_b(int it) const { return &A->maps[A->items[it].p].b[A->vi]; }
     __device__ __forceinline__ bool stall() const { return false; }
 };
 
 template <int TY, bool ZERO_IN, bool OMEGA1>
 __global__ void __launch_bounds__(RbtShape<TY>::THREADS, rbt_min_ctas<TY>())
-    k_batch_rb32_tma(const BLevel *__restrict__ lv, const Rb32Tma *__restrict__ maps, const Item *__restrict__ items,
-                     int nitems, int which, int vi, float omega, float omw, const int *__restrict__ done, int *err)
+    k_batch_rb32_tma(const __grid_constant__ BatchTmaArgs A, float omega, float omw, int *err)
 {
-    const BatchTmaSrc src{lv, maps, items, done, nitems, which, vi};
+    const BatchTmaSrc src{&A};
     rbt_cta<TY, ZERO_IN, OMEGA1>(
         src,
         [&](int it, const LevelK<float> *&L, float *&eo) {
-            const BLevel &D = lv[items[it].p];
+            const BLevel &D = A.lv[A.items[it].p];
             L = &D.L;
-            eo = D.e[1 - which];
+            eo = D.e[1 - A.which];
         },
         omega, omw, err);
 }
 
 // ---- residual + restriction into depth d+1, prolongation + correction back ----------------
-// An item is (problem, block of NTB consecutive columns, chunk of kXferPlanes coarse
-// planes): a column is one thread's marching column (a coarse column of the
-// residual-restriction, a fine x-pair column of the prolongation) or, where an axis is no
-// longer halved, one coarse cell per plane.  Items of equal size keep the CTAs of a launch
-// equally busy whatever the problems' sizes (items of whole planes left the CTAs holding the
-// largest problems' planes running long after the others).
-constexpr int kXferPlanes = 8;
+// An item is (problem, block bx of NTB consecutive columns, chunk of `by` coarse planes
+// from k0): a column is one thread's marching column (a coarse column of the residual-
+// restriction, a fine x-pair column of the prolongation) or, where an axis is no longer
+// halved, one coarse cell per plane.  One chunk length per depth (set from the depth's
+// total work, like the single-grid kernels' chunks) gives items of equal size, which keep
+// the CTAs of a launch equally busy whatever the problems' sizes.
 
 __global__ void __launch_bounds__(NTB, 3) k_batch_resrestrict(const BLevel *__restrict__ lvd,
                                                            const BLevel *__restrict__ lvc, const Item *__restrict__ items,
@@ -154,7 +164,7 @@ __global__ void __launch_bounds__(NTB, 3) k_batch_resrestrict(const BLevel *__re
         const LevelK<float> L = D.L;
         const float *e = D.e[which];
         float *bc = lvc[w.p].b;
-        const int m0 = w.k0, m1 = min(X.ncz, w.k0 + kXferPlanes - 1);
+        const int m0 = w.k0, m1 = min(X.ncz, w.k0 + w.by - 1);
         const int q = w.bx * NTB + threadIdx.x;
         if (q >= X.ncx * X.ncy) continue;
         const int i = q % X.ncx + 1, j = q / X.ncx + 1;
@@ -178,7 +188,7 @@ __global__ void __launch_bounds__(NTB, 3) k_batch_prolong(const BLevel *__restri
         // the coarsest depth of a problem is solved in place in buffer 0
         const float *ec = (d + 1 == D.nl) ? lvc[w.p].e[0] : lvc[w.p].e[which_c];
         float *e = D.e[which];
-        const int m0 = w.k0, m1 = min(X.ncz, w.k0 + kXferPlanes - 1);
+        const int m0 = w.k0, m1 = min(X.ncz, w.k0 + w.by - 1);
         const int q = w.bx * NTB + threadIdx.x;
         if (X.stx == 2 && X.stz == 2) {
             // one thread per fine x-pair column of the item's planes
@@ -441,7 +451,7 @@ struct Batch {
         Item *d = nullptr;
         int n = 0;
     };
-    std::vector<List> smooth[3];            // [variant][depth]
+    std::vector<List> smooth;               // [depth]: (problem, tile, k-chunk) items of the chosen variant
     std::vector<List> xfer_rr, xfer_pr;     // [depth]: items of the residual-restriction into depth+1 and
                                             // of the prolongation back (problems with nl > depth)
     struct OList {
@@ -463,8 +473,9 @@ struct Batch {
     double *rsd = nullptr;                  // packed FP64 residual
     const TailDesc<float> **d_tails = nullptr;
     int tail_threads = 64;
-    std::vector<int> variant;               // chosen smoother variant per depth (3..5: TMA-fed)
-    int slots[6] = {0, 0, 0, 0, 0, 0};
+    std::vector<BLevel> h_lv;               // host copy of d_lv
+    std::vector<int> variant, kchunk;       // chosen smoother variant (kVariantTY) and k-chunk per depth
+    int slots[kVariants] = {};
     Rb32Tma *d_maps = nullptr;              // [(dmax+1) * n] tensor maps of every depth and problem
     std::vector<bool> tma_ok;               // per depth: every problem with that depth has maps
     int *d_err = nullptr;                   // set by a TMA-fed launch whose bounded wait gave up
@@ -483,8 +494,7 @@ Batch::~Batch()
     if (graph) cudaGraphExecDestroy(graph);
     dev_free(d_lv);
     dev_free(d_outer);
-    for (auto &v : smooth)
-        for (auto &l : v) dev_free(l.d);
+    for (auto &l : smooth) dev_free(l.d);
     for (auto &l : xfer_rr) dev_free(l.d);
     for (auto &l : xfer_pr) dev_free(l.d);
     dev_free(outer.d);
@@ -539,7 +549,7 @@ int upload(const std::vector<T> &h, T **d)
     return cuda_status(cudaMemcpy(*d, h.data(), h.size() * sizeof(T), cudaMemcpyHostToDevice), "batch upload");
 }
 
-constexpr int kTY[3] = {14, 6, 10};   // tile heights of the smoother variants (as pmg_smooth32.cu)
+constexpr int kVariantTY[kVariants] = {14, 6, 10, 14, 6, 10, 22};   // tile height of each smoother variant
 
 template <int TY>
 int setup_variant(int *slots)
@@ -593,18 +603,15 @@ void launch_batch_tma(const Batch &B, int d, const Batch::List &Ls, int slots, i
     const Rb32Tma *mp = B.d_maps + (size_t)d * B.n;
     const bool one = om == 1.f;
     constexpr int nt = RbtShape<TY>::THREADS, sm = RbtShape<TY>::SMEM;
+    const BatchTmaArgs A{lv, mp, Ls.d, B.d_done, Ls.n, which, vi};
     if (zs && one)
-        k_batch_rb32_tma<TY, true, true><<<grid, nt, sm, B.stream>>>(lv, mp, Ls.d, Ls.n, which, vi, om, omw, B.d_done,
-                                                                    B.d_err);
+        k_batch_rb32_tma<TY, true, true><<<grid, nt, sm, B.stream>>>(A, om, omw, B.d_err);
     else if (zs)
-        k_batch_rb32_tma<TY, true, false><<<grid, nt, sm, B.stream>>>(lv, mp, Ls.d, Ls.n, which, vi, om, omw,
-                                                                     B.d_done, B.d_err);
+        k_batch_rb32_tma<TY, true, false><<<grid, nt, sm, B.stream>>>(A, om, omw, B.d_err);
     else if (one)
-        k_batch_rb32_tma<TY, false, true><<<grid, nt, sm, B.stream>>>(lv, mp, Ls.d, Ls.n, which, vi, om, omw,
-                                                                     B.d_done, B.d_err);
+        k_batch_rb32_tma<TY, false, true><<<grid, nt, sm, B.stream>>>(A, om, omw, B.d_err);
     else
-        k_batch_rb32_tma<TY, false, false><<<grid, nt, sm, B.stream>>>(lv, mp, Ls.d, Ls.n, which, vi, om, omw,
-                                                                      B.d_done, B.d_err);
+        k_batch_rb32_tma<TY, false, false><<<grid, nt, sm, B.stream>>>(A, om, omw, B.d_err);
 }
 
 template <int TY>
@@ -624,29 +631,51 @@ void launch_batch_rb(const Batch &B, int d, const Batch::List &Ls, int slots, in
         k_batch_rb32<TY, false, false><<<grid, nt, 0, B.stream>>>(lv, Ls.d, Ls.n, which, om, omw, B.d_done);
 }
 
-// v = 0, 1, 2: register-window kernel with 60 x 14 / 6 / 10 tiles; 3, 4, 5: TMA-fed kernel
-// with the same tiles (and the same work lists).
-void launch_rb(const Batch &B, int v, int d, int which, float om, float omw, bool zs)
+// Smoother over the work list Ls of depth d with variant v: 0, 1, 2 the register-window
+// kernel with 60 x 14 / 6 / 10 tiles; 3, 4, 5, 6 the TMA-fed kernel with 60 x 14 / 6 / 10
+// / 22 tiles (tensor-map variant v - 3).
+void launch_rb(const Batch &B, int v, int d, const Batch::List &Ls, int which, float om, float omw, bool zs)
 {
-    const Batch::List &Ls = B.smooth[v % 3][d];
     if (!Ls.n) return;
-    if (v >= 3) {
-        if (v == 3)
-            launch_batch_tma<14>(B, d, Ls, B.slots[3], 0, which, om, omw, zs);
-        else if (v == 4)
-            launch_batch_tma<6>(B, d, Ls, B.slots[4], 1, which, om, omw, zs);
-        else
-            launch_batch_tma<10>(B, d, Ls, B.slots[5], 2, which, om, omw, zs);
-        count_launches(1);
-        return;
+    switch (v) {
+    case 0: launch_batch_rb<14>(B, d, Ls, B.slots[0], which, om, omw, zs); break;
+    case 1: launch_batch_rb<6>(B, d, Ls, B.slots[1], which, om, omw, zs); break;
+    case 2: launch_batch_rb<10>(B, d, Ls, B.slots[2], which, om, omw, zs); break;
+    case 3: launch_batch_tma<14>(B, d, Ls, B.slots[3], 0, which, om, omw, zs); break;
+    case 4: launch_batch_tma<6>(B, d, Ls, B.slots[4], 1, which, om, omw, zs); break;
+    case 5: launch_batch_tma<10>(B, d, Ls, B.slots[5], 2, which, om, omw, zs); break;
+    default: launch_batch_tma<22>(B, d, Ls, B.slots[6], 3, which, om, omw, zs); break;
     }
-    if (v == 0)
-        launch_batch_rb<14>(B, d, Ls, B.slots[0], which, om, omw, zs);
-    else if (v == 1)
-        launch_batch_rb<6>(B, d, Ls, B.slots[1], which, om, omw, zs);
-    else
-        launch_batch_rb<10>(B, d, Ls, B.slots[2], which, om, omw, zs);
     count_launches(1);
+}
+
+// The (problem, tile, k-chunk) items of depth d for tile height ty and k-chunk kc (each
+// problem's chunk is min(nz, kc)), every problem with a level below depth d.
+std::vector<Item> smooth_items(const Batch &B, int d, int ty, int kc)
+{
+    std::vector<Item> it;
+    for (int p = 0; p < B.n; ++p) {
+        if (B.probs[p]->nl <= d) continue;
+        const BLevel &x = B.h_lv[(size_t)d * B.n + p];
+        const int kch = std::min(x.L.nz, kc);
+        const int ntx = (x.L.nx + RB_TX - 1) / RB_TX, nty = (x.L.ny + ty - 1) / ty;
+        for (int k0 = 1; k0 <= x.L.nz; k0 += kch)
+            for (int by = 0; by < nty; ++by)
+                for (int bx = 0; bx < ntx; ++bx) it.push_back({p, bx, by, k0});
+    }
+    return it;
+}
+
+// Sets the k-chunk of depth d's descriptors (host and device copies) to min(nz, kc).
+int set_kchunk(Batch &B, int d, int kc)
+{
+    for (int p = 0; p < B.n; ++p) {
+        BLevel &x = B.h_lv[(size_t)d * B.n + p];
+        x.kchunk = std::min(x.L.nz, kc);
+    }
+    return cuda_status(cudaMemcpy(B.d_lv + (size_t)d * B.n, B.h_lv.data() + (size_t)d * B.n, B.n * sizeof(BLevel),
+                                  cudaMemcpyHostToDevice),
+                       "batch descriptors");
 }
 
 int grid_for(int items) { return std::max(1, std::min(items, 8 * 152)); }
@@ -773,37 +802,45 @@ int batch_create(Batch **out, int n, const int *dims, const double *const *meshe
         PMG_TRY_B(cuda_status(dev_malloc(&B->d_err, sizeof(int)), "batch allocation"));
         PMG_TRY_B(cuda_status(cudaMemset(B->d_err, 0, sizeof(int)), "batch init"));
     }
-    // work lists
-    for (int v = 0; v < 3; ++v) {
-        B->smooth[v].resize((size_t)D);
-        for (int d = 0; d < D; ++d) {
-            std::vector<Item> it;
-            for (int p = 0; p < n; ++p) {
-                if (B->probs[p]->nl <= d) continue;
-                const BLevel &x = lv[(size_t)d * n + p];
-                const int ntx = (x.L.nx + RB_TX - 1) / RB_TX, nty = (x.L.ny + kTY[v] - 1) / kTY[v];
-                for (int k0 = 1; k0 <= x.L.nz; k0 += x.kchunk)
-                    for (int by = 0; by < nty; ++by)
-                        for (int bx = 0; bx < ntx; ++bx) it.push_back({p, bx, by, k0});
-            }
-            B->smooth[v][d].n = (int)it.size();
-            PMG_TRY_B(upload(it, &B->smooth[v][d].d));
-        }
-    }
+    // work lists: the smoother's are built by the autotuner at the first solve; the
+    // transfers' chunk length per depth gives about four waves of full SMs of threads (as the
+    // single-grid marching kernels' chunks)
+    B->h_lv = lv;
+    B->smooth.resize((size_t)D);
     B->xfer_rr.resize((size_t)D);
     B->xfer_pr.resize((size_t)D);
+    int sms = 0;
+    {
+        int dev = 0;
+        if (cudaGetDevice(&dev) != cudaSuccess ||
+            cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+            sms = 148;
+    }
+    const double want_threads = 4.0 * sms * 2048.0;
     for (int d = 0; d < D; ++d) {
         std::vector<Item> rr, pr;
+        double work_rr = 0.0, work_pr = 0.0;      // columns x coarse planes
+        for (int p = 0; p < n; ++p) {
+            if (B->probs[p]->nl <= d) continue;
+            const XferK<float> &X = lv[(size_t)d * n + p].X;
+            const double nfy = lv[(size_t)d * n + p].L.ny;
+            work_rr += (double)X.ncx * X.ncy * X.ncz;
+            work_pr += (X.stx == 2 && X.stz == 2 ? X.ncx * nfy : (double)X.ncx * X.ncy) * X.ncz;
+        }
+        // (the residual-restriction marches three fine planes per coarse plane and measured
+        // fastest with chunks of at most 8 coarse planes)
+        const int kc_rr = (int)std::max(1.0, std::min(8.0, std::ceil(work_rr / want_threads)));
+        const int kc_pr = (int)std::max(1.0, std::min(64.0, std::ceil(work_pr / want_threads)));
         for (int p = 0; p < n; ++p) {
             if (B->probs[p]->nl <= d) continue;
             const XferK<float> &X = lv[(size_t)d * n + p].X;
             const int nfy = lv[(size_t)d * n + p].L.ny;
             const int crr = X.ncx * X.ncy;
             const int cpr = (X.stx == 2 && X.stz == 2) ? X.ncx * nfy : X.ncx * X.ncy;
-            for (int k = 1; k <= X.ncz; k += kXferPlanes) {
-                for (int c = 0; c * NTB < crr; ++c) rr.push_back({p, c, 0, k});
-                for (int c = 0; c * NTB < cpr; ++c) pr.push_back({p, c, 0, k});
-            }
+            for (int k = 1; k <= X.ncz; k += kc_rr)
+                for (int c = 0; c * NTB < crr; ++c) rr.push_back({p, c, kc_rr, k});
+            for (int k = 1; k <= X.ncz; k += kc_pr)
+                for (int c = 0; c * NTB < cpr; ++c) pr.push_back({p, c, kc_pr, k});
         }
         B->xfer_rr[d].n = (int)rr.size();
         B->xfer_pr[d].n = (int)pr.size();
@@ -865,39 +902,80 @@ int batch_create(Batch **out, int n, const int *dims, const double *const *meshe
     PMG_TRY_B(setup_tma_variant<14>(&B->slots[3]));
     PMG_TRY_B(setup_tma_variant<6>(&B->slots[4]));
     PMG_TRY_B(setup_tma_variant<10>(&B->slots[5]));
+    PMG_TRY_B(setup_tma_variant<22>(&B->slots[6]));
     B->variant.assign((size_t)D, -1);
+    B->kchunk.assign((size_t)D, 0);
     B->h_outer.resize((size_t)n);
     *out = B.release();
     return PMG_OK;
 }
 
-// Times the three tile variants on each depth's work list; keeps the fastest.
+// Times every smoother variant with k-chunks of 8 .. 128 planes on each depth's work list
+// (the register-window kernel stages at most RB_ZC - 3 planes of z coefficients per item)
+// and keeps the fastest (variant, k-chunk) with its list.
 static int batch_autotune(Batch &B)
 {
     cudaEvent_t a, z;
     PMG_TRY_B(cuda_status(cudaEventCreate(&a), "batch tuner"));
     PMG_TRY_B(cuda_status(cudaEventCreate(&z), "batch tuner"));
-    for (int d = 0; d < B.dmax; ++d) {
+    const int kcs[] = {8, 16, 32, 64, 128};
+    const char *log_env = std::getenv("PEPS_MG_TUNE_LOG");   // print every candidate's time
+    const bool log = log_env && log_env[0] == '1';
+    int rc = PMG_OK;
+    for (int d = 0; d < B.dmax && rc == PMG_OK; ++d) {
+        int nzmax = 0;
+        for (int p = 0; p < B.n; ++p)
+            if (B.probs[p]->nl > d) nzmax = std::max(nzmax, B.h_lv[(size_t)d * B.n + p].L.nz);
         float best = 1e30f;
-        int bv = 0;
-        for (int v = 0; v < 6; ++v) {
-            if (!B.smooth[v % 3][d].n || (v >= 3 && !B.tma_ok[d])) continue;
-            launch_rb(B, v, d, 0, 1.f, 0.f, false);
-            cudaEventRecord(a, B.stream);
-            for (int r = 0; r < 3; ++r) launch_rb(B, v, d, 0, 1.f, 0.f, false);
-            cudaEventRecord(z, B.stream);
-            cudaEventSynchronize(z);
-            float ms = 0.f;
-            cudaEventElapsedTime(&ms, a, z);
-            if (ms < best) {
-                best = ms;
-                bv = v;
+        int bv = 0, bk = 32;
+        for (int v = 0; v < kVariants && rc == PMG_OK; ++v) {
+            if (v >= 3 && !B.tma_ok[d]) continue;
+            for (const int kc : kcs) {
+                if (v < 3 && kc > RB_ZC - 3) break;
+                const std::vector<Item> it = smooth_items(B, d, kVariantTY[v], kc);
+                if (it.empty()) break;
+                Batch::List L;
+                L.n = (int)it.size();
+                rc = upload(it, &L.d);
+                if (rc == PMG_OK) rc = set_kchunk(B, d, kc);
+                if (rc == PMG_OK) {
+                    launch_rb(B, v, d, L, 0, 1.f, 0.f, false);
+                    cudaEventRecord(a, B.stream);
+                    for (int r = 0; r < 3; ++r) launch_rb(B, v, d, L, 0, 1.f, 0.f, false);
+                    cudaEventRecord(z, B.stream);
+                    rc = cuda_status(cudaEventSynchronize(z), "batch tuner");
+                }
+                dev_free(L.d);
+                if (rc != PMG_OK) break;
+                float ms = 0.f;
+                cudaEventElapsedTime(&ms, a, z);
+                if (log)
+                    std::fprintf(stderr, "[peps_mg batch tune] depth %d %s TY=%d kchunk=%d items=%d: %.1f us\n", d,
+                                 v >= 3 ? "tma" : "window", kVariantTY[v], kc, L.n, ms * 1e3f / 3.f);
+                if (ms < best) {
+                    best = ms;
+                    bv = v;
+                    bk = kc;
+                }
+                if (kc >= nzmax) break;        // larger chunks give the same list
             }
         }
+        if (rc != PMG_OK) break;
         B.variant[d] = bv;
+        B.kchunk[d] = bk;
+        const std::vector<Item> it = smooth_items(B, d, kVariantTY[bv], bk);
+        dev_free(B.smooth[d].d);
+        B.smooth[d].d = nullptr;
+        B.smooth[d].n = (int)it.size();
+        rc = upload(it, &B.smooth[d].d);
+        if (rc == PMG_OK) rc = set_kchunk(B, d, bk);
     }
     cudaEventDestroy(a);
     cudaEventDestroy(z);
+    if (rc != PMG_OK) {
+        B.variant.assign(B.variant.size(), -1);
+        return rc;
+    }
     return cuda_status(cudaGetLastError(), "batch autotuning");
 }
 
@@ -908,7 +986,7 @@ static void batch_vcycle(Batch &B, int maxit, float om, float omw, bool zero_sta
     std::vector<int> par((size_t)D + 1, 0);
     auto smooth = [&](int d, bool zs) {
         for (int it = 0; it < maxit; ++it) {
-            launch_rb(B, B.variant[d], d, par[d], om, omw, zs && it == 0);
+            launch_rb(B, B.variant[d], d, B.smooth[d], par[d], om, omw, zs && it == 0);
             par[d] ^= 1;
         }
     };
