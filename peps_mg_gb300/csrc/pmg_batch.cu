@@ -924,16 +924,26 @@ static int batch_autotune(Batch &B)
     int rc = PMG_OK;
     for (int d = 0; d < B.dmax && rc == PMG_OK; ++d) {
         int nzmax = 0;
+        long long cells = 0;
         for (int p = 0; p < B.n; ++p)
-            if (B.probs[p]->nl > d) nzmax = std::max(nzmax, B.h_lv[(size_t)d * B.n + p].L.nz);
+            if (B.probs[p]->nl > d) {
+                const LevelK<float> &L = B.h_lv[(size_t)d * B.n + p].L;
+                nzmax = std::max(nzmax, L.nz);
+                cells += (long long)L.nx * L.ny * L.nz;
+            }
         float best = 1e30f;
         int bv = 0, bk = 32;
+        // the register-window kernel only wins on small depths (at most 2^22 cells); the
+        // time is unimodal in the k-chunk, so each variant's walk goes up from 16 planes
+        // while it stays within 10% of the variant's best (and down to 8 from a minimum at 16)
         for (int v = 0; v < kVariants && rc == PMG_OK; ++v) {
             if (v >= 3 && !B.tma_ok[d]) continue;
-            for (const int kc : kcs) {
-                if (v < 3 && kc > RB_ZC - 3) break;
+            if (v < 3 && B.tma_ok[d] && cells > (1LL << 22)) continue;
+            float v_best = 1e30f;
+            int v_best_kc = 0;
+            auto time_kc = [&](int kc, float *ms) -> bool {
                 const std::vector<Item> it = smooth_items(B, d, kVariantTY[v], kc);
-                if (it.empty()) break;
+                if (it.empty()) return false;
                 Batch::List L;
                 L.n = (int)it.size();
                 rc = upload(it, &L.d);
@@ -946,18 +956,32 @@ static int batch_autotune(Batch &B)
                     rc = cuda_status(cudaEventSynchronize(z), "batch tuner");
                 }
                 dev_free(L.d);
-                if (rc != PMG_OK) break;
-                float ms = 0.f;
-                cudaEventElapsedTime(&ms, a, z);
+                if (rc != PMG_OK) return false;
+                cudaEventElapsedTime(ms, a, z);
                 if (log)
                     std::fprintf(stderr, "[peps_mg batch tune] depth %d %s TY=%d kchunk=%d items=%d: %.1f us\n", d,
-                                 v >= 3 ? "tma" : "window", kVariantTY[v], kc, L.n, ms * 1e3f / 3.f);
-                if (ms < best) {
-                    best = ms;
+                                 v >= 3 ? "tma" : "window", kVariantTY[v], kc, L.n, *ms * 1e3f / 3.f);
+                if (*ms < v_best) {
+                    v_best = *ms;
+                    v_best_kc = kc;
+                }
+                if (*ms < best) {
+                    best = *ms;
                     bv = v;
                     bk = kc;
                 }
+                return true;
+            };
+            for (const int kc : kcs) {
+                if (kc < 16 && nzmax > 8) continue;
+                if (v < 3 && kc > RB_ZC - 3) break;
+                float ms = 0.f;
+                if (!time_kc(kc, &ms) || ms > 1.1f * v_best) break;
                 if (kc >= nzmax) break;        // larger chunks give the same list
+            }
+            if (rc == PMG_OK && v_best_kc == 16) {
+                float ms = 0.f;
+                time_kc(8, &ms);
             }
         }
         if (rc != PMG_OK) break;

@@ -334,18 +334,48 @@ int tune_smoother(const LevelK<float> &L, const Launch &ln, float *e0, float *e1
     const char *log_env = std::getenv("PEPS_MG_TUNE_LOG");   // print every candidate's time
     const bool log = log_env && log_env[0] == '1';
     // the register-window kernel stages at most RB_ZC - 3 planes of z coefficients
-    const int chunks_window[] = {0, 16, 32, 64}, chunks_tma[] = {0, 4, 8, 16, 32, 64, 128};
+    const int chunks_window[] = {0, 16, 32, 64}, chunks_tma[] = {4, 8, 16, 32, 64, 128};
     const int tys[4] = {14, 6, 10, 22};
     bool best_window = !use_tma;
-    // the TMA-fed kernel where its tensor maps exist, and the register-window kernel (no
-    // copy pipeline to fill: it can win on small levels)
+    // The register-window kernel (no copy pipeline to fill) only wins on small levels: it is
+    // timed where the TMA-fed one cannot run or the level has at most 2^22 cells.
+    const bool try_window = !use_tma || (long long)L.nx * L.ny * L.nz <= (1LL << 22);
+    auto time_one = [&](bool tk, int v, int c, float *ms) -> bool {
+        const Rb32Tma *tm = tk ? tma : nullptr;
+        if (rb32_fused(L, ln, e0, e1, b, 1.f, 0.f, false, s, v, c, tm, 0, err) != PMG_OK) return false;
+        cudaEventRecord(a, s);
+        for (int q = 0; q < 3; ++q) rb32_fused(L, ln, e0, e1, b, 1.f, 0.f, false, s, v, c, tm, 0, err);
+        cudaEventRecord(z, s);
+        if (cudaEventSynchronize(z) != cudaSuccess) return false;
+        cudaEventElapsedTime(ms, a, z);
+        if (log)
+            std::fprintf(stderr, "[peps_mg tune] %dx%dx%d %s TY=%d kchunk=%d: %.1f us\n", L.nx, L.ny, L.nz,
+                         tk ? "tma" : "window", tys[v], c, *ms * 1e3f / 3.f);
+        if (*ms < best) {
+            best = *ms;
+            bv = v;
+            bk = c;
+            best_window = !tk;
+        }
+        return true;
+    };
     for (int kind = use_tma ? 0 : 1; kind < 2; ++kind) {
-    const bool tk = kind == 0;
-    for (int v = 0; v < (tk ? 4 : 3); ++v) {
-        std::vector<int> cands(tk ? chunks_tma : chunks_window, tk ? chunks_tma + 7 : chunks_window + 4);
-        if (tk) {
+        const bool tk = kind == 0;
+        if (!tk && !try_window) break;
+        for (int v = 0; v < (tk ? 4 : 3); ++v) {
+            if (!tk) {
+                for (const int c : chunks_window) {
+                    float ms = 0.f;
+                    if (!time_one(false, v, c, &ms)) break;
+                }
+                continue;
+            }
             // k-chunks that spread the tiles' items evenly over the resident CTA slots (one
-            // to three rounds), besides the powers of two
+            // to three rounds), besides the powers of two, in increasing order; the time is
+            // unimodal in the chunk, so the walk starts at 16 planes, goes up while the
+            // time stays within 10% of this tile's best, and goes down only from a minimum
+            // at 16
+            std::vector<int> cands(chunks_tma, chunks_tma + 6);
             int slots = 0;
             const int r = v == 1 ? tma_slots<6>(&slots) : v == 2 ? tma_slots<10>(&slots)
                                                                : v == 3 ? tma_slots<22>(&slots) : tma_slots<14>(&slots);
@@ -356,27 +386,29 @@ int tune_smoother(const LevelK<float> &L, const Launch &ln, float *e0, float *e1
                     const int c = (L.nz + nch - 1) / nch;
                     if (c >= 4 && std::find(cands.begin(), cands.end(), c) == cands.end()) cands.push_back(c);
                 }
-        }
-        const Rb32Tma *tm = tk ? tma : nullptr;
-        for (const int c : cands) {
-            if (rb32_fused(L, ln, e0, e1, b, 1.f, 0.f, false, s, v, c, tm, 0, err) != PMG_OK) continue;
-            cudaEventRecord(a, s);
-            for (int q = 0; q < 3; ++q) rb32_fused(L, ln, e0, e1, b, 1.f, 0.f, false, s, v, c, tm, 0, err);
-            cudaEventRecord(z, s);
-            if (cudaEventSynchronize(z) != cudaSuccess) break;
-            float ms = 0.f;
-            cudaEventElapsedTime(&ms, a, z);
-            if (log)
-                std::fprintf(stderr, "[peps_mg tune] %dx%dx%d %s TY=%d kchunk=%d: %.1f us\n", L.nx, L.ny, L.nz,
-                             tk ? "tma" : "window", tys[v], c, ms * 1e3f / 3.f);
-            if (ms < best) {
-                best = ms;
-                bv = v;
-                bk = c;
-                best_window = !tk;
+            for (int &c : cands) c = std::min(c, L.nz);
+            std::sort(cands.begin(), cands.end());
+            cands.erase(std::unique(cands.begin(), cands.end()), cands.end());
+            const size_t start = std::lower_bound(cands.begin(), cands.end(), std::min(16, L.nz)) - cands.begin();
+            float ty_best = 1e30f;
+            size_t ty_best_at = start;
+            for (size_t q = start; q < cands.size(); ++q) {
+                float ms = 0.f;
+                if (!time_one(true, v, cands[q], &ms)) break;
+                if (ms < ty_best) {
+                    ty_best = ms;
+                    ty_best_at = q;
+                } else if (ms > 1.1f * ty_best) {
+                    break;
+                }
             }
+            if (ty_best_at == start)
+                for (size_t q = start; q-- > 0;) {
+                    float ms = 0.f;
+                    if (!time_one(true, v, cands[q], &ms) || ms > 1.1f * ty_best) break;
+                    ty_best = std::min(ty_best, ms);
+                }
         }
-    }
     }
     cudaEventDestroy(a);
     cudaEventDestroy(z);
