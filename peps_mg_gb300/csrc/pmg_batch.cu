@@ -126,6 +126,7 @@ struct BatchTmaSrc {
         return &A->maps[A->items[it].p].e[A->which][A->vi];
     }
     __device__ __forceinline__ const CUtensorMap *map_b(int it) const { return &A->maps[A->items[it].p].b[A->vi]; }
+    static constexpr bool kStall = false;
     __device__ __forceinline__ bool stall() const { return false; }
 };
 

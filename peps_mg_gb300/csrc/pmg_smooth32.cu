@@ -61,12 +61,12 @@ __global__ void __launch_bounds__(rb_threads<TY>(), rb_min_blocks<TY>()) k_rb32_
 template <int TY>
 constexpr int rbt_min_blocks() { return rbt_min_ctas<TY>(); }
 
-template <int TY, bool ZERO_IN, bool OMEGA1>
+template <int TY, bool ZERO_IN, bool OMEGA1, bool STALL = false>
 __global__ void __launch_bounds__(RbtShape<TY>::THREADS, rbt_min_blocks<TY>())
     k_rb32_tma(const __grid_constant__ CUtensorMap me, const __grid_constant__ CUtensorMap mb, LevelK<float> L,
                float *__restrict__ eout, float omega, float omw, RbtItems W, int *err)
 {
-    const RbtGridSrc src{&W, &me, &mb};
+    const RbtGridSrc<STALL> src{&W, &me, &mb};
     rbt_cta<TY, ZERO_IN, OMEGA1>(
         src,
         [&](int, const LevelK<float> *&Li, float *&eo) {
@@ -128,16 +128,17 @@ int launch_ty(const LevelK<float> &L, const Launch &ln, const float *ein, float 
     return cuda_status(cudaGetLastError(), "fused fp32 smoother");
 }
 
-template <int TY, bool Z, bool O>
+template <int TY, bool Z, bool O, bool STALL = false>
 int tma_attr()
 {
     static std::once_flag once;
     static cudaError_t err = cudaSuccess;
     std::call_once(once, [] {
-        err = cudaFuncSetAttribute(k_rb32_tma<TY, Z, O>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+        err = cudaFuncSetAttribute(k_rb32_tma<TY, Z, O, STALL>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                    RbtShape<TY>::SMEM);
         if (err == cudaSuccess)
-            err = cudaFuncSetAttribute(k_rb32_tma<TY, Z, O>, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+            err = cudaFuncSetAttribute(k_rb32_tma<TY, Z, O, STALL>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                       100);
     });
     return cuda_status(err, "TMA smoother shared memory attribute");
 }
@@ -181,7 +182,6 @@ int launch_tma(const LevelK<float> &L, const Launch &ln, const Rb32Tma &t, int v
     int slots = 0;
     PMG_TRY_S(tma_slots<TY>(&slots));
     RbtItems W;
-    W.stall = stall ? 1 : 0;
     W.ntx = (L.nx + RBT_TX - 1) / RBT_TX;
     W.nty = (L.ny + TY - 1) / TY;
     W.nz = L.nz;
@@ -197,7 +197,15 @@ int launch_tma(const LevelK<float> &L, const Launch &ln, const Rb32Tma &t, int v
     const bool one = omega == 1.f;
     const CUtensorMap &me = t.e[in_buf][vi], &mb = t.b[vi];
     constexpr int T = RbtShape<TY>::THREADS, SM = RbtShape<TY>::SMEM;
-    if (zero_in && one) {
+    if (stall) {
+        // the self-test instantiation: e_in read (no zero start), omega = 1
+        if (zero_in || !one) {
+            set_error("the stall self-test runs the omega = 1 iteration from a given e");
+            return PMG_EINVAL;
+        }
+        PMG_TRY_S((tma_attr<TY, false, true, true>()));
+        k_rb32_tma<TY, false, true, true><<<grid, T, SM, s>>>(me, mb, L, eout, omega, omw, W, err);
+    } else if (zero_in && one) {
         PMG_TRY_S((tma_attr<TY, true, true>()));
         k_rb32_tma<TY, true, true><<<grid, T, SM, s>>>(me, mb, L, eout, omega, omw, W, err);
     } else if (zero_in) {
@@ -370,12 +378,15 @@ int tune_smoother(const LevelK<float> &L, const Launch &ln, float *e0, float *e1
                 }
                 continue;
             }
-            // k-chunks that spread the tiles' items evenly over the resident CTA slots (one
-            // to three rounds), besides the powers of two, in increasing order; the time is
-            // unimodal in the chunk, so the walk starts at 16 planes, goes up while the
-            // time stays within 10% of this tile's best, and goes down only from a minimum
-            // at 16
-            std::vector<int> cands(chunks_tma, chunks_tma + 6);
+            // The k-chunks that spread the tiles' items evenly over the resident CTA slots
+            // (one to three rounds) are all timed: they are the fast ones where the level
+            // has few items.  The powers of two are walked from 16 planes up while they stay
+            // within 10% of this tile's best, and down only from a minimum at 16.
+            std::vector<int> pow2;
+            for (const int c : chunks_tma) pow2.push_back(std::min(c, L.nz));
+            std::sort(pow2.begin(), pow2.end());
+            pow2.erase(std::unique(pow2.begin(), pow2.end()), pow2.end());
+            std::vector<int> balanced;
             int slots = 0;
             const int r = v == 1 ? tma_slots<6>(&slots) : v == 2 ? tma_slots<10>(&slots)
                                                                : v == 3 ? tma_slots<22>(&slots) : tma_slots<14>(&slots);
@@ -383,30 +394,33 @@ int tune_smoother(const LevelK<float> &L, const Launch &ln, float *e0, float *e1
             if (r == PMG_OK && slots > 0)
                 for (int rounds = 1; rounds <= 3; ++rounds) {
                     const int nch = std::max(1, (rounds * slots) / std::max(1, tiles));
-                    const int c = (L.nz + nch - 1) / nch;
-                    if (c >= 4 && std::find(cands.begin(), cands.end(), c) == cands.end()) cands.push_back(c);
+                    const int c = std::min((L.nz + nch - 1) / nch, L.nz);
+                    if (c >= 4 && std::find(pow2.begin(), pow2.end(), c) == pow2.end() &&
+                        std::find(balanced.begin(), balanced.end(), c) == balanced.end())
+                        balanced.push_back(c);
                 }
-            for (int &c : cands) c = std::min(c, L.nz);
-            std::sort(cands.begin(), cands.end());
-            cands.erase(std::unique(cands.begin(), cands.end()), cands.end());
-            const size_t start = std::lower_bound(cands.begin(), cands.end(), std::min(16, L.nz)) - cands.begin();
-            float ty_best = 1e30f;
-            size_t ty_best_at = start;
-            for (size_t q = start; q < cands.size(); ++q) {
+            for (const int c : balanced) {
                 float ms = 0.f;
-                if (!time_one(true, v, cands[q], &ms)) break;
-                if (ms < ty_best) {
-                    ty_best = ms;
-                    ty_best_at = q;
-                } else if (ms > 1.1f * ty_best) {
+                time_one(true, v, c, &ms);
+            }
+            const size_t start = std::lower_bound(pow2.begin(), pow2.end(), std::min(16, L.nz)) - pow2.begin();
+            float walk_best = 1e30f;
+            size_t walk_best_at = start;
+            for (size_t q = start; q < pow2.size(); ++q) {
+                float ms = 0.f;
+                if (!time_one(true, v, pow2[q], &ms)) break;
+                if (ms < walk_best) {
+                    walk_best = ms;
+                    walk_best_at = q;
+                } else if (ms > 1.1f * walk_best) {
                     break;
                 }
             }
-            if (ty_best_at == start)
+            if (walk_best_at == start)
                 for (size_t q = start; q-- > 0;) {
                     float ms = 0.f;
-                    if (!time_one(true, v, cands[q], &ms) || ms > 1.1f * ty_best) break;
-                    ty_best = std::min(ty_best, ms);
+                    if (!time_one(true, v, pow2[q], &ms) || ms > 1.1f * walk_best) break;
+                    walk_best = std::min(walk_best, ms);
                 }
         }
     }

@@ -111,16 +111,17 @@ __device__ __forceinline__ bool mbar_wait_bounded(unsigned long long *bar, unsig
 constexpr long long kWaitCycles = 1LL << 31;
 constexpr long long kStallWaitCycles = 1LL << 13;
 
-// Slow path of a wait: spins until the phase completes, the CTA's wait limit passes (then
-// it raises the CTA's abort flag) or another thread has raised the flag.  The limit sits
-// in shared memory in the 8 bytes after the abort flag.  Returns false on failure.
+// Slow path of a wait: spins until the phase completes, LIMIT clock cycles pass (then it
+// raises the CTA's abort flag) or another thread has raised the flag.  Returns false on
+// failure.  The limit is a template constant: a limit read at run time costs the
+// production kernels' sweep loop registers (spills) around this call.
+template <long long LIMIT>
 static __device__ __noinline__ bool mbar_wait_slow(unsigned long long *bar, unsigned parity, volatile int *abort_flag)
 {
-    const long long limit = *(reinterpret_cast<volatile long long *>(abort_flag) + 1);
     const long long t0 = clock64();
     while (!mbar_try_wait(bar, parity)) {
         if (*abort_flag) return false;
-        if (clock64() - t0 > limit) {
+        if (clock64() - t0 > LIMIT) {
             *abort_flag = 1;
             return false;
         }
@@ -158,7 +159,6 @@ __device__ __forceinline__ void sq(float2 &v, float x)
 // Work item geometry of one level: item it -> tile (bx, by) and planes k0..k1.
 struct RbtItems {
     int ntx, nty, kchunk, nz, nitems;
-    int stall;   // self-test only: issue no copies, short wait limit
     __device__ __forceinline__ void decode(int it, int &bx, int &by, int &k0, int &k1) const
     {
         const int per = ntx * nty;
@@ -173,7 +173,10 @@ struct RbtItems {
 // A source of work items for the TMA-fed smoother: the CTA's items in order (first /
 // next / valid), each item's tile and planes (geom) and the tensor maps of its e_in and b
 // (map_e / map_b).  RbtGridSrc serves one level; the batched solver has its own source
-// over (problem, tile) lists.
+// over (problem, tile) lists.  STALL (a separate instantiation, so the production kernels
+// carry no trace of it): the self-test source, which issues no copies and gives every wait
+// a limit of a few microseconds.
+template <bool STALL>
 struct RbtGridSrc {
     const RbtItems *W;            // the kernel parameter (read from the constant bank)
     const CUtensorMap *me, *mb;
@@ -186,7 +189,8 @@ struct RbtGridSrc {
     }
     __device__ __forceinline__ const CUtensorMap *map_e(int) const { return me; }
     __device__ __forceinline__ const CUtensorMap *map_b(int) const { return mb; }
-    __device__ __forceinline__ bool stall() const { return W->stall != 0; }
+    static constexpr bool kStall = STALL;
+    __device__ __forceinline__ constexpr bool stall() const { return STALL; }
 };
 
 // The producer: one thread issuing the planes of the CTA's items, slot after slot.  Its
@@ -266,11 +270,13 @@ struct RbtItem {
     {
         return (unsigned)(slot & (RBT_NS - 1)) * (unsigned)S::STAGE;
     }
+    template <bool STALL>
     __device__ __forceinline__ void wait(int slot)
     {
         unsigned long long *bar = &bars[slot & (RBT_NS - 1)];
         const unsigned par = (unsigned)(slot / RBT_NS) & 1u;
-        if (!rbtdetail::mbar_try_wait(bar, par) && !rbtdetail::mbar_wait_slow(bar, par, abort_flag)) fail = true;
+        constexpr long long lim = STALL ? rbtdetail::kStallWaitCycles : rbtdetail::kWaitCycles;
+        if (!rbtdetail::mbar_try_wait(bar, par) && !rbtdetail::mbar_wait_slow<lim>(bar, par, abort_flag)) fail = true;
     }
     __device__ __forceinline__ float2 lds2(unsigned off) const
     {
@@ -309,7 +315,7 @@ struct RbtItem {
         constexpr int QB = 1 - Q;
         const int cs = cbase + (t - k0 + 2);      // slot of plane t
         const unsigned s0 = stage_off(cs), sp = stage_off(cs + 1), sm = stage_off(cs - 1);
-        wait(cs + 1);
+        wait<Src::kStall>(cs + 1);
         if (!ZERO_IN) {
             EA[ip1] = lds2(sp + oe);
             EB[ip1] = lds2(sp + oe + RBT_W * 4);
@@ -503,8 +509,8 @@ __device__ __forceinline__ bool rbt_item(unsigned char *smem, unsigned long long
     // window at the first step t = k0 - 1: positions 0..3 = planes k0-3 .. k0; position 0
     // (plane k0-3) is never read, position 3 is loaded by the step itself
     I.EA[0] = I.EB[0] = make_float2(0.f, 0.f);
-    I.wait(cbase);
-    I.wait(cbase + 1);
+    I.template wait<Src::kStall>(cbase);
+    I.template wait<Src::kStall>(cbase + 1);
     if (ZERO_IN) {
         I.EA[1] = I.EB[1] = I.EA[2] = I.EB[2] = make_float2(0.f, 0.f);
     } else {
@@ -533,8 +539,8 @@ __device__ __forceinline__ void rbt_cta(const Src &src, Per per, float omega, fl
 {
     using S = RbtShape<TY>;
     extern __shared__ unsigned char rbt_smem_raw[];
-    // 128-byte aligned stages (TMA destinations), then the mbarriers, the abort flag, the
-    // wait limit and the producer state
+    // 128-byte aligned stages (TMA destinations), then the mbarriers, the abort flag and
+    // the producer state
     unsigned char *smem = rbt_smem_raw + ((128u - (rbtdetail::smem_addr(rbt_smem_raw) & 127u)) & 127u);
     unsigned long long *bars = reinterpret_cast<unsigned long long *>(smem + RBT_NS * S::STAGE);
     volatile int *abort_flag = reinterpret_cast<volatile int *>(bars + RBT_NS);
@@ -544,8 +550,6 @@ __device__ __forceinline__ void rbt_cta(const Src &src, Per per, float omega, fl
     if (threadIdx.x == 0) {
         for (int q = 0; q < RBT_NS; ++q) rbtdetail::mbar_init(&bars[q], 1);
         *abort_flag = 0;
-        *reinterpret_cast<volatile long long *>(bars + RBT_NS + 1) =
-            src.stall() ? rbtdetail::kStallWaitCycles : rbtdetail::kWaitCycles;
         rbtdetail::fence_mbar_init();
     }
     __syncthreads();
