@@ -230,3 +230,37 @@ def test_mixed_nan_rhs_reports_divergence():
         with pytest.raises(pmg.PmgError) as e:
             mg.solve_vcycle(sol, torch.zeros_like(sol), to_dev(rhs), 1, 1e-10, 1.0)
         assert e.value.status == 3
+
+
+def test_mixed_pageable_host_buffers_registered_or_not(monkeypatch):
+    """Pageable host buffers are page-locked for the call (cudaHostRegister) and released
+    after it; with PEPS_MG_NO_HOST_REGISTER=1 they are copied as pageable memory, and three
+    buffers carved from one allocation (sharing pages, so not all can be registered) fall
+    back to pageable copies.  All three give the device-buffer result bit for bit, and the
+    arrays are not left page-locked."""
+    mesh, rhs, _ = problems.sine(48)
+    n = 48
+    shape = (n + 2,) * 3
+    size = (n + 2) ** 3
+    with pmg.Multigrid(mesh, 4, 50, precision="mixed") as mg:
+        ds = torch.zeros(shape, dtype=torch.float64, device="cuda")
+        dr = torch.zeros_like(ds)
+        rep_d = mg.solve_vcycle(ds, dr, to_dev(rhs), 2, 1e-10, 1.0)
+        ref_s, ref_r = ds.cpu().numpy(), dr.cpu().numpy()
+        b = np.ascontiguousarray(np.asfortranarray(rhs).T)
+        for env in ("0", "1"):
+            monkeypatch.setenv("PEPS_MG_NO_HOST_REGISTER", env)
+            hs, hr = np.zeros(shape), np.zeros(shape)
+            rep = mg.solve_vcycle(hs, hr, b, 2, 1e-10, 1.0)
+            assert np.array_equal(rep.history, rep_d.history)
+            assert np.array_equal(hs, ref_s) and np.array_equal(hr, ref_r)
+            for a in (hs, hr, b):       # released: a new registration of the same range works
+                assert int(torch.cuda.cudart().cudaHostRegister(a.ctypes.data, a.nbytes, 0)) == 0
+                assert int(torch.cuda.cudart().cudaHostUnregister(a.ctypes.data)) == 0
+        monkeypatch.setenv("PEPS_MG_NO_HOST_REGISTER", "0")
+        one = np.zeros(3 * size + 7)
+        hs, hr, hb = (one[1 + q * size:1 + (q + 1) * size].reshape(shape) for q in range(3))
+        hb[...] = b
+        rep = mg.solve_vcycle(hs, hr, hb, 2, 1e-10, 1.0)
+        assert np.array_equal(rep.history, rep_d.history)
+        assert np.array_equal(hs, ref_s) and np.array_equal(hr, ref_r)
