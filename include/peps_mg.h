@@ -88,8 +88,9 @@ int pmg_create(pmg_ctx **ctx, const pmg_config_t *cfg, void *stream);
 /* multigrid_solve_vcycle(sol, rsd, a_poisson, rhs, sdm, maxiteration, tolerance,
  * omega_sor) -- src/multigrid.f90:1864.  sol (in/out), rsd (out: final residual,
  * ghosts zero) and rhs (in) are (nx+2)(ny+2)(nz+2) doubles, either all device memory
- * or all host memory (host buffers are staged through the device).  report may be
- * NULL. */
+ * or all host memory (host buffers are staged through the device; pageable ones are
+ * page-locked for the duration of the call unless PEPS_MG_NO_HOST_REGISTER=1, and
+ * released before it returns).  report may be NULL. */
 int pmg_solve_vcycle(pmg_ctx *ctx, double *sol, double *rsd, const double *rhs, int maxiteration,
                      double tolerance, double omega_sor, pmg_report_t *report);
 
