@@ -747,6 +747,18 @@ int Ctx::build(const pmg_config_t *c, cudaStream_t s)
         PMG_CUDA(cudaStreamCreateWithFlags(&copy_stream, cudaStreamNonBlocking), "copy stream");
     }
     if (precision == PMG_FP64_FAST) PMG_TRY(setup_fast64());
+    if (precision == PMG_FP64) {
+        // per-cell diagonal tables of the plain FP64 path (the grid kernels read c0 instead
+        // of summing five 1-D table entries per cell; the values are diag_f64's bits)
+        c0t.assign((size_t)nl + 1, nullptr);
+        for (int l = 0; l <= nl; ++l) {
+            PMG_CUDA(dev_malloc(&c0t[l], lv[l].total * sizeof(double)), "diagonal table");
+            PMG_CUDA(cudaMemsetAsync(c0t[l], 0, lv[l].total * sizeof(double), stream), "diagonal table");
+            PMG_TRY(f64_diag_table(K[l], c0t[l], stream));
+        }
+        // complete before any other stream (a decomposed solve's) reads the tables
+        PMG_CUDA(cudaStreamSynchronize(stream), "diagonal table");
+    }
     return PMG_OK;
 }
 
@@ -812,6 +824,7 @@ Ctx::~Ctx()
         dev_free(L.r);
     }
     dev_free(d_tables);
+    for (auto p : c0t) dev_free(p);
     dev_free(d_partials);
     dev_free(d_scal);
     dev_free(d_iscal);
@@ -851,7 +864,7 @@ int Ctx::dot(int l, const double *x, const double *y, int slot)
 int Ctx::residual_norm(int l, double *r, const double *x, const double *b, int slot)
 {
     int np = 0;
-    PMG_TRY(f64_residual(K[l], launch[l], r, x, b, d_partials, &np, stream));
+    PMG_TRY(f64_residual(K[l], launch[l], r, x, b, d_partials, &np, stream, diag(l)));
     return f64_reduce(d_partials, np, d_scal + slot, stream);
 }
 
@@ -936,11 +949,11 @@ int Ctx::vcycle_f64(double *sol, double *rsd, const double *rhs, int maxit, doub
     const bool fast = fast64;
     auto sweeps = [&](int l, double *x, const double *b) {
         return fast ? fast_rbgs_sweeps(K[l], fastK[l], launch[l], x, b, maxit, omega, stream)
-                    : f64_rbgs_sweeps(K[l], launch[l], x, b, maxit, omega, stream);
+                    : f64_rbgs_sweeps(K[l], launch[l], x, b, maxit, omega, stream, diag(l));
     };
     auto resid = [&](int l, double *r, const double *x, const double *b) {
         return fast ? fast_residual(K[l], fastK[l], launch[l], r, x, b, nullptr, nullptr, stream)
-                    : f64_residual(K[l], launch[l], r, x, b, nullptr, nullptr, stream);
+                    : f64_residual(K[l], launch[l], r, x, b, nullptr, nullptr, stream, diag(l));
     };
     auto restr = [&](int l, const double *vf, double *vc) {
         return fast ? fast_restrict(X[l], fastX[l], launch[l + 1], vf, vc, stream)
@@ -1141,7 +1154,7 @@ int Ctx::rbgs_solver_dev(int l, double *x, const double *b, int maxit, double to
     int it = 0;
     for (it = 0; it < maxit; ++it) {
         if (aborted()) return abort_status();
-        PMG_TRY(f64_rbgs_sweeps(K[l], launch[l], x, b, 1, omega, stream));
+        PMG_TRY(f64_rbgs_sweeps(K[l], launch[l], x, b, 1, omega, stream, diag(l)));
         PMG_TRY(residual_norm(l, rs, x, b, 3));
         PMG_TRY(fetch_scalars(h, 4));
         rn = h[3];
@@ -1167,13 +1180,14 @@ int Ctx::cg_dev(int l, double *x, const double *b, int maxit, double tol, bool c
         set_error("cg: partial-sum buffer too small for the level");
         return PMG_EINVAL;
     }
-    PMG_TRY(f64_cg_init(K[l], launch[l], rs, p, x, b, d_partials, d_cg, stream));
+    PMG_TRY(f64_cg_init(K[l], launch[l], rs, p, x, b, d_partials, d_cg, stream, diag(l)));
     CgState h{};
     for (int it0 = 0; it0 < maxit; it0 += kCgCheckEvery) {
         if (aborted()) return abort_status();
         const int it1 = std::min(maxit, it0 + kCgCheckEvery);
         for (int it = it0; it < it1; ++it)
-            PMG_TRY(f64_cg_iteration(K[l], launch[l], x, rs, p, ap, d_partials, d_cg, tol, check, it, stream));
+            PMG_TRY(f64_cg_iteration(K[l], launch[l], x, rs, p, ap, d_partials, d_cg, tol, check, it, stream,
+                                     diag(l)));
         if (check && it1 < maxit) {
             PMG_CUDA(cudaMemcpyAsync(&h, d_cg, sizeof(h), cudaMemcpyDeviceToHost, stream), "cg state read");
             PMG_CUDA(cudaStreamSynchronize(stream), "stream sync");
@@ -1466,7 +1480,7 @@ int pmg_mv_mul(pmg_ctx *ctx, int level, double *y, const double *x)
     const auto &L = c.lv[level];
     // y = 0 everywhere, then the interior (src/poisson_matrix_operator.f90:136-159)
     PMG_TRY(pmg::zero_ghosts_f64(y, L.n[0], L.n[1], L.n[2], c.stream));
-    return pmg::f64_mv_mul(c.K[level], c.launch[level], y, x, c.stream);
+    return pmg::f64_mv_mul(c.K[level], c.launch[level], y, x, c.stream, c.diag(level));
 }
 
 int pmg_vv_dot(pmg_ctx *ctx, int level, const double *x, const double *y, double *result)
@@ -1486,14 +1500,14 @@ int pmg_residual(pmg_ctx *ctx, int level, double *r, const double *x, const doub
     Ctx &c = ctx->impl;
     const auto &L = c.lv[level];
     PMG_TRY(pmg::zero_ghosts_f64(r, L.n[0], L.n[1], L.n[2], c.stream));
-    return pmg::f64_residual(c.K[level], c.launch[level], r, x, b, nullptr, nullptr, c.stream);
+    return pmg::f64_residual(c.K[level], c.launch[level], r, x, b, nullptr, nullptr, c.stream, c.diag(level));
 }
 
 int pmg_rbgs_iterator(pmg_ctx *ctx, int level, double *x, const double *b, int maxiteration, double omega)
 {
     PMG_TRY(check_ctx_level(ctx, level));
     Ctx &c = ctx->impl;
-    return pmg::f64_rbgs_sweeps(c.K[level], c.launch[level], x, b, maxiteration, omega, c.stream);
+    return pmg::f64_rbgs_sweeps(c.K[level], c.launch[level], x, b, maxiteration, omega, c.stream, c.diag(level));
 }
 
 int pmg_rbgs_solver(pmg_ctx *ctx, int level, double *x, const double *b, int maxiteration, double tolerance,

@@ -63,8 +63,11 @@ __device__ __forceinline__ double diag_f64(const LevelK<double> &L, int i, int j
 // RBGS update of one cell (src/rbgs_poisson_matrix.f90:244-250):
 //   temp = c1 x(i-1) + c2 x(i+1) + c3 x(j-1) + c4 x(j+1) + c5 x(k-1) + c6 x(k+1)
 //   x    = omega (rhs - temp) / c0 + (1 - omega) x
-__device__ __forceinline__ double rbgs_cell_f64(const LevelK<double> &L, const double *x, const double *b, int i,
-                                                int j, int k, double omega, double omw)
+// with c0 given (diag_f64's value, computed or read from a per-cell table).  OMEGA1: omega
+// is exactly 1, and 1 * v equals v for every double, so that product is not formed.
+template <bool OMEGA1>
+__device__ __forceinline__ double rbgs_cell_c0_f64(const LevelK<double> &L, const double *x, const double *b, int i,
+                                                   int j, int k, double omega, double omw, double c0)
 {
     const long long p = lin(i, j, k, L.sy, L.sz);
     double t = __dmul_rn(L.cxm[i], x[p - 1]);
@@ -73,13 +76,33 @@ __device__ __forceinline__ double rbgs_cell_f64(const LevelK<double> &L, const d
     t = __dadd_rn(t, __dmul_rn(L.cyp[j], x[p + L.sy]));
     t = __dadd_rn(t, __dmul_rn(L.czm[k], x[p - L.sz]));
     t = __dadd_rn(t, __dmul_rn(L.czp[k], x[p + L.sz]));
-    const double c0 = diag_f64(L, i, j, k);
-    const double q = __ddiv_rn(__dmul_rn(omega, __dsub_rn(b[p], t)), c0);
+    const double d = __dsub_rn(b[p], t);
+    const double q = __ddiv_rn(OMEGA1 ? d : __dmul_rn(omega, d), c0);
     return __dadd_rn(q, __dmul_rn(omw, x[p]));
 }
 
+__device__ __forceinline__ double rbgs_cell_f64(const LevelK<double> &L, const double *x, const double *b, int i,
+                                                int j, int k, double omega, double omw)
+{
+    return rbgs_cell_c0_f64<false>(L, x, b, i, j, k, omega, omw, diag_f64(L, i, j, k));
+}
+
 // (A x)(i,j,k) = c0 x + c1 x(i-1) + c2 x(i+1) + c3 x(j-1) + c4 x(j+1) + c5 x(k-1) + c6 x(k+1)
-// (src/poisson_matrix_operator.f90:150-156)
+// (src/poisson_matrix_operator.f90:150-156), with c0 given
+__device__ __forceinline__ double ax_cell_c0_f64(const LevelK<double> &L, const double *x, int i, int j, int k,
+                                                 double c0)
+{
+    const long long p = lin(i, j, k, L.sy, L.sz);
+    double t = __dmul_rn(c0, x[p]);
+    t = __dadd_rn(t, __dmul_rn(L.cxm[i], x[p - 1]));
+    t = __dadd_rn(t, __dmul_rn(L.cxp[i], x[p + 1]));
+    t = __dadd_rn(t, __dmul_rn(L.cym[j], x[p - L.sy]));
+    t = __dadd_rn(t, __dmul_rn(L.cyp[j], x[p + L.sy]));
+    t = __dadd_rn(t, __dmul_rn(L.czm[k], x[p - L.sz]));
+    t = __dadd_rn(t, __dmul_rn(L.czp[k], x[p + L.sz]));
+    return t;
+}
+
 __device__ __forceinline__ double ax_cell_f64(const LevelK<double> &L, const double *x, int i, int j, int k)
 {
     const long long p = lin(i, j, k, L.sy, L.sz);

@@ -319,7 +319,7 @@ int dd_rbgs(Dd &D, int l, int maxit, double omega)
             for (int r = 0; r < D.nr; ++r) {
                 Ctx &C = *D.rk[r];
                 PMG_TRY_D(f64_rbgs_colour(C.K[l], C.launch[l], dd_array(D, r, l, 0), dd_array(D, r, l, 1), omega,
-                                          D.offset[(size_t)r * (D.nl + 1) + l] + c, D.stream));
+                                          D.offset[(size_t)r * (D.nl + 1) + l] + c, D.stream, C.diag(l)));
             }
         }
     return PMG_OK;
@@ -336,7 +336,7 @@ int dd_residual(Dd &D, int l, double *norm)
             PMG_TRY_D(C.residual_norm(l, dd_array(D, r, l, 2), dd_array(D, r, l, 0), dd_array(D, r, l, 1), 0));
         else
             PMG_TRY_D(f64_residual(C.K[l], C.launch[l], dd_array(D, r, l, 2), dd_array(D, r, l, 0),
-                                   dd_array(D, r, l, 1), nullptr, nullptr, D.stream));
+                                   dd_array(D, r, l, 1), nullptr, nullptr, D.stream, C.diag(l)));
     }
     if (norm) {
         double s = 0.0;

@@ -29,36 +29,57 @@ __device__ __forceinline__ int block_lin()
     return blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z);
 }
 
+// The diagonal c0 of cell p: read from the level's per-cell table (TAB; the values
+// k_diag_f64 stored, diag_f64's bits) or formed from the 1-D tables.  The table takes four
+// of the 28 FP64 instructions of an RBGS update off a pipe that bounds these kernels.
+template <bool TAB>
+__device__ __forceinline__ double diag_at(const LevelK<double> &L, const double *c0t, long long p, int i, int j,
+                                          int k)
+{
+    return TAB ? c0t[p] : diag_f64(L, i, j, k);
+}
+
 // One colour of the red-black sweep.  colour 0 is the reference's first half-sweep:
 // ista = 1 + mod(j+k, 2) (src/rbgs_poisson_matrix.f90:242); colour 1 the second
 // (:260).  Thread t of a row updates i = 2t + ista.
+template <bool TAB, bool OMEGA1>
 __global__ void __launch_bounds__(kBX *kBY) k_rbgs_f64(LevelK<double> L, double *__restrict__ x,
                                                        const double *__restrict__ b, double omega, double omw,
-                                                       int colour)
+                                                       int colour, const double *__restrict__ c0t)
 {
     for (int k = blockIdx.z + 1; k <= L.nz; k += gridDim.z)
         for (int j = blockIdx.y * blockDim.y + threadIdx.y + 1; j <= L.ny; j += gridDim.y * blockDim.y) {
             const int ista = 1 + ((j + k + colour) & 1);
             for (int i = ista + 2 * (blockIdx.x * blockDim.x + threadIdx.x); i <= L.nx;
                  i += 2 * gridDim.x * blockDim.x) {
-                const double v = rbgs_cell_f64(L, x, b, i, j, k, omega, omw);
-                x[lin(i, j, k, L.sy, L.sz)] = v;
+                const long long p = lin(i, j, k, L.sy, L.sz);
+                x[p] = rbgs_cell_c0_f64<OMEGA1>(L, x, b, i, j, k, omega, omw, diag_at<TAB>(L, c0t, p, i, j, k));
             }
         }
 }
 
+// c0t = the diagonal of every interior cell (diag_f64); the ghosts are left as they are.
+__global__ void __launch_bounds__(kBX *kBY) k_diag_f64(LevelK<double> L, double *__restrict__ c0t)
+{
+    for (int k = blockIdx.z + 1; k <= L.nz; k += gridDim.z)
+        for (int j = blockIdx.y * blockDim.y + threadIdx.y + 1; j <= L.ny; j += gridDim.y * blockDim.y)
+            for (int i = blockIdx.x * blockDim.x + threadIdx.x + 1; i <= L.nx; i += gridDim.x * blockDim.x)
+                c0t[lin(i, j, k, L.sy, L.sz)] = diag_f64(L, i, j, k);
+}
+
 // r = b - A x on the interior (src/multigrid.f90:1795-1805); optional per-block sum of r^2.
-template <bool NORM>
+template <bool NORM, bool TAB>
 __global__ void __launch_bounds__(kBX *kBY) k_residual_f64(LevelK<double> L, double *__restrict__ r,
                                                            const double *__restrict__ x,
-                                                           const double *__restrict__ b, double *partials)
+                                                           const double *__restrict__ b, double *partials,
+                                                           const double *__restrict__ c0t)
 {
     double acc = 0.0;
     for (int k = blockIdx.z + 1; k <= L.nz; k += gridDim.z)
         for (int j = blockIdx.y * blockDim.y + threadIdx.y + 1; j <= L.ny; j += gridDim.y * blockDim.y)
             for (int i = blockIdx.x * blockDim.x + threadIdx.x + 1; i <= L.nx; i += gridDim.x * blockDim.x) {
                 const long long p = lin(i, j, k, L.sy, L.sz);
-                const double v = __dsub_rn(b[p], ax_cell_f64(L, x, i, j, k));
+                const double v = __dsub_rn(b[p], ax_cell_c0_f64(L, x, i, j, k, diag_at<TAB>(L, c0t, p, i, j, k)));
                 r[p] = v;
                 if (NORM) acc = __dadd_rn(acc, __dmul_rn(v, v));
             }
@@ -69,13 +90,16 @@ __global__ void __launch_bounds__(kBX *kBY) k_residual_f64(LevelK<double> L, dou
     }
 }
 
+template <bool TAB>
 __global__ void __launch_bounds__(kBX *kBY) k_mvmul_f64(LevelK<double> L, double *__restrict__ y,
-                                                        const double *__restrict__ x)
+                                                        const double *__restrict__ x, const double *__restrict__ c0t)
 {
     for (int k = blockIdx.z + 1; k <= L.nz; k += gridDim.z)
         for (int j = blockIdx.y * blockDim.y + threadIdx.y + 1; j <= L.ny; j += gridDim.y * blockDim.y)
-            for (int i = blockIdx.x * blockDim.x + threadIdx.x + 1; i <= L.nx; i += gridDim.x * blockDim.x)
-                y[lin(i, j, k, L.sy, L.sz)] = ax_cell_f64(L, x, i, j, k);
+            for (int i = blockIdx.x * blockDim.x + threadIdx.x + 1; i <= L.nx; i += gridDim.x * blockDim.x) {
+                const long long p = lin(i, j, k, L.sy, L.sz);
+                y[p] = ax_cell_c0_f64(L, x, i, j, k, diag_at<TAB>(L, c0t, p, i, j, k));
+            }
 }
 
 __global__ void __launch_bounds__(kBX *kBY) k_dot_f64(LevelK<double> L, const double *__restrict__ x,
@@ -194,16 +218,18 @@ __device__ __forceinline__ double cg_sum_partials(const double *partials, double
 }
 
 // r = b - A x, p = r (src/cg_poisson_matrix.f90:80-91), rsd0tol = temp1 = r.r (:94, :107)
+template <bool TAB>
 __global__ void __launch_bounds__(kBX *kBY) k_cg_init(LevelK<double> L, double *__restrict__ r,
                                                       double *__restrict__ p, const double *__restrict__ x,
-                                                      const double *__restrict__ b, double *partials, CgState *st)
+                                                      const double *__restrict__ b, double *partials, CgState *st,
+                                                      const double *__restrict__ c0t)
 {
     double acc = 0.0;
     for (int k = blockIdx.z + 1; k <= L.nz; k += gridDim.z)
         for (int j = blockIdx.y * blockDim.y + threadIdx.y + 1; j <= L.ny; j += gridDim.y * blockDim.y)
             for (int i = blockIdx.x * blockDim.x + threadIdx.x + 1; i <= L.nx; i += gridDim.x * blockDim.x) {
                 const long long q = lin(i, j, k, L.sy, L.sz);
-                const double v = __dsub_rn(b[q], ax_cell_f64(L, x, i, j, k));
+                const double v = __dsub_rn(b[q], ax_cell_c0_f64(L, x, i, j, k, diag_at<TAB>(L, c0t, q, i, j, k)));
                 r[q] = v;
                 p[q] = v;
                 acc = __dadd_rn(acc, __dmul_rn(v, v));
@@ -224,8 +250,10 @@ __global__ void __launch_bounds__(kBX *kBY) k_cg_init(LevelK<double> L, double *
 }
 
 // Ap = A p (src/poisson_matrix_operator.f90:146-159), temp2 = Ap.p (:112), alpha (:114)
+template <bool TAB>
 __global__ void __launch_bounds__(kBX *kBY) k_cg_apdot(LevelK<double> L, const double *__restrict__ p,
-                                                       double *__restrict__ ap, double *partials, CgState *st)
+                                                       double *__restrict__ ap, double *partials, CgState *st,
+                                                       const double *__restrict__ c0t)
 {
     if (st->done) return;
     double acc = 0.0;
@@ -233,7 +261,7 @@ __global__ void __launch_bounds__(kBX *kBY) k_cg_apdot(LevelK<double> L, const d
         for (int j = blockIdx.y * blockDim.y + threadIdx.y + 1; j <= L.ny; j += gridDim.y * blockDim.y)
             for (int i = blockIdx.x * blockDim.x + threadIdx.x + 1; i <= L.nx; i += gridDim.x * blockDim.x) {
                 const long long q = lin(i, j, k, L.sy, L.sz);
-                const double v = ax_cell_f64(L, p, i, j, k);
+                const double v = ax_cell_c0_f64(L, p, i, j, k, diag_at<TAB>(L, c0t, q, i, j, k));
                 ap[q] = v;
                 acc = __dadd_rn(acc, __dmul_rn(v, p[q]));
             }
@@ -439,44 +467,76 @@ void grid_for_cells(const LevelK<double> &L, const Launch &ln, dim3 *grid, dim3 
     *block = dim3(kBX, kBY, 1);
 }
 
+static void launch_rbgs_colour(const LevelK<double> &L, dim3 g, double *x, const double *b, double omega,
+                               double omw, int colour, const double *c0t, cudaStream_t s)
+{
+    const dim3 bl(kBX, kBY, 1);
+    // omega == 1 exactly: 1 * v is v for every double, so the OMEGA1 kernel's bits are the same
+    if (c0t && omega == 1.0)
+        k_rbgs_f64<true, true><<<g, bl, 0, s>>>(L, x, b, omega, omw, colour, c0t);
+    else if (c0t)
+        k_rbgs_f64<true, false><<<g, bl, 0, s>>>(L, x, b, omega, omw, colour, c0t);
+    else if (omega == 1.0)
+        k_rbgs_f64<false, true><<<g, bl, 0, s>>>(L, x, b, omega, omw, colour, nullptr);
+    else
+        k_rbgs_f64<false, false><<<g, bl, 0, s>>>(L, x, b, omega, omw, colour, nullptr);
+}
+
 int f64_rbgs_sweeps(const LevelK<double> &L, const Launch &ln, double *x, const double *b, int iters,
-                    double omega, cudaStream_t s)
+                    double omega, cudaStream_t s, const double *c0t)
 {
     const double omw = 1.0 - omega;   // (1.0d0-omega), src/rbgs_poisson_matrix.f90:250
-    const dim3 g = grid3((L.nx + 1) / 2, L.ny, L.nz, ln), bl(kBX, kBY, 1);
+    const dim3 g = grid3((L.nx + 1) / 2, L.ny, L.nz, ln);
     for (int it = 0; it < iters; ++it)
-        for (int c = 0; c < 2; ++c) k_rbgs_f64<<<g, bl, 0, s>>>(L, x, b, omega, omw, c);
+        for (int c = 0; c < 2; ++c) launch_rbgs_colour(L, g, x, b, omega, omw, c, c0t, s);
     count_launches(2LL * iters);
     return cuda_status(cudaGetLastError(), "rbgs sweep");
 }
 
 int f64_rbgs_colour(const LevelK<double> &L, const Launch &ln, double *x, const double *b, double omega, int colour,
-                    cudaStream_t s)
+                    cudaStream_t s, const double *c0t)
 {
-    const dim3 g = grid3((L.nx + 1) / 2, L.ny, L.nz, ln), bl(kBX, kBY, 1);
-    k_rbgs_f64<<<g, bl, 0, s>>>(L, x, b, omega, 1.0 - omega, colour & 1);
+    const dim3 g = grid3((L.nx + 1) / 2, L.ny, L.nz, ln);
+    launch_rbgs_colour(L, g, x, b, omega, 1.0 - omega, colour & 1, c0t, s);
     count_launches(1);
     return cuda_status(cudaGetLastError(), "rbgs half-sweep");
 }
 
+int f64_diag_table(const LevelK<double> &L, double *c0t, cudaStream_t s)
+{
+    const dim3 g = grid3(L.nx, L.ny, L.nz, Launch{{false, false, false}}), bl(kBX, kBY, 1);
+    k_diag_f64<<<g, bl, 0, s>>>(L, c0t);
+    count_launches(1);
+    return cuda_status(cudaGetLastError(), "diagonal table");
+}
+
 int f64_residual(const LevelK<double> &L, const Launch &ln, double *r, const double *x, const double *b,
-                 double *partials, int *npart, cudaStream_t s)
+                 double *partials, int *npart, cudaStream_t s, const double *c0t)
 {
     const dim3 g = grid3(L.nx, L.ny, L.nz, ln), bl(kBX, kBY, 1);
     if (partials) {
-        k_residual_f64<true><<<g, bl, 0, s>>>(L, r, x, b, partials);
+        if (c0t)
+            k_residual_f64<true, true><<<g, bl, 0, s>>>(L, r, x, b, partials, c0t);
+        else
+            k_residual_f64<true, false><<<g, bl, 0, s>>>(L, r, x, b, partials, nullptr);
         *npart = (int)(g.x * g.y * g.z);
+    } else if (c0t) {
+        k_residual_f64<false, true><<<g, bl, 0, s>>>(L, r, x, b, nullptr, c0t);
     } else {
-        k_residual_f64<false><<<g, bl, 0, s>>>(L, r, x, b, nullptr);
+        k_residual_f64<false, false><<<g, bl, 0, s>>>(L, r, x, b, nullptr, nullptr);
     }
     count_launches(1);
     return cuda_status(cudaGetLastError(), "residual");
 }
 
-int f64_mv_mul(const LevelK<double> &L, const Launch &ln, double *y, const double *x, cudaStream_t s)
+int f64_mv_mul(const LevelK<double> &L, const Launch &ln, double *y, const double *x, cudaStream_t s,
+               const double *c0t)
 {
     const dim3 g = grid3(L.nx, L.ny, L.nz, ln), bl(kBX, kBY, 1);
-    k_mvmul_f64<<<g, bl, 0, s>>>(L, y, x);
+    if (c0t)
+        k_mvmul_f64<true><<<g, bl, 0, s>>>(L, y, x, c0t);
+    else
+        k_mvmul_f64<false><<<g, bl, 0, s>>>(L, y, x, nullptr);
     count_launches(1);
     return cuda_status(cudaGetLastError(), "mv_mul");
 }
@@ -565,18 +625,25 @@ int f64_cg_partials(const LevelK<double> &L, const Launch &ln)
 }
 
 int f64_cg_init(const LevelK<double> &L, const Launch &ln, double *r, double *p, const double *x, const double *b,
-                double *partials, CgState *st, cudaStream_t s)
+                double *partials, CgState *st, cudaStream_t s, const double *c0t)
 {
-    k_cg_init<<<cg_grid(L, ln), dim3(kBX, kBY, 1), 0, s>>>(L, r, p, x, b, partials, st);
+    if (c0t)
+        k_cg_init<true><<<cg_grid(L, ln), dim3(kBX, kBY, 1), 0, s>>>(L, r, p, x, b, partials, st, c0t);
+    else
+        k_cg_init<false><<<cg_grid(L, ln), dim3(kBX, kBY, 1), 0, s>>>(L, r, p, x, b, partials, st, nullptr);
     count_launches(1);
     return cuda_status(cudaGetLastError(), "cg init");
 }
 
 int f64_cg_iteration(const LevelK<double> &L, const Launch &ln, double *x, double *r, double *p, double *ap,
-                     double *partials, CgState *st, double tol, bool check, int iter, cudaStream_t s)
+                     double *partials, CgState *st, double tol, bool check, int iter, cudaStream_t s,
+                     const double *c0t)
 {
     const dim3 g = cg_grid(L, ln), bl(kBX, kBY, 1);
-    k_cg_apdot<<<g, bl, 0, s>>>(L, p, ap, partials, st);
+    if (c0t)
+        k_cg_apdot<true><<<g, bl, 0, s>>>(L, p, ap, partials, st, c0t);
+    else
+        k_cg_apdot<false><<<g, bl, 0, s>>>(L, p, ap, partials, st, nullptr);
     k_cg_update<<<g, bl, 0, s>>>(L, x, r, p, ap, partials, st, tol, check ? 1 : 0, iter);
     k_cg_p<<<g, bl, 0, s>>>(L, p, r, st);
     count_launches(3);

@@ -64,17 +64,22 @@ struct HierDesc {
 // ---- FP64 (bitwise) launchers, pmg_f64.cu -------------------------------------
 // Builds the coarse meshes (unless given) and every level's tables on the device.
 int hierarchy_setup(const HierDesc *dev_desc, double *meshes, double *tables, cudaStream_t s);
+// c0t (optional, every FP64 grid launcher below): the level's per-cell diagonal table
+// (f64_diag_table), read instead of summing the 1-D tables per cell; the same bits.
 int f64_rbgs_sweeps(const LevelK<double> &L, const Launch &ln, double *x, const double *b, int iters,
-                    double omega, cudaStream_t s);
+                    double omega, cudaStream_t s, const double *c0t = nullptr);
 // One half-sweep: the cells with (i + j + k + colour) odd, i.e. ista = 1 + mod(j+k+colour, 2)
 // (src/rbgs_poisson_matrix.f90:242, :260; colour carries a rank's parity offset).
 int f64_rbgs_colour(const LevelK<double> &L, const Launch &ln, double *x, const double *b, double omega, int colour,
-                    cudaStream_t s);
+                    cudaStream_t s, const double *c0t = nullptr);
+// c0t = diag_f64 of every interior cell of level L (an array of the level's layout).
+int f64_diag_table(const LevelK<double> &L, double *c0t, cudaStream_t s);
 // r = b - A x (interior); if partials != nullptr also writes per-block sums of r^2
 // and returns the number of partials in *npart.
 int f64_residual(const LevelK<double> &L, const Launch &ln, double *r, const double *x, const double *b,
-                 double *partials, int *npart, cudaStream_t s);
-int f64_mv_mul(const LevelK<double> &L, const Launch &ln, double *y, const double *x, cudaStream_t s);
+                 double *partials, int *npart, cudaStream_t s, const double *c0t = nullptr);
+int f64_mv_mul(const LevelK<double> &L, const Launch &ln, double *y, const double *x, cudaStream_t s,
+               const double *c0t = nullptr);
 int f64_dot_partials(const LevelK<double> &L, const Launch &ln, const double *x, const double *y,
                      double *partials, int *npart, cudaStream_t s);
 // Sum partials[0..n) in a fixed order into *out (device).
@@ -103,11 +108,12 @@ struct CgState {
 int f64_cg_partials(const LevelK<double> &L, const Launch &ln);
 // r = b - A x, p = r, st->r0 = st->t1 = r.r, st->done = 0.
 int f64_cg_init(const LevelK<double> &L, const Launch &ln, double *r, double *p, const double *x, const double *b,
-                double *partials, CgState *st, cudaStream_t s);
+                double *partials, CgState *st, cudaStream_t s, const double *c0t = nullptr);
 // One CG iteration (three fused kernels); with check, the exit test sqrt(t2/r0) < tol sets
 // st->done and st->iter = iter, after which further iterations do nothing.
 int f64_cg_iteration(const LevelK<double> &L, const Launch &ln, double *x, double *r, double *p, double *ap,
-                     double *partials, CgState *st, double tol, bool check, int iter, cudaStream_t s);
+                     double *partials, CgState *st, double tol, bool check, int iter, cudaStream_t s,
+                     const double *c0t = nullptr);
 
 // ---- FP64 performance mode, pmg_f64fast.cu -----------------------------------------
 // Tables of one grid level: per-axis diagonal sums (x: LevelK::sx) and omega / c0 per cell.
