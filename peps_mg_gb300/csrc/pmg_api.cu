@@ -17,6 +17,7 @@
 #include <mutex>
 #include <new>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "../../include/peps_mg.h"
@@ -1260,6 +1261,40 @@ struct HostRegistration {
     ~HostRegistration() { release(); }
 };
 
+// True when every 64-bit word of the host array is zero (+0.0 everywhere, ghosts
+// included: the test of the device-side zero test, k_nonzero_f64).  Scanned by up to 16
+// host threads, each stopping at the first non-zero word it sees or once another thread
+// has found one; a solve from a zero initial guess then sends no initial guess over the
+// host link at all (the staging buffer is cleared on the device instead), and the scan runs
+// while the right-hand side is being copied.
+static bool host_all_zero(const double *a, size_t n)
+{
+    const unsigned long long *u = reinterpret_cast<const unsigned long long *>(a);
+    std::atomic<bool> found{false};
+    auto scan = [&](size_t b, size_t e) {
+        size_t q = b;
+        while (q < e && !found.load(std::memory_order_relaxed)) {
+            const size_t stop = std::min(e, q + 4096);
+            unsigned long long bits = 0;
+            for (; q < stop; ++q) bits |= u[q];
+            if (bits) found.store(true, std::memory_order_relaxed);
+        }
+    };
+    const size_t per_thread = (size_t)1 << 23;   // 64 MB
+    const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
+    const unsigned nt = (unsigned)std::min<size_t>(std::min(16u, hw), std::max<size_t>(1, n / per_thread));
+    if (nt <= 1) {
+        scan(0, n);
+        return !found.load();
+    }
+    std::vector<std::thread> th;
+    const size_t chunk = (n + nt - 1) / nt;
+    for (unsigned t = 1; t < nt; ++t) th.emplace_back(scan, std::min(n, t * chunk), std::min(n, (t + 1) * chunk));
+    scan(0, std::min(n, chunk));
+    for (auto &x : th) x.join();
+    return !found.load();
+}
+
 int Ctx::early_copy_sol(const double *sol)
 {
     if (!early_sol_host) return PMG_OK;
@@ -1316,8 +1351,13 @@ int Ctx::solve(double *sol, double *rsd, const double *rhs, int maxit, double to
             stage_rsd = a[1];
             stage_rhs = a[2];
         }
-        PMG_CUDA(cudaMemcpyAsync(stage_sol, sol, bytes, cudaMemcpyHostToDevice, stream), "H2D");
+        // the right-hand side first; the initial guess only if it is not all zero (tested
+        // on the host while the right-hand side is on its way)
         PMG_CUDA(cudaMemcpyAsync(stage_rhs, rhs, bytes, cudaMemcpyHostToDevice, stream), "H2D");
+        if (host_all_zero(sol, lv[0].total))
+            PMG_CUDA(cudaMemsetAsync(stage_sol, 0, bytes, stream), "staging init");
+        else
+            PMG_CUDA(cudaMemcpyAsync(stage_sol, sol, bytes, cudaMemcpyHostToDevice, stream), "H2D");
         s = stage_sol;
         r = stage_rsd;
         b = stage_rhs;
