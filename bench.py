@@ -539,8 +539,10 @@ def run_ours(args):
                         "frac": round(cg_gbs / peak, 4), "bytes_per_cell": 88,
                         "workload": "fused CG iterations (cg_iterator) on the 512^3 level, FP64 bitwise"},
             "cpu_baseline": cpu,
-            "e2e": {"value": round(e2e_ms, 3), "unit": "ms", "h2d_bytes_per_step": 2 * nbytes,
-                    "d2h_bytes_per_step": 2 * nbytes,
+            # host to device: the right-hand side; the initial guess (x0 = 0 here) is scanned on
+            # the host and not sent.  Device to host: the solution and the residual.
+            "e2e": {"value": round(e2e_ms, 3), "unit": "ms", "h2d_bytes_per_step": nbytes,
+                    "d2h_bytes_per_step": 2 * nbytes, "initial_guess": "zero (scanned on the host, not copied)",
                     "stream_ms": round(statistics.mean(e2e_stream), 3),
                     "host_buffers": "pinned",
                     "pageable_ms": round(statistics.mean(pageable), 3),

@@ -1354,7 +1354,8 @@ int Ctx::solve(double *sol, double *rsd, const double *rhs, int maxit, double to
         // the right-hand side first; the initial guess only if it is not all zero (tested
         // on the host while the right-hand side is on its way)
         PMG_CUDA(cudaMemcpyAsync(stage_rhs, rhs, bytes, cudaMemcpyHostToDevice, stream), "H2D");
-        if (host_all_zero(sol, lv[0].total))
+        x0_known_zero = host_all_zero(sol, lv[0].total);
+        if (x0_known_zero)
             PMG_CUDA(cudaMemsetAsync(stage_sol, 0, bytes, stream), "staging init");
         else
             PMG_CUDA(cudaMemcpyAsync(stage_sol, sol, bytes, cudaMemcpyHostToDevice, stream), "H2D");
@@ -1366,6 +1367,7 @@ int Ctx::solve(double *sol, double *rsd, const double *rhs, int maxit, double to
     early_valid = early_pending = false;
     int rc = precision == PMG_MIXED ? solve_mixed(s, r, b, maxit, tol, omega, rep)
                                     : solve_f64(s, r, b, maxit, tol, omega, rep);
+    x0_known_zero = false;
     early_sol_host = nullptr;
     if (rc != PMG_OK && rc != PMG_EDIVERGED) {
         if (early_pending) cudaStreamWaitEvent(stream, ev_copied, 0);

@@ -79,6 +79,7 @@ struct Ctx {
     double *d_cp = nullptr, *d_cap = nullptr, *d_crr = nullptr;
     CgState *d_cg = nullptr;   // scalars of the fused CG solver (lower API, large coarsest levels)
     std::vector<double *> c0t; // plain FP64 contexts: per-cell diagonal of every level (f64_diag_table)
+    bool x0_known_zero = false; // the staged initial guess of the running solve is all zero (host scan)
     const double *diag(int l) const { return (size_t)l < c0t.size() ? c0t[l] : nullptr; }
     // Abort flag (pmg_set_abort) in mapped page-locked host memory: the host loops read it
     // between cycles, the coarse solvers of the single-CTA tails poll it on the device.

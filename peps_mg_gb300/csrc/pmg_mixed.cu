@@ -771,11 +771,14 @@ int Ctx::outer_residual(double *sol, double *rsd, const double *rhs, int slot)
     int *nonzero = d_iscal + 3;
     if (slot == 0) {
         // the first residual of a solve: is the initial guess exactly zero?
+        // (skipped when a staged solve's host scan already found it zero)
         PMG_TRY_M(mstatus(cudaMemsetAsync(nonzero, 0, sizeof(int), stream), "zero test"));
         const long long n = (long long)lv[0].total;
-        k_nonzero_f64<<<(unsigned)std::max<long long>(1, std::min<long long>((n + 1023) / 1024, 4096)), 256, 0,
-                        stream>>>(sol, n, nonzero);
-        count_launches(1);
+        if (!x0_known_zero) {
+            k_nonzero_f64<<<(unsigned)std::max<long long>(1, std::min<long long>((n + 1023) / 1024, 4096)), 256, 0,
+                            stream>>>(sol, n, nonzero);
+            count_launches(1);
+        }
     }
     const int pi = prof.begin(stream);
     if (slot == 0)
