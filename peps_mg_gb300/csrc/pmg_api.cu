@@ -964,7 +964,11 @@ int Ctx::vcycle_f64(double *sol, double *rsd, const double *rhs, int maxit, doub
         return fast ? fast_prolong(X[l], fastX[l], launch[l + 1], vc, vf, stream)
                     : f64_prolong(X[l], launch[l + 1], vc, vf, true, stream);
     };
-    const double sweep_bytes = fast ? 20.0 : 16.0;
+    // algorithmic bytes per cell: a half-sweep reads x and half of b and writes half of x
+    // (16 B), plus half a diagonal value (4 B) where one is stored per cell (the performance
+    // mode's omega/c0, the plain path's c0); the residual 24 B, plus 8 B of the stored c0
+    const bool tab = !fast && diag(0);
+    const double sweep_bytes = (fast || tab) ? 20.0 : 16.0, resid_bytes = tab ? 32.0 : 24.0;
     int pi = prof.begin(stream);
     {
         NvtxRange r("pre-smoothing");
@@ -974,18 +978,18 @@ int Ctx::vcycle_f64(double *sol, double *rsd, const double *rhs, int maxit, doub
     NvtxRange down_range("residual, restriction, coarse levels, tail, prolongation");
     pi = prof.begin(stream);
     PMG_TRY(resid(0, rsd, sol, rhs));
-    prof.end(pi, PC_RES64, 1, 24.0 * N, stream);
+    prof.end(pi, PC_RES64, 1, resid_bytes * N, stream);
     pi = prof.begin(stream);
     PMG_TRY(restr(0, rsd, lv[1].b));
     prof.end(pi, PC_RESTRICT64, 1, 9.0 * N, stream);
     // grid levels below the finest, one profiler record each way: per cell of level l,
-    // 16 B per half-sweep, 24 B residual, 9 B restriction (down); 17 B prolongation + add,
-    // 16 B per half-sweep (up)
+    // sweep_bytes per half-sweep, resid_bytes residual, 9 B restriction (down); 17 B
+    // prolongation + add, sweep_bytes per half-sweep (up)
     auto coarse_bytes = [&](bool down) {
         double b = 0.0;
         for (int l = 1; l < grid_end; ++l) {
             const double n = (double)K[l].nx * K[l].ny * K[l].nz;
-            b += down ? (2.0 * sweep_bytes * maxit + 24.0 + 9.0) * n : (17.0 + 2.0 * sweep_bytes * maxit) * n;
+            b += down ? (2.0 * sweep_bytes * maxit + resid_bytes + 9.0) * n : (17.0 + 2.0 * sweep_bytes * maxit) * n;
         }
         return b;
     };
@@ -1083,7 +1087,7 @@ int Ctx::solve_f64(double *sol, double *rsd, const double *rhs, int maxit, doubl
         PMG_TRY(vcycle_f64(sol, rsd, rhs, maxit, omega, tol, rep && rep->coarse_iterations ? &ci : nullptr));
         int pr = prof.begin(stream);
         PMG_TRY(solve_residual_norm(rsd, sol, rhs, 1));  // :1970-1971
-        prof.end(pr, PC_RES64, 1, 24.0 * (double)K[0].nx * K[0].ny * K[0].nz, stream);
+        prof.end(pr, PC_RES64, 1, (!fast64 && diag(0) ? 32.0 : 24.0) * (double)K[0].nx * K[0].ny * K[0].nz, stream);
         PMG_TRY(fetch_scalars(h, 2));
         const double rsd_val = h[1];
         ratio = std::sqrt(rsd_val / res0tol);
