@@ -1293,8 +1293,16 @@ static bool host_all_zero(const double *a, size_t n)
     }
     std::vector<std::thread> th;
     const size_t chunk = (n + nt - 1) / nt;
-    for (unsigned t = 1; t < nt; ++t) th.emplace_back(scan, std::min(n, t * chunk), std::min(n, (t + 1) * chunk));
+    unsigned started = 1;
+    try {
+        for (; started < nt; ++started)
+            th.emplace_back(scan, std::min(n, started * chunk), std::min(n, (started + 1) * chunk));
+    } catch (...) {
+        // no thread to be had: the remaining chunks are scanned here (no exception may
+        // leave the C interface)
+    }
     scan(0, std::min(n, chunk));
+    for (unsigned t = started; t < nt; ++t) scan(std::min(n, t * chunk), std::min(n, (t + 1) * chunk));
     for (auto &x : th) x.join();
     return !found.load();
 }
