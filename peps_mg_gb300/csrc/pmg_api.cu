@@ -1452,7 +1452,7 @@ int pmg_create(pmg_ctx **ctx, const pmg_config_t *cfg, void *stream)
     pmg::NvtxRange r("pmg_create");
     pmg_ctx *c = new (std::nothrow) pmg_ctx();
     if (!c) return PMG_ENOMEM;
-    const int rc = c->impl.build(cfg, (cudaStream_t)stream);
+    const int rc = pmg::guarded([&] { return c->impl.build(cfg, (cudaStream_t)stream); });
     if (rc != PMG_OK) {
         delete c;
         return rc;
@@ -1476,7 +1476,7 @@ int pmg_solve_vcycle(pmg_ctx *ctx, double *sol, double *rsd, const double *rhs, 
         pmg::set_error("null context");
         return PMG_EINVAL;
     }
-    return ctx->impl.solve(sol, rsd, rhs, maxiteration, tolerance, omega_sor, report);
+    return pmg::guarded([&] { return ctx->impl.solve(sol, rsd, rhs, maxiteration, tolerance, omega_sor, report); });
 }
 
 int pmg_level_sizes(int nx, int ny, int nz, int n_levels, int aggregation_method, int cga_level, int *sizes,
@@ -1634,7 +1634,7 @@ int pmg_adjoint(pmg_ctx *ctx, const double *dLdu, double *dLdb, double dLdg[6], 
         pmg::set_error("pmg_adjoint takes device arrays");
         return PMG_EINVAL;
     }
-    return ctx->impl.adjoint(dLdu, dLdb, dLdg, maxiteration, tolerance, omega_sor, report);
+    return pmg::guarded([&] { return ctx->impl.adjoint(dLdu, dLdb, dLdg, maxiteration, tolerance, omega_sor, report); });
 }
 
 struct pmg_batch {
@@ -1650,7 +1650,8 @@ int pmg_batch_create(pmg_batch **batch, int n_problems, const int *dims, const d
     }
     *batch = nullptr;
     pmg::Batch *b = nullptr;
-    const int rc = pmg::batch_create(&b, n_problems, dims, meshes, mixed_inner_cycles, (cudaStream_t)stream);
+    const int rc = pmg::guarded(
+        [&] { return pmg::batch_create(&b, n_problems, dims, meshes, mixed_inner_cycles, (cudaStream_t)stream); });
     if (rc != PMG_OK) return rc;
     pmg_batch *h = new (std::nothrow) pmg_batch{b};
     if (!h) {
@@ -1672,8 +1673,10 @@ int pmg_batch_solve(pmg_batch *batch, double *sol, const double *rhs, int maxite
                     double omega_sor, int max_cycles, int *cycles, double *ratio, float *elapsed_ms)
 {
     if (!batch) return PMG_EINVAL;
-    return pmg::batch_solve(*batch->impl, sol, rhs, maxiteration, tolerance, omega_sor, max_cycles, cycles, ratio,
-                            elapsed_ms);
+    return pmg::guarded([&] {
+        return pmg::batch_solve(*batch->impl, sol, rhs, maxiteration, tolerance, omega_sor, max_cycles, cycles, ratio,
+                                elapsed_ms);
+    });
 }
 
 int pmg_batch_destroy(pmg_batch *batch)

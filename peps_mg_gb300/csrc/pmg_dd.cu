@@ -500,7 +500,7 @@ int pmg_dd_create(pmg_dd **dd, const pmg_config_t *cfg, const int procs[3], void
     }
     *dd = nullptr;
     pmg::Dd *d = nullptr;
-    const int rc = pmg::dd_create(&d, cfg, procs, static_cast<cudaStream_t>(stream));
+    const int rc = pmg::guarded([&] { return pmg::dd_create(&d, cfg, procs, static_cast<cudaStream_t>(stream)); });
     if (rc != PMG_OK) return rc;
     pmg_dd *h = new (std::nothrow) pmg_dd{d};
     if (!h) {
@@ -518,7 +518,7 @@ int pmg_dd_solve(pmg_dd *dd, double *sol, double *rsd, const double *rhs, int ma
         pmg::set_error("invalid decomposed solve arguments");
         return PMG_EINVAL;
     }
-    return pmg::dd_solve(*dd->impl, sol, rsd, rhs, maxiteration, tolerance, omega_sor, report);
+    return pmg::guarded([&] { return pmg::dd_solve(*dd->impl, sol, rsd, rhs, maxiteration, tolerance, omega_sor, report); });
 }
 
 int pmg_dd_destroy(pmg_dd *dd)

@@ -5,9 +5,12 @@
 #include <cuda_runtime.h>
 #include <nvtx3/nvToolsExt.h>
 
+#include <exception>
+#include <new>
 #include <string>
 #include <vector>
 
+#include "../../include/peps_mg.h"
 #include "pmg_common.cuh"
 
 namespace pmg {
@@ -259,5 +262,24 @@ struct NvtxRange {
 // ---- errors ---------------------------------------------------------------------
 void set_error(const std::string &msg);
 int cuda_status(cudaError_t e, const char *what);
+
+// Runs f() (returning a status) so that no C++ exception leaves the C interface: a host
+// allocation that throws becomes PMG_ENOMEM, anything else PMG_ECUDA with its message.
+template <class F>
+int guarded(F &&f)
+{
+    try {
+        return f();
+    } catch (const std::bad_alloc &) {
+        set_error("host allocation failed");
+        return PMG_ENOMEM;
+    } catch (const std::exception &e) {
+        set_error(std::string("internal error: ") + e.what());
+        return PMG_ECUDA;
+    } catch (...) {
+        set_error("internal error");
+        return PMG_ECUDA;
+    }
+}
 
 }  // namespace pmg
