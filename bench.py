@@ -544,6 +544,8 @@ def run_ours(args):
             "e2e": {"value": round(e2e_ms, 3), "unit": "ms", "h2d_bytes_per_step": nbytes,
                     "d2h_bytes_per_step": 2 * nbytes, "initial_guess": "zero (scanned on the host, not copied)",
                     "stream_ms": round(statistics.mean(e2e_stream), 3),
+                    "median_ms": round(statistics.median(e2e), 3),
+                    "steps_ms": [round(v, 2) for v in e2e],
                     "host_buffers": "pinned",
                     "pageable_ms": round(statistics.mean(pageable), 3),
                     "pageable_stream_ms": round(statistics.mean(pageable_stream), 3),
