@@ -80,6 +80,24 @@ __global__ void __launch_bounds__(kBX *kBY, 4) k_resrestrict32(LevelK<float> F, 
                 bc[lin(i, j, k, X.csy, X.csz)] = resrestrict_cell32(F, X, e, b, i, j, k);
 }
 
+// Squared norm of the finest level's inner residual b - A e (FP32 cells, FP64 sum; one
+// partial per CTA): the estimate of the outer residual after a correction that ends a
+// correction's V-cycles early (Ctx::run_vcycles).
+__global__ void __launch_bounds__(kBX *kBY) k_inner_norm(LevelK<float> L, const float *__restrict__ e,
+                                                        const float *__restrict__ b, double *partials)
+{
+    double acc = 0.0;
+    for (int k = blockIdx.z + 1; k <= L.nz; k += gridDim.z)
+        for (int j = blockIdx.y * blockDim.y + threadIdx.y + 1; j <= L.ny; j += gridDim.y * blockDim.y)
+            for (int i = blockIdx.x * blockDim.x + threadIdx.x + 1; i <= L.nx; i += gridDim.x * blockDim.x) {
+                const double v = resid32(L, e, b, i, j, k);
+                acc = fma(v, v, acc);
+            }
+    __shared__ double sw[kBX * kBY / 32];
+    const double s = block_sum(acc, sw);
+    if (tid2() == 0) partials[blin()] = s;
+}
+
 // e_f += P e_c with one thread per fine x-pair (the two x-children of a coarse cell share
 // its coarse values), or per fine cell along an x-axis that is no longer coarsened.
 __global__ void __launch_bounds__(kBX *kBY) k_prolong_add32(XferK<float> X, int nfy, int nfz,
@@ -799,12 +817,48 @@ int Ctx::outer_residual(double *sol, double *rsd, const double *rhs, int slot)
 // the first solve and again when maxit or omega change.  Back-to-back launches of the small
 // levels' kernels cost about 4 us each on the device, about 1 us inside a graph.  With the
 // event profiler on, the kernels are launched one by one.
-int Ctx::run_vcycles(int maxit, double omega)
+// The inner residual's squared norm at the finest level into *out (synchronises).
+int Ctx::inner_norm(double *out)
+{
+    MixedState *m = mixed;
+    const dim3 g = grid_outer(K[0], launch[0]), bl(kBX, kBY, 1);
+    k_inner_norm<<<g, bl, 0, stream>>>(m->K[0], m->E(0), m->b[0], d_partials);
+    count_launches(1);
+    PMG_TRY_M(cuda_status(cudaGetLastError(), "inner residual norm"));
+    PMG_TRY_M(f64_reduce(d_partials, (int)(g.x * g.y * g.z), d_scal + 2, stream));
+    double h[3];
+    PMG_TRY_M(fetch_scalars(h, 3));
+    *out = h[2];
+    return PMG_OK;
+}
+
+// The FP32 V-cycles of one correction: m->inner cycles, or (check_after > 0) fewer when,
+// after check_after of them, the inner residual's squared norm is below thresh2 (the
+// outer residual the correction leaves is that residual to about 1e-14 of the initial
+// one, so the FP64 recompute that follows confirms the stop).  *ran = cycles run.
+int Ctx::run_vcycles(int maxit, double omega, int check_after, double thresh2, int *ran)
 {
     NvtxRange nvtx_range("FP32 V-cycles of a correction");
     MixedState *m = mixed;
+    if (ran) *ran = m->inner;
+    auto stop_here = [&](int done, bool *stop) -> int {
+        *stop = false;
+        if (check_after <= 0 || done != check_after || done >= m->inner) return PMG_OK;
+        double v = 0.0;
+        PMG_TRY_M(inner_norm(&v));
+        if (std::isfinite(v) && v < thresh2) {
+            *stop = true;
+            if (ran) *ran = done;
+        }
+        return PMG_OK;
+    };
     if (prof.on || !m->use_graphs) {
-        for (int q = 0; q < m->inner; ++q) PMG_TRY_M(vcycle32(maxit, omega, q == 0));
+        for (int q = 0; q < m->inner; ++q) {
+            PMG_TRY_M(vcycle32(maxit, omega, q == 0));
+            bool stop = false;
+            PMG_TRY_M(stop_here(q + 1, &stop));
+            if (stop) break;
+        }
         return PMG_OK;
     }
     if (!m->vgraph[0] || m->vgraph_maxit != maxit || m->vgraph_omega != omega) {
@@ -844,6 +898,9 @@ int Ctx::run_vcycles(int maxit, double omega)
         const int f = q == 0 ? 0 : 1;
         PMG_TRY_M(mstatus(cudaGraphLaunch(m->vgraph[f], stream), "V-cycle graph launch"));
         count_launches(m->vgraph_launches[f]);
+        bool stop = false;
+        PMG_TRY_M(stop_here(q + 1, &stop));
+        if (stop) break;
     }
     return PMG_OK;
 }
@@ -931,9 +988,24 @@ int Ctx::solve_mixed(double *sol, double *rsd, const double *rhs, int maxit, dou
             }
             return abort_status();
         }
-        PMG_TRY_M(run_vcycles(maxit, omega));
-        inner_total += m->inner;
         const bool recompute = !m->update_residual || cyc == n_vcycles || prev_ratio * contraction < 0.1 * tol;
+        // A correction predicted to end the solve stops its V-cycles once the residual it
+        // leaves is below 0.95 tol: the cycles it needs at the last correction's rate per
+        // cycle, checked by one inner residual norm (the reference stops as soon as a cycle
+        // meets the tolerance, src/multigrid.f90:1973).
+        int check_after = 0;
+        double thresh2 = 0.0;
+        if (recompute && cyc > 1 && m->inner > 1 && contraction > 0.0 && contraction < 1.0 && prev_ratio > 0.0) {
+            const double per_cycle = std::pow(contraction, 1.0 / m->inner);
+            const double need = std::log(0.95 * tol / prev_ratio) / std::log(per_cycle);
+            if (std::isfinite(need) && need < m->inner - 0.5) {
+                check_after = std::max(1, (int)std::ceil(need));
+                thresh2 = 0.95 * 0.95 * tol * tol * res0tol;
+            }
+        }
+        int ran = m->inner;
+        PMG_TRY_M(run_vcycles(maxit, omega, check_after, thresh2, &ran));
+        inner_total += ran;
         if (recompute) {
             PMG_TRY_M(correct_and_recompute(sol, rsd, rhs));
             PMG_TRY_M(fetch_scalars(h, 2));

@@ -47,7 +47,9 @@ def test_mixed_sine_64(inner):
     ref, _ = oracle_solution(mesh, rhs, 4)
     sol, rsd, rep = mixed_solve(mesh, rhs, 4, inner=inner)
     assert rep.converged and rep.final_ratio < 1e-10
-    assert rep.inner_cycles == inner * rep.cycles
+    # every correction runs `inner` FP32 cycles, except that the last may stop early once
+    # the residual it leaves is below the tolerance
+    assert inner * (rep.cycles - 1) < rep.inner_cycles <= inner * rep.cycles
     assert rel(sol, ref) < SOL_TOL
     # the returned residual is the FP64 residual of the returned solution; at a 1e-10
     # relative residual both evaluations carry rounding noise of order 1e-13 |b|, so the
