@@ -227,9 +227,13 @@ __device__ __forceinline__ void prolong_column_march32(const XferK<float> &X, in
 // loads) is held for planes k-1 .. k+1 in registers; x- and y-neighbours and b are loaded
 // per plane.  Residuals and the restriction sum are those of resrestrict_cell32 (same
 // operations, same order).
+// NORM: also adds the squares of the fine residuals, times nscale^2 (a power of two that
+// keeps them in FP32's range), to *ss.
+template <bool NORM = false>
 __device__ __forceinline__ void resrestrict_column_march32(const LevelK<float> &F, const XferK<float> &X, int ic,
                                                            int jc, int m0, int m1, const float *__restrict__ e,
-                                                           const float *__restrict__ b, float *__restrict__ bc)
+                                                           const float *__restrict__ b, float *__restrict__ bc,
+                                                           float nscale = 1.f, float *ss = nullptr)
 {
     const int jz = 2 * jc - 1, jp = 2 * jc;
     const int iz = 2 * ic - 1, ip = 2 * ic;
@@ -311,6 +315,14 @@ __device__ __forceinline__ void resrestrict_column_march32(const LevelK<float> &
         float rz[4], rp[4];
         resid_plane(Wm, W0, Wp, kz, Nz, rz);
         resid_plane(W0, Wp, Wq, kp, Np, rp);
+        if (NORM) {
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                const float a = rz[q] * nscale, c = rp[q] * nscale;
+                *ss = fmaf(a, a, *ss);
+                *ss = fmaf(c, c, *ss);
+            }
+        }
         const float zz = X.wz[kz], zp = X.wz[kp];
         // children in the order of resrestrict_cell32: c = 0..7 with bit 0 ->
         // x (iz), bit 1 -> y (jz), bit 2 -> z (kz); unset bits take the p child

@@ -145,8 +145,9 @@ struct Ctx {
     int vcycle32(int maxit, double omega, bool zero_start);
     int outer_residual(double *sol, double *rsd, const double *rhs, int slot);
     int update_residual(double *sol, double *rsd, int slot, double res0);
-    int run_vcycles(int maxit, double omega, int check_after = 0, double thresh2 = 0.0, int *ran = nullptr);
-    int inner_norm(double *out);
+    int run_vcycles(int maxit, double omega, int check_after = 0, double thresh2 = 0.0, int *ran = nullptr,
+                    double res0 = 0.0);
+    int inner_norm(double *out, double res0);
     int correct_and_recompute(double *sol, double *rsd, const double *rhs);
     int check_pipeline();
     int resrestrict32(int l);

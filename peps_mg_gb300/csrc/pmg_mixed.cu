@@ -83,15 +83,24 @@ __global__ void __launch_bounds__(kBX *kBY, 4) k_resrestrict32(LevelK<float> F, 
 // Squared norm of the finest level's inner residual b - A e (FP32 cells, FP64 sum; one
 // partial per CTA): the estimate of the outer residual after a correction that ends a
 // correction's V-cycles early (Ctx::run_vcycles).
+template <int UV>
 __global__ void __launch_bounds__(kBX *kBY) k_inner_norm(LevelK<float> L, const float *__restrict__ e,
                                                         const float *__restrict__ b, double *partials)
 {
     double acc = 0.0;
     for (int k = blockIdx.z + 1; k <= L.nz; k += gridDim.z)
         for (int j = blockIdx.y * blockDim.y + threadIdx.y + 1; j <= L.ny; j += gridDim.y * blockDim.y)
-            for (int i = blockIdx.x * blockDim.x + threadIdx.x + 1; i <= L.nx; i += gridDim.x * blockDim.x) {
-                const double v = resid32(L, e, b, i, j, k);
-                acc = fma(v, v, acc);
+            for (int i0 = blockIdx.x * (blockDim.x * UV) + threadIdx.x + 1; i0 <= L.nx;
+                 i0 += gridDim.x * blockDim.x * UV) {
+                // UV cells of the row, 32 apart, computed together (their loads in flight at once)
+                float v[UV];
+#pragma unroll
+                for (int u = 0; u < UV; ++u) {
+                    const int i = i0 + u * kBX;
+                    v[u] = i <= L.nx ? resid32(L, e, b, i, j, k) : 0.f;
+                }
+#pragma unroll
+                for (int u = 0; u < UV; ++u) acc = fma((double)v[u], (double)v[u], acc);
             }
     __shared__ double sw[kBX * kBY / 32];
     const double s = block_sum(acc, sw);
@@ -154,16 +163,26 @@ __global__ void __launch_bounds__(kBX *kBY) k_prolong_march32(XferK<float> X, in
 // (ic, jc), marching up a chunk of coarse planes (resrestrict_column_march32).  Capped at
 // 80 registers (three CTAs per SM): the extra resident warps hide more load latency than
 // its few spilled bytes cost (measured 9% faster).
+// NORM: also the squared norm of the fine residual (one FP64 partial per CTA, the FP32
+// per-thread sums scaled by nscale^2): the inner residual check of Ctx::run_vcycles.
+template <bool NORM>
 __global__ void __launch_bounds__(kBX *kBY, 3) k_resrestrict_march32(LevelK<float> F, XferK<float> X, int kchunk,
                                                                   int nchunks, const float *__restrict__ e,
                                                                   const float *__restrict__ b,
-                                                                  float *__restrict__ bc)
+                                                                  float *__restrict__ bc, float nscale,
+                                                                  double *partials)
 {
+    float ss = 0.f;
     for (int ch = blockIdx.z; ch < nchunks; ch += gridDim.z) {
         const int m0 = 1 + ch * kchunk, m1 = min(X.ncz, m0 + kchunk - 1);
         for (int jc = blockIdx.y * blockDim.y + threadIdx.y + 1; jc <= X.ncy; jc += gridDim.y * blockDim.y)
             for (int ic = blockIdx.x * blockDim.x + threadIdx.x + 1; ic <= X.ncx; ic += gridDim.x * blockDim.x)
-                resrestrict_column_march32(F, X, ic, jc, m0, m1, e, b, bc);
+                resrestrict_column_march32<NORM>(F, X, ic, jc, m0, m1, e, b, bc, nscale, &ss);
+    }
+    if (NORM) {
+        __shared__ double sw[kBX * kBY / 32];
+        const double s = block_sum((double)ss, sw);
+        if (tid2() == 0) partials[blin()] = s / ((double)nscale * (double)nscale);
     }
 }
 
@@ -773,7 +792,8 @@ int Ctx::resrestrict32(int l)
         march_chunks((long long)X.ncx * X.ncy, X.ncz, launch[l + 1], &kchunk, &nchunks);
         dim3 g = grid3m(X.ncx, X.ncy, 1, launch[l + 1]);
         g.z = (unsigned)std::min(nchunks, kMaxGridZ);
-        k_resrestrict_march32<<<g, bl, 0, stream>>>(m->K[l], X, kchunk, nchunks, m->E(l), m->b[l], m->b[l + 1]);
+        k_resrestrict_march32<false><<<g, bl, 0, stream>>>(m->K[l], X, kchunk, nchunks, m->E(l), m->b[l], m->b[l + 1],
+                                                           1.f, nullptr);
     } else {
         k_resrestrict32<<<grid3m(X.ncx, X.ncy, X.ncz, launch[l + 1]), bl, 0, stream>>>(m->K[l], X, m->E(l), m->b[l],
                                                                                        m->b[l + 1]);
@@ -818,14 +838,38 @@ int Ctx::outer_residual(double *sol, double *rsd, const double *rhs, int slot)
 // levels' kernels cost about 4 us each on the device, about 1 us inside a graph.  With the
 // event profiler on, the kernels are launched one by one.
 // The inner residual's squared norm at the finest level into *out (synchronises).
-int Ctx::inner_norm(double *out)
+int Ctx::inner_norm(double *out, double res0)
 {
     MixedState *m = mixed;
-    const dim3 g = grid_outer(K[0], launch[0]), bl(kBX, kBY, 1);
-    k_inner_norm<<<g, bl, 0, stream>>>(m->K[0], m->E(0), m->b[0], d_partials);
+    const dim3 bl(kBX, kBY, 1);
+    int np = 0;
+    const XferK<float> &X = m->X[0];
+    if (nl >= 1 && tail32_l0 > 0 && m->march && X.stx == 2 && X.sty == 2 && X.stz == 2) {
+        // the marching residual-restriction of the finest level with the norm added (its
+        // restriction into level 1 is overwritten by the next cycle, if there is one)
+        int kchunk = 1, nchunks = 1;
+        march_chunks((long long)X.ncx * X.ncy, X.ncz, launch[1], &kchunk, &nchunks);
+        dim3 g = grid3m(X.ncx, X.ncy, 1, launch[1]);
+        g.z = (unsigned)std::min(nchunks, kMaxGridZ);
+        np = (int)(g.x * g.y * g.z);
+        if ((size_t)np > npart_cap) np = 0;
+        if (np) {
+            // nscale: a power of two near 1 / (1e-10 rms r0), so the squares of residuals near
+            // the tolerance stay well inside FP32's range
+            const double rms = std::sqrt(res0 / ((double)K[0].nx * K[0].ny * K[0].nz)) * 1e-10;
+            const int ex = rms > 0.0 && std::isfinite(rms) ? std::max(-100, std::min(100, (int)std::floor(std::log2(rms)))) : 0;
+            k_resrestrict_march32<true><<<g, bl, 0, stream>>>(m->K[0], X, kchunk, nchunks, m->E(0), m->b[0],
+                                                              m->b[1], std::ldexp(1.f, -ex), d_partials);
+        }
+    }
+    if (!np) {
+        const dim3 g = grid_outer(K[0], launch[0]);
+        k_inner_norm<1><<<g, bl, 0, stream>>>(m->K[0], m->E(0), m->b[0], d_partials);
+        np = (int)(g.x * g.y * g.z);
+    }
     count_launches(1);
     PMG_TRY_M(cuda_status(cudaGetLastError(), "inner residual norm"));
-    PMG_TRY_M(f64_reduce(d_partials, (int)(g.x * g.y * g.z), d_scal + 2, stream));
+    PMG_TRY_M(f64_reduce(d_partials, np, d_scal + 2, stream));
     double h[3];
     PMG_TRY_M(fetch_scalars(h, 3));
     *out = h[2];
@@ -836,7 +880,7 @@ int Ctx::inner_norm(double *out)
 // after check_after of them, the inner residual's squared norm is below thresh2 (the
 // outer residual the correction leaves is that residual to about 1e-14 of the initial
 // one, so the FP64 recompute that follows confirms the stop).  *ran = cycles run.
-int Ctx::run_vcycles(int maxit, double omega, int check_after, double thresh2, int *ran)
+int Ctx::run_vcycles(int maxit, double omega, int check_after, double thresh2, int *ran, double res0)
 {
     NvtxRange nvtx_range("FP32 V-cycles of a correction");
     MixedState *m = mixed;
@@ -845,7 +889,7 @@ int Ctx::run_vcycles(int maxit, double omega, int check_after, double thresh2, i
         *stop = false;
         if (check_after <= 0 || done != check_after || done >= m->inner) return PMG_OK;
         double v = 0.0;
-        PMG_TRY_M(inner_norm(&v));
+        PMG_TRY_M(inner_norm(&v, res0));
         if (std::isfinite(v) && v < thresh2) {
             *stop = true;
             if (ran) *ran = done;
@@ -1004,7 +1048,7 @@ int Ctx::solve_mixed(double *sol, double *rsd, const double *rhs, int maxit, dou
             }
         }
         int ran = m->inner;
-        PMG_TRY_M(run_vcycles(maxit, omega, check_after, thresh2, &ran));
+        PMG_TRY_M(run_vcycles(maxit, omega, check_after, thresh2, &ran, res0tol));
         inner_total += ran;
         if (recompute) {
             PMG_TRY_M(correct_and_recompute(sol, rsd, rhs));
