@@ -153,13 +153,22 @@ __global__ void __launch_bounds__(RbtShape<TY>::THREADS, rbt_min_ctas<TY>())
 // total work, like the single-grid kernels' chunks) gives items of equal size, which keep
 // the CTAs of a launch equally busy whatever the problems' sizes.
 
+// NORM (the inner residual check of a correction predicted to end a problem's solve):
+// also one partial per item of the fine residual's squared norm (FP32 per-thread sums
+// scaled by a power of two near 1 / (1e-10 rms r0), so residuals near the tolerance stay
+// in FP32's range), from the marching path only (a problem whose depth-0 transfer does not
+// halve every axis is never checked).
+template <bool NORM>
 __global__ void __launch_bounds__(NTB, 3) k_batch_resrestrict(const BLevel *__restrict__ lvd,
                                                            const BLevel *__restrict__ lvc, const Item *__restrict__ items,
-                                                           int nitems, int which, const int *__restrict__ done)
+                                                           int nitems, int which, const int *__restrict__ skip,
+                                                           double *__restrict__ partials,
+                                                           const double *__restrict__ res0)
 {
+    __shared__ double sw[NORM ? NTB / 32 : 1];
     for (int it = blockIdx.x; it < nitems; it += gridDim.x) {
         const Item w = items[it];
-        if (done[w.p]) continue;
+        if (skip[w.p]) continue;                                 // uniform over the block
         const BLevel &D = lvd[w.p];
         const XferK<float> X = D.X;
         const LevelK<float> L = D.L;
@@ -167,12 +176,24 @@ __global__ void __launch_bounds__(NTB, 3) k_batch_resrestrict(const BLevel *__re
         float *bc = lvc[w.p].b;
         const int m0 = w.k0, m1 = min(X.ncz, w.k0 + w.by - 1);
         const int q = w.bx * NTB + threadIdx.x;
-        if (q >= X.ncx * X.ncy) continue;
-        const int i = q % X.ncx + 1, j = q / X.ncx + 1;
-        if (X.stx == 2 && X.sty == 2 && X.stz == 2) {
-            resrestrict_column_march32(L, X, i, j, m0, m1, e, D.b, bc);
-        } else {
-            for (int k = m0; k <= m1; ++k) bc[lin(i, j, k, X.csy, X.csz)] = resrestrict_cell32(L, X, e, D.b, i, j, k);
+        float ss = 0.f, nscale = 1.f;
+        if (NORM) {
+            const double rms = sqrt(res0[w.p] / ((double)L.nx * L.ny * L.nz)) * 1e-10;
+            const int ex = rms > 0.0 && rms < 1e300 ? max(-100, min(100, ilogb(rms))) : 0;
+            nscale = ldexpf(1.0f, -ex);
+        }
+        if (q < X.ncx * X.ncy) {
+            const int i = q % X.ncx + 1, j = q / X.ncx + 1;
+            if (X.stx == 2 && X.sty == 2 && X.stz == 2) {
+                resrestrict_column_march32<NORM>(L, X, i, j, m0, m1, e, D.b, bc, nscale, &ss);
+            } else {
+                for (int k = m0; k <= m1; ++k)
+                    bc[lin(i, j, k, X.csy, X.csz)] = resrestrict_cell32(L, X, e, D.b, i, j, k);
+            }
+        }
+        if (NORM) {
+            const double t = block_sum((double)ss, sw);
+            if (threadIdx.x == 0) partials[it] = t / ((double)nscale * (double)nscale);
         }
     }
 }
@@ -434,6 +455,34 @@ __global__ void __launch_bounds__(NTB) k_batch_norms(const double *__restrict__ 
 
 }  // namespace
 
+// skip[p] = done[p]: the problems the V-cycles of a correction leave out, at its start.
+__global__ void k_batch_skip_init(const int *__restrict__ done, int *__restrict__ skip, int n)
+{
+    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < n; p += gridDim.x * blockDim.x) skip[p] = done[p];
+}
+
+// After all but the last V-cycle of a correction: a problem predicted to end its solve
+// with this correction (mode 1) whose fine inner residual |b - A e|^2 (its items' partials,
+// summed in item order) is below thresh (0.95 tol)^2 |r0|^2 runs no more cycles -- the
+// residual the correction leaves equals it to about 1e-14 of |r0|, and the FP64 recompute
+// of the outer step confirms convergence.  The reference stops after the first cycle that
+// meets the tolerance (src/multigrid.f90:1973).
+__global__ void __launch_bounds__(NTB) k_batch_inner_stop(const double *__restrict__ partials,
+                                                          const int *__restrict__ first,
+                                                          const double *__restrict__ res0,
+                                                          const int *__restrict__ mode,
+                                                          const int *__restrict__ can, int *__restrict__ skip,
+                                                          double thresh)
+{
+    __shared__ double sw[NTB / 32];
+    const int p = blockIdx.x;
+    if (skip[p] || !mode[p] || !can[p]) return;
+    double acc = 0.0;
+    for (int q = first[p] + threadIdx.x; q < first[p + 1]; q += NTB) acc += partials[q];
+    const double s = block_sum(acc, sw);
+    if (threadIdx.x == 0 && s < thresh * res0[p]) skip[p] = 1;
+}
+
 // ---------------------------------------------------------------------------------------
 // Batch object
 // ---------------------------------------------------------------------------------------
@@ -463,6 +512,13 @@ struct Batch {
     int *d_first = nullptr;
     double *d_partials = nullptr, *d_res0 = nullptr, *d_ratio = nullptr;
     int *d_done = nullptr, *d_cycles = nullptr, *d_ndone = nullptr;
+    // the V-cycles' problem mask (done, or stopped early within a correction) and the
+    // inner residual check: per-item partials of the depth-0 residual-restriction, each
+    // problem's first item there, whether the check applies to it (marching depth-0 transfer)
+    int *d_skip = nullptr;
+    double *d_rr_part = nullptr;
+    int *d_rr_first = nullptr, *d_can_check = nullptr;
+    bool any_check = false;
     // residual update state per problem: mode (1: recompute directly), check (recompute
     // after this correction's update), updated ratio, previous ratio, last contraction
     int *d_mode = nullptr, *d_check = nullptr;
@@ -504,6 +560,10 @@ Batch::~Batch()
     dev_free(d_res0);
     dev_free(d_ratio);
     dev_free(d_done);
+    dev_free(d_skip);
+    dev_free(d_rr_part);
+    dev_free(d_rr_first);
+    dev_free(d_can_check);
     dev_free(d_cycles);
     dev_free(d_mode);
     dev_free(d_nonzero);
@@ -604,7 +664,7 @@ void launch_batch_tma(const Batch &B, int d, const Batch::List &Ls, int slots, i
     const Rb32Tma *mp = B.d_maps + (size_t)d * B.n;
     const bool one = om == 1.f;
     constexpr int nt = RbtShape<TY>::THREADS, sm = RbtShape<TY>::SMEM;
-    const BatchTmaArgs A{lv, mp, Ls.d, B.d_done, Ls.n, which, vi};
+    const BatchTmaArgs A{lv, mp, Ls.d, B.d_skip, Ls.n, which, vi};
     if (zs && one)
         k_batch_rb32_tma<TY, true, true><<<grid, nt, sm, B.stream>>>(A, om, omw, B.d_err);
     else if (zs)
@@ -623,13 +683,13 @@ void launch_batch_rb(const Batch &B, int d, const Batch::List &Ls, int slots, in
     const bool one = om == 1.f;
     const int nt = rb_threads<TY>();
     if (zs && one)
-        k_batch_rb32<TY, true, true><<<grid, nt, 0, B.stream>>>(lv, Ls.d, Ls.n, which, om, omw, B.d_done);
+        k_batch_rb32<TY, true, true><<<grid, nt, 0, B.stream>>>(lv, Ls.d, Ls.n, which, om, omw, B.d_skip);
     else if (zs)
-        k_batch_rb32<TY, true, false><<<grid, nt, 0, B.stream>>>(lv, Ls.d, Ls.n, which, om, omw, B.d_done);
+        k_batch_rb32<TY, true, false><<<grid, nt, 0, B.stream>>>(lv, Ls.d, Ls.n, which, om, omw, B.d_skip);
     else if (one)
-        k_batch_rb32<TY, false, true><<<grid, nt, 0, B.stream>>>(lv, Ls.d, Ls.n, which, om, omw, B.d_done);
+        k_batch_rb32<TY, false, true><<<grid, nt, 0, B.stream>>>(lv, Ls.d, Ls.n, which, om, omw, B.d_skip);
     else
-        k_batch_rb32<TY, false, false><<<grid, nt, 0, B.stream>>>(lv, Ls.d, Ls.n, which, om, omw, B.d_done);
+        k_batch_rb32<TY, false, false><<<grid, nt, 0, B.stream>>>(lv, Ls.d, Ls.n, which, om, omw, B.d_skip);
 }
 
 // Smoother over the work list Ls of depth d with variant v: 0, 1, 2 the register-window
@@ -832,7 +892,9 @@ int batch_create(Batch **out, int n, const int *dims, const double *const *meshe
         // fastest with chunks of at most 8 coarse planes)
         const int kc_rr = (int)std::max(1.0, std::min(8.0, std::ceil(work_rr / want_threads)));
         const int kc_pr = (int)std::max(1.0, std::min(64.0, std::ceil(work_pr / want_threads)));
+        std::vector<int> rr_first((size_t)n + 1, 0), can((size_t)n, 0);
         for (int p = 0; p < n; ++p) {
+            rr_first[p] = (int)rr.size();
             if (B->probs[p]->nl <= d) continue;
             const XferK<float> &X = lv[(size_t)d * n + p].X;
             const int nfy = lv[(size_t)d * n + p].L.ny;
@@ -842,12 +904,24 @@ int batch_create(Batch **out, int n, const int *dims, const double *const *meshe
                 for (int c = 0; c * NTB < crr; ++c) rr.push_back({p, c, kc_rr, k});
             for (int k = 1; k <= X.ncz; k += kc_pr)
                 for (int c = 0; c * NTB < cpr; ++c) pr.push_back({p, c, kc_pr, k});
+            can[p] = X.stx == 2 && X.sty == 2 && X.stz == 2;
         }
+        rr_first[n] = (int)rr.size();
         B->xfer_rr[d].n = (int)rr.size();
         B->xfer_pr[d].n = (int)pr.size();
         PMG_TRY_B(upload(rr, &B->xfer_rr[d].d));
         PMG_TRY_B(upload(pr, &B->xfer_pr[d].d));
+        if (d == 0) {
+            // the inner residual check runs on the depth-0 residual-restriction's items
+            for (int p = 0; p < n; ++p) B->any_check = B->any_check || can[p];
+            PMG_TRY_B(upload(rr_first, &B->d_rr_first));
+            PMG_TRY_B(upload(can, &B->d_can_check));
+            if (!rr.empty())
+                PMG_TRY_B(cuda_status(dev_malloc(&B->d_rr_part, rr.size() * sizeof(double)), "batch allocation"));
+        }
     }
+    PMG_TRY_B(cuda_status(dev_malloc(&B->d_skip, n * sizeof(int)), "batch allocation"));
+    PMG_TRY_B(cuda_status(cudaMemset(B->d_skip, 0, n * sizeof(int)), "batch init"));
     {
         // outer items: whole planes (up to kOuterCells cells together) or row blocks of a
         // plane (multiples of kOuterWarps rows), in plane order per problem
@@ -1019,17 +1093,17 @@ static void batch_vcycle(Batch &B, int maxit, float om, float omw, bool zero_sta
         smooth(d, d > 0 || zero_start);
         const Batch::List &X = B.xfer_rr[d];
         if (X.n) {
-            k_batch_resrestrict<<<grid_for(X.n), NTB, 0, B.stream>>>(B.d_lv + (size_t)d * n, B.d_lv + (size_t)(d + 1) * n,
-                                                                     X.d, X.n, par[d], B.d_done);
+            k_batch_resrestrict<false><<<grid_for(X.n), NTB, 0, B.stream>>>(
+                B.d_lv + (size_t)d * n, B.d_lv + (size_t)(d + 1) * n, X.d, X.n, par[d], B.d_skip, nullptr, nullptr);
             count_launches(1);
         }
     }
-    batch_tail32(B.d_tails, n, B.d_done, B.tail_threads, B.stream);
+    batch_tail32(B.d_tails, n, B.d_skip, B.tail_threads, B.stream);
     for (int d = D - 1; d >= 0; --d) {
         const Batch::List &X = B.xfer_pr[d];
         if (X.n) {
             k_batch_prolong<<<grid_for(X.n), NTB, 0, B.stream>>>(B.d_lv + (size_t)d * n, B.d_lv + (size_t)(d + 1) * n,
-                                                                 X.d, X.n, par[d], par[d + 1], d, B.d_done);
+                                                                 X.d, X.n, par[d], par[d + 1], d, B.d_skip);
             count_launches(1);
         }
         smooth(d, false);
@@ -1118,7 +1192,21 @@ int batch_solve(Batch &B, double *sol, const double *rhs, int maxit, double tol,
         B.graph = nullptr;
         cudaGraph_t g;
         PMG_TRY_B(cuda_status(cudaStreamBeginCapture(B.stream, cudaStreamCaptureModeThreadLocal), "graph capture"));
-        for (int q = 0; q < B.inner; ++q) batch_vcycle(B, maxit, om, omw, q == 0);
+        k_batch_skip_init<<<(n + 255) / 256, 256, 0, B.stream>>>(B.d_done, B.d_skip, n);
+        count_launches(1);
+        for (int q = 0; q < B.inner; ++q) {
+            batch_vcycle(B, maxit, om, omw, q == 0);
+            if (q == B.inner - 2 && B.any_check && B.xfer_rr.size() > 0 && B.xfer_rr[0].n > 0) {
+                // the inner residual after all but the last cycle (depth-0 e is in buffer 0
+                // after a whole V-cycle); problems predicted to end here may stop
+                const Batch::List &X = B.xfer_rr[0];
+                k_batch_resrestrict<true><<<grid_for(X.n), NTB, 0, B.stream>>>(
+                    B.d_lv, B.d_lv + (size_t)n, X.d, X.n, 0, B.d_skip, B.d_rr_part, B.d_res0);
+                k_batch_inner_stop<<<n, NTB, 0, B.stream>>>(B.d_rr_part, B.d_rr_first, B.d_res0, B.d_mode,
+                                                            B.d_can_check, B.d_skip, 0.95 * 0.95 * tol * tol);
+                count_launches(2);
+            }
+        }
         batch_outer(B, false, tol, max_cycles);
         PMG_TRY_B(cuda_status(cudaStreamEndCapture(B.stream, &g), "graph capture"));
         const cudaError_t ie = cudaGraphInstantiate(&B.graph, g, 0);
