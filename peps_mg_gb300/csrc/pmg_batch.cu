@@ -163,12 +163,14 @@ __global__ void __launch_bounds__(NTB, 3) k_batch_resrestrict(const BLevel *__re
                                                            const BLevel *__restrict__ lvc, const Item *__restrict__ items,
                                                            int nitems, int which, const int *__restrict__ skip,
                                                            double *__restrict__ partials,
-                                                           const double *__restrict__ res0)
+                                                           const double *__restrict__ res0,
+                                                           const int *__restrict__ mode)
 {
     __shared__ double sw[NORM ? NTB / 32 : 1];
     for (int it = blockIdx.x; it < nitems; it += gridDim.x) {
         const Item w = items[it];
-        if (skip[w.p]) continue;                                 // uniform over the block
+        // (the check only concerns problems predicted to end with this correction)
+        if (skip[w.p] || (NORM && !mode[w.p])) continue;        // uniform over the block
         const BLevel &D = lvd[w.p];
         const XferK<float> X = D.X;
         const LevelK<float> L = D.L;
@@ -1094,7 +1096,8 @@ static void batch_vcycle(Batch &B, int maxit, float om, float omw, bool zero_sta
         const Batch::List &X = B.xfer_rr[d];
         if (X.n) {
             k_batch_resrestrict<false><<<grid_for(X.n), NTB, 0, B.stream>>>(
-                B.d_lv + (size_t)d * n, B.d_lv + (size_t)(d + 1) * n, X.d, X.n, par[d], B.d_skip, nullptr, nullptr);
+                B.d_lv + (size_t)d * n, B.d_lv + (size_t)(d + 1) * n, X.d, X.n, par[d], B.d_skip, nullptr, nullptr,
+                nullptr);
             count_launches(1);
         }
     }
@@ -1201,7 +1204,7 @@ int batch_solve(Batch &B, double *sol, const double *rhs, int maxit, double tol,
                 // after a whole V-cycle); problems predicted to end here may stop
                 const Batch::List &X = B.xfer_rr[0];
                 k_batch_resrestrict<true><<<grid_for(X.n), NTB, 0, B.stream>>>(
-                    B.d_lv, B.d_lv + (size_t)n, X.d, X.n, 0, B.d_skip, B.d_rr_part, B.d_res0);
+                    B.d_lv, B.d_lv + (size_t)n, X.d, X.n, 0, B.d_skip, B.d_rr_part, B.d_res0, B.d_mode);
                 k_batch_inner_stop<<<n, NTB, 0, B.stream>>>(B.d_rr_part, B.d_rr_first, B.d_res0, B.d_mode,
                                                             B.d_can_check, B.d_skip, 0.95 * 0.95 * tol * tol);
                 count_launches(2);
