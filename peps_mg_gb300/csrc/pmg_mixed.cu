@@ -14,7 +14,9 @@
 // coarsest-level solver, but in FP32 arithmetic with FMA contraction and approximate
 // reciprocals; the coarsest-level solver's dot products and convergence test stay in FP64.
 // The finest FP32 residual is fused with the restriction.  The V-cycles of a correction
-// are replayed as CUDA graphs (run_vcycles).
+// are replayed as CUDA graphs (run_vcycles); a correction predicted to end the solve stops
+// its cycles once one inner residual check shows the tolerance met, as the reference stops
+// after the first cycle that meets it.
 //
 // This translation unit is compiled with --fmad=true.
 #include <cuda_runtime.h>
