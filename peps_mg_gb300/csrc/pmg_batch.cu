@@ -9,10 +9,12 @@
 // outer correction -- the FP32 V-cycles, the FP64 correction, the FP64 residual, the
 // per-problem norms and convergence test -- is captured once in a CUDA graph and then
 // replayed.  Converged problems skip their work items, so their results stay those of
-// the correction at which they converged.
+// the correction at which they converged; a problem predicted to end with a correction
+// skips that correction's last V-cycle when its inner residual already meets the tolerance.
 //
-// The smoother's tile shape (64 x 8, 64 x 12 or 64 x 16) is chosen per depth by timing
-// the batch's own work lists (autotuning at the first solve).
+// The smoother (register-window or TMA-fed kernel, tiles of 60 columns by 6, 10, 14 or 22
+// rows, k-chunk) is chosen per depth by timing the batch's own work lists (autotuning at the
+// first solve).
 #include <cuda_runtime.h>
 
 #include <algorithm>
