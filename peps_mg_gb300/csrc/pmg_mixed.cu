@@ -373,6 +373,82 @@ __global__ void __launch_bounds__(kBX *kBY) k_update_residual(LevelK<double> L, 
     if (tid2() == 0) partials[blin()] = s;
 }
 
+// The same update with one thread per column (i, j) marching up a chunk of planes: e of the
+// planes below, at and above the current one stays in registers (the z-neighbours), and
+// the next plane's loads (its e neighbours, x and r) are in flight while a plane is
+// computed.  Per cell the same operations in the same order as k_update_residual, so x, r
+// and r32 are the same bits; only the norm's summation order differs.
+__global__ void __launch_bounds__(kBX *kBY, 3) k_update_residual_march(LevelK<double> L, SplitCoef C,
+                                                                     double *__restrict__ x,
+                                                                     const float *__restrict__ e,
+                                                                     double *__restrict__ r, float *__restrict__ r32,
+                                                                     int sy32, long long sz32, float nscale,
+                                                                     int kchunk, int nchunks, double *partials)
+{
+    float acc32 = 0.f;
+    for (int ch = blockIdx.z; ch < nchunks; ch += gridDim.z) {
+        const int k0 = 1 + ch * kchunk, k1 = min(L.nz, k0 + kchunk - 1);
+        for (int j = blockIdx.y * blockDim.y + threadIdx.y + 1; j <= L.ny; j += gridDim.y * blockDim.y) {
+            const float2 cym = C.cym[j], cyp = C.cyp[j];
+            for (int i = blockIdx.x * blockDim.x + threadIdx.x + 1; i <= L.nx; i += gridDim.x * blockDim.x) {
+                const float2 cm = C.cxm[i], cp = C.cxp[i];
+                const float *ec = e + lin(i, j, 0, sy32, sz32);     // the column at plane 0
+                float *rc32 = r32 + lin(i, j, 0, sy32, sz32);
+                double *xc = x + lin(i, j, 0, L.sy, L.sz);
+                double *rc = r + lin(i, j, 0, L.sy, L.sz);
+                // plane k: e below (em), at (e0), above (ep); its x/y neighbours, x and r
+                float em = ec[sz32 * (k0 - 1)], e0 = ec[sz32 * k0], ep = ec[sz32 * (k0 + 1)];
+                float xl = ec[sz32 * k0 - 1], xr = ec[sz32 * k0 + 1];
+                float yd = ec[sz32 * k0 - sy32], yu = ec[sz32 * k0 + sy32];
+                double xv = xc[L.sz * k0], rv = rc[L.sz * k0];
+                for (int k = k0; k <= k1; ++k) {
+                    // plane k+1's loads (its upper neighbour is plane k+2 <= nz+1)
+                    float ep2 = 0.f, nxl = 0.f, nxr = 0.f, nyd = 0.f, nyu = 0.f;
+                    double nxv = 0.0, nrv = 0.0;
+                    if (k < k1) {
+                        const long long o = sz32 * (k + 1);
+                        ep2 = ec[o + sz32];
+                        nxl = ec[o - 1];
+                        nxr = ec[o + 1];
+                        nyd = ec[o - sy32];
+                        nyu = ec[o + sy32];
+                        nxv = xc[L.sz * (k + 1)];
+                        nrv = rc[L.sz * (k + 1)];
+                    }
+                    const float2 czm = C.czm[k], czp = C.czp[k];
+                    float S = 0.f, Sl = 0.f;
+                    comp_term(cm, xl, e0, S, Sl);
+                    comp_term(cp, xr, e0, S, Sl);
+                    comp_term(cym, yd, e0, S, Sl);
+                    comp_term(cyp, yu, e0, S, Sl);
+                    comp_term(czm, em, e0, S, Sl);
+                    comp_term(czp, ep, e0, S, Sl);
+                    xc[L.sz * k] = xv + f32_to_f64(e0);
+                    const double v = __dsub_rn(__dsub_rn(rv, f32_to_f64_fast(S)), f32_to_f64_fast(Sl));
+                    rc[L.sz * k] = v;
+                    const float v32 = f64_to_f32_rn(v);
+                    rc32[sz32 * k] = v32;
+                    const float w = v32 * nscale;
+                    acc32 = fmaf(w, w, acc32);
+                    em = e0;
+                    e0 = ep;
+                    ep = ep2;
+                    xl = nxl;
+                    xr = nxr;
+                    yd = nyd;
+                    yu = nyu;
+                    xv = nxv;
+                    rv = nrv;
+                }
+            }
+        }
+    }
+    __shared__ double sw[kBX * kBY / 32];
+    const double inv = 1.0 / ((double)nscale * (double)nscale);
+    const double s = block_sum((double)acc32 * inv, sw);
+    if (tid2() == 0) partials[blin()] = s;
+}
+
 // Test hook: convert n values with the integer-pipe conversions.
 __global__ void k_convert_test(const double *in64, float *out32, const float *in32, double *out64, int n)
 {
@@ -965,13 +1041,24 @@ int Ctx::update_residual(double *sol, double *rsd, int slot, double res0)
     const int ex = rms0 > 0.0 && std::isfinite(rms0) ? std::max(-100, std::min(100, (int)std::floor(std::log2(rms0))))
                                                      : 0;
     const float nscale = std::ldexp(1.0f, -ex);
+    int kchunk = 1, nchunks = 1;
+    march_chunks((long long)L.nx * L.ny, L.nz, launch[0], &kchunk, &nchunks);
+    dim3 gm = grid3m(L.nx, L.ny, 1, launch[0]);
+    gm.z = (unsigned)std::min(nchunks, kMaxGridZ);
+    const bool march = (size_t)gm.x * gm.y * gm.z <= npart_cap;
     const int pi = prof.begin(stream);
-    k_update_residual<UV><<<g, bl, 0, stream>>>(L, mixed->sc, sol, mixed->E(0), rsd, mixed->b[0], mixed->K[0].sy,
-                                            mixed->K[0].sz, nscale, d_partials);
+    if (march)
+        k_update_residual_march<<<gm, bl, 0, stream>>>(L, mixed->sc, sol, mixed->E(0), rsd, mixed->b[0],
+                                                       mixed->K[0].sy, mixed->K[0].sz, nscale, kchunk, nchunks,
+                                                       d_partials);
+    else
+        k_update_residual<UV><<<g, bl, 0, stream>>>(L, mixed->sc, sol, mixed->E(0), rsd, mixed->b[0], mixed->K[0].sy,
+                                                mixed->K[0].sz, nscale, d_partials);
     prof.end(pi, PC_UPDATE_RES, 1, 40.0 * (double)L.nx * L.ny * L.nz, stream);
     count_launches(1);
     PMG_TRY_M(cuda_status(cudaGetLastError(), "residual update"));
-    return f64_reduce(d_partials, (int)(g.x * g.y * g.z), d_scal + slot, stream);
+    const dim3 gu = march ? gm : g;
+    return f64_reduce(d_partials, (int)(gu.x * gu.y * gu.z), d_scal + slot, stream);
 }
 
 // x += e followed by the FP64 residual b - A x (slot 1).
