@@ -149,6 +149,8 @@ struct Ctx {
                     double res0 = 0.0);
     int inner_norm(double *out, double res0);
     int correct_and_recompute(double *sol, double *rsd, const double *rhs);
+    int add_corrections(double *sol, bool with_e);
+    int flush_stash(double *sol);
     int check_pipeline();
     int resrestrict32(int l);
     int selftest_smooth32(int level, int impl, int variant, int kchunk, bool zero_in, double omega,

@@ -270,29 +270,44 @@ __global__ void __launch_bounds__(kBX *kBY) k_outer_residual(LevelK<double> L, c
     if (tid2() == 0) partials[blin()] = s;
 }
 
-// x = x + e (the FP64 correction); each thread handles kOuterVec cells of a row, 32
-// apart, with their loads issued together, on the grid of the outer kernels.
+// x = ((x + s0) + s1) + e: the NS stashed corrections s0, s1 (earlier corrections whose
+// residual update left x alone), then e unless WITH_E is false, added one at a time in
+// the order they were made, so x gets the same bits as when each correction was added at
+// once.  Each thread handles kOuterVec cells of a row, 32 apart, with their loads issued
+// together, on the grid of the outer kernels.
+template <int NS, bool WITH_E>
 __global__ void __launch_bounds__(kBX *kBY) k_add_correction(LevelK<double> L, double *__restrict__ x,
-                                                             const float *__restrict__ e, int sy32, long long sz32)
+                                                             const float *__restrict__ e,
+                                                             const float *__restrict__ s0,
+                                                             const float *__restrict__ s1, int sy32, long long sz32)
 {
     for (int k = blockIdx.z + 1; k <= L.nz; k += gridDim.z)
         for (int j = blockIdx.y * blockDim.y + threadIdx.y + 1; j <= L.ny; j += gridDim.y * blockDim.y)
             for (int i0 = blockIdx.x * (blockDim.x * kOuterVec) + threadIdx.x + 1; i0 <= L.nx;
                  i0 += gridDim.x * blockDim.x * kOuterVec) {
                 double xv[kOuterVec];
-                float ev[kOuterVec];
+                float ev[kOuterVec], a0[kOuterVec], a1[kOuterVec];
 #pragma unroll
                 for (int u = 0; u < kOuterVec; ++u) {
                     const int i = i0 + u * kBX;
                     if (i <= L.nx) {
+                        const long long q = lin(i, j, k, sy32, sz32);
                         xv[u] = x[lin(i, j, k, L.sy, L.sz)];
-                        ev[u] = e[lin(i, j, k, sy32, sz32)];
+                        if (NS > 0) a0[u] = s0[q];
+                        if (NS > 1) a1[u] = s1[q];
+                        if (WITH_E) ev[u] = e[q];
                     }
                 }
 #pragma unroll
                 for (int u = 0; u < kOuterVec; ++u) {
                     const int i = i0 + u * kBX;
-                    if (i <= L.nx) x[lin(i, j, k, L.sy, L.sz)] = xv[u] + f32_to_f64(ev[u]);
+                    if (i <= L.nx) {
+                        double v = xv[u];
+                        if (NS > 0) v = v + f32_to_f64(a0[u]);
+                        if (NS > 1) v = v + f32_to_f64(a1[u]);
+                        if (WITH_E) v = v + f32_to_f64(ev[u]);
+                        x[lin(i, j, k, L.sy, L.sz)] = v;
+                    }
                 }
             }
 }
@@ -376,15 +391,25 @@ __global__ void __launch_bounds__(kBX *kBY) k_update_residual(LevelK<double> L, 
 // The same update with one thread per column (i, j) marching up a chunk of planes: e of the
 // planes below, at and above the current one stays in registers (the z-neighbours), and
 // the next plane's loads (its e neighbours, x and r) are in flight while a plane is
-// computed.  Per cell the same operations in the same order as k_update_residual, so x, r
-// and r32 are the same bits; only the norm's summation order differs.
-__global__ void __launch_bounds__(kBX *kBY, 3) k_update_residual_march(LevelK<double> L, SplitCoef C,
+// computed.  Per cell the same operations in the same order as k_update_residual, so r
+// and r32 are the same bits; only the norm's summation order differs.  What happens to x:
+//  * XM_ADD: x += e;
+//  * XM_STASH: x is not touched, e is copied to the stash array s_out (a later
+//    k_add_correction or XM_FOLD adds it);
+//  * XM_FOLD: x = ((x + s0) + s1) + e, the two stashed corrections and this one.
+enum { XM_ADD = 0, XM_STASH = 1, XM_FOLD = 2 };
+template <int XM>
+__global__ void __launch_bounds__(kBX *kBY, 4) k_update_residual_march(LevelK<double> L, SplitCoef C,
                                                                      double *__restrict__ x,
                                                                      const float *__restrict__ e,
                                                                      double *__restrict__ r, float *__restrict__ r32,
                                                                      int sy32, long long sz32, float nscale,
-                                                                     int kchunk, int nchunks, double *partials)
+                                                                     int kchunk, int nchunks, double *partials,
+                                                                     float *__restrict__ s_out,
+                                                                     const float *__restrict__ s0,
+                                                                     const float *__restrict__ s1)
 {
+    constexpr bool kX = XM != XM_STASH;   // x is read and written
     float acc32 = 0.f;
     for (int ch = blockIdx.z; ch < nchunks; ch += gridDim.z) {
         const int k0 = 1 + ch * kchunk, k1 = min(L.nz, k0 + kchunk - 1);
@@ -392,18 +417,21 @@ __global__ void __launch_bounds__(kBX *kBY, 3) k_update_residual_march(LevelK<do
             const float2 cym = C.cym[j], cyp = C.cyp[j];
             for (int i = blockIdx.x * blockDim.x + threadIdx.x + 1; i <= L.nx; i += gridDim.x * blockDim.x) {
                 const float2 cm = C.cxm[i], cp = C.cxp[i];
-                const float *ec = e + lin(i, j, 0, sy32, sz32);     // the column at plane 0
-                float *rc32 = r32 + lin(i, j, 0, sy32, sz32);
+                const long long c32 = lin(i, j, 0, sy32, sz32);   // the column at plane 0
+                const float *ec = e + c32;
+                float *rc32 = r32 + c32;
                 double *xc = x + lin(i, j, 0, L.sy, L.sz);
                 double *rc = r + lin(i, j, 0, L.sy, L.sz);
                 // plane k: e below (em), at (e0), above (ep); its x/y neighbours, x and r
                 float em = ec[sz32 * (k0 - 1)], e0 = ec[sz32 * k0], ep = ec[sz32 * (k0 + 1)];
                 float xl = ec[sz32 * k0 - 1], xr = ec[sz32 * k0 + 1];
                 float yd = ec[sz32 * k0 - sy32], yu = ec[sz32 * k0 + sy32];
-                double xv = xc[L.sz * k0], rv = rc[L.sz * k0];
+                double xv = kX ? xc[L.sz * k0] : 0.0, rv = rc[L.sz * k0];
+                float a0 = XM == XM_FOLD ? s0[c32 + sz32 * k0] : 0.f;
+                float a1 = XM == XM_FOLD ? s1[c32 + sz32 * k0] : 0.f;
                 for (int k = k0; k <= k1; ++k) {
                     // plane k+1's loads (its upper neighbour is plane k+2 <= nz+1)
-                    float ep2 = 0.f, nxl = 0.f, nxr = 0.f, nyd = 0.f, nyu = 0.f;
+                    float ep2 = 0.f, nxl = 0.f, nxr = 0.f, nyd = 0.f, nyu = 0.f, na0 = 0.f, na1 = 0.f;
                     double nxv = 0.0, nrv = 0.0;
                     if (k < k1) {
                         const long long o = sz32 * (k + 1);
@@ -412,8 +440,12 @@ __global__ void __launch_bounds__(kBX *kBY, 3) k_update_residual_march(LevelK<do
                         nxr = ec[o + 1];
                         nyd = ec[o - sy32];
                         nyu = ec[o + sy32];
-                        nxv = xc[L.sz * (k + 1)];
+                        if (kX) nxv = xc[L.sz * (k + 1)];
                         nrv = rc[L.sz * (k + 1)];
+                        if (XM == XM_FOLD) {
+                            na0 = s0[c32 + o];
+                            na1 = s1[c32 + o];
+                        }
                     }
                     const float2 czm = C.czm[k], czp = C.czp[k];
                     float S = 0.f, Sl = 0.f;
@@ -423,13 +455,17 @@ __global__ void __launch_bounds__(kBX *kBY, 3) k_update_residual_march(LevelK<do
                     comp_term(cyp, yu, e0, S, Sl);
                     comp_term(czm, em, e0, S, Sl);
                     comp_term(czp, ep, e0, S, Sl);
-                    xc[L.sz * k] = xv + f32_to_f64(e0);
+                    if (XM == XM_ADD) xc[L.sz * k] = xv + f32_to_f64(e0);
+                    if (XM == XM_FOLD) xc[L.sz * k] = ((xv + f32_to_f64(a0)) + f32_to_f64(a1)) + f32_to_f64(e0);
+                    if (XM == XM_STASH) s_out[c32 + sz32 * k] = e0;
                     const double v = __dsub_rn(__dsub_rn(rv, f32_to_f64_fast(S)), f32_to_f64_fast(Sl));
                     rc[L.sz * k] = v;
                     const float v32 = f64_to_f32_rn(v);
                     rc32[sz32 * k] = v32;
                     const float w = v32 * nscale;
                     acc32 = fmaf(w, w, acc32);
+                    a0 = na0;
+                    a1 = na1;
                     em = e0;
                     e0 = ep;
                     ep = ep2;
@@ -490,9 +526,9 @@ dim3 grid3m(int nxt, int ny, int nz, const Launch &ln)
     return g;
 }
 
-// Chunks of coarse planes for the marching transfer kernels: about four resident
+// Chunks of coarse planes for the marching transfer kernels: about `waves` resident
 // threads' worth of (column, chunk) work per SM thread slot.
-void march_chunks(long long columns, int ncz, const Launch &ln, int *kchunk, int *nchunks)
+void march_chunks(long long columns, int ncz, const Launch &ln, int *kchunk, int *nchunks, int waves = 4)
 {
     static int sms = 0;
     if (!sms) {
@@ -501,7 +537,7 @@ void march_chunks(long long columns, int ncz, const Launch &ln, int *kchunk, int
                                                       cudaSuccess)
             sms = 148;
     }
-    long long want = (4LL * sms * 2048 + columns - 1) / std::max(1LL, columns);
+    long long want = ((long long)waves * sms * 2048 + columns - 1) / std::max(1LL, columns);
     if (ln.collapse[2]) want = 1;
     want = std::max(1LL, std::min<long long>(want, ncz));
     *kchunk = (int)((ncz + want - 1) / want);
@@ -655,6 +691,10 @@ int Ctx::build_mixed()
         const char *oe = std::getenv("PEPS_MG_OUTER");
         m->update_residual = !(oe && std::strcmp(oe, "recompute") == 0);
     }
+    // PEPS_MG_STASH=off: every residual update adds its correction to x at once (no stash
+    // arrays: two finest-level FP32 arrays less; x moves 16 more bytes per cell per update)
+    const char *se = std::getenv("PEPS_MG_STASH");
+    const bool use_stash = m->update_residual && !(se && std::strcmp(se, "off") == 0);
     auto F = [&](const double *p) { return (const float *)(m->tables + (p - d_tables)); };
     m->K.resize((size_t)nl + 1);
     m->X.resize((size_t)nl);
@@ -705,6 +745,14 @@ int Ctx::build_mixed()
         y.pxp = F(x.pxp); y.pxn = F(x.pxn); y.pyp = F(x.pyp); y.pyn = F(x.pyn);
         y.pzp = F(x.pzp); y.pzn = F(x.pzn);
     }
+    // the stash of the residual update: two more finest-level FP32 arrays
+    if (use_stash)
+        for (float *&st : m->stash) {
+            int pitch = 0;
+            long long plane = 0, rows = 0, planes = 0;
+            float *base = nullptr;
+            PMG_TRY_M(alloc_f32(m, K[0].nx, K[0].ny, K[0].nz, &pitch, &plane, &st, &base, &rows, &planes));
+        }
     PMG_TRY_M(mstatus(dev_malloc(&m->d_tail, sizeof(TailDesc<float>)), "mixed tail descriptor"));
     PMG_TRY_M(mstatus(dev_malloc(&m->d_err, sizeof(int)), "mixed error flag"));
     PMG_TRY_M(mstatus(cudaMemset(m->d_err, 0, sizeof(int)), "mixed error flag"));
@@ -1041,40 +1089,90 @@ int Ctx::update_residual(double *sol, double *rsd, int slot, double res0)
     const int ex = rms0 > 0.0 && std::isfinite(rms0) ? std::max(-100, std::min(100, (int)std::floor(std::log2(rms0))))
                                                      : 0;
     const float nscale = std::ldexp(1.0f, -ex);
+    // eight waves of chunks: shorter columns at four CTAs per SM measured 6% faster
     int kchunk = 1, nchunks = 1;
-    march_chunks((long long)L.nx * L.ny, L.nz, launch[0], &kchunk, &nchunks);
+    march_chunks((long long)L.nx * L.ny, L.nz, launch[0], &kchunk, &nchunks, 8);
     dim3 gm = grid3m(L.nx, L.ny, 1, launch[0]);
     gm.z = (unsigned)std::min(nchunks, kMaxGridZ);
     const bool march = (size_t)gm.x * gm.y * gm.z <= npart_cap;
+    MixedState *m = mixed;
+    const int sy32 = m->K[0].sy;
+    const long long sz32 = m->K[0].sz;
+    // x: the correction goes to a free stash array (x untouched), or, with both taken, all
+    // three are added to x here; the plane-grid kernel adds to x directly (after the stash)
+    if (!march) PMG_TRY_M(flush_stash(sol));
+    const int xm = !march ? XM_ADD : !m->stash[0] ? XM_ADD : m->nstash < 2 ? XM_STASH : XM_FOLD;
+    const double bytes = xm == XM_STASH ? 28.0 : xm == XM_FOLD ? 48.0 : 40.0;
     const int pi = prof.begin(stream);
-    if (march)
-        k_update_residual_march<<<gm, bl, 0, stream>>>(L, mixed->sc, sol, mixed->E(0), rsd, mixed->b[0],
-                                                       mixed->K[0].sy, mixed->K[0].sz, nscale, kchunk, nchunks,
-                                                       d_partials);
+    if (!march)
+        k_update_residual<UV><<<g, bl, 0, stream>>>(L, m->sc, sol, m->E(0), rsd, m->b[0], sy32, sz32, nscale,
+                                                d_partials);
+    else if (xm == XM_STASH)
+        k_update_residual_march<XM_STASH><<<gm, bl, 0, stream>>>(L, m->sc, sol, m->E(0), rsd, m->b[0], sy32, sz32,
+                                                                 nscale, kchunk, nchunks, d_partials,
+                                                                 m->stash[m->nstash], nullptr, nullptr);
+    else if (xm == XM_FOLD)
+        k_update_residual_march<XM_FOLD><<<gm, bl, 0, stream>>>(L, m->sc, sol, m->E(0), rsd, m->b[0], sy32, sz32,
+                                                                nscale, kchunk, nchunks, d_partials, nullptr,
+                                                                m->stash[0], m->stash[1]);
     else
-        k_update_residual<UV><<<g, bl, 0, stream>>>(L, mixed->sc, sol, mixed->E(0), rsd, mixed->b[0], mixed->K[0].sy,
-                                                mixed->K[0].sz, nscale, d_partials);
-    prof.end(pi, PC_UPDATE_RES, 1, 40.0 * (double)L.nx * L.ny * L.nz, stream);
+        k_update_residual_march<XM_ADD><<<gm, bl, 0, stream>>>(L, m->sc, sol, m->E(0), rsd, m->b[0], sy32, sz32,
+                                                               nscale, kchunk, nchunks, d_partials, nullptr,
+                                                               nullptr, nullptr);
+    if (xm == XM_STASH) ++m->nstash;
+    if (xm == XM_FOLD) m->nstash = 0;
+    prof.end(pi, PC_UPDATE_RES, 1, bytes * (double)L.nx * L.ny * L.nz, stream);
     count_launches(1);
     PMG_TRY_M(cuda_status(cudaGetLastError(), "residual update"));
     const dim3 gu = march ? gm : g;
     return f64_reduce(d_partials, (int)(gu.x * gu.y * gu.z), d_scal + slot, stream);
 }
 
-// x += e followed by the FP64 residual b - A x (slot 1).
+// x += e (with the stashed corrections before it) followed by the FP64 residual b - A x
+// (slot 1).
 int Ctx::correct_and_recompute(double *sol, double *rsd, const double *rhs)
 {
     NvtxRange nvtx_range("correction and FP64 residual");
-    const LevelK<double> &L = K[0];
-    const dim3 g = grid_outer(L, launch[0]), bl(kBX, kBY, 1);
     PMG_TRY_M(before_x_change());
-    const int pi = prof.begin(stream);
-    k_add_correction<<<g, bl, 0, stream>>>(L, sol, mixed->E(0), mixed->K[0].sy, mixed->K[0].sz);
-    prof.end(pi, PC_ADDCORR, 1, 20.0 * (double)L.nx * L.ny * L.nz, stream);
-    count_launches(1);
-    PMG_TRY_M(cuda_status(cudaGetLastError(), "correction"));
+    PMG_TRY_M(add_corrections(sol, true));
     PMG_TRY_M(early_copy_sol(sol));
     return outer_residual(sol, rsd, rhs, 1);
+}
+
+// x = ((x + s0) + s1) + e with the stashed corrections (none, one or two) and, with
+// with_e, the current one; the stash is empty afterwards.
+int Ctx::add_corrections(double *sol, bool with_e)
+{
+    MixedState *m = mixed;
+    const int ns = m->nstash;
+    if (ns == 0 && !with_e) return PMG_OK;
+    const LevelK<double> &L = K[0];
+    const dim3 g = grid_outer(L, launch[0]), bl(kBX, kBY, 1);
+    const float *e = m->E(0), *s0 = m->stash[0], *s1 = m->stash[1];
+    const int sy32 = m->K[0].sy;
+    const long long sz32 = m->K[0].sz;
+    const int pi = prof.begin(stream);
+    if (with_e) {
+        if (ns == 0) k_add_correction<0, true><<<g, bl, 0, stream>>>(L, sol, e, s0, s1, sy32, sz32);
+        else if (ns == 1) k_add_correction<1, true><<<g, bl, 0, stream>>>(L, sol, e, s0, s1, sy32, sz32);
+        else k_add_correction<2, true><<<g, bl, 0, stream>>>(L, sol, e, s0, s1, sy32, sz32);
+    } else {
+        if (ns == 1) k_add_correction<1, false><<<g, bl, 0, stream>>>(L, sol, e, s0, s1, sy32, sz32);
+        else k_add_correction<2, false><<<g, bl, 0, stream>>>(L, sol, e, s0, s1, sy32, sz32);
+    }
+    prof.end(pi, PC_ADDCORR, 1, (16.0 + 4.0 * (ns + (with_e ? 1 : 0))) * (double)L.nx * L.ny * L.nz, stream);
+    count_launches(1);
+    m->nstash = 0;
+    return cuda_status(cudaGetLastError(), "correction");
+}
+
+// Adds the stashed corrections to x (the point where x has to hold every correction: the
+// FP64 residual b - A x, or the end of the solve).
+int Ctx::flush_stash(double *sol)
+{
+    if (!mixed || mixed->nstash == 0) return PMG_OK;
+    PMG_TRY_M(before_x_change());
+    return add_corrections(sol, false);
 }
 
 // Defect correction.  After a correction the residual is normally updated (r -= A e,
@@ -1087,6 +1185,7 @@ int Ctx::solve_mixed(double *sol, double *rsd, const double *rhs, int maxit, dou
 {
     PMG_TRY_M(setup_mixed());
     MixedState *m = mixed;
+    m->nstash = 0;
     const Level &S = lv[0];
     // the residual's ghost cells are zero (src/multigrid.f90:1795); the outer residual
     // writes every interior cell
@@ -1119,6 +1218,7 @@ int Ctx::solve_mixed(double *sol, double *rsd, const double *rhs, int maxit, dou
                 rep->final_ratio = ratio;
                 rep->inner_cycles = inner_total;
             }
+            PMG_TRY_M(flush_stash(sol));
             return abort_status();
         }
         const bool recompute = !m->update_residual || cyc == n_vcycles || prev_ratio * contraction < 0.1 * tol;
@@ -1147,6 +1247,7 @@ int Ctx::solve_mixed(double *sol, double *rsd, const double *rhs, int maxit, dou
             PMG_TRY_M(update_residual(sol, rsd, 1, res0tol));
             PMG_TRY_M(fetch_scalars(h, 2));
             if (std::isfinite(h[1]) && std::sqrt(h[1] / res0tol) < tol) {
+                PMG_TRY_M(flush_stash(sol));
                 PMG_TRY_M(early_copy_sol(sol));
                 PMG_TRY_M(outer_residual(sol, rsd, rhs, 1));
                 PMG_TRY_M(fetch_scalars(h, 2));
@@ -1175,6 +1276,7 @@ int Ctx::solve_mixed(double *sol, double *rsd, const double *rhs, int maxit, dou
                 rep->final_ratio = ratio;
                 rep->inner_cycles = inner_total;
             }
+            PMG_TRY_M(flush_stash(sol));
             set_error("residual norm is not finite");
             return PMG_EDIVERGED;
         }
@@ -1183,6 +1285,9 @@ int Ctx::solve_mixed(double *sol, double *rsd, const double *rhs, int maxit, dou
             break;
         }
     }
+    // every way out of the loop above has emptied the stash already (the FP64 residual that
+    // ends a solve needs x whole); this keeps it so should that change
+    PMG_TRY_M(flush_stash(sol));
     if (rep) {
         rep->cycles = cycles;
         rep->converged = converged;

@@ -25,6 +25,10 @@ struct MixedState {
     std::vector<XferK<float>> X;
     std::vector<float *> alloc;      // raw allocations
     std::vector<float *> e[2], b;    // e[buf][l] (two buffers for out-of-place sweeps), b[l]
+    // Finest-level corrections not yet added to x (the residual update leaves x alone for
+    // up to two corrections; x = ((x + stash[0]) + stash[1]) + e when it is needed)
+    float *stash[2] = {nullptr, nullptr};
+    int nstash = 0;
     std::vector<int> cur;            // current buffer of e at each level
     std::vector<bool> fused;         // level uses the fused out-of-place smoother
     std::vector<bool> window;        // the autotuner chose the register-window kernel over the TMA-fed one

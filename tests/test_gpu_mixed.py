@@ -204,6 +204,58 @@ np.savez(sys.argv[1], sol=from_dev(sol), rsd=from_dev(rsd), hist=rep.history, co
     assert np.max(np.abs(u["rsd"] - r)) < noise
 
 
+def test_residual_update_stash_same_bits(tmp_path):
+    """The residual update leaves x alone and keeps the corrections in two stash arrays; x
+    gets them, one at a time in the order they were made, where it is needed (the FP64
+    residual, the third correction in a row, the end of the solve).  The solution, the
+    residual and every residual norm have the same bits as with each correction added at
+    once (PEPS_MG_STASH=off).  One FP32 cycle per correction gives runs of updates longer
+    than the stash; the Dirichlet face and stretched mesh give a non-zero x0 and
+    corrections of every size."""
+    import os
+    import subprocess
+    import sys
+    code = r'''
+import sys, numpy as np, torch, peps_mg_gb300 as pmg
+from tests.helpers import to_dev, from_dev
+n = (72, 64, 56)
+rng = np.random.default_rng(5)
+mesh = [pmg.geometry.mesh_from_widths(rng.uniform(0.7, 1.3, m) / m) for m in n]
+rhs = pmg.geometry.field(*n); rhs[1:-1, 1:-1, 1:-1] = rng.uniform(-1, 1, n)
+sol0 = pmg.geometry.field(*n); sol0[0, :, :] = 0.5
+out = {}
+for inner in (1, 2, 4):
+    with pmg.Multigrid(mesh, 4, 50, "cgs", precision="mixed", mixed_inner_cycles=inner) as mg:
+        sol = to_dev(sol0)
+        rsd = torch.zeros_like(sol)
+        rep = mg.solve_vcycle(sol, rsd, to_dev(rhs), 2, 1e-10, 1.0)
+    out["sol%d" % inner] = from_dev(sol)
+    out["rsd%d" % inner] = from_dev(rsd)
+    out["hist%d" % inner] = rep.history
+    out["n%d" % inner] = np.array([rep.cycles, rep.inner_cycles, rep.converged])
+np.savez(sys.argv[1], **out)
+'''
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    res = {}
+    for mode in ("on", "off"):
+        env = dict(os.environ, PEPS_MG_STASH=mode, PYTHONPATH=root)
+        path = str(tmp_path / (mode + ".npz"))
+        r = subprocess.run([sys.executable, "-c", code, path], cwd=root, env=env, capture_output=True, text=True,
+                           timeout=300)
+        assert r.returncode == 0, r.stderr[-2000:]
+        res[mode] = np.load(path)
+    a, b = res["on"], res["off"]
+    for inner in (1, 2, 4):
+        assert a["n%d" % inner][2] == 1
+        assert np.array_equal(a["n%d" % inner], b["n%d" % inner])
+        # one FP32 cycle per correction: more updates in a row than stash arrays
+        if inner == 1:
+            assert a["n1"][0] >= 4
+        for key in ("sol", "rsd", "hist"):
+            assert np.array_equal(a["%s%d" % (key, inner)].view(np.uint64), b["%s%d" % (key, inner)].view(np.uint64)), \
+                (key, inner)
+
+
 def test_mixed_pinned_host_buffers():
     """Pinned host buffers: the solution's copy back starts while the final residual is
     computed; the results equal those of device buffers."""
