@@ -263,8 +263,9 @@ int pmg_selftest_convert(const double *in64, float *out32, const float *in32, do
 /* Self-test of the fused FP32 smoother of a mixed-precision context (no counterpart in the
  * reference): e_out = one red-black iteration (src/rbgs_poisson_matrix.f90:235-273) of
  * e_in for right-hand side b on `level`, computed in FP32 by the fused kernel.
- * impl: 0 = TMA-fed kernel, 1 = register-window kernel; variant 0/1/2/3 = tiles 60 x 14 /
- * 60 x 6 / 60 x 10 / 60 x 22 (3: TMA-fed kernel only); kchunk: planes per work item (0 = automatic); zero_in: treat e_in as
+ * impl: 0 = TMA-fed kernel, 1 = register-window kernel, 2 = one-launch cell-pair kernel
+ * (variant and kchunk unused); variant 0/1/2/3 = tiles 60 x 14 / 60 x 6 / 60 x 10 /
+ * 60 x 22 (3: TMA-fed kernel only); kchunk: planes per work item (0 = automatic); zero_in: treat e_in as
  * zero.  Host arrays of the level's (0:nx+1,0:ny+1,0:nz+1) Fortran layout (ghosts of
  * e_in and b must be zero); e_out receives every cell.  PMG_EINVAL when the level has no
  * fused smoother or impl 0 is unavailable for it.  Synchronous; overwrites the context's

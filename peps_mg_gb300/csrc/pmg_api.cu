@@ -1752,7 +1752,7 @@ int pmg_selftest_smooth32(pmg_ctx *ctx, int level, int impl, int variant, int kc
                           const double *e_in, const double *b, double *e_out)
 {
     PMG_TRY(check_ctx_level(ctx, level));
-    if (!e_in || !b || !e_out || impl < 0 || impl > 1 || variant < 0 || variant > (impl == 0 ? 3 : 2) ||
+    if (!e_in || !b || !e_out || impl < 0 || impl > 2 || variant < 0 || variant > (impl == 0 ? 3 : 2) ||
         kchunk < 0) {
         pmg::set_error("invalid smoother self-test arguments");
         return PMG_EINVAL;

@@ -174,8 +174,15 @@ int rb32_fused(const LevelK<float> &L, const Launch &ln, const float *ein, float
 // register-window one wins, *variant carries kTuneWindow on top of the tile variant and the
 // caller must run that level without its maps.
 constexpr int kTuneWindow = 8;
+// variant of rb32_fused (and tune_smoother's answer) for the one-launch cell-pair kernel
+// (no tiles, no marching: levels that live in L2, where the marching kernels' serial plane
+// pipeline is the longer path)
+constexpr int kCellVariant = 4;
+// allow_cell: the one-launch cell-pair kernel is a candidate too (on levels of at most 2^22
+// cells), answered as kCellVariant.
 int tune_smoother(const LevelK<float> &L, const Launch &ln, float *e0, float *e1, const float *b, cudaStream_t s,
-                  int *variant, int *kchunk, const Rb32Tma *tma = nullptr, int *err = nullptr);
+                  int *variant, int *kchunk, const Rb32Tma *tma = nullptr, int *err = nullptr,
+                  bool allow_cell = true);
 // Integer-pipe precision conversions used by the outer kernels (self-test hook).
 int convert_selftest(const double *in64, float *out32, const float *in32, double *out64, int n, cudaStream_t s);
 

@@ -709,9 +709,11 @@ int Ctx::build_mixed()
     m->tma.assign((size_t)nl + 1, Rb32Tma());
     m->rows.assign((size_t)nl + 1, 0);
     m->planes.assign((size_t)nl + 1, 0);
-    // PEPS_MG_SMOOTHER=window selects the register-window smoother everywhere
+    // PEPS_MG_SMOOTHER=window selects the register-window smoother everywhere, =cell the
+    // one-launch cell-pair kernel everywhere (otherwise the autotuner picks per level)
     const char *sm_env = std::getenv("PEPS_MG_SMOOTHER");
     const bool use_tma = !(sm_env && std::strcmp(sm_env, "window") == 0);
+    const bool force_cell = sm_env && std::strcmp(sm_env, "cell") == 0;
     // PEPS_MG_TRANSFER=cell selects the one-thread-per-cell transfer kernels everywhere
     const char *tr_env = std::getenv("PEPS_MG_TRANSFER");
     m->march = !(tr_env && std::strcmp(tr_env, "cell") == 0);
@@ -757,9 +759,11 @@ int Ctx::build_mixed()
     PMG_TRY_M(mstatus(dev_malloc(&m->d_err, sizeof(int)), "mixed error flag"));
     PMG_TRY_M(mstatus(cudaMemset(m->d_err, 0, sizeof(int)), "mixed error flag"));
     for (int l = 0; l < tail32_l0; ++l)
-        if (m->fused[l] && autotune) {
+        if (m->fused[l] && force_cell) {
+            m->variant[l] = kCellVariant;
+        } else if (m->fused[l] && autotune) {
             PMG_TRY_M(tune_smoother(m->K[l], launch[l], m->e[0][l], m->e[1][l], m->b[l], stream, &m->variant[l],
-                                    &m->kchunk[l], &m->tma[l], m->d_err));
+                                    &m->kchunk[l], &m->tma[l], m->d_err, use_tma));
             if (m->variant[l] & kTuneWindow) {
                 m->variant[l] &= ~kTuneWindow;
                 m->window[l] = true;   // the register-window kernel is faster on this level
@@ -1326,7 +1330,8 @@ int Ctx::selftest_smooth32(int level, int impl, int variant, int kchunk, bool ze
     PMG_TRY_M(mstatus(cudaMemset(bo, 0, total * sizeof(float)), "self-test init"));
     const float om = (float)omega, omw = (float)(1.0 - omega);
     PMG_TRY_M(rb32_fused(L, launch[level], m->e[0][level], m->e[1][level], m->b[level], om, omw, zero_in, stream,
-                         variant, kchunk, impl == 0 ? &m->tma[level] : nullptr, 0, m->d_err));
+                         impl == 2 ? kCellVariant : variant, kchunk, impl == 0 ? &m->tma[level] : nullptr, 0,
+                         m->d_err));
     PMG_TRY_M(check_pipeline());
     PMG_TRY_M(mstatus(cudaMemcpy(he.data(), bo, total * sizeof(float), cudaMemcpyDeviceToHost), "self-test read"));
     for (int k = 0; k <= nz + 1; ++k)

@@ -57,6 +57,96 @@ __global__ void __launch_bounds__(rb_threads<TY>(), rb_min_blocks<TY>()) k_rb32_
     }
 }
 
+// One red-black iteration (src/rbgs_poisson_matrix.f90:235-273), out of place, one thread
+// per cell pair (i odd, i + 1) and no marching.  The pair's first-colour cell (i + j + k
+// odd) is updated from e_in; its second-colour cell from its six neighbours' first-colour
+// updates, one of them the pair's own and five recomputed here from e_in.  Each update
+// has the operations, in order, of the marching kernels' (s = cxm e_w, then FMAs of the
+// east, south, north, lower and upper terms; d = (sx + (cym + cyp)) + (czm + czp); e =
+// (s - b) / d, or (1 - omega) e + omega (s - b) / d), so the result has their bits.  Cells
+// outside the grid are not updated and read as e_in (their zero ghosts); ZERO_IN reads e_in
+// as zero everywhere.  The redundant updates cost FP32 work and L1/L2 reads, not DRAM
+// traffic, on the levels it is chosen for (those that live in L2).
+template <bool ZERO_IN, bool OMEGA1>
+struct RbCell {
+    const LevelK<float> &L;
+    const float *ein, *b;
+    float omega, omw;
+    __device__ __forceinline__ float ld(long long p) const { return ZERO_IN ? 0.f : ein[p]; }
+    __device__ __forceinline__ float upd(float old, float bb, float s, float d) const
+    {
+        if (OMEGA1) return __fdividef(s - bb, d);
+        return fmaf(omw, old, __fdividef(omega * (s - bb), d));
+    }
+    __device__ __forceinline__ float diag(int i, int j, int k) const
+    {
+        return (L.sx[i] + (L.cym[j] + L.cyp[j])) + (L.czm[k] + L.czp[k]);
+    }
+    // update of cell (i, j, k) from neighbour values w, e (x), s, n (y), l, u (z)
+    __device__ __forceinline__ float update(int i, int j, int k, long long p, float w, float e, float so, float no,
+                                            float lo, float up) const
+    {
+        float s = L.cxm[i] * w;
+        s = fmaf(L.cxp[i], e, s);
+        s = fmaf(L.cym[j], so, s);
+        s = fmaf(L.cyp[j], no, s);
+        s = fmaf(L.czm[k], lo, s);
+        s = fmaf(L.czp[k], up, s);
+        return upd(ld(p), b[p], s, diag(i, j, k));
+    }
+    // first-colour value of cell (i, j, k) after the first half of the iteration
+    __device__ __forceinline__ float first(int i, int j, int k) const
+    {
+        const long long p = lin(i, j, k, L.sy, L.sz);
+        if (i < 1 || i > L.nx || j < 1 || j > L.ny || k < 1 || k > L.nz) return ld(p);
+        if (ZERO_IN) return upd(0.f, b[p], 0.f, diag(i, j, k));
+        return update(i, j, k, p, ein[p - 1], ein[p + 1], ein[p - L.sy], ein[p + L.sy], ein[p - L.sz],
+                      ein[p + L.sz]);
+    }
+};
+
+template <bool ZERO_IN, bool OMEGA1>
+__global__ void __launch_bounds__(256) k_rb32_cell(LevelK<float> L, const float *__restrict__ ein,
+                                                   float *__restrict__ eout, const float *__restrict__ b, float omega,
+                                                   float omw)
+{
+    const RbCell<ZERO_IN, OMEGA1> C{L, ein, b, omega, omw};
+    const int npx = (L.nx + 1) / 2;
+    for (int k = blockIdx.z + 1; k <= L.nz; k += gridDim.z)
+        for (int j = blockIdx.y * blockDim.y + threadIdx.y + 1; j <= L.ny; j += gridDim.y * blockDim.y)
+            for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < npx; t += gridDim.x * blockDim.x) {
+                const int i = 2 * t + 1;
+                // (i + j + k) odd: cell i takes the first colour, else cell i + 1
+                const int f = ((j + k) & 1) ? i + 1 : i, sc = ((j + k) & 1) ? i : i + 1;
+                const float vf = C.first(f, j, k);
+                if (f <= L.nx) eout[lin(f, j, k, L.sy, L.sz)] = vf;
+                if (sc <= L.nx) {
+                    const long long p = lin(sc, j, k, L.sy, L.sz);
+                    const float w = sc - 1 == f ? vf : C.first(sc - 1, j, k);
+                    const float e = sc + 1 == f ? vf : C.first(sc + 1, j, k);
+                    eout[p] = C.update(sc, j, k, p, w, e, C.first(sc, j - 1, k), C.first(sc, j + 1, k),
+                                       C.first(sc, j, k - 1), C.first(sc, j, k + 1));
+                }
+            }
+}
+
+int launch_cell(const LevelK<float> &L, const Launch &ln, const float *ein, float *eout, const float *b, float omega,
+                float omw, bool zero_in, cudaStream_t s)
+{
+    const dim3 bl(32, 8, 1);
+    dim3 g;
+    g.x = ln.collapse[0] ? 1u : (unsigned)std::max(1, ((L.nx + 1) / 2 + 31) / 32);
+    g.y = ln.collapse[1] ? 1u : (unsigned)std::max(1, (L.ny + 7) / 8);
+    g.z = ln.collapse[2] ? 1u : (unsigned)std::max(1, std::min(L.nz, 65535));
+    const bool one = omega == 1.f;
+    if (zero_in && one) k_rb32_cell<true, true><<<g, bl, 0, s>>>(L, ein, eout, b, omega, omw);
+    else if (zero_in) k_rb32_cell<true, false><<<g, bl, 0, s>>>(L, ein, eout, b, omega, omw);
+    else if (one) k_rb32_cell<false, true><<<g, bl, 0, s>>>(L, ein, eout, b, omega, omw);
+    else k_rb32_cell<false, false><<<g, bl, 0, s>>>(L, ein, eout, b, omega, omw);
+    count_launches(1);
+    return cuda_status(cudaGetLastError(), "fp32 cell smoother");
+}
+
 // blocks per SM the TMA-fed kernel's register budget is sized for
 template <int TY>
 constexpr int rbt_min_blocks() { return rbt_min_ctas<TY>(); }
@@ -285,6 +375,13 @@ int rb32_fused(const LevelK<float> &L, const Launch &ln, const float *ein, float
                float omw, bool zero_in, cudaStream_t s, int variant, int kchunk, const Rb32Tma *tma, int in_buf,
                int *err, bool stall)
 {
+    if (variant == kCellVariant) {
+        if (stall) {
+            set_error("the stall self-test needs the TMA-fed smoother");
+            return PMG_EINVAL;
+        }
+        return launch_cell(L, ln, ein, eout, b, omega, omw, zero_in, s);
+    }
     if (tma && tma->ok && err) {
         switch (variant) {
         case 1: return launch_tma<6>(L, ln, *tma, 1, in_buf, eout, omega, omw, zero_in, kchunk, err, s, stall);
@@ -316,12 +413,12 @@ bool rb32_fused_layout_ok(const LevelK<float> &L, const void *e, const void *b)
 }
 
 int tune_smoother(const LevelK<float> &L, const Launch &ln, float *e0, float *e1, const float *b, cudaStream_t s,
-                  int *variant, int *kchunk, const Rb32Tma *tma, int *err)
+                  int *variant, int *kchunk, const Rb32Tma *tma, int *err, bool allow_cell)
 {
     static std::mutex mu;
-    static std::map<std::array<int, 5>, std::pair<int, int>> cache;
+    static std::map<std::array<int, 6>, std::pair<int, int>> cache;
     const bool use_tma = tma && tma->ok && err;
-    const std::array<int, 5> key = {L.nx, L.ny, L.nz, ln.collapse[2] ? 1 : 0, use_tma ? 1 : 0};
+    const std::array<int, 6> key = {L.nx, L.ny, L.nz, ln.collapse[2] ? 1 : 0, use_tma ? 1 : 0, allow_cell ? 1 : 0};
     *variant = 0;
     *kchunk = 0;
 
@@ -348,6 +445,7 @@ int tune_smoother(const LevelK<float> &L, const Launch &ln, float *e0, float *e1
     // The register-window kernel (no copy pipeline to fill) only wins on small levels: it is
     // timed where the TMA-fed one cannot run or the level has at most 2^22 cells.
     const bool try_window = !use_tma || (long long)L.nx * L.ny * L.nz <= (1LL << 22);
+    bool best_cell = false;
     auto time_one = [&](bool tk, int v, int c, float *ms) -> bool {
         const Rb32Tma *tm = tk ? tma : nullptr;
         if (rb32_fused(L, ln, e0, e1, b, 1.f, 0.f, false, s, v, c, tm, 0, err) != PMG_OK) return false;
@@ -356,17 +454,24 @@ int tune_smoother(const LevelK<float> &L, const Launch &ln, float *e0, float *e1
         cudaEventRecord(z, s);
         if (cudaEventSynchronize(z) != cudaSuccess) return false;
         cudaEventElapsedTime(ms, a, z);
+        const bool cell = v == kCellVariant;
         if (log)
             std::fprintf(stderr, "[peps_mg tune] %dx%dx%d %s TY=%d kchunk=%d: %.1f us\n", L.nx, L.ny, L.nz,
-                         tk ? "tma" : "window", tys[v], c, *ms * 1e3f / 3.f);
+                         cell ? "cell" : tk ? "tma" : "window", cell ? 0 : tys[v], c, *ms * 1e3f / 3.f);
         if (*ms < best) {
             best = *ms;
             bv = v;
             bk = c;
-            best_window = !tk;
+            best_window = !tk && !cell;
+            best_cell = cell;
         }
         return true;
     };
+    // the one-launch cell-pair kernel, on the levels where the register-window one is tried
+    if (try_window && allow_cell) {
+        float ms = 0.f;
+        time_one(false, kCellVariant, 0, &ms);
+    }
     for (int kind = use_tma ? 0 : 1; kind < 2; ++kind) {
         const bool tk = kind == 0;
         if (!tk && !try_window) break;
@@ -429,12 +534,13 @@ int tune_smoother(const LevelK<float> &L, const Launch &ln, float *e0, float *e1
     PMG_TRY_S(cuda_status(cudaGetLastError(), "smoother autotuning"));
     // a level with tensor maps whose fastest kernel is the register-window one is flagged
     // (kTuneWindow): its caller runs the window kernel there
-    const int code = bv + (use_tma && best_window ? kTuneWindow : 0);
+    const int code = best_cell ? kCellVariant : bv + (use_tma && best_window ? kTuneWindow : 0);
     *variant = code;
     *kchunk = bk;
     if (log)
         std::fprintf(stderr, "[peps_mg tune] %dx%dx%d chosen %s TY=%d kchunk=%d (%.1f us)\n", L.nx, L.ny, L.nz,
-                     best_window ? "window" : "tma", tys[bv], bk, best * 1e3f / 3.f);
+                     best_cell ? "cell" : best_window ? "window" : "tma", best_cell ? 0 : tys[bv], bk,
+                     best * 1e3f / 3.f);
     std::lock_guard<std::mutex> g(mu);
     cache[key] = {code, bk};
     return PMG_OK;

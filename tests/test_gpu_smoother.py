@@ -1,7 +1,7 @@
 """The fused FP32 red-black smoother, one iteration at a time, against the oracle's FP64
 rbgs_iterator (src/rbgs_poisson_matrix.f90:191) on stretched meshes whose tiles and
-plane chunks end part-way through the grid; the TMA-fed and register-window kernels must
-agree bit for bit."""
+plane chunks end part-way through the grid; the TMA-fed, register-window and one-launch
+cell-pair kernels must agree bit for bit."""
 import ctypes
 
 import numpy as np
@@ -64,10 +64,14 @@ def test_one_iteration_against_oracle(n):
                             assert err < FP32_TOL, (impl, variant, kchunk, zero_in, omega, err)
                             outs.append(got)
                         assert all(np.array_equal(outs[0], o) for o in outs[1:]), (variant, kchunk, zero_in, omega)
+                # the cell-pair kernel (no tiles, no chunks) against the tiled kernels' bits
+                got = run_selftest(mg, 2, 0, 0, zero_in, omega, e0, b)
+                assert np.array_equal(got, outs[0]), (zero_in, omega)
 
 
 def test_kernel_variants_give_identical_solves(tmp_path):
-    """A whole mixed-precision solve gives the same bits with either smoother kernel, with
+    """A whole mixed-precision solve gives the same bits with any smoother kernel (TMA-fed,
+    register-window or one-launch cell-pair, or the autotuner's mix of them), with
     either kind of transfer kernel (marching or one thread per cell), and with the FP32
     V-cycles replayed as CUDA graphs or launched kernel by kernel."""
     import os
@@ -89,7 +93,8 @@ print(rep.cycles)
 '''
     root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
     outs = []
-    for sm, tr, gr in (("tma", "march", "1"), ("window", "march", "1"), ("tma", "cell", "1"), ("tma", "march", "0")):
+    for sm, tr, gr in (("tma", "march", "1"), ("window", "march", "1"), ("tma", "cell", "1"), ("tma", "march", "0"),
+                       ("cell", "march", "1")):
         env = dict(os.environ, PEPS_MG_SMOOTHER=sm, PEPS_MG_TRANSFER=tr, PEPS_MG_GRAPHS=gr, PYTHONPATH=root)
         path = str(tmp_path / ("%s_%s_%s.npy" % (sm, tr, gr)))
         r = subprocess.run([sys.executable, "-c", code, path], cwd=root, env=env, capture_output=True, text=True,
@@ -99,3 +104,4 @@ print(rep.cycles)
     assert np.array_equal(outs[0], outs[1])
     assert np.array_equal(outs[0], outs[2])
     assert np.array_equal(outs[0], outs[3])
+    assert np.array_equal(outs[0], outs[4])
