@@ -42,6 +42,11 @@ OMEGA = 1.0
 METRIC = "time_to_1e-10_rel_residual_512cubed_mixed"
 
 
+def metric_for(n, prec="mixed"):
+    """The metric's name for an n^3 problem (METRIC at the default size)."""
+    return "time_to_1e-10_rel_residual_%dcubed_%s" % (n, prec)
+
+
 def parse():
     p = argparse.ArgumentParser()
     p.add_argument("--gpus", type=int, default=1)
@@ -232,11 +237,11 @@ def run_reference(args):
         if s >= args.warmup:
             per.append(dt)
     value = statistics.mean(per) * 1e3
-    line = {"metric": METRIC, "value": round(value, 3), "unit": "ms", "n_gpus": args.gpus, "steps": args.steps,
+    line = {"metric": metric_for(n), "value": round(value, 3), "unit": "ms", "n_gpus": args.gpus, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": round(value, 3), "higher_is_better": False, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded Gaussian blobs, PCG64(3))",
             "impl": "reference",
-            "config": {"workload": "512^3 Poisson, FP64 V(2,2) RBGS cycles of the reference algorithm to 1e-10",
+            "config": {"workload": "%d^3 Poisson, FP64 V(2,2) RBGS cycles of the reference algorithm to 1e-10" % n,
                        "n": n, "levels": LEVELS[n], "cycles_to_tolerance": cycles,
                        "step_s_min": round(min(per), 3), "step_s_max": round(max(per), 3)},
             "cpu_baseline": {"value": round(value, 3), "unit": "ms", "cores": threads, "cpu": name, "kind": "port",
@@ -365,7 +370,7 @@ def run_ours(args):
 
     if args.quick:
         if rank == 0:
-            print(json.dumps({"metric": METRIC, "value": round(ms, 3), "unit": "ms", "quick": True, "n": n,
+            print(json.dumps({"metric": metric_for(n, prec), "value": round(ms, 3), "unit": "ms", "quick": True, "n": n,
                               "precision": prec, "cycles": rep.cycles,
                               "ratios": [float(v) for v in rep.history[:, 2]],
                               "coarse_iterations": [int(v) for v in rep.coarse_iterations],
@@ -512,11 +517,11 @@ def run_ours(args):
             cpu = {"value": None, "error": str(exc)}
     if rank == 0:
         line = {
-            "metric": METRIC, "value": round(ms, 3), "unit": "ms", "n_gpus": world, "steps": args.steps,
+            "metric": metric_for(n), "value": round(ms, 3), "unit": "ms", "n_gpus": world, "steps": args.steps,
             "warmup": max(args.warmup, 3), "ms_per_step": round(ms, 3), "higher_is_better": False,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64",
             "data": "synthetic (seeded Gaussian blobs, PCG64(3))",
-            "config": {"workload": "512^3 Poisson, mixed FP32 V(2,2) in FP64 defect correction to 1e-10 "
+            "config": {"workload": "%d^3 Poisson, mixed FP32 V(2,2) in FP64 defect correction to 1e-10 " % n +
                                    "(replicas only across GPUs)",
                        "n": n, "levels": nl, "inner_cycles_per_correction": args.inner,
                        "outer_corrections": rep.cycles, "fp32_vcycles": rep.inner_cycles,
