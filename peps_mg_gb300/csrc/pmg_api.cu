@@ -1266,11 +1266,12 @@ struct HostRegistration {
 };
 
 // True when every 64-bit word of the host array is zero (+0.0 everywhere, ghosts
-// included: the test of the device-side zero test, k_nonzero_f64).  Scanned by up to 16
-// host threads, each stopping at the first non-zero word it sees or once another thread
-// has found one; a solve from a zero initial guess then sends no initial guess over the
-// host link at all (the staging buffer is cleared on the device instead), and the scan runs
-// while the right-hand side is being copied.
+// included: the test of the device-side zero test, k_nonzero_f64).  Scanned by up to 8
+// host threads, at most half the cores (a scan thread that has to wait for a core holds
+// up the whole solve), each stopping at the first non-zero word it sees or once another
+// thread has found one; a solve from a zero initial guess then sends no initial guess over
+// the host link at all (the staging buffer is cleared on the device instead), and the scan
+// runs while the right-hand side is being copied.
 static bool host_all_zero(const double *a, size_t n)
 {
     const unsigned long long *u = reinterpret_cast<const unsigned long long *>(a);
@@ -1286,7 +1287,7 @@ static bool host_all_zero(const double *a, size_t n)
     };
     const size_t per_thread = (size_t)1 << 23;   // 64 MB
     const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
-    const unsigned nt = (unsigned)std::min<size_t>(std::min(16u, hw), std::max<size_t>(1, n / per_thread));
+    const unsigned nt = (unsigned)std::min<size_t>(std::min(8u, std::max(1u, hw / 2)), std::max<size_t>(1, n / per_thread));
     if (nt <= 1) {
         scan(0, n);
         return !found.load();
