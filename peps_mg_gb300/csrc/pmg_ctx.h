@@ -143,12 +143,13 @@ struct Ctx {
     int build_mixed();
     int upload_tail32(int maxit, double omega, double tol);
     int vcycle32(int maxit, double omega, bool zero_start);
-    int outer_residual(double *sol, double *rsd, const double *rhs, int slot);
+    int outer_residual(double *sol, double *rsd, const double *rhs, int slot, double res0 = 0.0);
+    int norm_exponent(double res0) const;
     int update_residual(double *sol, double *rsd, int slot, double res0);
     int run_vcycles(int maxit, double omega, int check_after = 0, double thresh2 = 0.0, int *ran = nullptr,
                     double res0 = 0.0);
     int inner_norm(double *out, double res0);
-    int correct_and_recompute(double *sol, double *rsd, const double *rhs);
+    int correct_and_recompute(double *sol, double *rsd, const double *rhs, double res0);
     int add_corrections(double *sol, bool with_e);
     int flush_stash(double *sol);
     int check_pipeline();

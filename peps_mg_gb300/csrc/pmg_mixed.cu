@@ -215,18 +215,56 @@ __global__ void __launch_bounds__(256) k_nonzero_f64(const double *__restrict__ 
 }
 
 
+// The part of v that its round-to-nearest FP32 value v32 (f64_to_f32_rn) leaves out, v -
+// v32, times 2^nexp, rounded to FP32, from the encodings on the integer pipe: the 29
+// mantissa bits the rounding dropped, as a signed count of units 2^(e-52) (negative when
+// the rounding went up).  Zero outside the normal FP32 range and where the scaled unit is
+// not a normal FP32 number (values far below the ones that make up a norm).
+__device__ __forceinline__ float f64_low_part_scaled(double v, int nexp)
+{
+    const unsigned long long bits = (unsigned long long)__double_as_longlong(v);
+    const int e = (int)((bits >> 52) & 0x7ff) - 1023;
+    const int k = e - 52 + nexp;
+    if (e < -126 || e > 127 || k < -126 || k > 127) return 0.f;
+    const unsigned long long m = bits & 0xFFFFFFFFFFFFFull;
+    const unsigned hi = (unsigned)(m >> 29);
+    const int rem = (int)(m & 0x1FFFFFFFull);
+    const bool up = rem > 0x10000000 || (rem == 0x10000000 && (hi & 1u));
+    const float d = (float)(up ? rem - 0x20000000 : rem) * __int_as_float((k + 127) << 23);
+    return (bits >> 63) ? -d : d;
+}
+
+// (S, Sl) += (w + wl)^2 to about 2^-46 relative: w^2 exactly as a product and its FMA
+// rounding error, 2 w wl on top (wl^2 is below 2^-46 w^2), two-sum into S.
+__device__ __forceinline__ void norm_add_ff(float w, float wl, float &S, float &Sl)
+{
+    const float p = __fmul_rn(w, w);
+    float pe = __fmaf_rn(w, w, -p);
+    pe = __fmaf_rn(__fmul_rn(2.f, w), wl, pe);
+    float sum, err;
+    two_sum32(S, p, sum, err);
+    S = sum;
+    Sl = __fadd_rn(Sl, __fadd_rn(err, pe));
+}
+
 // ZS (the first residual of a solve): *nonzero, set by k_nonzero_f64, tells whether the
 // initial guess has a non-zero value; where it has none, every product of the FMA chain
 // is a signed zero and the chain returns b + 0, so the kernel streams b alone.
-template <bool ZS>
+// CN: the squared norm is summed on the FP32 and integer pipes instead of by one FP64 FMA
+// per cell (the FP64 pipe bounds this kernel): each r = r32 + rl (r32 the FP32 copy, rl
+// the low part), scaled by nscale = 2^nexp, squared and summed in an FP32 pair per thread,
+// to about 1e-11 relative.  The FP64 residual itself is unchanged.
+template <bool ZS, bool CN>
 __global__ void __launch_bounds__(kBX *kBY) k_outer_residual(LevelK<double> L, const double *__restrict__ dyy,
                                                              const double *__restrict__ dzz,
                                                              const double *__restrict__ x,
                                                              const double *__restrict__ b, double *__restrict__ r,
                                                              float *__restrict__ r32, int sy32, long long sz32,
-                                                             double *partials, const int *__restrict__ nonzero)
+                                                             double *partials, const int *__restrict__ nonzero,
+                                                             float nscale, int nexp)
 {
     double acc = 0.0;
+    float accS = 0.f, accL = 0.f;
     const bool zero_x = ZS && *nonzero == 0;
     for (int k = blockIdx.z + 1; k <= L.nz; k += gridDim.z) {
         const double dz = dzz[k];
@@ -258,13 +296,18 @@ __global__ void __launch_bounds__(kBX *kBY) k_outer_residual(LevelK<double> L, c
                         const long long p = lin(i, j, k, L.sy, L.sz);
                         const double v = outer_residual_cell(L, dyz, x, b, i, j, k, p);
                         r[p] = v;
-                        r32[lin(i, j, k, sy32, sz32)] = f64_to_f32_rn(v);
-                        acc = fma(v, v, acc);
+                        const float v32 = f64_to_f32_rn(v);
+                        r32[lin(i, j, k, sy32, sz32)] = v32;
+                        if (CN)
+                            norm_add_ff(v32 * nscale, f64_low_part_scaled(v, nexp), accS, accL);
+                        else
+                            acc = fma(v, v, acc);
                     }
                 }
             }
         }
     }
+    if (CN) acc = ((double)accS + (double)accL) / ((double)nscale * (double)nscale);
     __shared__ double sw[kBX * kBY / 32];
     const double s = block_sum(acc, sw);
     if (tid2() == 0) partials[blin()] = s;
@@ -931,7 +974,7 @@ int Ctx::resrestrict32(int l)
     return PMG_OK;
 }
 
-int Ctx::outer_residual(double *sol, double *rsd, const double *rhs, int slot)
+int Ctx::outer_residual(double *sol, double *rsd, const double *rhs, int slot, double res0)
 {
     NvtxRange nvtx_range("FP64 outer residual");
     const LevelK<double> &L = K[0];
@@ -948,13 +991,24 @@ int Ctx::outer_residual(double *sol, double *rsd, const double *rhs, int slot)
             count_launches(1);
         }
     }
+    // a recomputed residual (the initial one known) sums its norm with the FP32 pair, scaled
+    // like the residual update's norm
+    const int ex = norm_exponent(res0);
+    const bool cn = slot != 0 && res0 > 0.0 && std::isfinite(res0);
+    const float nscale = std::ldexp(1.0f, -ex);
     const int pi = prof.begin(stream);
     if (slot == 0)
-        k_outer_residual<true><<<g, bl, 0, stream>>>(L, mixed->dyy[0], mixed->dzz[0], sol, rhs, rsd, mixed->b[0],
-                                                     mixed->K[0].sy, mixed->K[0].sz, d_partials, nonzero);
+        k_outer_residual<true, false><<<g, bl, 0, stream>>>(L, mixed->dyy[0], mixed->dzz[0], sol, rhs, rsd,
+                                                            mixed->b[0], mixed->K[0].sy, mixed->K[0].sz, d_partials,
+                                                            nonzero, 1.f, 0);
+    else if (cn)
+        k_outer_residual<false, true><<<g, bl, 0, stream>>>(L, mixed->dyy[0], mixed->dzz[0], sol, rhs, rsd,
+                                                            mixed->b[0], mixed->K[0].sy, mixed->K[0].sz, d_partials,
+                                                            nonzero, nscale, -ex);
     else
-        k_outer_residual<false><<<g, bl, 0, stream>>>(L, mixed->dyy[0], mixed->dzz[0], sol, rhs, rsd, mixed->b[0],
-                                                      mixed->K[0].sy, mixed->K[0].sz, d_partials, nonzero);
+        k_outer_residual<false, false><<<g, bl, 0, stream>>>(L, mixed->dyy[0], mixed->dzz[0], sol, rhs, rsd,
+                                                             mixed->b[0], mixed->K[0].sy, mixed->K[0].sz, d_partials,
+                                                             nonzero, 1.f, 0);
     prof.end(pi, PC_OUTER_RES, 1, 28.0 * (double)L.nx * L.ny * L.nz, stream);
     count_launches(1);
     PMG_TRY_M(cuda_status(cudaGetLastError(), "outer residual"));
@@ -1089,9 +1143,7 @@ int Ctx::update_residual(double *sol, double *rsd, int slot, double res0)
     dim3 g = grid_outer(L, launch[0]);
     if (!launch[0].collapse[0]) g.x = (unsigned)std::max(1, (L.nx + UV * kBX - 1) / (UV * kBX));
     const dim3 bl(kBX, kBY, 1);
-    const double rms0 = std::sqrt(res0 / ((double)L.nx * L.ny * L.nz));
-    const int ex = rms0 > 0.0 && std::isfinite(rms0) ? std::max(-100, std::min(100, (int)std::floor(std::log2(rms0))))
-                                                     : 0;
+    const int ex = norm_exponent(res0);
     const float nscale = std::ldexp(1.0f, -ex);
     // eight waves of chunks: shorter columns at four CTAs per SM measured 6% faster
     int kchunk = 1, nchunks = 1;
@@ -1132,15 +1184,24 @@ int Ctx::update_residual(double *sol, double *rsd, int slot, double res0)
     return f64_reduce(d_partials, (int)(gu.x * gu.y * gu.z), d_scal + slot, stream);
 }
 
+// The power of two 2^ex nearest below the finest level's RMS initial residual
+// sqrt(res0 / N): the scaled FP32 norms sum r 2^-ex (0 when res0 is not a positive number).
+int Ctx::norm_exponent(double res0) const
+{
+    const LevelK<double> &L = K[0];
+    const double rms0 = std::sqrt(res0 / ((double)L.nx * L.ny * L.nz));
+    return rms0 > 0.0 && std::isfinite(rms0) ? std::max(-100, std::min(100, (int)std::floor(std::log2(rms0)))) : 0;
+}
+
 // x += e (with the stashed corrections before it) followed by the FP64 residual b - A x
 // (slot 1).
-int Ctx::correct_and_recompute(double *sol, double *rsd, const double *rhs)
+int Ctx::correct_and_recompute(double *sol, double *rsd, const double *rhs, double res0)
 {
     NvtxRange nvtx_range("correction and FP64 residual");
     PMG_TRY_M(before_x_change());
     PMG_TRY_M(add_corrections(sol, true));
     PMG_TRY_M(early_copy_sol(sol));
-    return outer_residual(sol, rsd, rhs, 1);
+    return outer_residual(sol, rsd, rhs, 1, res0);
 }
 
 // x = ((x + s0) + s1) + e with the stashed corrections (none, one or two) and, with
@@ -1244,7 +1305,7 @@ int Ctx::solve_mixed(double *sol, double *rsd, const double *rhs, int maxit, dou
         PMG_TRY_M(run_vcycles(maxit, omega, check_after, thresh2, &ran, res0tol));
         inner_total += ran;
         if (recompute) {
-            PMG_TRY_M(correct_and_recompute(sol, rsd, rhs));
+            PMG_TRY_M(correct_and_recompute(sol, rsd, rhs, res0tol));
             PMG_TRY_M(fetch_scalars(h, 2));
         } else {
             PMG_TRY_M(before_x_change());
@@ -1253,7 +1314,7 @@ int Ctx::solve_mixed(double *sol, double *rsd, const double *rhs, int maxit, dou
             if (std::isfinite(h[1]) && std::sqrt(h[1] / res0tol) < tol) {
                 PMG_TRY_M(flush_stash(sol));
                 PMG_TRY_M(early_copy_sol(sol));
-                PMG_TRY_M(outer_residual(sol, rsd, rhs, 1));
+                PMG_TRY_M(outer_residual(sol, rsd, rhs, 1, res0tol));
                 PMG_TRY_M(fetch_scalars(h, 2));
             }
         }
