@@ -7,7 +7,8 @@
 // repeated until sqrt(|r|^2 / |r0|^2) < tolerance, the reference's convergence test
 // (src/multigrid.f90:1970-1973), always decided on a residual recomputed in FP64.  Between
 // corrections that cannot end the solve the residual is updated as r -= A e instead (A e
-// in compensated FP32 arithmetic, k_update_residual).
+// in compensated FP32 arithmetic, k_update_residual_march), and x gets those corrections,
+// in order, where it is next needed (the stash).
 //
 // The FP32 V-cycle follows the operation sequence of the reference cycle
 // (src/multigrid.f90:1931-1967) with the same smoother, transfer operators and
@@ -1133,8 +1134,9 @@ int Ctx::run_vcycles(int maxit, double omega, int check_after, double thresh2, i
     return PMG_OK;
 }
 
-// x += e and r -= A e with its norm into d_scal[slot] (after a correction); res0 = the
-// initial residual's squared norm (sets the norm's FP32 scale).
+// r -= A e with its norm into d_scal[slot] (after a correction); e goes to a free stash
+// array (x untouched), or, with both taken, x gets the two stashed corrections and e here;
+// res0 = the initial residual's squared norm (sets the norm's FP32 scale).
 int Ctx::update_residual(double *sol, double *rsd, int slot, double res0)
 {
     NvtxRange nvtx_range("correction and residual update");
@@ -1240,8 +1242,8 @@ int Ctx::flush_stash(double *sol)
     return add_corrections(sol, false);
 }
 
-// Defect correction.  After a correction the residual is normally updated (r -= A e,
-// x += e in one pass, no FP64 stencil); the FP64 residual b - A x is recomputed where the
+// Defect correction.  After a correction the residual is normally updated (r -= A e in
+// one pass, no FP64 stencil, e stashed for x); the FP64 residual b - A x is recomputed where the
 // solve may end: when the updated residual passes the test (the recomputed one decides,
 // and it is the residual returned), when the previous contraction predicts that this
 // correction passes it by a margin of 10, and after the last allowed correction.
